@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""bench.py -- IFGF forward-map throughput of the GB300 build on the kite at k = 500.
+
+Workload (the configuration the headline metric is quoted on): Colton-Kress kite
+x(t) = (cos t + 0.65 cos 2t - 0.65, 1.5 sin t), k = 500, 512 equal-parameter patches x 16
+Fejer nodes (N = 8192), single-layer operator, IFGF with 5 x 5 Chebyshev nodes per cone,
+the deepest tree that keeps singular points in the leaf neighbourhood, FP64 (plain form).
+A step is one forward map y = A x (singular correction + IFGF far field) on a seeded
+mt19937(0) density.  Synthetic geometry, no dataset.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  value: matvecs/s with vectors resident in HBM; e2e: the same
+through the C ABI (ifgf2d_apply) with pinned host buffers, copies inside the timed region;
+roofline: the dominant phase from live CUDA-event timings; cpu_baseline: the CPU oracle
+(single-threaded restatement of the reference path) on a bounded sample.  Multi-GPU runs
+are independent replicas (the path has no exchange step); value sums all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+K_WAVE = 500.0
+NPATCH, NP, DELTA = 512, 16, 0.01
+METRIC = "IFGF matvecs/s (kite k=500, N=8192, FP64 single layer)"
+UNIT = "matvec/s"
+WORKLOAD = "kite k=500, 512 equal patches x 16 Fejer nodes (N=8192), IFGF 5x5 cones, FP64"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def make_ours():
+    import ifgf2d_gb300 as G
+    fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, K_WAVE, Np=NP, patches_per_curve=NPATCH)
+    fm.precomps_and_setup(K_WAVE, 0)
+    return G, fm
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def phase_model(wc, N, P, ncones_leaf, nparent):
+    """Algorithmic bytes and flops of each apply phase (FP64: complex = 16 B)."""
+    C = 16
+    near, leaf, prop, interp, cones, sing = (wc["near_pairs"], wc["leaf_evals"], wc["prop_evals"],
+                                            wc["interp_evals"], wc["cones"], wc["sing_entries"])
+    return {
+        "sing_correction": (sing * C + 2 * N * C, sing * 8),
+        "intensities": (N * (C + 8 + 8 + C), N * 2),
+        "leaf_cones": (leaf * C + N * C + ncones_leaf * P * C, leaf * 8),
+        "propagation": (prop * 40 + cones * P * C, prop * (4 * P + 18) + nparent * P * P * 4),
+        "near_interp": (near * C + interp * 40 + cones * P * C + 3 * N * C, near * 8 + interp * (4 * P + 18)),
+    }
+
+
+def run_ours(args, rank, local_rank, world):
+    import torch
+    torch.cuda.set_device(local_rank)
+    from oracle.oracle import seeded_density
+    G, fm = make_ours()
+    N = fm.total_num_unknowns_
+    wc = fm.work_counts()
+    L = G._lib.load()
+    ext = torch.cuda.ExternalStream(fm.stream())
+    x_h = seeded_density(N)
+    x = torch.from_numpy(x_h).to("cuda")
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    # warm-up
+    for _ in range(max(args.warmup, 3)):
+        fm.apply_device(x, y)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize()
+        e0.record(ext)
+        for _ in range(args.steps):
+            fm.apply_device(x, y)
+        e1.record(ext)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * args.steps / (ms * 1e-3)
+    # end to end: host buffers through the C ABI (copies in the timed region)
+    xp = torch.from_numpy(x_h).pin_memory()
+    yp = torch.empty_like(xp).pin_memory()
+    k_e2e = max(1, min(args.steps, 500))
+    for _ in range(3):
+        L.ifgf2d_apply(fm.handle, G._dp(xp.numpy().view(np.float64)), G._dp(yp.numpy().view(np.float64)), 1)
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(ext)
+    for _ in range(k_e2e):
+        rc = L.ifgf2d_apply(fm.handle, G._dp(xp.numpy().view(np.float64)), G._dp(yp.numpy().view(np.float64)), 1)
+        assert rc == 0
+    e3.record(ext)
+    torch.cuda.synchronize()
+    e2e_ms = e2.elapsed_time(e3) / k_e2e
+    y_dev = y.cpu().numpy()
+    assert np.allclose(yp.numpy(), y_dev, rtol=0, atol=1e-12 * np.abs(y_dev).max()), "e2e result differs"
+    # per-phase timings (CUDA events between the phases, on the context's stream)
+    phases = ["sing_correction", "intensities", "leaf_cones", "propagation", "near_interp"]
+    acc = np.zeros(5)
+    nrep = max(10, min(args.steps, 200))
+    buf = (ctypes.c_double * 5)()
+    for _ in range(nrep):
+        rc = L.ifgf2d_apply_timed(fm.handle, x.data_ptr(), y.data_ptr(), 1, buf)
+        assert rc == 0
+        acc += np.array(buf[:])
+    acc /= nrep
+    P = fm.Ps * fm.Pang
+    nl = fm.nlevels
+    # coefficient writes are bounded by the total cone count (a small term)
+    model = phase_model(wc, N, P, ncones_leaf=wc["cones"], nparent=wc["cones"])
+    dom = int(np.argmax(acc))
+    dname = phases[dom]
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    fp64_peak = ctypes.c_double(0.0)
+    L.ifgf2d_measure_fp64_peak(ctypes.byref(fp64_peak))
+    bytes_d, flops_d = model[dname]
+    achieved = bytes_d / (acc[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dname)
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "fp64": {"achieved_tflops": flops_d / (acc[dom] * 1e-3) / 1e12, "peak_tflops": fp64_peak.value,
+                         "frac": (flops_d / (acc[dom] * 1e-3) / 1e12) / max(fp64_peak.value, 1e-9),
+                         "peak_source": "measured (ifgf2d_measure_fp64_peak)"},
+                "phase_ms": dict(zip(phases, [float(v) for v in acc]))}
+    # GMRES solve to 1e-6 (plane wave at angle 0), plain FP64 IFGF
+    b = -np.exp(1j * K_WAVE * fm.xs_)
+    t0 = time.perf_counter()
+    xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000)
+    solve_s = time.perf_counter() - t0
+    true_res = float(np.linalg.norm(fm.compute_Ax_acc(xs) - b) / np.linalg.norm(b))
+    solve = {"seconds": solve_s, "iters": fm.last_solve["iters"], "converged": fm.last_solve["converged"],
+             "true_rel_residual": true_res, "tol": 1e-6, "restart": 300}
+    launches_per_apply = 3 + (nl - 3) + 1
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded kite geometry, mt19937(0) density)",
+        "config": {"workload": WORKLOAD, "N": N, "k": K_WAVE, "nlevels": nl, "patches": NPATCH, "Np": NP,
+                   "Ps": fm.Ps, "Pang": fm.Pang, "parallelism": f"replicas x{world}",
+                   "l2": f"per-step streamed tables {wc['resident_bytes'] / 1e6:.0f} MB > 129 MB L2 (no flush)"},
+        "e2e": {"value": world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
+                "ms_per_step": e2e_ms},
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "gpu_launches": launches_per_apply * args.steps,
+        "solve": solve,
+        "work": wc,
+    }
+    return out
+
+
+def time_oracle(budget_s=12.0, max_steps=None):
+    """CPU oracle (single-threaded restatement of the reference path) on the same workload."""
+    from oracle import oracle as O
+    O.build()
+    om = O.OracleForwardMap([O.curve_kite()], NP, DELTA, 1.0, K_WAVE, patches_per_curve=NPATCH)
+    om.precompute(K_WAVE)
+    import ifgf2d_gb300 as G
+    # same tree depth rule as the product: deepest nlevels passing the neighbourhood check
+    for nl in range(16, 2, -1):
+        try:
+            om.setup_ifgf(K_WAVE, nl)
+            break
+        except RuntimeError:
+            continue
+    d = O.seeded_density(om.N)
+    steps, t_total = 0, 0.0
+    while t_total < budget_s and (max_steps is None or steps < max_steps):
+        t0 = time.perf_counter()
+        om.compute_Ax_acc(d)
+        t_total += time.perf_counter() - t0
+        steps += 1
+    return {"value": steps / t_total, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} full IFGF matvecs of the same workload (nlevels {nl}), {t_total:.1f} s, 1 thread"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    r = time_oracle(budget_s=float(os.environ.get("IFGF2D_REF_BUDGET_S", "60")),
+                    max_steps=max(1, args.steps))
+    return {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded kite geometry, mt19937(0) density)", "impl": "reference",
+        "config": {"workload": WORKLOAD, "parallelism": "host cores"},
+        "cpu_baseline": r,
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, local_rank, world = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    out = run_ours(args, rank, local_rank, world)
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = time_oracle(budget_s=12.0)
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,329 @@
+"""ifgf2d_gb300 -- GB300-native forward map of IFGF2D (2D Helmholtz boundary integral operator).
+
+Python mirror of the reference's C++ interface for the matvec that GMRES calls:
+
+* ``ForwardMap``      -- ForwardMap<Np, SingleLayer, Ps, Pang> (ForwardMap/ForwardMap.hpp:49-177):
+                         constructor (discretisation), ``compute_precomputations``,
+                         ``precomps_and_setup``, ``compute_Ax_unacc`` / ``compute_Ax_acc``,
+                         ``solve``, ``propagate_unacc`` and the public arrays ``xs_`` ... ``nys_``.
+* ``LinearOperator``  -- ForwardMap/LinearOperator.hpp:27-58 (rows, cols, mapping, ``A * x``).
+* curve constructors  -- Geometry/Curve.hpp:106-161 (``Circle``, ``Kite``, ``Line``) plus ``Star``.
+
+All arithmetic runs in libifgf2d.so (C++ host + sm_103a CUDA kernels, include/ifgf2d.h).  The
+reference throws std::logic_error / std::invalid_argument; these bindings raise the Python
+equivalents (``RuntimeError`` subclasses below, ``ValueError`` for bad arguments).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import numpy as np
+
+from . import _lib
+from ._lib import APPLY_DIRECT, APPLY_IFGF
+
+__all__ = ["ForwardMap", "LinearOperator", "Circle", "Kite", "Line", "Star", "Junction", "hankel1",
+           "IFGF2DError", "NeighbourhoodError", "NoConvergence", "load_library"]
+
+
+class IFGF2DError(RuntimeError):
+    """Error status from libifgf2d (the reference throws std::logic_error)."""
+
+
+class NeighbourhoodError(IFGF2DError):
+    """A singular / near-singular point lies outside the leaf neighbourhood (BoxTree.h:1112-1153)."""
+
+
+class NoConvergence(IFGF2DError):
+    """GMRES stopped at max_iters before reaching the tolerance (Eigen NoConvergence)."""
+
+
+def load_library():
+    return _lib.load()
+
+
+def _check(rc, ctx=None):
+    if rc == 0:
+        return
+    msg = _lib.load().ifgf2d_last_error(ctx).decode() if ctx else ""
+    name = _lib.STATUS.get(rc, str(rc))
+    if rc == 1:
+        raise ValueError(f"ifgf2d: {name}: {msg}")
+    if rc == 3:
+        raise NeighbourhoodError(f"ifgf2d: {name}: {msg}")
+    raise IFGF2DError(f"ifgf2d: {name}: {msg}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _cview(x, n=None):
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    if n is not None and x.shape != (n,):
+        raise ValueError(f"expected a vector of {n} complex values, got shape {x.shape}")
+    return x
+
+
+# ---------------------------------------------------------------- curves
+def _curve(kind, closed, t1, t2, params):
+    c = _lib.Curve()
+    c.type, c.closed, c.tlim1, c.tlim2 = kind, 1 if closed else 0, float(t1), float(t2)
+    for i, v in enumerate(params):
+        c.params[i] = float(v)
+    return c
+
+
+def Circle(centerx=0.0, centery=0.0, radius=1.0):
+    """Geometry/Curve.hpp:106-125 (parametrised on [0, 2 pi])."""
+    return _curve(_lib.CURVE_CIRCLE, True, 0.0, 2 * math.pi, [centerx, centery, radius])
+
+
+def Kite(A=1.0, B=0.65, C=-0.65, D=1.5):
+    """Geometry/Curve.hpp:128-146: x = A cos t + B cos 2t + C, y = D sin t."""
+    return _curve(_lib.CURVE_KITE, True, 0.0, 2 * math.pi, [A, B, C, D])
+
+
+def Line(x1, y1, x2, y2):
+    """Geometry/Curve.hpp:148-161: open segment on t in [-1, 1]."""
+    return _curve(_lib.CURVE_LINE, False, -1.0, 1.0, [x1, y1, x2, y2])
+
+
+def Star(a, b, centerx=0.0, centery=0.0):
+    """Star-shaped curve r(t) = 1 + sum_m a_m cos mt + b_m sin mt (m <= 6; not in the reference)."""
+    a = list(a); b = list(b)
+    if len(a) != len(b) or len(a) > 6:
+        raise ValueError("Star: a and b must have the same length <= 6")
+    return _curve(_lib.CURVE_STAR, True, 0.0, 2 * math.pi, [centerx, centery, len(a)] + a + b)
+
+
+def Junction(curve, touching_curve, t1_touches_t1):
+    """Geometry/Curve.hpp:10-17 (with the owning curve index made explicit)."""
+    j = _lib.Junction()
+    j.curve, j.touching_curve, j.t1_touches_t1 = curve, touching_curve, 1 if t1_touches_t1 else 0
+    return j
+
+
+def hankel1(order: int, x) -> np.ndarray:
+    """H_order^(1)(x) for real x > 0 on the GPU (device evaluator; replaces sp_bessel::hankelH1)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty(2 * x.size)
+    _check(_lib.load().ifgf2d_hankel(order, x.size, _dp(x), _dp(out)))
+    return out[0::2] + 1j * out[1::2]
+
+
+# ---------------------------------------------------------------- LinearOperator
+class LinearOperator:
+    """ForwardMap/LinearOperator.hpp:43-58: an operator defined by a mapping(x, out) callable."""
+
+    def __init__(self, rows, cols, mapping):
+        self._rows, self._cols, self.mapping_ = int(rows), int(cols), mapping
+
+    def rows(self):
+        return self._rows
+
+    def cols(self):
+        return self._cols
+
+    def __mul__(self, x):
+        out = np.empty(self._rows, dtype=np.complex128)
+        self.mapping_(x, out)
+        return out
+
+
+# ---------------------------------------------------------------- ForwardMap
+class ForwardMap:
+    """ForwardMap<Np, SingleLayer, Ps, Pang> on one GB300.
+
+    ForwardMap(delta, curves, curve_touch_tracker, wavelengths_per_patch, patch_split_wavenumber, p=4)
+    with ``Np``, ``Ps``, ``Pang`` given as keyword arguments (template parameters in C++).
+    ``patches_per_curve > 0`` selects an equal-parameter split instead of the arc-length rule.
+    """
+
+    def __init__(self, delta, curves, curve_touch_tracker=(), wavelengths_per_patch=1.0,
+                 patch_split_wavenumber=1.0, p=4.0, *, Np=10, Ps=5, Pang=5, patches_per_curve=0):
+        L = _lib.load()
+        curves = list(curves)
+        if not curves:
+            raise ValueError("ForwardMap needs at least one curve")
+        carr = (_lib.Curve * len(curves))(*curves)
+        jl = list(curve_touch_tracker)
+        jarr = (_lib.Junction * max(len(jl), 1))(*jl) if jl else None
+        opt = _lib.Options(Np, delta, wavelengths_per_patch, patch_split_wavenumber, p, patches_per_curve, Ps, Pang)
+        h = ctypes.c_void_p()
+        rc = L.ifgf2d_create(carr, len(curves), jarr, len(jl), ctypes.byref(opt), ctypes.byref(h))
+        self._h = h.value
+        if rc != 0:
+            msg = L.ifgf2d_last_error(self._h).decode() if self._h else ""
+            if self._h:
+                L.ifgf2d_destroy(self._h)
+                self._h = None
+            if rc == 2:
+                raise ValueError(f"ifgf2d_create: {msg}")
+            _check(rc)
+        self.Np, self.Ps, self.Pang = Np, Ps, Pang
+        self.delta_, self.p_ = delta, p
+        self.total_num_unknowns_ = int(L.ifgf2d_num_unknowns(self._h))
+        self.num_patches_ = int(L.ifgf2d_num_patches(self._h))
+        n = self.total_num_unknowns_
+        self.xs_, self.ys_, self.nxs_, self.nys_ = (np.empty(n) for _ in range(4))
+        _check(L.ifgf2d_get_points(self._h, _dp(self.xs_), _dp(self.ys_), _dp(self.nxs_), _dp(self.nys_)), self._h)
+        self.GMRES_MAX_ITER_ = 300
+        self.GMRES_TOLERANCE_ = 1e-10
+        self.wavenumber = None
+        self.nlevels = None
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().ifgf2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- geometry queries
+    def patches(self):
+        """(num_patches, 2) patch limits and the near-singular point count per patch."""
+        t = np.empty(2 * self.num_patches_)
+        c = np.empty(self.num_patches_, dtype=np.int64)
+        _check(_lib.load().ifgf2d_get_patches(self._h, _dp(t), c.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)
+        return t.reshape(-1, 2), c
+
+    def near_singular(self):
+        """(counts per patch, concatenated point indices, concatenated Brent t values)."""
+        _, cnt = self.patches()
+        tot = int(cnt.sum())
+        idx = np.empty(max(tot, 1), dtype=np.int64)
+        t = np.empty(max(tot, 1))
+        _check(_lib.load().ifgf2d_get_near_singular(self._h, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), _dp(t)), self._h)
+        return cnt, idx[:tot], t[:tot]
+
+    # -- set-up
+    def compute_precomputations(self, wavenumber):
+        """ForwardMap.tpp:391-423 (rectangular-polar weights, computed on the GPU)."""
+        _check(_lib.load().ifgf2d_precompute(self._h, float(wavenumber)), self._h)
+        self.wavenumber = float(wavenumber)
+
+    def precomputations(self, patch):
+        """Patch.hpp:55 precomputations_: Np x (Np + n_ns) complex matrix of one patch."""
+        _, cnt = self.patches()
+        ncol = self.Np + int(cnt[patch])
+        out = np.empty(2 * self.Np * ncol)
+        _check(_lib.load().ifgf2d_get_precomputations(self._h, int(patch), _dp(out)), self._h)
+        return (out[0::2] + 1j * out[1::2]).reshape(ncol, self.Np).T
+
+    def precomps_and_setup(self, wavenumber, nlevels=0):
+        """ForwardMap.tpp:542-565; nlevels <= 0 picks the deepest tree that passes the neighbourhood check."""
+        _check(_lib.load().ifgf2d_setup(self._h, float(wavenumber), int(nlevels)), self._h)
+        self.wavenumber = float(wavenumber)
+        self.nlevels = int(_lib.load().ifgf2d_get_nlevels(self._h))
+
+    def getSorting(self):
+        s = np.empty(self.total_num_unknowns_, dtype=np.int64)
+        _check(_lib.load().ifgf2d_get_sorting(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)
+        return s
+
+    def work_counts(self):
+        c = np.zeros(8, dtype=np.int64)
+        _check(_lib.load().ifgf2d_work_counts(self._h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)
+        keys = ["near_pairs", "leaf_evals", "prop_evals", "interp_evals", "cones", "nlevels", "sing_entries", "resident_bytes"]
+        return dict(zip(keys, (int(v) for v in c)))
+
+    # -- the matvec
+    def _apply(self, x, mode):
+        n = self.total_num_unknowns_
+        xin = _cview(x, n)
+        out = np.empty(n, dtype=np.complex128)
+        _check(_lib.load().ifgf2d_apply(self._h, _dp(xin.view(np.float64)), _dp(out.view(np.float64)), mode), self._h)
+        return out
+
+    def compute_Ax_unacc(self, density, out=None):
+        """ForwardMap.tpp:517-540: singular correction + direct O(N^2) far sum."""
+        y = self._apply(density, APPLY_DIRECT)
+        if out is not None:
+            out[...] = y
+        return y
+
+    def compute_Ax_acc(self, density, out=None):
+        """ForwardMap.tpp:609-655: singular correction + IFGF far sum (BoxTree::Solve)."""
+        y = self._apply(density, APPLY_IFGF)
+        if out is not None:
+            out[...] = y
+        return y
+
+    def ifgf_far(self, intensities):
+        """BoxTree::Solve on given intensities (IFGF_Source/BoxTree.h:1020-1071)."""
+        n = self.total_num_unknowns_
+        xin = _cview(intensities, n)
+        out = np.empty(n, dtype=np.complex128)
+        _check(_lib.load().ifgf2d_ifgf_far(self._h, _dp(xin.view(np.float64)), _dp(out.view(np.float64))), self._h)
+        return out
+
+    def apply_device(self, d_x, d_y, accelerated=True):
+        """y = A x on device pointers (ints or objects with data_ptr(); N complex128 each)."""
+        px = d_x.data_ptr() if hasattr(d_x, "data_ptr") else int(d_x)
+        py = d_y.data_ptr() if hasattr(d_y, "data_ptr") else int(d_y)
+        _check(_lib.load().ifgf2d_apply_device(self._h, px, py, APPLY_IFGF if accelerated else APPLY_DIRECT), self._h)
+
+    def stream(self):
+        return _lib.load().ifgf2d_stream(self._h)
+
+    # -- solver
+    def solve(self, rhs, wavenumber, nlevels=0, accelerated=True, tol=None, restart=None, max_iters=None,
+              raise_on_noconv=False):
+        """ForwardMap.tpp:658-697: set-up, then GMRES (initial guess 0) on the device.
+
+        Returns the density; ``self.last_solve`` holds iterations and the estimated error.
+        """
+        if accelerated:
+            self.precomps_and_setup(wavenumber, nlevels)
+        else:
+            self.compute_precomputations(wavenumber)
+        return self.gmres(rhs, accelerated, tol, restart, max_iters, raise_on_noconv)
+
+    def gmres(self, rhs, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False):
+        n = self.total_num_unknowns_
+        b = _cview(rhs, n)
+        x = np.empty(n, dtype=np.complex128)
+        it = ctypes.c_int(0)
+        err = ctypes.c_double(0.0)
+        tol = self.GMRES_TOLERANCE_ if tol is None else tol
+        restart = self.GMRES_MAX_ITER_ if restart is None else restart
+        max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
+        rc = _lib.load().ifgf2d_solve(self._h, _dp(b.view(np.float64)), _dp(x.view(np.float64)),
+                                      APPLY_IFGF if accelerated else APPLY_DIRECT, float(tol), int(restart),
+                                      int(max_iters), ctypes.byref(it), ctypes.byref(err))
+        self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0))
+        if rc == 8:
+            if raise_on_noconv:
+                raise NoConvergence(f"GMRES: {it.value} iterations, estimated error {err.value:.3e}")
+        else:
+            _check(rc, self._h)
+        return x
+
+    def linear_operator(self, accelerated=True):
+        """LinearOperator wrapping compute_Ax_acc / compute_Ax_unacc, as ForwardMap::solve builds it."""
+        f = self.compute_Ax_acc if accelerated else self.compute_Ax_unacc
+        return LinearOperator(self.total_num_unknowns_, self.total_num_unknowns_, lambda x, out: f(x, out))
+
+    def propagate_unacc(self, x_prop, y_prop, density, wavenumber=None):
+        """ForwardMap.tpp:701-727: direct evaluation of the layer potential off the surface."""
+        if wavenumber is not None and self.wavenumber != float(wavenumber):
+            self.compute_precomputations(wavenumber)
+        xp = np.ascontiguousarray(x_prop, dtype=np.float64)
+        yp = np.ascontiguousarray(y_prop, dtype=np.float64)
+        if xp.shape != yp.shape:
+            raise ValueError("x_prop and y_prop must have the same length")
+        d = _cview(density, self.total_num_unknowns_)
+        out = np.empty(xp.size, dtype=np.complex128)
+        _check(_lib.load().ifgf2d_propagate(self._h, xp.size, _dp(xp), _dp(yp), _dp(d.view(np.float64)),
+                                            _dp(out.view(np.float64))), self._h)
+        return out

@@ -1,0 +1,86 @@
+// hankel.cuh -- device Hankel functions H0^(1), H1^(1) of real argument, FP64.
+//
+// Replaces sp_bessel::hankelH1 (complex_bessel-master/include/complex_bessel_bits/
+// besselFunctions.h:313-341 -> AMOS zbesh) on the GPU.  Real wavenumber, real x > 0.
+// Three regions (coefficients in hankel_tables.inc, generated by gen_hankel_tables.py):
+//   x < HK_XA        ascending series in q = x^2/4 (A&S 9.1.10-11), Horner;
+//   HK_XA <= x < XC  piecewise Chebyshev expansions of J_nu and Y_nu (width HK_W), Clenshaw;
+//   x >= HK_XC       Hankel asymptotic expansion (A&S 9.2.5-10), P, Q polynomials in 1/x^2.
+// |H| never vanishes for real x, so errors are stated relative to |H| (~1e-15, tested
+// against scipy.special.hankel1 in tests/test_gpu_parity.py).
+#pragma once
+#include <cuda_runtime.h>
+
+#define HK_TABLE __device__ const
+#include "hankel_tables.inc"
+
+namespace ifgf {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kTwoOverPi = 0.63661977236758134308;
+constexpr double kEulerGamma = 0.57721566490153286061;
+
+template <int NU>
+__device__ __forceinline__ double2 hankel1(double x) {
+    if (x < HK_XA) {
+        const double* a = NU == 0 ? hk_ser_a0 : hk_ser_a1;
+        const double* b = NU == 0 ? hk_ser_b0 : hk_ser_b1;
+        const double q = 0.25 * x * x;
+        double J = __ldg(a + HK_NSER - 1), S = __ldg(b + HK_NSER - 1);
+#pragma unroll
+        for (int k = HK_NSER - 2; k >= 0; --k) { J = fma(J, q, __ldg(a + k)); S = fma(S, q, __ldg(b + k)); }
+        const double L = kTwoOverPi * (log(0.5 * x) + kEulerGamma);
+        if (NU == 0) return make_double2(J, fma(L, J, S));
+        const double h = 0.5 * x;
+        const double J1 = h * J;
+        return make_double2(J1, fma(L, J1, h * S) - kTwoOverPi / x);
+    } else if (x < HK_XC) {
+        int p = (int)((x - HK_XA) * (1.0 / HK_W));
+        p = p < 0 ? 0 : (p >= HK_NPIECES ? HK_NPIECES - 1 : p);
+        const double t = (x - (HK_XA + p * HK_W)) * (2.0 / HK_W) - 1.0;
+        const double* cj = (NU == 0 ? hk_cheb0 : hk_cheb1) + p * 2 * (HK_DEG + 1);
+        const double* cy = cj + (HK_DEG + 1);
+        double bj1 = 0.0, bj2 = 0.0, by1 = 0.0, by2 = 0.0;
+        const double t2 = 2.0 * t;
+#pragma unroll
+        for (int k = HK_DEG; k >= 1; --k) {
+            const double bj = fma(t2, bj1, __ldg(cj + k) - bj2);
+            const double by = fma(t2, by1, __ldg(cy + k) - by2);
+            bj2 = bj1; bj1 = bj; by2 = by1; by1 = by;
+        }
+        return make_double2(fma(t, bj1, __ldg(cj) - bj2), fma(t, by1, __ldg(cy) - by2));
+    } else {
+        const double* P = NU == 0 ? hk_asyP0 : hk_asyP1;
+        const double* Q = NU == 0 ? hk_asyQ0 : hk_asyQ1;
+        const double w = 1.0 / x, w2 = w * w;
+        double pp = __ldg(P + HK_NASY - 1), qq = __ldg(Q + HK_NASY - 1);
+#pragma unroll
+        for (int k = HK_NASY - 2; k >= 0; --k) { pp = fma(pp, w2, __ldg(P + k)); qq = fma(qq, w2, __ldg(Q + k)); }
+        qq *= w;
+        double s, c;
+        sincos(x, &s, &c);
+        // e^{i(x - pi/4)} = (c + s + i(s - c))/sqrt2 ; e^{i(x - 3pi/4)} = (s - c - i(s + c))/sqrt2
+        const double er = NU == 0 ? (c + s) : (s - c);
+        const double ei = NU == 0 ? (s - c) : -(s + c);
+        const double amp = sqrt(w * (1.0 / kPi));   // sqrt(2/(pi x)) / sqrt(2)
+        return make_double2(amp * (pp * er - qq * ei), amp * (pp * ei + qq * er));
+    }
+}
+
+// Single-layer kernel (i/4) H0(k r), 0 for r < 1e-14 (ForwardMap/GreenFunctions.hpp:87-108)
+__device__ __forceinline__ double2 green_sl(double dx, double dy, double k) {
+    const double r = sqrt(dx * dx + dy * dy);
+    if (r < 1e-14) return make_double2(0.0, 0.0);
+    const double2 h = hankel1<0>(k * r);
+    return make_double2(-0.25 * h.y, 0.25 * h.x);
+}
+
+// e^{ikr}/sqrt(r) (GreenFunctions.hpp:125-131)
+__device__ __forceinline__ double2 factorization(double r, double k) {
+    double s, c;
+    sincos(k * r, &s, &c);
+    const double a = 1.0 / sqrt(r);
+    return make_double2(c * a, s * a);
+}
+
+}  // namespace ifgf

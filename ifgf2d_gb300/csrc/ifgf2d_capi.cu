@@ -1,0 +1,685 @@
+// ifgf2d_capi.cu -- the C ABI (include/ifgf2d.h): context, set-up, apply, GMRES, propagation.
+//
+// Host orchestration of the GB300 forward map.  The context owns every device buffer; set-up
+// sizes them once, so an apply or a GMRES iteration allocates nothing.
+#include "../../include/ifgf2d.h"
+#include "geometry.hpp"
+#include "tree.hpp"
+#include "ifgf2d_kernels.cuh"
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <complex>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace ifgf;
+
+namespace {
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+    cudaError_t alloc(size_t cnt) {
+        release();
+        n = cnt;
+        if (cnt == 0) return cudaSuccess;
+        return cudaMalloc((void**)&p, cnt * sizeof(T));
+    }
+    cudaError_t upload(const T* src, size_t cnt) {
+        cudaError_t e = alloc(cnt);
+        if (e != cudaSuccess || cnt == 0) return e;
+        return cudaMemcpy(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice);
+    }
+    cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
+};
+
+}  // namespace
+
+struct ifgf2d_ctx {
+    Discretisation D;
+    ifgf2d_options opt{};
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    double k = 0.0;
+    bool device_ready = false, precomputed = false, ifgf_ready = false;
+    std::vector<int> h_nsp_ptr, h_nsp, h_srow_ptr, h_srow_col;
+    int nlevels = 0;
+    // geometry (original order)
+    DBuf<double> x, y, wq, edge;
+    DBuf<int> patch_of;
+    DBuf<DevCurve> curves;
+    DBuf<DevPatch> patches;
+    DBuf<double> nsn, nsw;
+    DBuf<int> nsp_ptr, nsp;        // per point: patches it is near-singular to
+    // rectangular-polar correction
+    std::vector<RPColumn> hcols;
+    std::vector<int> col_ptr;      // per patch: first column
+    DBuf<RPColumn> cols;
+    DBuf<double2> M, W;
+    DBuf<int> srow_ptr, srow_col;
+    // IFGF tree
+    Tree T;
+    DBuf<long long> sorting;
+    DBuf<double> xs_s, ys_s;
+    DBuf<int> patch_s, nsp_ptr_s, nsp_s;
+    DBuf<int> leaf_start, leaf_count, point_leaf, nbr_ptr, nbr_box;
+    DBuf<long long> near_off;
+    DBuf<double2> near;
+    DBuf<int> leaf_cone_box;
+    DBuf<long long> leaf_off;
+    DBuf<LeafNode> leaf_nodes_d;
+    DBuf<double2> leafL;
+    DBuf<long long> pp_ptr;
+    DBuf<int> pp_nchild;
+    DBuf<PropEntryD> pp;
+    DBuf<int> ip_ptr;
+    DBuf<InterpEntryD> ip;
+    DBuf<double2> coef;
+    DBuf<double> Gm;
+    // work vectors
+    DBuf<double2> rho, vin, vout;
+    long long counts[8] = {0};
+};
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                \
+            return IFGF2D_ERR_CUDA;                                                       \
+        }                                                                                 \
+    } while (0)
+
+static int fail(ifgf2d_ctx* ctx, int code, const std::string& msg) { ctx->err = msg; return code; }
+
+// ------------------------------------------------------------------ create / destroy
+extern "C" int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf2d_junction* junctions, int njunctions,
+                             const ifgf2d_options* opts, ifgf2d_ctx** out) {
+    if (!out || !opts) return IFGF2D_ERR_ARG;
+    *out = nullptr;
+    ifgf2d_ctx* ctx = new ifgf2d_ctx;
+    ctx->opt = *opts;
+    if (ctx->opt.Ps <= 0) ctx->opt.Ps = 5;
+    if (ctx->opt.Pang <= 0) ctx->opt.Pang = 5;
+    {
+        // cone interpolants compiled for the device (IFGF_DISPATCH_P in ifgf2d_kernels.cu)
+        const int ps = ctx->opt.Ps, pa = ctx->opt.Pang;
+        const bool ok = (ps == 5 && pa == 5) || (ps == 5 && pa == 7) || (ps == 3 && pa == 5) || (ps == 3 && pa == 3) ||
+                        (ps == 7 && pa == 7) || (ps == 4 && pa == 4) || (ps == 6 && pa == 6);
+        if (!ok) { *out = ctx; ctx->err = "(Ps, Pang) must be one of (3,3) (3,5) (4,4) (5,5) (5,7) (6,6) (7,7)"; return IFGF2D_ERR_ARG; }
+    }
+    std::string msg = discretise(curves, ncurves, junctions, njunctions, ctx->opt, ctx->D);
+    if (!msg.empty()) {
+        // report through a context so the caller can read the message, as the reference prints it
+        *out = ctx; ctx->err = msg; return IFGF2D_ERR_GEOMETRY;
+    }
+    *out = ctx;
+    const Discretisation& D = ctx->D;
+    // per point: the patches it is near-singular to (ForwardMap.tpp:596-604)
+    ctx->h_nsp_ptr.assign(D.N + 1, 0);
+    {
+        std::vector<std::vector<int>> per(D.N);
+        for (long long p = 0; p < D.num_patches; ++p)
+            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) per[D.ns_idx[q]].push_back((int)p);
+        for (long long i = 0; i < D.N; ++i) {
+            if (per[i].size() > 8) { ctx->err = "a point is near-singular to more than 8 patches (reduce delta)"; return IFGF2D_ERR_GEOMETRY; }
+            for (int p : per[i]) ctx->h_nsp.push_back(p);
+            ctx->h_nsp_ptr[i + 1] = (int)ctx->h_nsp.size();
+        }
+    }
+    // rectangular-polar columns: per patch Np singular columns then its near-singular ones
+    ctx->col_ptr.assign(D.num_patches + 1, 0);
+    for (long long p = 0; p < D.num_patches; ++p) {
+        ctx->col_ptr[p] = (int)ctx->hcols.size();
+        for (int j = 0; j < D.Np; ++j) {
+            const long long i = p * D.Np + j;
+            ctx->hcols.push_back(RPColumn{(int)p, 0, D.t[i], D.x[i], D.y[i]});
+        }
+        for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q)
+            ctx->hcols.push_back(RPColumn{(int)p, 0, D.ns_t[q], D.x[D.ns_idx[q]], D.y[D.ns_idx[q]]});
+    }
+    ctx->col_ptr[D.num_patches] = (int)ctx->hcols.size();
+    // per output row: the columns that add to it, in patch order (ForwardMap.tpp:486-512)
+    {
+        std::vector<std::vector<std::pair<int, int>>> rows(D.N);
+        for (long long p = 0; p < D.num_patches; ++p) {
+            for (int j = 0; j < D.Np; ++j) rows[p * D.Np + j].push_back({(int)p, ctx->col_ptr[p] + j});
+            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q)
+                rows[D.ns_idx[q]].push_back({(int)p, ctx->col_ptr[p] + D.Np + (q - D.ns_ptr[p])});
+        }
+        ctx->h_srow_ptr.assign(D.N + 1, 0);
+        for (long long i = 0; i < D.N; ++i) {
+            std::sort(rows[i].begin(), rows[i].end());
+            for (auto& e : rows[i]) ctx->h_srow_col.push_back(e.second);
+            ctx->h_srow_ptr[i + 1] = (int)ctx->h_srow_col.size();
+        }
+    }
+    return IFGF2D_OK;
+}
+
+// Device-side copies of the discretisation; made on first use so that the constructor, like
+// the reference's, is host work only.
+static int ensure_device(ifgf2d_ctx* ctx) {
+    if (ctx->device_ready) return IFGF2D_OK;
+    CK(cudaGetDevice(&ctx->device));
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    const Discretisation& D = ctx->D;
+    CK(ctx->x.upload(D.x)); CK(ctx->y.upload(D.y)); CK(ctx->wq.upload(D.wq)); CK(ctx->edge.upload(D.edge_jac));
+    CK(ctx->patch_of.upload(D.patch_of));
+    std::vector<DevCurve> dc(D.curves.size());
+    for (size_t c = 0; c < D.curves.size(); ++c) { dc[c].type = D.curves[c].type; dc[c].pad = 0; std::memcpy(dc[c].p, D.curves[c].p, sizeof(dc[c].p)); }
+    CK(ctx->curves.upload(dc));
+    std::vector<DevPatch> dp(D.num_patches);
+    for (long long p = 0; p < D.num_patches; ++p) dp[p] = DevPatch{D.t1[p], D.t2[p], D.curve_of[p], D.ist1sing[p], D.ist2sing[p], 0};
+    CK(ctx->patches.upload(dp));
+    CK(ctx->nsn.upload(D.fej_ns_n)); CK(ctx->nsw.upload(D.fej_ns_w));
+    CK(ctx->nsp_ptr.upload(ctx->h_nsp_ptr)); CK(ctx->nsp.upload(ctx->h_nsp));
+    CK(ctx->cols.upload(ctx->hcols));
+    CK(ctx->srow_ptr.upload(ctx->h_srow_ptr)); CK(ctx->srow_col.upload(ctx->h_srow_col));
+    CK(ctx->rho.alloc(D.N)); CK(ctx->vin.alloc(D.N)); CK(ctx->vout.alloc(D.N));
+    ctx->device_ready = true;
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (ctx->stream) { cudaStreamSynchronize(ctx->stream); cudaStreamDestroy(ctx->stream); }
+    delete ctx;
+    return IFGF2D_OK;
+}
+extern "C" const char* ifgf2d_last_error(const ifgf2d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+extern "C" long long ifgf2d_num_unknowns(const ifgf2d_ctx* ctx) { return ctx ? ctx->D.N : -1; }
+extern "C" long long ifgf2d_num_patches(const ifgf2d_ctx* ctx) { return ctx ? ctx->D.num_patches : -1; }
+extern "C" void* ifgf2d_stream(ifgf2d_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+extern "C" int ifgf2d_get_nlevels(const ifgf2d_ctx* ctx) { return ctx ? ctx->nlevels : -1; }
+
+extern "C" int ifgf2d_get_points(const ifgf2d_ctx* ctx, double* xs, double* ys, double* nxs, double* nys) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    const Discretisation& D = ctx->D;
+    if (xs) std::copy(D.x.begin(), D.x.end(), xs);
+    if (ys) std::copy(D.y.begin(), D.y.end(), ys);
+    if (nxs) std::copy(D.nx.begin(), D.nx.end(), nxs);
+    if (nys) std::copy(D.ny.begin(), D.ny.end(), nys);
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_get_patches(const ifgf2d_ctx* ctx, double* t1t2, long long* ns_count) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    const Discretisation& D = ctx->D;
+    for (long long p = 0; p < D.num_patches; ++p) {
+        if (t1t2) { t1t2[2 * p] = D.t1[p]; t1t2[2 * p + 1] = D.t2[p]; }
+        if (ns_count) ns_count[p] = D.ns_ptr[p + 1] - D.ns_ptr[p];
+    }
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_get_near_singular(const ifgf2d_ctx* ctx, long long* idx, double* t) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    for (size_t q = 0; q < ctx->D.ns_idx.size(); ++q) { if (idx) idx[q] = ctx->D.ns_idx[q]; if (t) t[q] = ctx->D.ns_t[q]; }
+    return IFGF2D_OK;
+}
+
+// ------------------------------------------------------------------ rectangular-polar precomputation
+extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
+    if (int rc = ensure_device(ctx)) return rc;
+    const Discretisation& D = ctx->D;
+    const int ncols = (int)ctx->hcols.size();
+    CK(ctx->M.alloc((size_t)ncols * D.Np));
+    CK(ctx->W.alloc((size_t)ncols * D.Np));
+    launch_rp_precompute(ctx->cols.p, ncols, ctx->patches.p, ctx->curves.p, ctx->nsn.p, ctx->nsw.p, D.Np, D.p, k, ctx->M.p, ctx->stream);
+    CK(cudaGetLastError());
+    launch_rp_fold(ctx->M.p, ctx->cols.p, ncols, ctx->edge.p, ctx->patches.p, D.Np, ctx->W.p, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->k = k;
+    ctx->precomputed = true;
+    ctx->ifgf_ready = false;
+    ctx->counts[6] = (long long)ncols * D.Np;
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, double* out) {
+    if (!ctx || !out || patch < 0 || patch >= ctx->D.num_patches) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute first");
+    const int c0 = ctx->col_ptr[patch], c1 = ctx->col_ptr[patch + 1];
+    CK(cudaMemcpy(out, ctx->M.p + (size_t)c0 * ctx->D.Np, sizeof(double2) * (size_t)(c1 - c0) * ctx->D.Np, cudaMemcpyDeviceToHost));
+    return IFGF2D_OK;
+}
+
+// ------------------------------------------------------------------ IFGF set-up
+// BoxTree::CheckIfSingandNearSingInNeighborhood (BoxTree.h:1079-1161) on leaf box coordinates
+static bool neighbourhood_ok(const Discretisation& D, int nlevels) {
+    double mx, my, size;
+    tree_root_box(D.x, D.y, mx, my, size);
+    const int lev = nlevels - 1;
+    const double bs = size / (double)(1LL << lev);
+    std::vector<long long> bx(D.N), by(D.N);
+    for (long long i = 0; i < D.N; ++i) {
+        bx[i] = (long long)((D.x[i] - mx) / bs); by[i] = (long long)((D.y[i] - my) / bs);
+        if (bx[i] < 0 || by[i] < 0 || bx[i] >= (1LL << lev) || by[i] >= (1LL << lev)) return false;
+    }
+    auto adj = [&](long long i, long long j) { return std::llabs(bx[i] - bx[j]) <= 1 && std::llabs(by[i] - by[j]) <= 1; };
+    for (long long i = 0; i < D.N; ++i) {
+        const long long p0 = (i / D.Np) * D.Np;
+        for (long long j = p0; j < p0 + D.Np; ++j) if (j != i && !adj(i, j)) return false;
+    }
+    for (long long p = 0; p < D.num_patches; ++p)
+        for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q)
+            for (long long j = p * D.Np; j < p * D.Np + D.Np; ++j) if (!adj(D.ns_idx[q], j)) return false;
+    return true;
+}
+
+extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed || ctx->k != k) {
+        int rc = ifgf2d_precompute(ctx, k);
+        if (rc != IFGF2D_OK) return rc;
+    }
+    const Discretisation& D = ctx->D;
+    if (nlevels <= 0) {
+        nlevels = 0;
+        for (int nl = 16; nl >= 3; --nl) if (neighbourhood_ok(D, nl)) { nlevels = nl; break; }
+        if (!nlevels) return fail(ctx, IFGF2D_ERR_NEIGHBORHOOD, "no tree depth >= 3 keeps singular points in the leaf neighbourhood");
+    } else {
+        if (nlevels < 3) return fail(ctx, IFGF2D_ERR_NLEVELS, "IFGF accelerator requires at least 3 levels.");
+        if (nlevels > 20) return fail(ctx, IFGF2D_ERR_NLEVELS, "nlevels too large");
+        if (!neighbourhood_ok(D, nlevels)) return fail(ctx, IFGF2D_ERR_NEIGHBORHOOD, "Singular point not in neighborhood");
+    }
+    ctx->ifgf_ready = false;
+    Tree& T = ctx->T;
+    std::string msg = build_tree(D.x, D.y, nlevels, k, ctx->opt.Ps, ctx->opt.Pang, T);
+    if (!msg.empty()) return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
+    ctx->nlevels = nlevels;
+    const long long N = D.N;
+    const int P = T.P, Dl = nlevels - 1;
+    // sorted-order tables
+    std::vector<int> patch_s(N), nptr(N + 1, 0), nl;
+    for (long long i = 0; i < N; ++i) {
+        const long long o = T.sorting[i];
+        patch_s[i] = D.patch_of[o];
+    }
+    {
+        std::vector<std::vector<int>> per(N);
+        for (long long p = 0; p < D.num_patches; ++p)
+            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) per[T.inverse[D.ns_idx[q]]].push_back((int)p);
+        for (long long i = 0; i < N; ++i) { for (int p : per[i]) nl.push_back(p); nptr[i + 1] = (int)nl.size(); }
+    }
+    CK(ctx->sorting.upload(T.sorting)); CK(ctx->xs_s.upload(T.xs)); CK(ctx->ys_s.upload(T.ys));
+    CK(ctx->patch_s.upload(patch_s)); CK(ctx->nsp_ptr_s.upload(nptr)); CK(ctx->nsp_s.upload(nl));
+    CK(ctx->leaf_start.upload(T.leaf_start)); CK(ctx->leaf_count.upload(T.leaf_count)); CK(ctx->point_leaf.upload(T.point_leaf));
+    CK(ctx->nbr_ptr.upload(T.nbr_ptr)); CK(ctx->nbr_box.upload(T.nbr_box));
+    // near-field blocks
+    const int nleaf = (int)T.leaf_start.size();
+    std::vector<long long> noff(nleaf + 1, 0);
+    for (int b = 0; b < nleaf; ++b) {
+        long long nsrc = 0;
+        for (int q = T.nbr_ptr[b]; q < T.nbr_ptr[b + 1]; ++q) nsrc += T.leaf_count[T.nbr_box[q]];
+        noff[b + 1] = noff[b] + nsrc * T.leaf_count[b];
+    }
+    CK(ctx->near_off.upload(noff));
+    CK(ctx->near.alloc(noff[nleaf]));
+    launch_near_setup(ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p, ctx->near_off.p, nleaf,
+                      ctx->xs_s.p, ctx->ys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k, ctx->near.p, ctx->stream);
+    CK(cudaGetLastError());
+    // values-to-coefficients matrix of the cone interpolant (Interpolator.h:81-120)
+    {
+        const int Ps = T.Ps, Pa = T.Pang;
+        std::vector<double> xs(Ps), xa(Pa);
+        for (int i = 0; i < Ps; ++i) xs[Ps - 1 - i] = std::cos(kPiH * (2.0 * i + 1.0) / (2.0 * Ps));
+        for (int i = 0; i < Pa; ++i) xa[Pa - 1 - i] = std::cos(kPiH * (2.0 * i + 1.0) / (2.0 * Pa));
+        auto Tn = [](int n, double x) { double a = 1.0, b = x; if (n == 0) return a; for (int i = 1; i < n; ++i) { double c = 2.0 * x * b - a; a = b; b = c; } return b; };
+        std::vector<double> G((size_t)P * P);
+        for (int m = 0; m < Ps; ++m)
+            for (int n = 0; n < Pa; ++n)
+                for (int kk = 0; kk < Ps; ++kk)
+                    for (int l = 0; l < Pa; ++l) {
+                        const double am = m == 0 ? 1.0 : 2.0, an = n == 0 ? 1.0 : 2.0;
+                        G[(size_t)(n * Ps + m) * P + (l * Ps + kk)] = Tn(m, xs[kk]) * Tn(n, xa[l]) * (am * an / (Ps * Pa));
+                    }
+        CK(ctx->Gm.upload(G));
+    }
+    // leaf cones
+    const TreeLevel& LD = T.L[Dl];
+    const int ncl = (int)LD.cone_nonrel.size();
+    std::vector<long long> loff(ncl + 1, 0);
+    for (int c = 0; c < ncl; ++c) loff[c + 1] = loff[c] + (long long)P * T.leaf_count[LD.cone_box[c]];
+    {
+        std::vector<double> nx, ny, nir, nii;
+        leaf_nodes(T, nx, ny, nir, nii);
+        std::vector<LeafNode> nodes(nx.size());
+        for (size_t i = 0; i < nx.size(); ++i) nodes[i] = LeafNode{nx[i], ny[i], nir[i], nii[i]};
+        CK(ctx->leaf_nodes_d.upload(nodes));
+    }
+    CK(ctx->leaf_cone_box.upload(LD.cone_box)); CK(ctx->leaf_off.upload(loff));
+    CK(ctx->leafL.alloc(loff[ncl]));
+    launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,
+                      ctx->xs_s.p, ctx->ys_s.p, P, k, ctx->Gm.p, ctx->leafL.p, ctx->stream);
+    CK(cudaGetLastError());
+    // propagation and interpolation plans
+    {
+        std::vector<PropEntryD> pe(T.pp.size());
+        for (size_t i = 0; i < T.pp.size(); ++i) { const PropEntry& e = T.pp[i]; pe[i] = PropEntryD{e.child_cone, 0, e.s, e.th, e.wr, e.wi}; }
+        CK(ctx->pp.upload(pe));
+        CK(ctx->pp_ptr.upload(T.pp_ptr)); CK(ctx->pp_nchild.upload(T.pp_nchild));
+        std::vector<InterpEntryD> ie(T.ip.size());
+        for (size_t i = 0; i < T.ip.size(); ++i) { const InterpEntry& e = T.ip[i]; ie[i] = InterpEntryD{e.cone, 0, e.s, e.th, e.fr, e.fi}; }
+        CK(ctx->ip.upload(ie));
+        CK(ctx->ip_ptr.upload(T.ip_ptr));
+    }
+    CK(ctx->coef.alloc((size_t)T.total_cones * P));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
+    ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
+    ctx->counts[7] = (long long)(ctx->near.n + ctx->leafL.n + ctx->coef.n + ctx->W.n) * 16 + (long long)ctx->pp.n * sizeof(PropEntryD) +
+                     (long long)ctx->ip.n * sizeof(InterpEntryD);
+    ctx->ifgf_ready = true;
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* s) {
+    if (!ctx || !s) return IFGF2D_ERR_ARG;
+    if (!ctx->ifgf_ready) return IFGF2D_ERR_STATE;
+    std::copy(ctx->T.sorting.begin(), ctx->T.sorting.end(), s);
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]) {
+    if (!ctx || !out) return IFGF2D_ERR_ARG;
+    for (int i = 0; i < 8; ++i) out[i] = ctx->counts[i];
+    return IFGF2D_OK;
+}
+
+// ------------------------------------------------------------------ apply
+static int far_ifgf(ifgf2d_ctx* ctx, double2* y) {
+    // y += far field of ctx->rho (Morton-ordered intensities)
+    const Tree& T = ctx->T;
+    const int Dl = ctx->nlevels - 1, P = T.P;
+    const TreeLevel& LD = T.L[Dl];
+    launch_leaf_apply(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                      ctx->leaf_off.p, ctx->leafL.p, ctx->rho.p, P, ctx->coef.p, ctx->stream);
+    for (int l = Dl; l >= 3; --l) {
+        const TreeLevel& Lp = T.L[l - 1];
+        launch_propagate(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, ctx->pp.p,
+                         T.Ps, T.Pang, ctx->Gm.p, ctx->coef.p, ctx->stream);
+    }
+    launch_final((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
+                 ctx->near_off.p, ctx->near.p, ctx->rho.p, ctx->ip_ptr.p, ctx->ip.p, ctx->coef.p, T.Ps, T.Pang,
+                 ctx->sorting.p, y, ctx->stream);
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
+    const Discretisation& D = ctx->D;
+    const int N = (int)D.N;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
+    if (mode == IFGF2D_APPLY_IFGF && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT) return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, ctx->stream);
+    if (mode == IFGF2D_APPLY_IFGF) {
+        launch_intensities(x, ctx->wq.p, ctx->sorting.p, N, ctx->rho.p, ctx->stream);
+        return far_ifgf(ctx, y);
+    }
+    launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
+    launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->patch_of.p,
+                      ctx->rho.p, N, ctx->k, y, 1, ctx->stream);
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]) {
+    if (!ctx || !d_x || !d_y || !ms) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
+    if (mode == IFGF2D_APPLY_IFGF && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT) return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    const double2* x = (const double2*)d_x;
+    double2* y = (double2*)d_y;
+    const Discretisation& D = ctx->D;
+    const int N = (int)D.N;
+    cudaEvent_t ev[6];
+    for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
+    cudaStream_t s = ctx->stream;
+    CK(cudaEventRecord(ev[0], s));
+    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, s);
+    CK(cudaEventRecord(ev[1], s));
+    if (mode == IFGF2D_APPLY_IFGF) {
+        launch_intensities(x, ctx->wq.p, ctx->sorting.p, N, ctx->rho.p, s);
+        CK(cudaEventRecord(ev[2], s));
+        const Tree& T = ctx->T;
+        const int Dl = ctx->nlevels - 1, P = T.P;
+        const TreeLevel& LD = T.L[Dl];
+        launch_leaf_apply(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                          ctx->leaf_off.p, ctx->leafL.p, ctx->rho.p, P, ctx->coef.p, s);
+        CK(cudaEventRecord(ev[3], s));
+        for (int l = Dl; l >= 3; --l) {
+            const TreeLevel& Lp = T.L[l - 1];
+            launch_propagate(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, ctx->pp.p,
+                             T.Ps, T.Pang, ctx->Gm.p, ctx->coef.p, s);
+        }
+        CK(cudaEventRecord(ev[4], s));
+        launch_final(N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
+                     ctx->near_off.p, ctx->near.p, ctx->rho.p, ctx->ip_ptr.p, ctx->ip.p, ctx->coef.p, T.Ps, T.Pang,
+                     ctx->sorting.p, y, s);
+    } else {
+        launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, s);
+        CK(cudaEventRecord(ev[2], s));
+        CK(cudaEventRecord(ev[3], s));
+        CK(cudaEventRecord(ev[4], s));
+        launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->patch_of.p,
+                          ctx->rho.p, N, ctx->k, y, 1, s);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev[5], s));
+    CK(cudaEventSynchronize(ev[5]));
+    for (int i = 0; i < 5; ++i) { float t = 0; CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1])); ms[i] = t; }
+    for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_measure_fp64_peak(double* tflops) {
+    if (!tflops) return IFGF2D_ERR_ARG;
+    return launch_fp64_peak(tflops) ? IFGF2D_OK : IFGF2D_ERR_CUDA;
+}
+
+extern "C" int ifgf2d_apply_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode) {
+    if (!ctx || !d_x || !d_y) return IFGF2D_ERR_ARG;
+    return apply_dev(ctx, (const double2*)d_x, (double2*)d_y, mode);
+}
+
+extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mode) {
+    if (!ctx || !x || !y) return IFGF2D_ERR_ARG;
+    const size_t bytes = sizeof(double2) * ctx->D.N;
+    CK(cudaMemcpyAsync(ctx->vin.p, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, mode);
+    if (rc != IFGF2D_OK) return rc;
+    CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intens, double* y) {
+    if (!ctx || !intens || !y) return IFGF2D_ERR_ARG;
+    if (!ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup first");
+    const size_t bytes = sizeof(double2) * ctx->D.N;
+    CK(cudaMemcpyAsync(ctx->vin.p, intens, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // rho = intensities in Morton order (unit weights)
+    std::vector<double> ones(ctx->D.N, 1.0);
+    DBuf<double> w1; CK(w1.upload(ones));
+    launch_intensities(ctx->vin.p, w1.p, ctx->sorting.p, (int)ctx->D.N, ctx->rho.p, ctx->stream);
+    CK(cudaMemsetAsync(ctx->vout.p, 0, bytes, ctx->stream));
+    int rc = far_ifgf(ctx, ctx->vout.p);
+    if (rc != IFGF2D_OK) return rc;
+    CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return IFGF2D_OK;
+}
+
+// ------------------------------------------------------------------ propagation (off-surface)
+extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp, const double* dens, double* out) {
+    if (!ctx || m < 0 || (m > 0 && (!xp || !yp || !out)) || !dens) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) first: the wavenumber is set there");
+    if (m == 0) return IFGF2D_OK;
+    const int N = (int)ctx->D.N;
+    DBuf<double> tx, ty; DBuf<double2> o;
+    CK(tx.upload(xp, m)); CK(ty.upload(yp, m)); CK(o.alloc(m));
+    CK(cudaMemcpyAsync(ctx->vin.p, dens, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
+    launch_intensities(ctx->vin.p, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
+    launch_direct_far(tx.p, ty.p, (int)m, nullptr, nullptr, nullptr, ctx->x.p, ctx->y.p, nullptr, ctx->rho.p, N, ctx->k, o.p, 0, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, o.p, sizeof(double2) * m, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return IFGF2D_OK;
+}
+
+// ------------------------------------------------------------------ GMRES on the device
+// Arnoldi with classical Gram-Schmidt and one re-orthogonalisation pass (CGS2); the Krylov
+// basis lives on the device; the (restart+1) x restart Hessenberg least-squares problem is
+// reduced with Givens rotations on the host.  Same iterates as the reference's Householder
+// Arnoldi (ForwardMap/opGMRES.hpp:68-269) in exact arithmetic; the stopping test is the same
+// residual estimate |w_k| / ||r_0||.
+namespace {
+struct Giv { std::complex<double> c, s; };
+Giv make_giv(std::complex<double> p, std::complex<double> q) {
+    Giv g;
+    if (q == 0.0) { g.c = p.real() < 0 ? -1.0 : 1.0; g.s = 0.0; return g; }
+    if (p == 0.0) { g.c = 0.0; g.s = -q / std::abs(q); return g; }
+    const double p1 = std::fabs(p.real()) + std::fabs(p.imag()), q1 = std::fabs(q.real()) + std::fabs(q.imag());
+    if (p1 >= q1) {
+        std::complex<double> ps = p / p1, qs = q / p1;
+        const double p2 = std::norm(ps), q2 = std::norm(qs);
+        double u = std::sqrt(1.0 + q2 / p2); if (p.real() < 0) u = -u;
+        g.c = 1.0 / u; g.s = -qs * std::conj(ps) * (g.c.real() / p2);
+    } else {
+        std::complex<double> ps = p / q1, qs = q / q1;
+        const double p2 = std::norm(ps), q2 = std::norm(qs);
+        double u = q1 * std::sqrt(p2 + q2); if (p.real() < 0) u = -u;
+        const double pa = std::abs(p); ps = p / pa;
+        g.c = pa / u; g.s = -std::conj(ps) * (q / u);
+    }
+    return g;
+}
+// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]: G^* [p; q] = [r; 0]
+void rot(const Giv& g, std::complex<double>& x, std::complex<double>& y) {
+    const std::complex<double> nx = std::conj(g.c) * x - std::conj(g.s) * y, ny = g.s * x + g.c * y;
+    x = nx; y = ny;
+}
+}  // namespace
+
+extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, int mode, double tol, int restart, int max_iters,
+                            int* iters_out, double* err_out) {
+    if (!ctx || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
+    const long long N = ctx->D.N;
+    const int m = restart;
+    cudaStream_t s = ctx->stream;
+    DBuf<double2> V, b, x, w, h, t;
+    CK(V.alloc((size_t)N * (m + 1))); CK(b.alloc(N)); CK(x.alloc(N)); CK(w.alloc(N)); CK(h.alloc(m + 2)); CK(t.alloc(N));
+    CK(cudaMemcpyAsync(b.p, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(x.p, 0, sizeof(double2) * N, s));
+    auto dnorm = [&](const double2* v, double& out) -> int {
+        launch_multidot(v, N, 1, v, N, h.p + m + 1, s);
+        double2 r; CK(cudaMemcpyAsync(&r, h.p + m + 1, sizeof(double2), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        out = std::sqrt(std::max(r.x, 0.0));
+        return IFGF2D_OK;
+    };
+    int rc;
+    double bn; if ((rc = dnorm(b.p, bn))) return rc;
+    if (bn <= 2.2250738585072014e-308) {
+        std::fill(xout, xout + 2 * N, 0.0);
+        if (iters_out) *iters_out = 0;
+        if (err_out) *err_out = 0.0;
+        return IFGF2D_OK;
+    }
+    // r0 = b - A x0 with x0 = 0 (the reference applies the operator to the zero guess too)
+    if ((rc = apply_dev(ctx, x.p, t.p, mode))) return rc;
+    launch_sub(b.p, t.p, N, w.p, s);
+    double beta; if ((rc = dnorm(w.p, beta))) return rc;
+    const double r0n = beta;
+    int iters = 0;
+    double est = 1.0;
+    bool done = (beta == 0.0);
+    std::vector<std::complex<double>> H((size_t)(m + 1) * m), g(m + 1), hv(m + 1);
+    std::vector<Giv> G(m);
+    std::vector<double2> hh(m + 1), yv(m);
+    while (!done) {
+        launch_scale(w.p, make_double2(1.0 / beta, 0.0), N, V.p, s);
+        std::fill(H.begin(), H.end(), 0.0); std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        bool stop = false;
+        for (; j < m; ++j) {
+            double2* vj = V.p + (size_t)j * N;
+            if ((rc = apply_dev(ctx, vj, w.p, mode))) return rc;
+            // CGS2
+            std::fill(hv.begin(), hv.end(), 0.0);
+            for (int pass = 0; pass < 2; ++pass) {
+                launch_multidot(V.p, N, j + 1, w.p, N, h.p, s);
+                launch_multi_axpy(V.p, N, j + 1, h.p, -1.0, N, w.p, s);
+                CK(cudaMemcpyAsync(hh.data(), h.p, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                for (int i = 0; i <= j; ++i) hv[i] += std::complex<double>(hh[i].x, hh[i].y);
+            }
+            double hn; if ((rc = dnorm(w.p, hn))) return rc;
+            ++iters;
+            for (int i = 0; i <= j; ++i) H[(size_t)j * (m + 1) + i] = hv[i];
+            H[(size_t)j * (m + 1) + j + 1] = hn;
+            std::complex<double>* col = &H[(size_t)j * (m + 1)];
+            for (int i = 0; i < j; ++i) rot(G[i], col[i], col[i + 1]);
+            if (col[j + 1] != 0.0) {
+                G[j] = make_giv(col[j], col[j + 1]);
+                rot(G[j], col[j], col[j + 1]);
+                rot(G[j], g[j], g[j + 1]);
+            } else {
+                G[j] = Giv{1.0, 0.0};
+            }
+            est = std::abs(g[j + 1]) / r0n;
+            stop = (iters >= N || est < tol || iters >= max_iters || hn == 0.0);
+            if (stop) { ++j; break; }
+            if (j + 1 < m) launch_scale(w.p, make_double2(1.0 / hn, 0.0), N, V.p + (size_t)(j + 1) * N, s);
+        }
+        if (j > m) j = m;
+        // y = R^{-1} g, x += V y
+        std::vector<std::complex<double>> y(j);
+        for (int i = j - 1; i >= 0; --i) {
+            std::complex<double> acc = g[i];
+            for (int q = i + 1; q < j; ++q) acc -= H[(size_t)q * (m + 1) + i] * y[q];
+            y[i] = acc / H[(size_t)i * (m + 1) + i];
+        }
+        for (int i = 0; i < j; ++i) yv[i] = make_double2(y[i].real(), y[i].imag());
+        CK(cudaMemcpyAsync(h.p, yv.data(), sizeof(double2) * j, cudaMemcpyHostToDevice, s));
+        launch_multi_axpy(V.p, N, j, h.p, 1.0, N, x.p, s);
+        if (stop) break;
+        // restart: r = b - A x
+        if ((rc = apply_dev(ctx, x.p, t.p, mode))) return rc;
+        launch_sub(b.p, t.p, N, w.p, s);
+        if ((rc = dnorm(w.p, beta))) return rc;
+        if (beta == 0.0) break;
+    }
+    CK(cudaMemcpyAsync(xout, x.p, sizeof(double2) * N, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (iters_out) *iters_out = iters;
+    if (err_out) *err_out = est;
+    return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}
+
+// ------------------------------------------------------------------ Hankel test entry
+extern "C" int ifgf2d_hankel(int order, long long n, const double* x, double* out) {
+    if (order < 0 || order > 1 || n < 0 || (n > 0 && (!x || !out))) return IFGF2D_ERR_ARG;
+    if (n == 0) return IFGF2D_OK;
+    if (n > (1LL << 30)) return IFGF2D_ERR_ARG;
+    DBuf<double> dx; DBuf<double2> dout;
+    if (dx.upload(x, n) != cudaSuccess || dout.alloc(n) != cudaSuccess) return IFGF2D_ERR_CUDA;
+    launch_hankel(order, dx.p, (int)n, dout.p, 0);
+    if (cudaGetLastError() != cudaSuccess) return IFGF2D_ERR_CUDA;
+    if (cudaMemcpy(out, dout.p, sizeof(double2) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return IFGF2D_ERR_CUDA;
+    return IFGF2D_OK;
+}

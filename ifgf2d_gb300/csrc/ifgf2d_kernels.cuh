@@ -1,0 +1,79 @@
+// ifgf2d_kernels.cuh -- device data layouts and kernel launchers of the forward map.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace ifgf {
+
+// Curve on the device (twin of HostCurve, Geometry/Curve.hpp:106-161)
+struct DevCurve {
+    int type;
+    int pad;
+    double p[16];
+};
+
+// One rectangular-polar column: a target point (singular or near-singular) on a patch
+struct RPColumn {
+    int patch;
+    int pad;
+    double tsing, xs, ys;
+};
+
+struct DevPatch {
+    double t1, t2;
+    int curve, ist1, ist2, pad;
+};
+
+// Leaf cone interpolation node: position and 1/(e^{ikr}/sqrt r) at the node radius
+struct LeafNode {
+    double x, y;
+    double ir, ii;
+};
+
+struct InterpEntryD { int cone; int pad; double s, th, fr, fi; };
+struct PropEntryD { int child_cone; int pad; double s, th, wr, wi; };
+
+constexpr int kMaxP = 64;          // Ps * Pang limit of the device interpolator
+
+// ---------------- setup kernels ----------------
+void launch_rp_precompute(const RPColumn* cols, int ncols, const DevPatch* patches, const DevCurve* curves,
+                          const double* ns_nodes, const double* ns_weights, int Np, double p, double k,
+                          double2* M, cudaStream_t s);
+void launch_rp_fold(const double2* M, const RPColumn* cols, int ncols, const double* edge_jac, const DevPatch* patches,
+                    int Np, double2* W, cudaStream_t s);
+void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* nbr_ptr, const int* nbr_box,
+                       const long long* near_off, int nleaf, const double* xs, const double* ys,
+                       const int* patch_s, const int* nsp_ptr, const int* nsp, double k, double2* near,
+                       cudaStream_t s);
+void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count,
+                       const long long* leaf_off, const LeafNode* nodes, const double* xs, const double* ys, int P,
+                       double k, const double* Gm, double2* L, cudaStream_t s);
+
+// ---------------- per-apply kernels ----------------
+void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col,
+                       const RPColumn* cols, int N, int Np, double2* y, cudaStream_t s);
+void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s);
+void launch_direct_far(const double* tx, const double* ty, int ntarget, const int* t_patch, const int* t_nsp_ptr,
+                       const int* t_nsp, const double* sx, const double* sy, const int* s_patch,
+                       const double2* rho, int nsource, double k, double2* y, int accumulate, cudaStream_t s);
+void launch_leaf_apply(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                       const long long* leaf_off, const double2* L, const double2* rho, int P, double2* coef,
+                       cudaStream_t s);
+void launch_propagate(int parent_begin, int parent_end, const long long* pp_ptr, const int* pp_nchild,
+                      const PropEntryD* pp, int Ps, int Pang, const double* Gm, double2* coef, cudaStream_t s);
+void launch_final(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
+                  const int* nbr_box, const long long* near_off, const double2* near, const double2* rho,
+                  const int* ip_ptr, const InterpEntryD* ip, const double2* coef, int Ps, int Pang,
+                  const long long* sorting, double2* y, cudaStream_t s);
+
+// ---------------- tests / GMRES helpers ----------------
+void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s);
+void launch_multidot(const double2* V, long long ldv, int ncols, const double2* w, long long n, double2* h, cudaStream_t s);
+void launch_multi_axpy(const double2* V, long long ldv, int ncols, const double2* h, double sign, long long n, double2* w, cudaStream_t s);
+void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaStream_t s);
+void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s);
+void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream_t s);
+// FP64 FMA throughput (TFLOP/s) of the current device; false on a CUDA error
+bool launch_fp64_peak(double* tflops);
+
+}  // namespace ifgf

@@ -1,0 +1,403 @@
+// tree.cpp -- host build of the flattened IFGF tree (see tree.hpp).
+#include "tree.hpp"
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <unordered_map>
+#include <array>
+
+namespace ifgf {
+
+static constexpr double kPiT = 3.14159265358979323846;
+
+// ---------------------------------------------------------------- Morton codes (Level.h:172-245)
+static inline uint64_t spread_bits(uint64_t x) {
+    x &= 0xFFFFFFFFull;
+    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+static inline uint64_t gather_bits(uint64_t x) {
+    x &= 0x5555555555555555ull;
+    x = (x ^ (x >> 1)) & 0x3333333333333333ull;
+    x = (x ^ (x >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x ^ (x >> 4)) & 0x00FF00FF00FF00FFull;
+    x = (x ^ (x >> 8)) & 0x0000FFFF0000FFFFull;
+    x = (x ^ (x >> 16)) & 0xFFFFFFFFull;
+    return x;
+}
+static inline long long morton_of(long long bx, long long by) { return (long long)(spread_bits((uint64_t)bx) | (spread_bits((uint64_t)by) << 1)); }
+static inline void box_of(long long m, long long& bx, long long& by) { bx = (long long)gather_bits((uint64_t)m); by = (long long)gather_bits((uint64_t)m >> 1); }
+
+long long point_morton(double x, double y, double min_x, double min_y, double boxsize, int level) {
+    const long long px = (long long)((x - min_x) / boxsize), py = (long long)((y - min_y) / boxsize);
+    if (px < 0 || py < 0 || px >= (1LL << level) || py >= (1LL << level)) return -1;
+    return morton_of(px, py);
+}
+
+void tree_root_box(const std::vector<double>& x, const std::vector<double>& y, double& min_x, double& min_y, double& size) {
+    double x0 = 1e308, y0 = 1e308, x1 = -1e308, y1 = -1e308;
+    for (size_t i = 0; i < x.size(); ++i) { x0 = std::min(x0, x[i]); y0 = std::min(y0, y[i]); x1 = std::max(x1, x[i]); y1 = std::max(y1, y[i]); }
+    x1 += 1e-10; y1 += 1e-10; x0 -= 1e-10; y0 -= 1e-10;   // BoxTree.h:196-200
+    min_x = x0; min_y = y0; size = std::max(x1 - x0, y1 - y0);
+}
+
+int TreeLevel::find_box(long long m) const {
+    auto it = std::lower_bound(boxes.begin(), boxes.end(), m);
+    return (it != boxes.end() && *it == m) ? (int)(it - boxes.begin()) : -1;
+}
+int TreeLevel::find_cone(int b, long long nonrel) const {
+    auto first = cone_nonrel.begin() + cone_ptr[b], last = cone_nonrel.begin() + cone_ptr[b + 1];
+    auto it = std::lower_bound(first, last, nonrel);
+    return (it != last && *it == nonrel) ? (int)(it - cone_nonrel.begin()) : -1;
+}
+
+// ---------------------------------------------------------------- per-level geometry
+namespace {
+struct LevelGeo {
+    const TreeLevel* L; double min_x, min_y;
+    void center(long long m, double& cx, double& cy) const {   // Level.h:291-298
+        long long bx, by; box_of(m, bx, by);
+        cx = min_x + bx * L->boxsize + 0.5 * L->boxsize;
+        cy = min_y + by * L->boxsize + 0.5 * L->boxsize;
+    }
+    static double atan_0_2pi(double y, double x) {             // PolarCoordinates.h:8-27
+        if (x > 0 && y >= 0) return std::atan(y / x);
+        if (x > 0 && y < 0) return std::atan(y / x) + 2.0 * kPiT;
+        if (x < 0 && y > 0) return std::atan(y / x) + kPiT;
+        if (x < 0 && y == 0) return kPiT;
+        if (x < 0 && y < 0) return std::atan(y / x) + kPiT;
+        if (x == 0 && y > 0) return kPiT / 2;
+        if (x == 0 && y < 0) return 3.0 * kPiT / 2;
+        return 0;
+    }
+    static void to_polar(double& x, double& y) {
+        const double r = std::sqrt(x * x + y * y);
+        if (r == 0.0) { x = 0.0; y = 0.0; return; }
+        const double th = atan_0_2pi(y, x);
+        x = r; y = th;
+    }
+    long long rpos(double r) const {
+        return (long long)(std::upper_bound(L->radial.begin(), L->radial.end(), r) - L->radial.begin()) - 1;
+    }
+    long long nonrel_of(long long m, double x, double y) const {   // Level.h:310-323
+        double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
+        return (long long)(y * L->ntheta / kPiT) * L->nrad + rpos(x);
+    }
+    double cheb_to_radius(long long pr, double s) const {          // Level.h:347-356
+        const double rmin = L->scaling_r2s / L->radial[pr + 1];
+        const double dr = L->scaling_r2s / L->radial[pr] - rmin;
+        return L->scaling_r2s / ((s + 1.0) / 2.0 * dr + rmin);
+    }
+    double radius_to_cheb(long long pr, double r) const {          // Level.h:413-422
+        const double rmin = L->scaling_r2s / L->radial[pr + 1];
+        const double dr = L->scaling_r2s / L->radial[pr] - rmin;
+        return (L->scaling_r2s / r - rmin) / dr * 2.0 - 1.0;
+    }
+    void cheb_to_cart(long long m, long long nonrel, double& x, double& y) const {   // Level.h:358-375
+        const long long pr = nonrel % L->nrad, pt = nonrel / L->nrad;
+        const double da = kPiT / L->ntheta;
+        const double r = cheb_to_radius(pr, x);
+        const double th = (y + 1.0) / 2.0 * da + da * pt;
+        double cx, cy; center(m, cx, cy);
+        x = r * std::cos(th) + cx; y = r * std::sin(th) + cy;
+    }
+    void cart_to_cheb(long long m, long long nonrel, double& x, double& y) const {   // Level.h:424-437
+        double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
+        const long long pr = nonrel % L->nrad, pt = nonrel / L->nrad;
+        const double da = kPiT / L->ntheta;
+        x = radius_to_cheb(pr, x);
+        y = (y - da * pt) / da * 2.0 - 1.0;
+    }
+    long long cart_to_cheb_cone(long long m, double& x, double& y) const {            // Level.h:439-453
+        double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
+        const long long pr = rpos(x), pt = (long long)(y * L->ntheta / kPiT);
+        const double da = kPiT / L->ntheta;
+        x = radius_to_cheb(pr, x);
+        y = (y - da * pt) / da * 2.0 - 1.0;
+        return pt * L->nrad + pr;
+    }
+};
+
+// Level.h:88-142 (Helmholtz cone refinement)
+void init_cones(TreeLevel& L, double k) {
+    const double minsize = (3.0 / 2.0 * L.boxsize) * (1.0 - 1e-10);
+    const double maxsize = (std::sqrt(2.0) * L.boxsize * L.nside - std::sqrt(2.0) / 2.0 * L.boxsize) * (1.0 + 1e-10);
+    long long scal = 1;
+    if (L.level > 1) scal = std::max<long long>(1, (long long)std::ceil(k * L.boxsize * (1.0 / kPiT) * 1.2));
+    L.ntheta = 2 * scal;
+    L.scaling_r2s = std::sqrt(2.0) / 2.0 * L.boxsize;
+    const double eta = std::sqrt(2.0) / 3.0 - 1e-5;
+    const double span = maxsize - minsize + 1e-10;
+    const double ds = std::min(eta / scal, L.scaling_r2s * (1.0 / minsize - 1.0 / (minsize + span)));
+    const long long n = (long long)std::ceil(L.scaling_r2s * (1.0 / minsize - 1.0 / maxsize) / ds);
+    L.radial.assign(n + 1, 0.0);
+    L.radial[0] = minsize;
+    const double step = L.scaling_r2s * (1.0 / minsize - 1.0 / maxsize) / n;
+    for (long long i = n - 1; i >= 0; --i) L.radial[n - i] = L.scaling_r2s * maxsize / (L.scaling_r2s + maxsize * i * step);
+    L.nrad = n;
+}
+
+// relevant boxes of `L` within the even-aligned 6x6 block around m, minus the 3x3 (Level.h:261-289)
+void cousins_of(const TreeLevel& L, long long m, std::vector<int>& out) {
+    out.clear();
+    long long bx, by; box_of(m, bx, by);
+    const long long ex = (bx / 2) * 2, ey = (by / 2) * 2;
+    const long long x0 = std::max<long long>(ex - 2, 0), x1 = std::min<long long>(L.nside - 1, ex + 3);
+    const long long y0 = std::max<long long>(ey - 2, 0), y1 = std::min<long long>(L.nside - 1, ey + 3);
+    std::vector<std::pair<long long, int>> tmp;
+    for (long long j = y0; j <= y1; ++j)
+        for (long long i = x0; i <= x1; ++i)
+            if (std::llabs(i - bx) > 1 || std::llabs(j - by) > 1) {
+                const long long cm = morton_of(i, j);
+                const int b = L.find_box(cm);
+                if (b >= 0) tmp.push_back({cm, b});
+            }
+    std::sort(tmp.begin(), tmp.end());
+    for (auto& t : tmp) out.push_back(t.second);
+}
+}  // namespace
+
+// ---------------------------------------------------------------- build
+std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
+                       int Ps, int Pang, Tree& T) {
+    if (nlevels < 3) return "IFGF accelerator requires at least 3 levels.";
+    if (nlevels > 24) return "nlevels too large";
+    T = Tree();
+    T.nlevels = nlevels; T.k = k; T.Ps = Ps; T.Pang = Pang; T.P = Ps * Pang; T.N = (long long)x.size();
+    const long long N = T.N;
+    const int D = nlevels - 1;
+    tree_root_box(x, y, T.min_x, T.min_y, T.boxsize0);
+    // Morton sort at the leaf level (stable), BoxTree.h:73-106
+    std::vector<long long> code(N);
+    const double leaf_size = T.boxsize0 / (double)(1LL << D);
+    for (long long i = 0; i < N; ++i) {
+        code[i] = point_morton(x[i], y[i], T.min_x, T.min_y, leaf_size, D);
+        if (code[i] < 0) return "The 2D box index cannot be < 0 or larger than the number of boxes";
+    }
+    T.sorting.resize(N);
+    std::iota(T.sorting.begin(), T.sorting.end(), 0LL);
+    std::stable_sort(T.sorting.begin(), T.sorting.end(), [&](long long a, long long b) { return code[a] < code[b]; });
+    T.inverse.resize(N);
+    T.xs.resize(N); T.ys.resize(N);
+    std::vector<long long> scode(N);
+    for (long long i = 0; i < N; ++i) {
+        T.inverse[T.sorting[i]] = i;
+        T.xs[i] = x[T.sorting[i]]; T.ys[i] = y[T.sorting[i]]; scode[i] = code[T.sorting[i]];
+    }
+    // levels, relevant boxes (BoxTree.h:111-174, 205-231)
+    T.L.resize(nlevels);
+    for (int l = 1; l < nlevels; ++l) {
+        TreeLevel& L = T.L[l];
+        L.level = l; L.nside = 1LL << l; L.boxsize = T.boxsize0 / (double)(1LL << l);
+        init_cones(L, k);
+    }
+    {
+        TreeLevel& LD = T.L[D];
+        for (long long i = 0; i < N; ++i) {
+            if (i == 0 || scode[i] != scode[i - 1]) {
+                LD.boxes.push_back(scode[i]);
+                T.leaf_start.push_back((int)i);
+                T.leaf_count.push_back(0);
+            }
+            T.leaf_count.back()++;
+            T.point_leaf.push_back((int)LD.boxes.size() - 1);
+        }
+        for (int l = D - 1; l >= 2; --l) {
+            std::vector<long long>& b = T.L[l].boxes;
+            for (long long m : T.L[l + 1].boxes) b.push_back(m / 4);
+            b.erase(std::unique(b.begin(), b.end()), b.end());   // parents of a sorted list stay sorted
+        }
+    }
+    // leaf neighbours (Level.h:378-404)
+    {
+        const TreeLevel& LD = T.L[D];
+        T.nbr_ptr.assign(LD.boxes.size() + 1, 0);
+        for (size_t b = 0; b < LD.boxes.size(); ++b) {
+            long long bx, by; box_of(LD.boxes[b], bx, by);
+            std::vector<std::pair<long long, int>> nb;
+            for (long long j = std::max<long long>(0, by - 1); j <= std::min<long long>(LD.nside - 1, by + 1); ++j)
+                for (long long i = std::max<long long>(0, bx - 1); i <= std::min<long long>(LD.nside - 1, bx + 1); ++i) {
+                    const long long m = morton_of(i, j);
+                    const int q = LD.find_box(m);
+                    if (q >= 0) nb.push_back({m, q});
+                }
+            std::sort(nb.begin(), nb.end());
+            for (auto& e : nb) T.nbr_box.push_back(e.second);
+            T.nbr_ptr[b + 1] = (int)T.nbr_box.size();
+            long long nsrc = 0;
+            for (auto& e : nb) nsrc += T.leaf_count[e.second];
+            T.near_pairs += nsrc * T.leaf_count[b];
+        }
+    }
+    // Chebyshev nodes of the cone interpolant (ascending, Chebyshev.h:10-24); GetInterpolationPoint
+    std::vector<double> ns(Ps), na(Pang);
+    for (int i = 0; i < Ps; ++i) ns[Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Ps));
+    for (int i = 0; i < Pang; ++i) na[Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Pang));
+    const int P = T.P;
+
+    // relevant cones, level by level (BoxTree.h:553-583)
+    std::vector<int> cous;
+    for (int l = 2; l < nlevels; ++l) {
+        TreeLevel& L = T.L[l];
+        LevelGeo G{&L, T.min_x, T.min_y};
+        std::vector<std::pair<int, long long>> want;   // (box index, nonrel cone)
+        // cones seen by the cousins' points (BoxTree.h:235-277)
+        long long old = -1;
+        const int shift = 2 * (D - l);
+        for (long long i = 0; i < N; ++i) {
+            const long long m = scode[i] >> shift;
+            if (m != old) { cousins_of(L, m, cous); old = m; }
+            for (int c : cous) want.push_back({c, G.nonrel_of(L.boxes[c], T.xs[i], T.ys[i])});
+        }
+        // cones needed by the parents' interpolation nodes, through the protobox routing
+        // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
+        // routing is computed once, from the first parent box (in cone order) that has it.
+        if (l > 2) {
+            const TreeLevel& Lp = T.L[l - 1];
+            LevelGeo Gp{&Lp, T.min_x, T.min_y};
+            std::unordered_map<long long, std::array<std::vector<std::pair<long long, int>>, 4>> proto;  // nonrel -> pos -> (child nonrel, node)
+            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
+                const int pb = Lp.cone_box[pc];
+                const long long pm = Lp.boxes[pb], pnc = Lp.cone_nonrel[pc];
+                auto& entry = proto[pnc];
+                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
+                    const int cb = L.find_box(cm);
+                    if (cb < 0) continue;
+                    auto& v = entry[cm % 4];
+                    if (!v.empty()) continue;
+                    for (int it = 0; it < P; ++it) {
+                        double px = ns[it % Ps], py = na[it / Ps];
+                        Gp.cheb_to_cart(pm, pnc, px, py);
+                        v.push_back({G.nonrel_of(cm, px, py), it});
+                    }
+                }
+            }
+            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
+                const long long pm = Lp.boxes[Lp.cone_box[pc]];
+                const auto& entry = proto.at(Lp.cone_nonrel[pc]);
+                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
+                    const int cb = L.find_box(cm);
+                    if (cb < 0) continue;
+                    for (auto& e : entry[cm % 4]) want.push_back({cb, e.first});
+                }
+            }
+            // merged cone list first (sorted by box, then nonrel cone), then the plan,
+            // which needs the child cone ids
+            std::sort(want.begin(), want.end());
+            want.erase(std::unique(want.begin(), want.end()), want.end());
+            if (want.empty()) return "The number of cone segments on any level cannot be 0";
+            L.cone_ptr.assign(L.boxes.size() + 1, 0);
+            for (auto& w : want) { L.cone_box.push_back(w.first); L.cone_nonrel.push_back(w.second); L.cone_ptr[w.first + 1]++; }
+            for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
+            L.cone_base = T.total_cones;
+            T.total_cones += (int)L.cone_nonrel.size();
+            // propagation plan of this level: parents are the cones of level l-1
+            if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
+            // parent cones of level l-1 get their entries in global-id order; levels are
+            // built upwards, so level l-1's entries are appended now (its id range is final)
+            const int pbase = Lp.cone_base;
+            if ((long long)T.pp_ptr.size() - 1 != pbase) return "internal: propagation plan out of order";
+            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
+                const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
+                const auto& entry = proto.at(pnc);
+                int nch = 0;
+                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
+                    const int cb = L.find_box(cm);
+                    if (cb < 0) continue;
+                    ++nch;
+                    std::vector<PropEntry> slot(P);
+                    for (auto& e : entry[cm % 4]) {
+                        const int it = e.second;
+                        double px = ns[it % Ps], py = na[it / Ps];
+                        const double rp = Gp.cheb_to_radius(pnc % Lp.nrad, px);
+                        Gp.cheb_to_cart(pm, pnc, px, py);
+                        double lx = px, ly = py;
+                        G.cart_to_cheb(cm, e.first, lx, ly);
+                        const double rc = G.cheb_to_radius(e.first % L.nrad, lx);
+                        const int cc = L.find_cone(cb, e.first);
+                        if (cc < 0) return "internal: child cone missing";
+                        const std::complex<double> fc = std::complex<double>(std::cos(k * rc), std::sin(k * rc)) / std::sqrt(rc);
+                        const std::complex<double> fp = std::complex<double>(std::cos(k * rp), std::sin(k * rp)) / std::sqrt(rp);
+                        const std::complex<double> w = fc / fp;
+                        slot[it] = PropEntry{L.cone_base + cc, it, lx, ly, w.real(), w.imag()};
+                    }
+                    T.pp.insert(T.pp.end(), slot.begin(), slot.end());
+                }
+                T.pp_nchild.push_back(nch);
+                T.pp_ptr.push_back((long long)T.pp.size());
+                T.prop_evals += (long long)nch * P;
+            }
+            continue;
+        }
+        std::sort(want.begin(), want.end());
+        want.erase(std::unique(want.begin(), want.end()), want.end());
+        if (want.empty()) return "The number of cone segments on any level cannot be 0";
+        L.cone_ptr.assign(L.boxes.size() + 1, 0);
+        for (auto& w : want) { L.cone_box.push_back(w.first); L.cone_nonrel.push_back(w.second); L.cone_ptr[w.first + 1]++; }
+        for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
+        L.cone_base = T.total_cones;
+        T.total_cones += (int)L.cone_nonrel.size();
+    }
+    // leaf-level cones have no children: close the propagation CSR for them
+    if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
+    while ((long long)T.pp_ptr.size() - 1 < T.total_cones) { T.pp_ptr.push_back((long long)T.pp.size()); T.pp_nchild.push_back(0); }
+    for (size_t c = 0; c < T.L[D].cone_nonrel.size(); ++c) T.leaf_evals += (long long)P * T.leaf_count[T.L[D].cone_box[c]];
+
+    // interpolation plan (BoxTree.h:876-937): per sorted target, all levels, all cousins
+    T.ip_ptr.assign(N + 1, 0);
+    {
+        std::vector<std::vector<InterpEntry>> per(N);
+        for (int l = D; l >= 2; --l) {   // the reference interpolates level D first (BoxTree.h:1049-1061)
+            const TreeLevel& L = T.L[l];
+            LevelGeo G{&L, T.min_x, T.min_y};
+            const int shift = 2 * (D - l);
+            long long old = -1;
+            for (long long i = 0; i < N; ++i) {
+                const long long m = scode[i] >> shift;
+                if (m != old) { cousins_of(L, m, cous); old = m; }
+                for (int c : cous) {
+                    double lx = T.xs[i], ly = T.ys[i];
+                    const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
+                    const int cc = L.find_cone(c, nonrel);
+                    if (cc < 0) return "internal: interpolation cone missing";
+                    const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
+                    const double sr = std::sqrt(r);
+                    per[i].push_back(InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(k * r) / sr, std::sin(k * r) / sr});
+                }
+            }
+        }
+        for (long long i = 0; i < N; ++i) T.ip_ptr[i + 1] = T.ip_ptr[i] + (int)per[i].size();
+        T.ip.reserve(T.ip_ptr[N]);
+        for (long long i = 0; i < N; ++i) T.ip.insert(T.ip.end(), per[i].begin(), per[i].end());
+        T.interp_evals = T.ip_ptr[N];
+    }
+    return "";
+}
+
+void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, std::vector<double>& ir, std::vector<double>& ii) {
+    const int D = T.nlevels - 1;
+    const TreeLevel& L = T.L[D];
+    LevelGeo G{&L, T.min_x, T.min_y};
+    std::vector<double> ns(T.Ps), na(T.Pang);
+    for (int i = 0; i < T.Ps; ++i) ns[T.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * T.Ps));
+    for (int i = 0; i < T.Pang; ++i) na[T.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * T.Pang));
+    const size_t n = L.cone_nonrel.size() * T.P;
+    x.resize(n); y.resize(n); ir.resize(n); ii.resize(n);
+    for (size_t c = 0; c < L.cone_nonrel.size(); ++c) {
+        const long long m = L.boxes[L.cone_box[c]], nonrel = L.cone_nonrel[c];
+        for (int it = 0; it < T.P; ++it) {
+            double px = ns[it % T.Ps], py = na[it / T.Ps];
+            const double r = G.cheb_to_radius(nonrel % L.nrad, px);
+            G.cheb_to_cart(m, nonrel, px, py);
+            const std::complex<double> f = std::complex<double>(std::cos(T.k * r), std::sin(T.k * r)) / std::sqrt(r);
+            const std::complex<double> inv = 1.0 / f;
+            x[c * T.P + it] = px; y[c * T.P + it] = py; ir[c * T.P + it] = inv.real(); ii[c * T.P + it] = inv.imag();
+        }
+    }
+}
+
+}  // namespace ifgf

@@ -1,0 +1,89 @@
+// tree.hpp -- host build of the IFGF box tree, flattened for the device.
+//
+// Reproduces the tree of IFGF_Source/BoxTree.h + Level.h (Morton sort, relevant boxes,
+// cone segments, cousin/neighbour rules, protobox routing) and turns it into plain arrays:
+//   * points in Morton order (BoxTree.h:73-106), leaf boxes as contiguous point ranges;
+//   * all relevant cones of all levels numbered globally (one coefficient buffer);
+//   * an interpolation plan: per target point, its (cone, s, theta, e^{ikr}/sqrt r) entries
+//     over all levels and cousins (BoxTree.h:876-937);
+//   * a propagation plan: per parent cone, per child and interpolation node, the child cone,
+//     its Chebyshev coordinates and the factor ratio (BoxTree.h:767-868);
+//   * per leaf box, the neighbour ranges of the near field (BoxTree.h:614-683).
+#pragma once
+
+#include <vector>
+#include <string>
+#include <cstdint>
+#include <complex>
+
+namespace ifgf {
+
+struct TreeLevel {
+    int level = 0;
+    double boxsize = 0.0;
+    long long nside = 0;
+    double scaling_r2s = 0.0;
+    long long ntheta = 0, nrad = 0;
+    std::vector<double> radial;            // nrad + 1 radial interval ends (Level.h:131-140)
+    std::vector<long long> boxes;          // relevant boxes, ascending Morton codes
+    std::vector<int> cone_ptr;             // per box: its cones [cone_ptr[b], cone_ptr[b+1])
+    std::vector<long long> cone_nonrel;    // per cone (local numbering)
+    std::vector<int> cone_box;             // per cone: box index
+    int cone_base = 0;                     // global id of this level's first cone
+
+    int find_box(long long morton) const;
+    int find_cone(int box, long long nonrel) const;   // local cone id or -1
+};
+
+struct InterpEntry {   // one (target, level, cousin) term of the interpolation
+    int cone;          // global cone id
+    int pad;
+    double s, th;      // Chebyshev coordinates in the cousin's cone
+    double fr, fi;     // e^{ikr}/sqrt(r)
+};
+
+struct PropEntry {     // one (parent cone, child, node) term of the propagation
+    int child_cone;    // global cone id at the child level
+    int pad;
+    double s, th;      // Chebyshev coordinates of the parent node in the child cone
+    double wr, wi;     // e^{ik r_child}/sqrt(r_child) / (e^{ik r_parent}/sqrt(r_parent))
+};
+
+struct Tree {
+    int nlevels = 0, Ps = 5, Pang = 5, P = 25;
+    long long N = 0;
+    double k = 0.0;
+    double min_x = 0, min_y = 0, boxsize0 = 0;
+    std::vector<long long> sorting, inverse;   // sorted position -> original index, and back
+    std::vector<double> xs, ys;                // Morton-sorted coordinates
+    std::vector<TreeLevel> L;                  // index = level; 0 and 1 unused
+    // leaf boxes (level D = nlevels-1)
+    std::vector<int> leaf_start, leaf_count, point_leaf;
+    std::vector<int> nbr_ptr, nbr_box;         // per leaf box: neighbour leaf boxes (<= 9)
+    int total_cones = 0;
+    // interpolation plan (CSR over sorted target points)
+    std::vector<int> ip_ptr;
+    std::vector<InterpEntry> ip;
+    // propagation plan: for each level l in [3, D] the parent cones are those of level l-1;
+    // CSR over parent global cone ids: pp_ptr[c] .. pp_ptr[c+1], grouped by child then node
+    std::vector<long long> pp_ptr;
+    std::vector<PropEntry> pp;
+    std::vector<int> pp_nchild;                // per parent cone: number of relevant children
+    long long prop_evals = 0, interp_evals = 0, leaf_evals = 0, near_pairs = 0;
+};
+
+// Build the tree for the given points (original order).  Returns "" or an error message.
+std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
+                       int Ps, int Pang, Tree& T);
+
+// Morton code of (x, y) at `level` for a root box [min_x, min_x + size] (Level.h:145-161);
+// returns -1 when the point is outside.
+long long point_morton(double x, double y, double min_x, double min_y, double boxsize, int level);
+void tree_root_box(const std::vector<double>& x, const std::vector<double>& y, double& min_x, double& min_y, double& size);
+
+// Leaf-cone interpolation nodes (BoxTree.h:714-745): per leaf cone and node, the Cartesian
+// position and 1/(e^{ikr}/sqrt r) at the node radius.  Arrays of size ncones_leaf * P.
+void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, std::vector<double>& ir,
+                std::vector<double>& ii);
+
+}  // namespace ifgf

@@ -1,0 +1,141 @@
+/* ifgf2d.h -- C ABI of the GB300 IFGF2D forward map (libifgf2d.so).
+ *
+ * Drop-in boundary for the matvec that GMRES calls in IFGF2D: the reference's
+ * ForwardMap<Np, SingleLayer, Ps, Pang> / LinearOperator / opGMRES path.  Plain pointers
+ * and sizes only; complex vectors are interleaved (re, im) doubles, i.e. the memory layout
+ * of std::complex<double> / Eigen::VectorXcd.  Every call returns an int status (IFGF2D_OK
+ * or an IFGF2D_ERR_* code) and never throws; ifgf2d_last_error() gives the message.
+ * Calls on one context are serialised on the context's own CUDA stream; distinct contexts
+ * are independent.  Reference citations are paths inside the IFGF2D repository.
+ */
+#ifndef IFGF2D_H
+#define IFGF2D_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* curve types (Geometry/Curve.hpp:106-161; STAR is an extension) */
+#define IFGF2D_CURVE_CIRCLE 0 /* params: cx, cy, r */
+#define IFGF2D_CURVE_KITE 1   /* params: A, B, C, D: x = A cos t + B cos 2t + C, y = D sin t */
+#define IFGF2D_CURVE_LINE 2   /* params: x1, y1, x2, y2 on t in [-1, 1] (open) */
+#define IFGF2D_CURVE_STAR 3   /* params: cx, cy, M, a_1..a_M, b_1..b_M (M <= 6) */
+
+/* status codes */
+#define IFGF2D_OK 0
+#define IFGF2D_ERR_ARG 1          /* bad argument (size, pointer, option) */
+#define IFGF2D_ERR_GEOMETRY 2     /* point outside the tree box, empty curve, ... */
+#define IFGF2D_ERR_NEIGHBORHOOD 3 /* singular/near-singular point outside the leaf neighbourhood */
+#define IFGF2D_ERR_NLEVELS 4      /* nlevels < 3 or too deep */
+#define IFGF2D_ERR_CUDA 5         /* CUDA runtime error (message in ifgf2d_last_error) */
+#define IFGF2D_ERR_STATE 6        /* call out of order (apply before setup, ...) */
+#define IFGF2D_ERR_NONFINITE 7    /* non-finite value in an output */
+#define IFGF2D_ERR_NOCONV 8       /* GMRES did not reach the tolerance */
+
+/* apply modes */
+#define IFGF2D_APPLY_DIRECT 0 /* ForwardMap::compute_Ax_unacc  (ForwardMap/ForwardMap.tpp:517-540) */
+#define IFGF2D_APPLY_IFGF 1   /* ForwardMap::compute_Ax_acc    (ForwardMap/ForwardMap.tpp:609-655) */
+
+typedef struct ifgf2d_curve {
+    int type;        /* IFGF2D_CURVE_* */
+    int closed;      /* Curve::is_closed */
+    double tlim1;    /* Curve::tlim1 */
+    double tlim2;    /* Curve::tlim2 */
+    double params[16];
+} ifgf2d_curve;
+
+/* Junction (Geometry/Curve.hpp:10-17): curve `curve` touches `touching_curve` */
+typedef struct ifgf2d_junction {
+    int curve;
+    int touching_curve;
+    int t1_touches_t1;
+} ifgf2d_junction;
+
+/* ForwardMap template and constructor parameters (ForwardMap/ForwardMap.hpp:49, 94-97) */
+typedef struct ifgf2d_options {
+    int Np;                        /* points per patch (template Np) */
+    double delta;                  /* rectangular-polar near-singularity distance */
+    double wavelengths_per_patch;  /* patch size rule (Curve.cpp:37-68) */
+    double patch_split_wavenumber; /* wavenumber of the patch size rule */
+    double p;                      /* change-of-variables order (default 4) */
+    int patches_per_curve;         /* > 0: equal-parameter split instead (extension) */
+    int Ps;                        /* IFGF radial Chebyshev nodes (template Ps, default 5) */
+    int Pang;                      /* IFGF angular Chebyshev nodes (template Pang, default 5) */
+} ifgf2d_options;
+
+typedef struct ifgf2d_ctx ifgf2d_ctx;
+
+/* ForwardMap::ForwardMap (ForwardMap/ForwardMap.tpp:15-35): discretise the curves. */
+int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf2d_junction* junctions,
+                  int njunctions, const ifgf2d_options* opts, ifgf2d_ctx** out);
+int ifgf2d_destroy(ifgf2d_ctx* ctx);
+const char* ifgf2d_last_error(const ifgf2d_ctx* ctx);
+
+/* ForwardMap::total_num_unknowns_, num_patches_ (ForwardMap/ForwardMap.hpp:52-53) */
+long long ifgf2d_num_unknowns(const ifgf2d_ctx* ctx);
+long long ifgf2d_num_patches(const ifgf2d_ctx* ctx);
+/* ForwardMap::xs_, ys_, nxs_, nys_ (ForwardMap/ForwardMap.hpp:72-75); any pointer may be NULL */
+int ifgf2d_get_points(const ifgf2d_ctx* ctx, double* xs, double* ys, double* nxs, double* nys);
+/* per patch: t1, t2 and near-singular point count (Geometry/Patch.hpp:40, 69-74) */
+int ifgf2d_get_patches(const ifgf2d_ctx* ctx, double* t1t2, long long* ns_count);
+/* concatenated near-singular lists, patch by patch: point index and Brent t value */
+int ifgf2d_get_near_singular(const ifgf2d_ctx* ctx, long long* idx, double* t);
+
+/* ForwardMap::compute_precomputations (ForwardMap/ForwardMap.tpp:391-423), on the GPU. */
+int ifgf2d_precompute(ifgf2d_ctx* ctx, double wavenumber);
+/* patch p's rectangular-polar matrix, Np x (Np + n_ns), column-major, interleaved complex */
+int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, double* out);
+
+/* ForwardMap::precomps_and_setup (ForwardMap/ForwardMap.tpp:542-565): precomputations,
+ * BoxTree::Reinitialize (IFGF_Source/BoxTree.h:995-1008), the neighbourhood check
+ * (BoxTree.h:1079-1161) and the exclusion sets (ForwardMap.tpp:567-607), all flattened into
+ * device tables.  nlevels <= 0 picks the deepest tree that passes the neighbourhood check. */
+int ifgf2d_setup(ifgf2d_ctx* ctx, double wavenumber, int nlevels);
+int ifgf2d_get_nlevels(const ifgf2d_ctx* ctx);
+/* BoxTree::getSorting (IFGF_Source/BoxTree.h:1163-1165) */
+int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* sorting);
+
+/* y = A x, host vectors of N complex values (LinearOperator::operator*,
+ * ForwardMap/LinearOperator.cpp:14-22 -> compute_Ax_unacc / compute_Ax_acc). */
+int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mode);
+/* the same on device-resident vectors (cudaMalloc'ed, N complex each) */
+int ifgf2d_apply_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode);
+/* BoxTree::Solve alone (IFGF_Source/BoxTree.h:1020-1071) on given intensities, host vectors:
+ * the far-field sum that excludes self, same-patch and near-singular pairs. */
+int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intensities, double* y);
+
+/* ForwardMap::solve (ForwardMap/ForwardMap.tpp:658-697): GMRES on the device, initial guess 0,
+ * stop when the residual estimate |w_k|/||r0|| < tol, restart after `restart` steps.
+ * Returns IFGF2D_ERR_NOCONV (with x filled) when max_iters is reached first. */
+int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* x, int mode, double tol, int restart,
+                 int max_iters, int* iters, double* est_error);
+
+/* ForwardMap::propagate_unacc (ForwardMap/ForwardMap.tpp:701-727): direct off-surface field */
+int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp,
+                     const double* density, double* out);
+
+/* Device Hankel evaluator (replaces sp_bessel::hankelH1, complex_bessel
+ * besselFunctions.h:313-341, for real arguments): out[i] = H_order^(1)(x[i]), order 0 or 1. */
+int ifgf2d_hankel(int order, long long n, const double* x, double* out);
+
+/* The context's CUDA stream (cudaStream_t) for callers that time or order work on it. */
+void* ifgf2d_stream(ifgf2d_ctx* ctx);
+/* Algorithmic work of one IFGF apply: near pairs, leaf evaluations, propagation evaluations,
+ * interpolation evaluations, cones, levels, singular-correction entries, bytes resident. */
+int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]);
+
+/* Timed apply on device vectors: CUDA events on the context's stream between the phases
+ * (no counterpart in the reference, whose timers are std::chrono prints, ForwardMap.tpp:545-563).
+ * ms[0..4] = singular correction, intensities (+ Morton permutation), leaf cones,
+ * propagation (all levels), near field + interpolation; the direct mode reports its far sum
+ * in ms[4]. */
+int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]);
+
+/* FP64 FMA throughput of the current GPU in TFLOP/s (a dependent-FMA microbenchmark); the
+ * roofline denominator of the FP64 kernels (no counterpart in the reference). */
+int ifgf2d_measure_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IFGF2D_H */

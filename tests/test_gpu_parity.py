@@ -1,0 +1,167 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle -- needs a GPU.
+
+Tolerances: FP64 device Hankel within 5e-15 of scipy (relative to |H|); rectangular-polar
+weights and the direct forward map within 1e-12 of the oracle (relative, as the north-star
+bar for the plain form); the IFGF apply within 1e-11 of the oracle's own IFGF (same algorithm,
+same tree); the IFGF far field within the IFGF tolerance (5e-4 for 5x5 cones) of the
+exclusion-matched O(N^2) sum.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_gpu_hankel_matches_scipy_golden(lib):
+    g = np.load(os.path.join(GOLD, "hankel.npz"))
+    for order, ref in ((0, g["h0"]), (1, g["h1"])):
+        h = lib.hankel1(order, g["x"])
+        r = np.abs(h - ref) / np.abs(ref)
+        assert r.max() < 5e-15, (order, r.max(), g["x"][r.argmax()])
+
+
+def test_gpu_hankel_dense_sweep(lib, oracle):
+    x = np.logspace(-6, 5, 1_000_000)
+    for order in (0, 1):
+        r = np.abs(lib.hankel1(order, x) - oracle.hankel1(order, x)) / np.abs(oracle.hankel1(order, x))
+        assert r.max() < 5e-15, (order, r.max(), x[r.argmax()])
+
+
+def _pair(lib, oracle, kind, Np, delta, wl, k, p=4.0, ppc=0):
+    gc = {"circle": lib.Circle(), "kite": lib.Kite(), "line": lib.Line(-1, -0.2, 1, -0.2)}[kind]
+    oc = {"circle": oracle.curve_circle(), "kite": oracle.curve_kite(), "line": oracle.curve_line(-1, -0.2, 1, -0.2)}[kind]
+    fm = lib.ForwardMap(delta, [gc], (), wl, k, p, Np=Np, patches_per_curve=ppc)
+    om = oracle.OracleForwardMap([oc], Np, delta, wl, k, p, patches_per_curve=ppc)
+    return fm, om
+
+
+@pytest.mark.parametrize("kind,Np,delta,wl,k,p,ppc", [
+    ("circle", 10, 0.01, 1.0, 10.0, 4.0, 20),
+    ("kite", 16, 0.01, 1.0, 100.0, 4.0, 64),
+    ("line", 20, 0.1, 0.5, 3.0, 6.0, 0),
+])
+def test_gpu_precomputations_match_oracle(lib, oracle, kind, Np, delta, wl, k, p, ppc):
+    fm, om = _pair(lib, oracle, kind, Np, delta, wl, k, p, ppc)
+    fm.compute_precomputations(k)
+    om.precompute(k)
+    for patch in range(fm.num_patches_):
+        a, b = fm.precomputations(patch), om.precomp_matrix(patch)
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), patch
+
+
+def test_gpu_direct_forward_map_config1(lib, oracle):
+    """Config 1 geometry: unit circle, k=10, 20 equal patches x 10 Fejer nodes (N=200)."""
+    g = np.load(os.path.join(GOLD, "oracle_cfg1.npz"))
+    fm = lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, 10.0, Np=10, patches_per_curve=20)
+    fm.compute_precomputations(10.0)
+    y = fm.compute_Ax_unacc(g["density"])
+    assert rel(y, g["y_direct"]) < 1e-12
+
+
+@pytest.mark.parametrize("kind,Np,delta,wl,k,p,ppc", [
+    ("kite", 16, 0.01, 1.0, 100.0, 4.0, 128),
+    ("line", 20, 0.1, 0.5, 3.0, 6.0, 0),
+    ("circle", 10, 0.01, 1.0, 20.0, 4.0, 0),
+])
+def test_gpu_direct_forward_map_matches_oracle(lib, oracle, kind, Np, delta, wl, k, p, ppc):
+    fm, om = _pair(lib, oracle, kind, Np, delta, wl, k, p, ppc)
+    fm.compute_precomputations(k)
+    om.precompute(k)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    assert rel(fm.compute_Ax_unacc(d), om.compute_Ax_unacc(d)) < 1e-12
+
+
+@pytest.mark.parametrize("k,npatch,nlevels", [(100.0, 128, 0), (100.0, 128, 4), (200.0, 256, 0)])
+def test_gpu_ifgf_matches_oracle_ifgf(lib, oracle, k, npatch, nlevels):
+    fm, om = _pair(lib, oracle, "kite", 16, 0.01, 1.0, k, 4.0, npatch)
+    fm.precomps_and_setup(k, nlevels)
+    om.precompute(k)
+    om.setup_ifgf(k, fm.nlevels)
+    assert np.array_equal(fm.getSorting(), om.sorting())
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    assert rel(fm.compute_Ax_acc(d), om.compute_Ax_acc(d)) < 1e-11
+    w = om.point_weights()[0]
+    far = fm.ifgf_far(d * w)
+    assert rel(far, om.ifgf_far(d * w)) < 1e-11
+    assert rel(far, om.direct_excluded(d * w)) < 5e-4
+
+
+def test_gpu_ifgf_against_direct_config2_size(lib, oracle):
+    """Config 2 geometry (kite, k=500, 512 patches x 16 = 8192): IFGF vs the direct map."""
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 500.0, Np=16, patches_per_curve=512)
+    fm.precomps_and_setup(500.0, 0)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    ya, yd = fm.compute_Ax_acc(d), fm.compute_Ax_unacc(d)
+    assert rel(ya, yd) < 1e-3
+    # linearity of the accelerated operator
+    d2 = oracle.seeded_density(fm.total_num_unknowns_, seed=1)
+    a, b = 0.3 - 1.1j, 2.0 + 0.5j
+    assert rel(fm.compute_Ax_acc(a * d + b * d2), a * ya + b * fm.compute_Ax_acc(d2)) < 1e-12
+
+
+def test_gpu_gmres_direct_config1_matches_oracle(lib, oracle):
+    k = 10.0
+    fm, om = _pair(lib, oracle, "circle", 10, 0.01, 1.0, k, 4.0, 20)
+    b = -np.exp(1j * k * fm.xs_)
+    x = fm.solve(b, k, accelerated=False, tol=1e-10)
+    om.precompute(k)
+    xo, info = om.solve(b, False, tol=1e-10)
+    assert fm.last_solve["converged"]
+    assert abs(fm.last_solve["iters"] - info["iters"]) <= 2
+    assert rel(fm.compute_Ax_unacc(x), b) < 1e-9
+    assert rel(x, xo) < 1e-8
+
+
+def test_gpu_gmres_ifgf_kite(lib, oracle):
+    k = 100.0
+    fm, om = _pair(lib, oracle, "kite", 16, 0.01, 1.0, k, 4.0, 128)
+    b = -np.exp(1j * k * fm.xs_)
+    x = fm.solve(b, k, nlevels=0, accelerated=True, tol=1e-6)
+    assert fm.last_solve["converged"]
+    assert rel(fm.compute_Ax_acc(x), b) < 2e-6
+    om.precompute(k)
+    om.setup_ifgf(k, fm.nlevels)
+    xo, info = om.solve(b, True, tol=1e-6)
+    assert abs(fm.last_solve["iters"] - info["iters"]) <= 2
+    assert rel(x, xo) < 1e-4
+
+
+def test_gpu_helsing_jiang_known_answer(lib):
+    """tests/ForwardMap/SolveAndPropagate.cpp: open line, k=3 (direct map; see test_oracle)."""
+    ref = np.load(os.path.join(GOLD, "known.npz"))["helsing_jiang"]
+    fm = lib.ForwardMap(0.05, [lib.Line(-1, -0.2, 1, -0.2)], (), 0.125, 3.0, 6.0, Np=16)
+    f = 4 * fm.xs_ ** 3 + 2 * fm.xs_ ** 2 - 3 * fm.xs_ - 1
+    x = fm.solve(f, 3.0, accelerated=False, tol=1e-10)
+    u = fm.propagate_unacc([0.17], [0.62], x)[0]
+    assert abs(u - ref) < 5e-3
+
+
+def test_gpu_propagate_matches_oracle(lib, oracle):
+    k = 20.0
+    fm, om = _pair(lib, oracle, "circle", 10, 0.01, 1.0, k)
+    fm.compute_precomputations(k)
+    om.precompute(k)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    th = np.linspace(0, 2 * np.pi, 37)
+    xp, yp = 1.7 * np.cos(th), 1.7 * np.sin(th) + 0.1
+    assert rel(fm.propagate_unacc(xp, yp, d), om.propagate_unacc(xp, yp, d)) < 1e-12
+
+
+def test_gpu_error_paths(lib):
+    fm = lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, 20.0, Np=10)
+    with pytest.raises(lib.IFGF2DError):
+        fm.precomps_and_setup(20.0, 2)
+    with pytest.raises(lib.NeighbourhoodError):
+        fm.precomps_and_setup(20.0, 9)
+    with pytest.raises(ValueError):
+        fm.compute_precomputations(-1.0)
+    fm.precomps_and_setup(20.0, 0)
+    with pytest.raises(ValueError):
+        fm.compute_Ax_acc(np.ones(3, complex))

@@ -1,0 +1,81 @@
+"""Host-side logic and the C ABI without a GPU (CPU only).
+
+The discretisation (ForwardMap constructor) is host C++ inside libifgf2d.so; it must match
+the oracle bit for bit.  The library must load and export every symbol of include/ifgf2d.h.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from ifgf2d_gb300 import _lib
+    header = open(os.path.join(ROOT, "include", "ifgf2d.h")).read()
+    declared = set(re.findall(r"\b(ifgf2d_[a-z0-9_]+)\s*\(", header))
+    assert declared == set(_lib.EXPORTS)
+    L = ctypes.CDLL(_lib.library_path())
+    for name in declared:
+        assert hasattr(L, name), name
+
+
+CASES = [
+    ("circle", lambda G: G.Circle(), lambda O: O.curve_circle(), (10, 0.01, 0.5, 10.0, 4.0, 0)),
+    ("circle20", lambda G: G.Circle(), lambda O: O.curve_circle(), (10, 0.01, 1.0, 10.0, 4.0, 20)),
+    ("kite500", lambda G: G.Kite(), lambda O: O.curve_kite(), (16, 0.01, 1.0, 500.0, 4.0, 512)),
+    ("kite_rule", lambda G: G.Kite(), lambda O: O.curve_kite(), (16, 0.01, 1.0, 100.0, 4.0, 0)),
+    ("line", lambda G: G.Line(-1, -0.2, 1, -0.2), lambda O: O.curve_line(-1, -0.2, 1, -0.2), (20, 0.1, 0.5, 3.0, 6.0, 0)),
+    ("star", lambda G: G.Star([0.03, -0.02, 0.01], [0.01, 0.04, -0.03]),
+     lambda O: O.curve_star([0.03, -0.02, 0.01], [0.01, 0.04, -0.03]), (16, 0.01, 1.0, 50.0, 4.0, 0)),
+]
+
+
+@pytest.mark.parametrize("name,gc,oc,args", CASES, ids=[c[0] for c in CASES])
+def test_discretisation_matches_oracle_bitwise(lib, oracle, name, gc, oc, args):
+    Np, delta, wl, k, p, ppc = args
+    fm = lib.ForwardMap(delta, [gc(lib)], (), wl, k, p, Np=Np, patches_per_curve=ppc)
+    om = oracle.OracleForwardMap([oc(oracle)], Np, delta, wl, k, p, patches_per_curve=ppc)
+    assert fm.total_num_unknowns_ == om.N and fm.num_patches_ == om.num_patches
+    xs, ys, nx, ny = om.points()
+    for a, b in ((fm.xs_, xs), (fm.ys_, ys), (fm.nxs_, nx), (fm.nys_, ny)):
+        assert np.array_equal(a, b)
+    t_g, c_g = fm.patches()
+    t_o, c_o = om.patch_info()
+    assert np.array_equal(t_g, t_o) and np.array_equal(c_g, c_o)
+    _, i_g, tv_g = fm.near_singular()
+    _, i_o, tv_o = om.near_singular()
+    assert np.array_equal(i_g, i_o) and np.array_equal(tv_g, tv_o)
+
+
+def test_bad_arguments_raise(lib):
+    with pytest.raises(ValueError):
+        lib.ForwardMap(0.01, [], (), 1.0, 10.0, Np=10)
+    with pytest.raises(ValueError):
+        lib.ForwardMap(-1.0, [lib.Circle()], (), 1.0, 10.0, Np=10)
+    with pytest.raises(ValueError):
+        lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, 10.0, Np=1)
+    with pytest.raises(ValueError):
+        lib.Star([0.1] * 7, [0.0] * 7)
+
+
+def test_apply_before_setup_is_a_state_error(lib):
+    fm = lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, 10.0, Np=10)
+    with pytest.raises(lib.IFGF2DError):
+        fm.compute_Ax_acc(np.ones(fm.total_num_unknowns_, complex))
+
+
+def test_rectangle_junctions_discretise(lib, oracle):
+    """make_rect (Geometry/Obstacles.cpp:6-23): four lines joined by junctions."""
+    c1x, c1y, c2x, c2y = -0.5, 0.5, 0.5, -0.5
+    lines = [(c2x, c2y, c2x, c1y), (c2x, c1y, c1x, c1y), (c1x, c1y, c1x, c2y), (c1x, c2y, c2x, c2y)]
+    junc = [(0, 1, 0), (0, 3, 0), (1, 0, 0), (1, 2, 0), (2, 1, 0), (2, 3, 0), (3, 2, 0), (3, 0, 0)]
+    fm = lib.ForwardMap(0.05, [lib.Line(*l) for l in lines], [lib.Junction(*j) for j in junc], 1.0, 5.0, 4.0, Np=10)
+    om = oracle.OracleForwardMap([oracle.curve_line(*l) for l in lines], 10, 0.05, 1.0, 5.0, 4.0, junctions=junc)
+    assert np.array_equal(fm.xs_, om.points()[0])
+    _, i_g, _ = fm.near_singular()
+    _, i_o, _ = om.near_singular()
+    assert np.array_equal(i_g, i_o)
