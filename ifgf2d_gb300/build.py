@@ -18,7 +18,9 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libifgf2d.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["geometry.cpp", "tree.cpp", "ifgf2d_kernels.cu", "ifgf2d_capi.cu"]
+SOURCES = ["geometry.cpp", "tree.cpp", "ifgf2d_kernels.cu", "rp_precompute.cu", "ifgf2d_capi.cu"]
+# translation units whose arithmetic must round like the host restatement (no FMA contraction)
+NO_FMAD = {"rp_precompute.cu"}
 
 
 def nvcc() -> str:
@@ -31,8 +33,10 @@ def nvcc() -> str:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-ffp-contract=off" if src.endswith(".cpp") else "-O3",
+           "-Xcompiler", "-ffp-contract=off",
            "-c", os.path.join(CSRC, src), "-o", obj]
+    if src in NO_FMAD:
+        cmd[1:1] = ["-fmad=false"]
     if src.endswith(".cu"):
         cmd[1:1] = ["-Xptxas", "-v"] if verbose else []
     r = subprocess.run(cmd, capture_output=True, text=True)

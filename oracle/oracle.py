@@ -65,7 +65,7 @@ def lib():
         L.orc_fm_ifgf_far.argtypes = [P, D, D]
         L.orc_fm_direct_excluded.argtypes = [P, D, D, ctypes.c_longlong, ctypes.c_longlong]
         L.orc_fm_solve.argtypes = [P, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_longlong,
-                                   ctypes.c_longlong, I64, D, I64]
+                                   ctypes.c_longlong, I64, D, I64, ctypes.c_int]
         L.orc_fm_solve.restype = ctypes.c_int
         L.orc_fm_propagate.argtypes = [P, ctypes.c_longlong, D, D, D, D]
         _lib = L
@@ -231,12 +231,13 @@ class OracleForwardMap:
         lib().orc_fm_level_stats(self.h, _i64(b), _i64(c))
         return b, c
 
-    def solve(self, rhs, accelerated, tol=1e-10, restart=300, maxit=300):
+    def solve(self, rhs, accelerated, tol=1e-10, restart=300, maxit=300, exact_adjoint=False):
+        """Householder GMRES (opGMRES.hpp:68-269); exact_adjoint selects the minimal-residual variant."""
         r = _cvec(rhs)
         x = np.empty(2 * self.N)
         it = np.zeros(1, dtype=np.int64); mv = np.zeros(1, dtype=np.int64); err = np.zeros(1)
         rc = lib().orc_fm_solve(self.h, _d(r), _d(x), 1 if accelerated else 0, tol, restart, maxit,
-                                _i64(it), _d(err), _i64(mv))
+                                _i64(it), _d(err), _i64(mv), 1 if exact_adjoint else 0)
         return x[0::2] + 1j * x[1::2], dict(rc=rc, iters=int(it[0]), error=float(err[0]), matvecs=int(mv[0]))
 
     def propagate_unacc(self, xp, yp, density):

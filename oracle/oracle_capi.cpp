@@ -166,7 +166,7 @@ void orc_fm_direct_excluded(void* hh, const double* in, double* out, long long r
 
 // ForwardMap.tpp:658-697 (precomputations / IFGF set-up must have been done)
 int orc_fm_solve(void* hh, const double* rhs, double* x, int accelerated, double tol, long long restart,
-                 long long maxit, long long* iters, double* err, long long* matvecs) {
+                 long long maxit, long long* iters, double* err, long long* matvecs, int exact_adjoint) {
     OracleFM* h = (OracleFM*)hh; ForwardMap& F = *h->fm;
     auto A = [&](const std::vector<cd>& in, std::vector<cd>& o) {
         if (accelerated) {
@@ -181,7 +181,7 @@ int orc_fm_solve(void* hh, const double* rhs, double* x, int accelerated, double
         }
     };
     std::vector<cd> xv;
-    GmresResult R = householder_gmres(A, to_c(rhs, F.N), xv, restart, maxit, tol);
+    GmresResult R = householder_gmres(A, to_c(rhs, F.N), xv, restart, maxit, tol, exact_adjoint != 0);
     from_c(xv, x);
     *iters = R.iters; *err = R.error; *matvecs = R.matvecs;
     return R.ok ? (R.error <= tol ? 0 : 1) : 2;

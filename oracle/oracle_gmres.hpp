@@ -5,6 +5,12 @@
 // opGMRES wrapper (:323-396): initial guess 0, stopping test |w(k)|/||r0|| < tol,
 // restart after `restart` steps.  Householder and Givens conventions follow Eigen's
 // makeHouseholder / applyHouseholderOnTheLeft / JacobiRotation::makeGivens.
+//
+// With complex tau the reflector H = I - tau u u^H is unitary but not Hermitian, and the
+// reference applies H (not H^{-1} = H^H) when it forms the basis vector P_1..P_k e_k and the
+// update (opGMRES.hpp:147-149, 224-229).  The iteration stays consistent (estimate = true
+// residual) but is not the minimal-residual one.  exact_adjoint = true applies H^H there,
+// which gives the minimal-residual (textbook GMRES) iterates; false restates the reference.
 #pragma once
 
 #include "oracle_math.hpp"
@@ -77,7 +83,8 @@ struct GmresResult { bool ok; long long iters; double error; long long matvecs; 
 
 static inline GmresResult householder_gmres(const std::function<void(const std::vector<cd>&, std::vector<cd>&)>& A,
                                             const std::vector<cd>& rhs, std::vector<cd>& x,
-                                            long long restart, long long max_iters, double tol) {
+                                            long long restart, long long max_iters, double tol,
+                                            bool exact_adjoint = false) {
     const long long m = (long long)rhs.size();
     GmresResult R{true, 0, 0.0, 0};
     x.assign(m, 0.0);
@@ -97,7 +104,8 @@ static inline GmresResult householder_gmres(const std::function<void(const std::
     for (long long k = 1; k <= restart; ++k) {
         ++R.iters;
         std::fill(v.begin(), v.end(), cd(0.0)); v[k - 1] = 1.0;
-        for (long long i = k - 1; i >= 0; --i) apply_householder(&v[i], m - i, col(i) + i + 1, tau[i]);
+        for (long long i = k - 1; i >= 0; --i)
+            apply_householder(&v[i], m - i, col(i) + i + 1, exact_adjoint ? std::conj(tau[i]) : tau[i]);
         A(v, t); R.matvecs++;
         v = t;
         for (long long i = 0; i < k; ++i) apply_householder(&v[i], m - i, col(i) + i + 1, tau[i]);
@@ -125,7 +133,7 @@ static inline GmresResult householder_gmres(const std::function<void(const std::
             std::fill(xnew.begin(), xnew.end(), cd(0.0));
             for (long long i = k - 1; i >= 0; --i) {
                 xnew[i] += y[i];
-                apply_householder(&xnew[i], m - i, col(i) + i + 1, tau[i]);
+                apply_householder(&xnew[i], m - i, col(i) + i + 1, exact_adjoint ? std::conj(tau[i]) : tau[i]);
             }
             for (long long i = 0; i < m; ++i) x[i] += xnew[i];
             if (stop) return R;
