@@ -29,6 +29,7 @@ EXPORTS = [
     "ifgf2d_get_precomputations", "ifgf2d_setup", "ifgf2d_get_nlevels", "ifgf2d_get_sorting", "ifgf2d_apply",
     "ifgf2d_apply_device", "ifgf2d_ifgf_far", "ifgf2d_solve", "ifgf2d_propagate", "ifgf2d_hankel",
     "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
+    "ifgf2d_apply_direct_noalloc",
 ]
 
 
@@ -91,5 +92,6 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_work_counts.argtypes = [P, I64]
         L.ifgf2d_apply_timed.argtypes = [P, P, P, ctypes.c_int, D]
         L.ifgf2d_measure_fp64_peak.argtypes = [D]
+        L.ifgf2d_apply_direct_noalloc.argtypes = [P, P, P]
         _lib = L
         return L

@@ -683,3 +683,18 @@ extern "C" int ifgf2d_hankel(int order, long long n, const double* x, double* ou
     if (cudaMemcpy(out, dout.p, sizeof(double2) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return IFGF2D_ERR_CUDA;
     return IFGF2D_OK;
 }
+
+// ------------------------------------------------------------------ views for other translation units
+#include "direct_view.hpp"
+
+int ifgf::direct_view(ifgf2d_ctx* ctx, ifgf::DirectView* v) {
+    if (!ctx || !v) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
+    v->N = (int)ctx->D.N; v->Np = ctx->D.Np; v->device = ctx->device; v->k = ctx->k; v->stream = ctx->stream;
+    v->W = ctx->W.p; v->srow_ptr = ctx->srow_ptr.p; v->srow_col = ctx->srow_col.p; v->cols = ctx->cols.p;
+    v->wq = ctx->wq.p; v->x = ctx->x.p; v->y = ctx->y.p; v->patch_of = ctx->patch_of.p;
+    v->nsp_ptr = ctx->nsp_ptr.p; v->nsp = ctx->nsp.p;
+    return IFGF2D_OK;
+}
+
+void ifgf::set_error(ifgf2d_ctx* ctx, const char* msg) { if (ctx) ctx->err = msg; }

@@ -135,6 +135,23 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
  * roofline denominator of the FP64 kernels (no counterpart in the reference). */
 int ifgf2d_measure_fp64_peak(double* tflops);
 
+/* Largest N accepted by ifgf2d_apply_direct_noalloc. */
+#define IFGF2D_NOALLOC_MAX_N 65536
+
+/* The direct forward map (as ifgf2d_apply_device with IFGF2D_APPLY_DIRECT) on caller-owned
+ * device vectors, with no device allocation inside the call.  No counterpart in the reference.
+ * For callers that cannot allocate at the call site: a host application or plugin framework
+ * that owns the device memory budget, or a latency-critical loop that cannot take the implicit
+ * synchronisation of cudaMalloc / cudaFree.  Its scratch (the weighted density) is a fixed
+ * 1 MiB device array inside the library, so N must not exceed IFGF2D_NOALLOC_MAX_N
+ * (IFGF2D_ERR_ARG otherwise).  The context must have been precomputed (ifgf2d_precompute or
+ * ifgf2d_setup) and its device must be current.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Work is queued on the context's stream; synchronise before reading d_y.  All
+ * calls share the one array, so calls that overlap on the GPU (several contexts or streams
+ * at once) race. */
+int ifgf2d_apply_direct_noalloc(ifgf2d_ctx* ctx, const void* d_x, void* d_y);
+
 #ifdef __cplusplus
 }
 #endif
