@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import APPLY_DIRECT, APPLY_IFGF
+from ._lib import APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED
 
 __all__ = ["ForwardMap", "LinearOperator", "Circle", "Kite", "Line", "Star", "Junction", "hankel1",
            "IFGF2DError", "NeighbourhoodError", "NoConvergence", "load_library"]
@@ -252,9 +252,13 @@ class ForwardMap:
             out[...] = y
         return y
 
-    def compute_Ax_acc(self, density, out=None):
-        """ForwardMap.tpp:609-655: singular correction + IFGF far sum (BoxTree::Solve)."""
-        y = self._apply(density, APPLY_IFGF)
+    def compute_Ax_acc(self, density, out=None, mixed=False):
+        """ForwardMap.tpp:609-655: singular correction + IFGF far sum (BoxTree::Solve).
+
+        mixed=True evaluates the IFGF far field in complex64 (FP32 arithmetic on tables
+        computed in FP64); the singular correction stays FP64.
+        """
+        y = self._apply(density, APPLY_IFGF_MIXED if mixed else APPLY_IFGF)
         if out is not None:
             out[...] = y
         return y
@@ -267,18 +271,22 @@ class ForwardMap:
         _check(_lib.load().ifgf2d_ifgf_far(self._h, _dp(xin.view(np.float64)), _dp(out.view(np.float64))), self._h)
         return out
 
-    def apply_device(self, d_x, d_y, accelerated=True):
-        """y = A x on device pointers (ints or objects with data_ptr(); N complex128 each)."""
+    def apply_device(self, d_x, d_y, accelerated=True, mixed=False):
+        """y = A x on device pointers (ints or objects with data_ptr(); N complex128 each).
+
+        Work is queued on the context's stream (``stream()``); synchronise before reading y.
+        """
         px = d_x.data_ptr() if hasattr(d_x, "data_ptr") else int(d_x)
         py = d_y.data_ptr() if hasattr(d_y, "data_ptr") else int(d_y)
-        _check(_lib.load().ifgf2d_apply_device(self._h, px, py, APPLY_IFGF if accelerated else APPLY_DIRECT), self._h)
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        _check(_lib.load().ifgf2d_apply_device(self._h, px, py, mode), self._h)
 
     def stream(self):
         return _lib.load().ifgf2d_stream(self._h)
 
     # -- solver
     def solve(self, rhs, wavenumber, nlevels=0, accelerated=True, tol=None, restart=None, max_iters=None,
-              raise_on_noconv=False):
+              raise_on_noconv=False, mixed=False):
         """ForwardMap.tpp:658-697: set-up, then GMRES (initial guess 0) on the device.
 
         Returns the density; ``self.last_solve`` holds iterations and the estimated error.
@@ -287,9 +295,11 @@ class ForwardMap:
             self.precomps_and_setup(wavenumber, nlevels)
         else:
             self.compute_precomputations(wavenumber)
-        return self.gmres(rhs, accelerated, tol, restart, max_iters, raise_on_noconv)
+        return self.gmres(rhs, accelerated, tol, restart, max_iters, raise_on_noconv, mixed)
 
-    def gmres(self, rhs, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False):
+    def gmres(self, rhs, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False, mixed=False):
+        """Device GMRES; mixed=True: FP64 iterative refinement around complex64 inner solves
+        (stop test on the FP64 relative residual)."""
         n = self.total_num_unknowns_
         b = _cview(rhs, n)
         x = np.empty(n, dtype=np.complex128)
@@ -299,7 +309,8 @@ class ForwardMap:
         restart = self.GMRES_MAX_ITER_ if restart is None else restart
         max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
         rc = _lib.load().ifgf2d_solve(self._h, _dp(b.view(np.float64)), _dp(x.view(np.float64)),
-                                      APPLY_IFGF if accelerated else APPLY_DIRECT, float(tol), int(restart),
+                                      (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT,
+                                      float(tol), int(restart),
                                       int(max_iters), ctypes.byref(it), ctypes.byref(err))
         self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0))
         if rc == 8:

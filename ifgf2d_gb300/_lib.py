@@ -19,7 +19,7 @@ STATUS = {
     0: "OK", 1: "ERR_ARG", 2: "ERR_GEOMETRY", 3: "ERR_NEIGHBORHOOD", 4: "ERR_NLEVELS",
     5: "ERR_CUDA", 6: "ERR_STATE", 7: "ERR_NONFINITE", 8: "ERR_NOCONV",
 }
-APPLY_DIRECT, APPLY_IFGF = 0, 1
+APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED = 0, 1, 2
 CURVE_CIRCLE, CURVE_KITE, CURVE_LINE, CURVE_STAR = 0, 1, 2, 3
 
 # every symbol include/ifgf2d.h declares

@@ -84,7 +84,13 @@ struct ifgf2d_ctx {
     DBuf<int> ip_ptr;
     DBuf<InterpEntryD> ip;
     DBuf<double2> coef;
-    DBuf<double> Gm;
+    DBuf<double> Gm, Gsep;          // full and separable values->coefficients maps
+    DBuf<int> near_rowlen;          // per leaf box: sources in its 3x3 neighbourhood
+    // complex64 copies of the IFGF tables (mixed form)
+    DBuf<float2> near32, leafL32, coef32, rho32;
+    DBuf<PropE<float>> pp32;
+    DBuf<InterpE<float>> ip32;
+    DBuf<float> Gsep32;
     // work vectors
     DBuf<double2> rho, vin, vout;
     long long counts[8] = {0};
@@ -326,6 +332,11 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         noff[b + 1] = noff[b] + nsrc * T.leaf_count[b];
     }
     CK(ctx->near_off.upload(noff));
+    {
+        std::vector<int> rl(nleaf);
+        for (int b = 0; b < nleaf; ++b) rl[b] = (int)((noff[b + 1] - noff[b]) / std::max(1, T.leaf_count[b]));
+        CK(ctx->near_rowlen.upload(rl));
+    }
     CK(ctx->near.alloc(noff[nleaf]));
     launch_near_setup(ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p, ctx->near_off.p, nleaf,
                       ctx->xs_s.p, ctx->ys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k, ctx->near.p, ctx->stream);
@@ -346,6 +357,15 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
                         G[(size_t)(n * Ps + m) * P + (l * Ps + kk)] = Tn(m, xs[kk]) * Tn(n, xa[l]) * (am * an / (Ps * Pa));
                     }
         CK(ctx->Gm.upload(G));
+        // separable form: Gs[m][k] = (alpha_m / Ps) T_m(x_k), Ga[n][l] = (alpha_n / Pang) T_n(x_l)
+        std::vector<double> Gs((size_t)Ps * Ps + (size_t)Pa * Pa);
+        for (int m = 0; m < Ps; ++m)
+            for (int kk = 0; kk < Ps; ++kk) Gs[(size_t)m * Ps + kk] = Tn(m, xs[kk]) * ((m == 0 ? 1.0 : 2.0) / Ps);
+        for (int n = 0; n < Pa; ++n)
+            for (int l = 0; l < Pa; ++l) Gs[(size_t)Ps * Ps + (size_t)n * Pa + l] = Tn(n, xa[l]) * ((n == 0 ? 1.0 : 2.0) / Pa);
+        CK(ctx->Gsep.upload(Gs));
+        std::vector<float> Gs32(Gs.begin(), Gs.end());
+        CK(ctx->Gsep32.upload(Gs32));
     }
     // leaf cones
     const TreeLevel& LD = T.L[Dl];
@@ -374,8 +394,28 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         for (size_t i = 0; i < T.ip.size(); ++i) { const InterpEntry& e = T.ip[i]; ie[i] = InterpEntryD{e.cone, 0, e.s, e.th, e.fr, e.fi}; }
         CK(ctx->ip.upload(ie));
         CK(ctx->ip_ptr.upload(T.ip_ptr));
+        // complex64 copies for the mixed form (values computed in FP64, rounded once)
+        std::vector<PropE<float>> pf(T.pp.size());
+        for (size_t i = 0; i < T.pp.size(); ++i) {
+            const PropEntry& e = T.pp[i];
+            pf[i] = PropE<float>{e.child_cone, (float)e.s, (float)e.th, (float)e.wr, (float)e.wi};
+        }
+        CK(ctx->pp32.upload(pf));
+        std::vector<InterpE<float>> jf(T.ip.size());
+        for (size_t i = 0; i < T.ip.size(); ++i) {
+            const InterpEntry& e = T.ip[i];
+            jf[i] = InterpE<float>{e.cone, (float)e.s, (float)e.th, (float)e.fr, (float)e.fi};
+        }
+        CK(ctx->ip32.upload(jf));
     }
     CK(ctx->coef.alloc((size_t)T.total_cones * P));
+    CK(ctx->coef32.alloc((size_t)T.total_cones * P));
+    CK(ctx->rho32.alloc(N));
+    CK(ctx->near32.alloc(ctx->near.n));
+    CK(ctx->leafL32.alloc(ctx->leafL.n));
+    launch_d2f(ctx->near.p, (long long)ctx->near.n, ctx->near32.p, ctx->stream);
+    launch_d2f(ctx->leafL.p, (long long)ctx->leafL.n, ctx->leafL32.p, ctx->stream);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
     ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
@@ -398,21 +438,41 @@ extern "C" int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]) {
 }
 
 // ------------------------------------------------------------------ apply
-static int far_ifgf(ifgf2d_ctx* ctx, double2* y) {
-    // y += far field of ctx->rho (Morton-ordered intensities)
+// y += far field of the Morton-ordered intensities (rho / rho32), BoxTree.h:1037-1061
+template <typename R>
+static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* leafL, const PropE<R>* pp,
+                       const InterpE<R>* ip, const R* Gsep, V2<R>* coef, double2* y, cudaEvent_t* ev) {
     const Tree& T = ctx->T;
     const int Dl = ctx->nlevels - 1, P = T.P;
     const TreeLevel& LD = T.L[Dl];
-    launch_leaf_apply(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
-                      ctx->leaf_off.p, ctx->leafL.p, ctx->rho.p, P, ctx->coef.p, ctx->stream);
+    cudaStream_t s = ctx->stream;
+    launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                           ctx->leaf_off.p, leafL, rho, P, coef, s);
+    if (ev) cudaEventRecord(ev[0], s);
     for (int l = Dl; l >= 3; --l) {
         const TreeLevel& Lp = T.L[l - 1];
-        launch_propagate(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, ctx->pp.p,
-                         T.Ps, T.Pang, ctx->Gm.p, ctx->coef.p, ctx->stream);
+        launch_propagate_t<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pp,
+                              T.Ps, T.Pang, Gsep, coef, s);
     }
-    launch_final((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
-                 ctx->near_off.p, ctx->near.p, ctx->rho.p, ctx->ip_ptr.p, ctx->ip.p, ctx->coef.p, T.Ps, T.Pang,
-                 ctx->sorting.p, y, ctx->stream);
+    if (ev) cudaEventRecord(ev[1], s);
+    launch_final_t<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
+                      ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p, y, s);
+}
+
+// the IFGF far field in the precision of `mode`; x in original order, y += result
+static int far_apply(ifgf2d_ctx* ctx, const double2* x, const double* wq, double2* y, int mode, cudaEvent_t* ev) {
+    const int N = (int)ctx->D.N;
+    if (mode == IFGF2D_APPLY_IFGF_MIXED) {
+        launch_intensities_t<float>(x, wq, ctx->sorting.p, N, ctx->rho32.p, ctx->stream);
+        if (ev) cudaEventRecord(ev[0], ctx->stream);
+        far_ifgf_t<float>(ctx, ctx->rho32.p, ctx->near32.p, ctx->leafL32.p, ctx->pp32.p, ctx->ip32.p, ctx->Gsep32.p,
+                          ctx->coef32.p, y, ev ? ev + 1 : nullptr);
+    } else {
+        launch_intensities_t<double>(x, wq, ctx->sorting.p, N, ctx->rho.p, ctx->stream);
+        if (ev) cudaEventRecord(ev[0], ctx->stream);
+        far_ifgf_t<double>(ctx, ctx->rho.p, ctx->near.p, ctx->leafL.p, ctx->pp.p, ctx->ip.p, ctx->Gsep.p, ctx->coef.p, y,
+                           ev ? ev + 1 : nullptr);
+    }
     CK(cudaGetLastError());
     return IFGF2D_OK;
 }
@@ -421,13 +481,11 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
     const Discretisation& D = ctx->D;
     const int N = (int)D.N;
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
-    if (mode == IFGF2D_APPLY_IFGF && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
-    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT) return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
     launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, ctx->stream);
-    if (mode == IFGF2D_APPLY_IFGF) {
-        launch_intensities(x, ctx->wq.p, ctx->sorting.p, N, ctx->rho.p, ctx->stream);
-        return far_ifgf(ctx, y);
-    }
+    if (mode != IFGF2D_APPLY_DIRECT) return far_apply(ctx, x, ctx->wq.p, y, mode, nullptr);
     launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
     launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->patch_of.p,
                       ctx->rho.p, N, ctx->k, y, 1, ctx->stream);
@@ -438,8 +496,9 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
 extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]) {
     if (!ctx || !d_x || !d_y || !ms) return IFGF2D_ERR_ARG;
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
-    if (mode == IFGF2D_APPLY_IFGF && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
-    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT) return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
     const double2* x = (const double2*)d_x;
     double2* y = (double2*)d_y;
     const Discretisation& D = ctx->D;
@@ -450,24 +509,9 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
     CK(cudaEventRecord(ev[0], s));
     launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, s);
     CK(cudaEventRecord(ev[1], s));
-    if (mode == IFGF2D_APPLY_IFGF) {
-        launch_intensities(x, ctx->wq.p, ctx->sorting.p, N, ctx->rho.p, s);
-        CK(cudaEventRecord(ev[2], s));
-        const Tree& T = ctx->T;
-        const int Dl = ctx->nlevels - 1, P = T.P;
-        const TreeLevel& LD = T.L[Dl];
-        launch_leaf_apply(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
-                          ctx->leaf_off.p, ctx->leafL.p, ctx->rho.p, P, ctx->coef.p, s);
-        CK(cudaEventRecord(ev[3], s));
-        for (int l = Dl; l >= 3; --l) {
-            const TreeLevel& Lp = T.L[l - 1];
-            launch_propagate(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, ctx->pp.p,
-                             T.Ps, T.Pang, ctx->Gm.p, ctx->coef.p, s);
-        }
-        CK(cudaEventRecord(ev[4], s));
-        launch_final(N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
-                     ctx->near_off.p, ctx->near.p, ctx->rho.p, ctx->ip_ptr.p, ctx->ip.p, ctx->coef.p, T.Ps, T.Pang,
-                     ctx->sorting.p, y, s);
+    if (mode != IFGF2D_APPLY_DIRECT) {
+        int rc = far_apply(ctx, x, ctx->wq.p, y, mode, ev + 2);
+        if (rc != IFGF2D_OK) return rc;
     } else {
         launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, s);
         CK(cudaEventRecord(ev[2], s));
@@ -513,9 +557,8 @@ extern "C" int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intens, double* y)
     // rho = intensities in Morton order (unit weights)
     std::vector<double> ones(ctx->D.N, 1.0);
     DBuf<double> w1; CK(w1.upload(ones));
-    launch_intensities(ctx->vin.p, w1.p, ctx->sorting.p, (int)ctx->D.N, ctx->rho.p, ctx->stream);
     CK(cudaMemsetAsync(ctx->vout.p, 0, bytes, ctx->stream));
-    int rc = far_ifgf(ctx, ctx->vout.p);
+    int rc = far_apply(ctx, ctx->vin.p, w1.p, ctx->vout.p, IFGF2D_APPLY_IFGF, nullptr);
     if (rc != IFGF2D_OK) return rc;
     CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -573,78 +616,80 @@ void rot(const Giv& g, std::complex<double>& x, std::complex<double>& y) {
 }
 }  // namespace
 
-extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, int mode, double tol, int restart, int max_iters,
-                            int* iters_out, double* err_out) {
-    if (!ctx || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
-    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
+struct GmresWork {
+    DBuf<double2> V, w, h, t;
+    long long n = 0;
+    int m = 0;
+};
+
+// GMRES core on device vectors: x = A^{-1} b from the initial guess 0 (the reference's guess,
+// opGMRES.hpp:383-392).  Stops when |g_{j+1}| / ||r0|| < tol or after max_iters iterations.
+static int gmres_core(ifgf2d_ctx* ctx, GmresWork& G, const double2* b, double2* x, int mode, double tol, int restart,
+                      int max_iters, int& iters, double& est) {
     const long long N = ctx->D.N;
     const int m = restart;
     cudaStream_t s = ctx->stream;
-    DBuf<double2> V, b, x, w, h, t;
-    CK(V.alloc((size_t)N * (m + 1))); CK(b.alloc(N)); CK(x.alloc(N)); CK(w.alloc(N)); CK(h.alloc(m + 2)); CK(t.alloc(N));
-    CK(cudaMemcpyAsync(b.p, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(x.p, 0, sizeof(double2) * N, s));
+    if (G.n != N || G.m < m) {
+        CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N));
+        G.n = N; G.m = m;
+    }
+    double2 *V = G.V.p, *w = G.w.p, *h = G.h.p, *t = G.t.p;
+    CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, s));
     auto dnorm = [&](const double2* v, double& out) -> int {
-        launch_multidot(v, N, 1, v, N, h.p + m + 1, s);
-        double2 r; CK(cudaMemcpyAsync(&r, h.p + m + 1, sizeof(double2), cudaMemcpyDeviceToHost, s));
+        launch_multidot(v, N, 1, v, N, h + m + 1, s);
+        double2 r; CK(cudaMemcpyAsync(&r, h + m + 1, sizeof(double2), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         out = std::sqrt(std::max(r.x, 0.0));
         return IFGF2D_OK;
     };
     int rc;
-    double bn; if ((rc = dnorm(b.p, bn))) return rc;
-    if (bn <= 2.2250738585072014e-308) {
-        std::fill(xout, xout + 2 * N, 0.0);
-        if (iters_out) *iters_out = 0;
-        if (err_out) *err_out = 0.0;
-        return IFGF2D_OK;
-    }
+    iters = 0; est = 0.0;
+    double bn; if ((rc = dnorm(b, bn))) return rc;
+    if (bn <= 2.2250738585072014e-308) return IFGF2D_OK;
     // r0 = b - A x0 with x0 = 0 (the reference applies the operator to the zero guess too)
-    if ((rc = apply_dev(ctx, x.p, t.p, mode))) return rc;
-    launch_sub(b.p, t.p, N, w.p, s);
-    double beta; if ((rc = dnorm(w.p, beta))) return rc;
+    if ((rc = apply_dev(ctx, x, t, mode))) return rc;
+    launch_sub(b, t, N, w, s);
+    double beta; if ((rc = dnorm(w, beta))) return rc;
     const double r0n = beta;
-    int iters = 0;
-    double est = 1.0;
-    bool done = (beta == 0.0);
+    est = 1.0;
+    if (beta == 0.0) { est = 0.0; return IFGF2D_OK; }
     std::vector<std::complex<double>> H((size_t)(m + 1) * m), g(m + 1), hv(m + 1);
-    std::vector<Giv> G(m);
+    std::vector<Giv> Gr(m);
     std::vector<double2> hh(m + 1), yv(m);
-    while (!done) {
-        launch_scale(w.p, make_double2(1.0 / beta, 0.0), N, V.p, s);
+    for (;;) {
+        launch_scale(w, make_double2(1.0 / beta, 0.0), N, V, s);
         std::fill(H.begin(), H.end(), 0.0); std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
         bool stop = false;
         for (; j < m; ++j) {
-            double2* vj = V.p + (size_t)j * N;
-            if ((rc = apply_dev(ctx, vj, w.p, mode))) return rc;
-            // CGS2
+            double2* vj = V + (size_t)j * N;
+            if ((rc = apply_dev(ctx, vj, w, mode))) return rc;
             std::fill(hv.begin(), hv.end(), 0.0);
-            for (int pass = 0; pass < 2; ++pass) {
-                launch_multidot(V.p, N, j + 1, w.p, N, h.p, s);
-                launch_multi_axpy(V.p, N, j + 1, h.p, -1.0, N, w.p, s);
-                CK(cudaMemcpyAsync(hh.data(), h.p, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, s));
+            for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice (CGS2)
+                launch_multidot(V, N, j + 1, w, N, h, s);
+                launch_multi_axpy(V, N, j + 1, h, -1.0, N, w, s);
+                CK(cudaMemcpyAsync(hh.data(), h, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, s));
                 CK(cudaStreamSynchronize(s));
                 for (int i = 0; i <= j; ++i) hv[i] += std::complex<double>(hh[i].x, hh[i].y);
             }
-            double hn; if ((rc = dnorm(w.p, hn))) return rc;
+            double hn; if ((rc = dnorm(w, hn))) return rc;
             ++iters;
-            for (int i = 0; i <= j; ++i) H[(size_t)j * (m + 1) + i] = hv[i];
-            H[(size_t)j * (m + 1) + j + 1] = hn;
             std::complex<double>* col = &H[(size_t)j * (m + 1)];
-            for (int i = 0; i < j; ++i) rot(G[i], col[i], col[i + 1]);
+            for (int i = 0; i <= j; ++i) col[i] = hv[i];
+            col[j + 1] = hn;
+            for (int i = 0; i < j; ++i) rot(Gr[i], col[i], col[i + 1]);
             if (col[j + 1] != 0.0) {
-                G[j] = make_giv(col[j], col[j + 1]);
-                rot(G[j], col[j], col[j + 1]);
-                rot(G[j], g[j], g[j + 1]);
+                Gr[j] = make_giv(col[j], col[j + 1]);
+                rot(Gr[j], col[j], col[j + 1]);
+                rot(Gr[j], g[j], g[j + 1]);
             } else {
-                G[j] = Giv{1.0, 0.0};
+                Gr[j] = Giv{1.0, 0.0};
             }
             est = std::abs(g[j + 1]) / r0n;
             stop = (iters >= N || est < tol || iters >= max_iters || hn == 0.0);
             if (stop) { ++j; break; }
-            if (j + 1 < m) launch_scale(w.p, make_double2(1.0 / hn, 0.0), N, V.p + (size_t)(j + 1) * N, s);
+            if (j + 1 < m) launch_scale(w, make_double2(1.0 / hn, 0.0), N, V + (size_t)(j + 1) * N, s);
         }
         if (j > m) j = m;
         // y = R^{-1} g, x += V y
@@ -655,14 +700,69 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
             y[i] = acc / H[(size_t)i * (m + 1) + i];
         }
         for (int i = 0; i < j; ++i) yv[i] = make_double2(y[i].real(), y[i].imag());
-        CK(cudaMemcpyAsync(h.p, yv.data(), sizeof(double2) * j, cudaMemcpyHostToDevice, s));
-        launch_multi_axpy(V.p, N, j, h.p, 1.0, N, x.p, s);
+        CK(cudaMemcpyAsync(h, yv.data(), sizeof(double2) * j, cudaMemcpyHostToDevice, s));
+        launch_multi_axpy(V, N, j, h, 1.0, N, x, s);
         if (stop) break;
-        // restart: r = b - A x
-        if ((rc = apply_dev(ctx, x.p, t.p, mode))) return rc;
-        launch_sub(b.p, t.p, N, w.p, s);
-        if ((rc = dnorm(w.p, beta))) return rc;
-        if (beta == 0.0) break;
+        // restart: r = b - A x (the residual estimate keeps the first ||r0||, opGMRES.hpp:207)
+        if ((rc = apply_dev(ctx, x, t, mode))) return rc;
+        launch_sub(b, t, N, w, s);
+        if ((rc = dnorm(w, beta))) return rc;
+        if (beta == 0.0) { est = 0.0; break; }
+    }
+    CK(cudaStreamSynchronize(s));
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, int mode, double tol, int restart, int max_iters,
+                            int* iters_out, double* err_out) {
+    if (!ctx || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
+    const long long N = ctx->D.N;
+    cudaStream_t s = ctx->stream;
+    GmresWork G;
+    DBuf<double2> b, x;
+    CK(b.alloc(N)); CK(x.alloc(N));
+    CK(cudaMemcpyAsync(b.p, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+    int iters = 0, rc;
+    double est = 0.0;
+    if (mode != IFGF2D_APPLY_IFGF_MIXED) {
+        if ((rc = gmres_core(ctx, G, b.p, x.p, mode, tol, restart, max_iters, iters, est))) return rc;
+    } else {
+        // FP64 iterative refinement: r = b - A x with the FP64 IFGF operator, inner GMRES on the
+        // complex64 operator for the correction, x += d, until ||r|| / ||b|| < tol
+        DBuf<double2> r, d, t, hb;
+        CK(r.alloc(N)); CK(d.alloc(N)); CK(t.alloc(N)); CK(hb.alloc(1));
+        CK(cudaMemsetAsync(x.p, 0, sizeof(double2) * N, s));
+        auto nrm = [&](const double2* v, double& out) -> int {
+            launch_multidot(v, N, 1, v, N, hb.p, s);
+            double2 q; CK(cudaMemcpyAsync(&q, hb.p, sizeof(double2), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            out = std::sqrt(std::max(q.x, 0.0));
+            return IFGF2D_OK;
+        };
+        double bn; if ((rc = nrm(b.p, bn))) return rc;
+        CK(cudaMemcpyAsync(r.p, b.p, sizeof(double2) * N, cudaMemcpyDeviceToDevice, s));
+        double rn = bn;
+        est = bn > 0 ? 1.0 : 0.0;
+        for (int outer = 0; outer < 30 && est >= tol && iters < max_iters; ++outer) {
+            // the inner solve only has to beat the complex64 operator's own accuracy
+            const double inner_tol = std::max(1e-5, 0.5 * tol * bn / rn);
+            int it = 0; double e = 0.0;
+            if ((rc = gmres_core(ctx, G, r.p, d.p, IFGF2D_APPLY_IFGF_MIXED, inner_tol, restart, max_iters - iters, it, e))) return rc;
+            iters += it;
+            {
+                double2 one = make_double2(1.0, 0.0);
+                CK(cudaMemcpyAsync(hb.p, &one, sizeof(double2), cudaMemcpyHostToDevice, s));
+                launch_multi_axpy(d.p, N, 1, hb.p, 1.0, N, x.p, s);   // x += d
+            }
+            if ((rc = apply_dev(ctx, x.p, t.p, IFGF2D_APPLY_IFGF))) return rc;
+            launch_sub(b.p, t.p, N, r.p, s);
+            if ((rc = nrm(r.p, rn))) return rc;
+            est = rn / bn;
+        }
     }
     CK(cudaMemcpyAsync(xout, x.p, sizeof(double2) * N, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

@@ -29,8 +29,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // ------------------------------------------------------------------ set-up: near field
-// One CTA per leaf box: block [source][target] over the neighbour boxes' points, zero for
-// excluded pairs (self, same patch, near-singular patches of the target).
+// One CTA per leaf box: block [target][source] over the neighbour boxes' points (sources in
+// neighbour order), zero for excluded pairs (self, same patch, near-singular patches of the
+// target).
 __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr_box,
                              const long long* __restrict__ near_off, const double* __restrict__ xs,
@@ -44,7 +45,7 @@ __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __re
     for (int q = n0; q < n1; ++q) nsrc += leaf_count[nbr_box[q]];
     const long long total = (long long)nsrc * nB;
     for (long long e = threadIdx.x; e < total; e += blockDim.x) {
-        const int s = (int)(e / nB), t = (int)(e % nB);
+        const int t = (int)(e / nsrc), s = (int)(e % nsrc);
         int rem = s, j = -1;
         for (int q = n0; q < n1; ++q) {
             const int c = leaf_count[nbr_box[q]];
@@ -109,16 +110,6 @@ __global__ void k_sing_apply(const double2* __restrict__ x, const double2* __res
     y[o] = acc;
 }
 
-__global__ void k_intensities(const double2* __restrict__ x, const double* __restrict__ wq, const long long* __restrict__ perm,
-                              int N, double2* __restrict__ rho) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const long long o = perm ? perm[i] : i;
-    const double2 v = x[o];
-    const double w = wq[o];
-    rho[i] = make_double2(v.x * w, v.y * w);
-}
-
 // ------------------------------------------------------------------ apply: direct far sum
 // Tiled all-pairs sum, one thread per target, sources staged in shared memory 128 at a time.
 // A tile whose patch range holds neither the target's patch nor a patch the target is
@@ -165,108 +156,6 @@ __global__ void __launch_bounds__(kTile) k_direct_far(const double* __restrict__
     if (active) {
         if (accumulate) { double2 v = y[i]; y[i] = cadd(v, acc); } else y[i] = acc;
     }
-}
-
-// ------------------------------------------------------------------ apply: IFGF
-template <int PS, int PA>
-__device__ __forceinline__ double2 interp_eval(const double2* __restrict__ c, double s, double th) {
-    double Ts[PS], Tt[PA];
-    Ts[0] = 1.0; if (PS > 1) Ts[1] = s;
-#pragma unroll
-    for (int i = 2; i < PS; ++i) Ts[i] = 2.0 * s * Ts[i - 1] - Ts[i - 2];
-    Tt[0] = 1.0; if (PA > 1) Tt[1] = th;
-#pragma unroll
-    for (int i = 2; i < PA; ++i) Tt[i] = 2.0 * th * Tt[i - 1] - Tt[i - 2];
-    double2 r = make_double2(0.0, 0.0);
-#pragma unroll
-    for (int a = 0; a < PA; ++a)
-#pragma unroll
-        for (int q = 0; q < PS; ++q) {
-            const double w = Tt[a] * Ts[q];
-            const double2 v = c[a * PS + q];
-            r.x = fma(w, v.x, r.x); r.y = fma(w, v.y, r.y);
-        }
-    return r;
-}
-
-// one warp per leaf cone; lane m accumulates coefficient m over the box's sources
-__global__ void k_leaf_apply(const int* __restrict__ cone_box, int ncones, int cone_base, const int* __restrict__ leaf_start,
-                             const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
-                             const double2* __restrict__ L, const double2* __restrict__ rho, int P, double2* __restrict__ coef) {
-    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (c >= ncones || lane >= P) return;
-    const int b = cone_box[c];
-    const int n = leaf_count[b], s0 = leaf_start[b];
-    const double2* Lc = L + leaf_off[c];
-    double2 acc = make_double2(0.0, 0.0);
-    for (int s = 0; s < n; ++s) cfma(acc, Lc[(long long)s * P + lane], rho[s0 + s]);
-    coef[(long long)(cone_base + c) * P + lane] = acc;
-}
-
-// one warp per parent cone; lane = parent interpolation node (BoxTree.h:767-868), then the
-// values-to-coefficients map through shared memory
-template <int PS, int PA>
-__global__ void k_propagate(int pbegin, int pend, const long long* __restrict__ pp_ptr, const int* __restrict__ pp_nchild,
-                            const PropEntryD* __restrict__ pp, const double* __restrict__ Gm, double2* __restrict__ coef) {
-    constexpr int P = PS * PA;
-    __shared__ double sG[P * P];
-    __shared__ double2 sv[8][P];
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) sG[i] = Gm[i];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pc = pbegin + blockIdx.x * (blockDim.x >> 5) + warp;
-    if (pc >= pend) return;
-    const long long e0 = pp_ptr[pc];
-    const int nch = pp_nchild[pc];
-    if (lane < P) {
-        double2 v = make_double2(0.0, 0.0);
-        for (int ch = 0; ch < nch; ++ch) {
-            const PropEntryD E = pp[e0 + (long long)ch * P + lane];
-            const double2 it = interp_eval<PS, PA>(coef + (long long)E.child_cone * P, E.s, E.th);
-            cfma(v, it, make_double2(E.wr, E.wi));
-        }
-        sv[warp][lane] = v;
-    }
-    __syncwarp();
-    if (lane < P) {
-        double2 acc = make_double2(0.0, 0.0);
-#pragma unroll 5
-        for (int q = 0; q < P; ++q) { const double g = sG[lane * P + q]; acc.x = fma(g, sv[warp][q].x, acc.x); acc.y = fma(g, sv[warp][q].y, acc.y); }
-        coef[(long long)pc * P + lane] = acc;
-    }
-}
-
-// one thread per Morton-sorted target: near field, then every level's cousin interpolants,
-// then the result is added to y at the target's original index
-template <int PS, int PA>
-__global__ void k_final(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
-                        const int* __restrict__ leaf_count, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr_box,
-                        const long long* __restrict__ near_off, const double2* __restrict__ near, const double2* __restrict__ rho,
-                        const int* __restrict__ ip_ptr, const InterpEntryD* __restrict__ ip, const double2* __restrict__ coef,
-                        const long long* __restrict__ sorting, double2* __restrict__ y) {
-    constexpr int P = PS * PA;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const int b = point_leaf[i];
-    const int nB = leaf_count[b], t = i - leaf_start[b];
-    const double2* nb = near + near_off[b] + t;
-    double2 acc = make_double2(0.0, 0.0);
-    long long sg = 0;
-    for (int q = nbr_ptr[b]; q < nbr_ptr[b + 1]; ++q) {
-        const int bb = nbr_box[q];
-        const int c = leaf_count[bb], s0 = leaf_start[bb];
-        for (int s = 0; s < c; ++s) cfma(acc, nb[(sg + s) * nB], rho[s0 + s]);
-        sg += c;
-    }
-    for (int e = ip_ptr[i]; e < ip_ptr[i + 1]; ++e) {
-        const InterpEntryD E = ip[e];
-        const double2 it = interp_eval<PS, PA>(coef + (long long)E.cone * P, E.s, E.th);
-        cfma(acc, it, make_double2(E.fr, E.fi));
-    }
-    const long long o = sorting[i];
-    const double2 v = y[o];
-    y[o] = cadd(v, acc);
 }
 
 // ------------------------------------------------------------------ tests and GMRES helpers
@@ -356,41 +245,11 @@ void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, c
                        int N, int Np, double2* y, cudaStream_t s) {
     k_sing_apply<<<nblk(N, 128), 128, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, y);
 }
-void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s) {
-    k_intensities<<<nblk(N, 256), 256, 0, s>>>(x, wq, perm, N, rho);
-}
 void launch_direct_far(const double* tx, const double* ty, int nt, const int* t_patch, const int* t_nsp_ptr, const int* t_nsp,
                        const double* sx, const double* sy, const int* s_patch, const double2* rho, int ns, double k,
                        double2* y, int accumulate, cudaStream_t s) {
     if (nt <= 0) return;
     k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, s_patch, rho, ns, k, y, accumulate);
-}
-void launch_leaf_apply(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
-                       const long long* leaf_off, const double2* L, const double2* rho, int P, double2* coef, cudaStream_t s) {
-    if (ncones <= 0) return;
-    k_leaf_apply<<<nblk((long long)ncones * 32, 128), 128, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count, leaf_off, L, rho, P, coef);
-}
-
-#define IFGF_DISPATCH_P(PS_, PA_, ...)                                              \
-    if (PS_ == 5 && PA_ == 5) { constexpr int PS = 5, PA = 5; __VA_ARGS__; }        \
-    else if (PS_ == 5 && PA_ == 7) { constexpr int PS = 5, PA = 7; __VA_ARGS__; }   \
-    else if (PS_ == 3 && PA_ == 5) { constexpr int PS = 3, PA = 5; __VA_ARGS__; }   \
-    else if (PS_ == 3 && PA_ == 3) { constexpr int PS = 3, PA = 3; __VA_ARGS__; }   \
-    else if (PS_ == 7 && PA_ == 7) { constexpr int PS = 7, PA = 7; __VA_ARGS__; }   \
-    else if (PS_ == 4 && PA_ == 4) { constexpr int PS = 4, PA = 4; __VA_ARGS__; }   \
-    else if (PS_ == 6 && PA_ == 6) { constexpr int PS = 6, PA = 6; __VA_ARGS__; }
-
-void launch_propagate(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropEntryD* pp, int Ps,
-                      int Pang, const double* Gm, double2* coef, cudaStream_t s) {
-    if (pend <= pbegin) return;
-    const int warps = 4;
-    IFGF_DISPATCH_P(Ps, Pang, (k_propagate<PS, PA><<<nblk(pend - pbegin, warps), warps * 32, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gm, coef)));
-}
-void launch_final(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
-                  const int* nbr_box, const long long* near_off, const double2* near, const double2* rho, const int* ip_ptr,
-                  const InterpEntryD* ip, const double2* coef, int Ps, int Pang, const long long* sorting, double2* y,
-                  cudaStream_t s) {
-    IFGF_DISPATCH_P(Ps, Pang, (k_final<PS, PA><<<nblk(N, 128), 128, 0, s>>>(N, point_leaf, leaf_start, leaf_count, nbr_ptr, nbr_box, near_off, near, rho, ip_ptr, ip, coef, sorting, y)));
 }
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s) {
     if (n <= 0) return;

@@ -30,8 +30,22 @@ struct LeafNode {
     double ir, ii;
 };
 
-struct InterpEntryD { int cone; int pad; double s, th, fr, fi; };
-struct PropEntryD { int child_cone; int pad; double s, th, wr, wi; };
+// complex vector type of a real type
+template <typename R> struct Cx;
+template <> struct Cx<double> { using V = double2; };
+template <> struct Cx<float> { using V = float2; };
+template <typename R> using V2 = typename Cx<R>::V;
+
+// one (target, level, cousin) interpolation term: cone id, Chebyshev (s, theta), e^{ikr}/sqrt r
+template <typename R> struct InterpE;
+template <> struct InterpE<double> { int cone; int pad; double s, th, fr, fi; };
+template <> struct InterpE<float> { int cone; float s, th, fr, fi; };
+// one (parent cone, child, node) propagation term: child cone id, (s, theta), factor ratio
+template <typename R> struct PropE;
+template <> struct PropE<double> { int child_cone; int pad; double s, th, wr, wi; };
+template <> struct PropE<float> { int child_cone; float s, th, wr, wi; };
+using InterpEntryD = InterpE<double>;
+using PropEntryD = PropE<double>;
 
 constexpr int kMaxP = 64;          // Ps * Pang limit of the device interpolator
 
@@ -52,19 +66,29 @@ void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, c
 // ---------------- per-apply kernels ----------------
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col,
                        const RPColumn* cols, int N, int Np, double2* y, cudaStream_t s);
-void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s);
 void launch_direct_far(const double* tx, const double* ty, int ntarget, const int* t_patch, const int* t_nsp_ptr,
                        const int* t_nsp, const double* sx, const double* sy, const int* s_patch,
                        const double2* rho, int nsource, double k, double2* y, int accumulate, cudaStream_t s);
-void launch_leaf_apply(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
-                       const long long* leaf_off, const double2* L, const double2* rho, int P, double2* coef,
-                       cudaStream_t s);
-void launch_propagate(int parent_begin, int parent_end, const long long* pp_ptr, const int* pp_nchild,
-                      const PropEntryD* pp, int Ps, int Pang, const double* Gm, double2* coef, cudaStream_t s);
-void launch_final(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
-                  const int* nbr_box, const long long* near_off, const double2* near, const double2* rho,
-                  const int* ip_ptr, const InterpEntryD* ip, const double2* coef, int Ps, int Pang,
-                  const long long* sorting, double2* y, cudaStream_t s);
+
+// precision-templated IFGF apply (ifgf_apply.cu); R = double (plain) or float (mixed)
+template <typename R>
+void launch_intensities_t(const double2* x, const double* wq, const long long* perm, int N, V2<R>* rho, cudaStream_t s);
+template <typename R>
+void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s);
+template <typename R>
+void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
+                        int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s);
+template <typename R>
+void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
+                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,
+                    const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
+                    const long long* sorting, double2* y, cudaStream_t s);
+void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s);
+// direct path intensities (patch order), as in ForwardMap::compute_intensities
+inline void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s) {
+    launch_intensities_t<double>(x, wq, perm, N, rho, s);
+}
 
 // ---------------- tests / GMRES helpers ----------------
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s);

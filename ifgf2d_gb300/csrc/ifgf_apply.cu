@@ -1,0 +1,247 @@
+// ifgf_apply.cu -- per-apply IFGF kernels, templated on the arithmetic type.
+//
+// R = double: the plain form (complex128 tables, FP64 arithmetic).
+// R = float : the mixed form (complex64 copies of the same FP64-computed tables, FP32
+//             arithmetic; the rectangular-polar correction stays FP64).
+//
+//   k_intensities  density * quadrature weight, Morton permutation   ForwardMap.tpp:425-435, BoxTree.h:954-963
+//   k_leaf_apply   leaf cone coefficients (one thread per cone x coefficient)      BoxTree.h:685-762
+//   k_propagate    child -> parent coefficients (one thread per cone x node),
+//                  separable values->coefficients map                             BoxTree.h:767-868, Interpolator.h:81-120
+//   k_final        near field + every level's cousin interpolants, one warp per target,
+//                  result added to y at the target's original index               BoxTree.h:614-683, 876-937, 1063-1069
+#include "ifgf2d_kernels.cuh"
+
+namespace ifgf {
+
+__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename R>
+__device__ __forceinline__ void cmac(V2<R>& acc, V2<R> a, V2<R> b) {
+    acc.x = rfma(a.x, b.x, rfma(-a.y, b.y, acc.x));
+    acc.y = rfma(a.x, b.y, rfma(a.y, b.x, acc.y));
+}
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// sum_a T_a(th) sum_q T_q(s) c[a*PS + q]  (Interpolator.h:55-77, evaluated separably)
+template <typename R, int PS, int PA>
+__device__ __forceinline__ V2<R> interp_eval(const V2<R>* __restrict__ c, R s, R th) {
+    R Ts[PS], Tt[PA];
+    Ts[0] = R(1); if (PS > 1) Ts[1] = s;
+#pragma unroll
+    for (int i = 2; i < PS; ++i) Ts[i] = R(2) * s * Ts[i - 1] - Ts[i - 2];
+    Tt[0] = R(1); if (PA > 1) Tt[1] = th;
+#pragma unroll
+    for (int i = 2; i < PA; ++i) Tt[i] = R(2) * th * Tt[i - 1] - Tt[i - 2];
+    V2<R> r; r.x = R(0); r.y = R(0);
+#pragma unroll
+    for (int a = 0; a < PA; ++a) {
+        V2<R> u; u.x = R(0); u.y = R(0);
+#pragma unroll
+        for (int q = 0; q < PS; ++q) {
+            const V2<R> v = c[a * PS + q];
+            u.x = rfma(Ts[q], v.x, u.x); u.y = rfma(Ts[q], v.y, u.y);
+        }
+        r.x = rfma(Tt[a], u.x, r.x); r.y = rfma(Tt[a], u.y, r.y);
+    }
+    return r;
+}
+
+template <typename R>
+__global__ void k_intensities_t(const double2* __restrict__ x, const double* __restrict__ wq, const long long* __restrict__ perm,
+                                int N, V2<R>* __restrict__ rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const long long o = perm ? perm[i] : i;
+    const double2 v = x[o];
+    const double w = wq[o];
+    V2<R> r; r.x = (R)(v.x * w); r.y = (R)(v.y * w);
+    rho[i] = r;
+}
+
+// thread = (leaf cone, coefficient); 256/P cones per block
+template <typename R>
+__global__ void k_leaf_apply_t(const int* __restrict__ cone_box, int ncones, int cone_base, const int* __restrict__ leaf_start,
+                               const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
+                               const V2<R>* __restrict__ L, const V2<R>* __restrict__ rho, int P, V2<R>* __restrict__ coef) {
+    const int cpb = blockDim.x / P;
+    const int local = threadIdx.x / P, m = threadIdx.x - local * P;
+    const int c = blockIdx.x * cpb + local;
+    if (local >= cpb || c >= ncones) return;
+    const int b = cone_box[c];
+    const int n = leaf_count[b], s0 = leaf_start[b];
+    const V2<R>* Lc = L + leaf_off[c] + m;
+    const V2<R>* rh = rho + s0;
+    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    int s = 0;
+    for (; s + 1 < n; s += 2) {
+        const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
+        const V2<R> r0 = rh[s], r1 = rh[s + 1];
+        cmac<R>(acc, l0, r0); cmac<R>(acc, l1, r1);
+    }
+    if (s < n) cmac<R>(acc, Lc[(long long)s * P], rh[s]);
+    coef[(long long)(cone_base + c) * P + m] = acc;
+}
+
+// thread = (parent cone, interpolation node); CPB cones per block.  Gsep = [PS x PS radial
+// map | PA x PA angular map] of the values->coefficients transform, normalisation included.
+template <typename R, int PS, int PA>
+__global__ void __launch_bounds__(256) k_propagate_t(int pbegin, int pend, const long long* __restrict__ pp_ptr,
+                                                     const int* __restrict__ pp_nchild, const PropE<R>* __restrict__ pp,
+                                                     const R* __restrict__ Gsep, V2<R>* __restrict__ coef) {
+    constexpr int P = PS * PA, CPB = 256 / P;
+    __shared__ V2<R> sv[CPB][P];
+    __shared__ V2<R> su[CPB][P];
+    __shared__ R sGs[PS * PS], sGa[PA * PA];
+    for (int i = threadIdx.x; i < PS * PS; i += blockDim.x) sGs[i] = Gsep[i];
+    for (int i = threadIdx.x; i < PA * PA; i += blockDim.x) sGa[i] = Gsep[PS * PS + i];
+    const int local = threadIdx.x / P, pt = threadIdx.x - local * P;
+    const int pc = pbegin + blockIdx.x * CPB + local;
+    const bool active = local < CPB && pc < pend;
+    if (active) {
+        const long long e0 = pp_ptr[pc];
+        const int nch = pp_nchild[pc];
+        V2<R> v; v.x = R(0); v.y = R(0);
+        for (int ch = 0; ch < nch; ++ch) {
+            const PropE<R> E = pp[e0 + (long long)ch * P + pt];
+            const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.child_cone * P, E.s, E.th);
+            V2<R> w; w.x = E.wr; w.y = E.wi;
+            cmac<R>(v, it, w);
+        }
+        sv[local][pt] = v;
+    }
+    __syncthreads();
+    const int m = pt % PS, l = pt / PS;
+    if (active) {            // u[l][m] = sum_k Gs[m][k] v[l*PS + k]
+        V2<R> u; u.x = R(0); u.y = R(0);
+#pragma unroll
+        for (int k = 0; k < PS; ++k) {
+            const R g = sGs[m * PS + k];
+            const V2<R> v = sv[local][l * PS + k];
+            u.x = rfma(g, v.x, u.x); u.y = rfma(g, v.y, u.y);
+        }
+        su[local][l * PS + m] = u;
+    }
+    __syncthreads();
+    if (active) {            // c[n][m] = sum_l Ga[n][l] u[l][m], stored at n*PS + m
+        const int n = l;
+        V2<R> c; c.x = R(0); c.y = R(0);
+#pragma unroll
+        for (int q = 0; q < PA; ++q) {
+            const R g = sGa[n * PA + q];
+            const V2<R> u = su[local][q * PS + m];
+            c.x = rfma(g, u.x, c.x); c.y = rfma(g, u.y, c.y);
+        }
+        coef[(long long)pc * P + n * PS + m] = c;
+    }
+}
+
+// one warp per Morton-sorted target; near row layout [target][neighbour sources]
+template <typename R, int PS, int PA>
+__global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
+                                                 const int* __restrict__ leaf_count, const int* __restrict__ nbr_ptr,
+                                                 const int* __restrict__ nbr_box, const int* __restrict__ near_rowlen,
+                                                 const long long* __restrict__ near_off, const V2<R>* __restrict__ near,
+                                                 const V2<R>* __restrict__ rho, const int* __restrict__ ip_ptr,
+                                                 const InterpE<R>* __restrict__ ip, const V2<R>* __restrict__ coef,
+                                                 const long long* __restrict__ sorting, double2* __restrict__ y) {
+    constexpr int P = PS * PA;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= N) return;
+    const int b = point_leaf[i];
+    const int t = i - leaf_start[b];
+    const V2<R>* row = near + near_off[b] + (long long)t * near_rowlen[b];
+    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    int sg = 0;
+    for (int q = nbr_ptr[b]; q < nbr_ptr[b + 1]; ++q) {
+        const int bb = nbr_box[q];
+        const int c = leaf_count[bb], s0 = leaf_start[bb];
+        for (int s = lane; s < c; s += 32) cmac<R>(acc, row[sg + s], rho[s0 + s]);
+        sg += c;
+    }
+    for (int e = ip_ptr[i] + lane; e < ip_ptr[i + 1]; e += 32) {
+        const InterpE<R> E = ip[e];
+        const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.cone * P, E.s, E.th);
+        V2<R> f; f.x = E.fr; f.y = E.fi;
+        cmac<R>(acc, it, f);
+    }
+    acc.x = warp_sum_r<R>(acc.x);
+    acc.y = warp_sum_r<R>(acc.y);
+    if (lane == 0) {
+        const long long o = sorting[i];
+        double2 v = y[o];
+        v.x += (double)acc.x; v.y += (double)acc.y;
+        y[o] = v;
+    }
+}
+
+__global__ void k_d2f(const double2* __restrict__ a, long long n, float2* __restrict__ b) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// ------------------------------------------------------------------ launchers
+static inline unsigned nblk_a(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+#define IFGF_DISPATCH_P(PS_, PA_, ...)                                              \
+    if (PS_ == 5 && PA_ == 5) { constexpr int PS = 5, PA = 5; __VA_ARGS__; }        \
+    else if (PS_ == 5 && PA_ == 7) { constexpr int PS = 5, PA = 7; __VA_ARGS__; }   \
+    else if (PS_ == 3 && PA_ == 5) { constexpr int PS = 3, PA = 5; __VA_ARGS__; }   \
+    else if (PS_ == 3 && PA_ == 3) { constexpr int PS = 3, PA = 3; __VA_ARGS__; }   \
+    else if (PS_ == 7 && PA_ == 7) { constexpr int PS = 7, PA = 7; __VA_ARGS__; }   \
+    else if (PS_ == 4 && PA_ == 4) { constexpr int PS = 4, PA = 4; __VA_ARGS__; }   \
+    else if (PS_ == 6 && PA_ == 6) { constexpr int PS = 6, PA = 6; __VA_ARGS__; }
+
+template <typename R>
+void launch_intensities_t(const double2* x, const double* wq, const long long* perm, int N, V2<R>* rho, cudaStream_t s) {
+    k_intensities_t<R><<<nblk_a(N, 256), 256, 0, s>>>(x, wq, perm, N, rho);
+}
+template <typename R>
+void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s) {
+    if (ncones <= 0) return;
+    const int cpb = 256 / P;
+    k_leaf_apply_t<R><<<nblk_a(ncones, cpb), cpb * P, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count, leaf_off, L, rho, P, coef);
+}
+template <typename R>
+void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps, int Pang,
+                        const R* Gsep, V2<R>* coef, cudaStream_t s) {
+    if (pend <= pbegin) return;
+    IFGF_DISPATCH_P(Ps, Pang, {
+        constexpr int CPB = 256 / (PS * PA);
+        k_propagate_t<R, PS, PA><<<nblk_a(pend - pbegin, CPB), CPB * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);
+    });
+}
+template <typename R>
+void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
+                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
+                    const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang, const long long* sorting,
+                    double2* y, cudaStream_t s) {
+    IFGF_DISPATCH_P(Ps, Pang, (k_final_t<R, PS, PA><<<nblk_a((long long)N * 32, 256), 256, 0, s>>>(
+                                   N, point_leaf, leaf_start, leaf_count, nbr_ptr, nbr_box, near_rowlen, near_off, near, rho,
+                                   ip_ptr, ip, coef, sorting, y)));
+}
+void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
+    if (n > 0) k_d2f<<<nblk_a(n, 256), 256, 0, s>>>(a, n, b);
+}
+
+#define IFGF_INSTANTIATE(R)                                                                                          \
+    template void launch_intensities_t<R>(const double2*, const double*, const long long*, int, V2<R>*, cudaStream_t); \
+    template void launch_leaf_apply_t<R>(const int*, int, int, const int*, const int*, const long long*, const V2<R>*,  \
+                                         const V2<R>*, int, V2<R>*, cudaStream_t);                                    \
+    template void launch_propagate_t<R>(int, int, const long long*, const int*, const PropE<R>*, int, int, const R*,   \
+                                        V2<R>*, cudaStream_t);                                                         \
+    template void launch_final_t<R>(int, const int*, const int*, const int*, const int*, const int*, const int*,       \
+                                    const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,       \
+                                    const V2<R>*, int, int, const long long*, double2*, cudaStream_t);
+IFGF_INSTANTIATE(double)
+IFGF_INSTANTIATE(float)
+
+}  // namespace ifgf

@@ -35,6 +35,9 @@ extern "C" {
 /* apply modes */
 #define IFGF2D_APPLY_DIRECT 0 /* ForwardMap::compute_Ax_unacc  (ForwardMap/ForwardMap.tpp:517-540) */
 #define IFGF2D_APPLY_IFGF 1   /* ForwardMap::compute_Ax_acc    (ForwardMap/ForwardMap.tpp:609-655) */
+#define IFGF2D_APPLY_IFGF_MIXED 2 /* compute_Ax_acc with the IFGF far field in complex64 (FP32
+                                   * arithmetic on tables computed in FP64); the rectangular-polar
+                                   * correction stays FP64.  No counterpart in the reference. */
 
 typedef struct ifgf2d_curve {
     int type;        /* IFGF2D_CURVE_* */
@@ -106,6 +109,9 @@ int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intensities, double* y);
 
 /* ForwardMap::solve (ForwardMap/ForwardMap.tpp:658-697): GMRES on the device, initial guess 0,
  * stop when the residual estimate |w_k|/||r0|| < tol, restart after `restart` steps.
+ * mode IFGF2D_APPLY_IFGF_MIXED: FP64 iterative refinement -- the residual b - A x is formed with
+ * the FP64 IFGF operator, corrections come from GMRES on the complex64 operator, and the stop
+ * test is the FP64 relative residual; *iters counts inner GMRES iterations.
  * Returns IFGF2D_ERR_NOCONV (with x filled) when max_iters is reached first. */
 int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* x, int mode, double tol, int restart,
                  int max_iters, int* iters, double* est_error);

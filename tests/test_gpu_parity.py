@@ -106,6 +106,27 @@ def test_gpu_ifgf_against_direct_config2_size(lib, oracle):
     assert rel(fm.compute_Ax_acc(a * d + b * d2), a * ya + b * fm.compute_Ax_acc(d2)) < 1e-12
 
 
+def test_gpu_mixed_ifgf_apply_close_to_fp64(lib, oracle):
+    """complex64 far field on FP64-computed tables: within 2e-6 of the FP64 apply."""
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 500.0, Np=16, patches_per_curve=512)
+    fm.precomps_and_setup(500.0, 0)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    y64, y32 = fm.compute_Ax_acc(d), fm.compute_Ax_acc(d, mixed=True)
+    assert rel(y32, y64) < 2e-6
+
+
+def test_gpu_mixed_refinement_solve(lib):
+    """FP64 iterative refinement around complex64 inner GMRES reaches the FP64 tolerance."""
+    k = 40.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
+    b = -np.exp(1j * k * fm.xs_)
+    x = fm.solve(b, k, nlevels=0, accelerated=True, tol=1e-8, max_iters=4000, restart=300, mixed=True)
+    assert fm.last_solve["converged"]
+    assert rel(fm.compute_Ax_acc(x), b) < 1e-8
+    x64 = fm.gmres(b, accelerated=True, tol=1e-8, max_iters=4000, restart=300)
+    assert rel(x, x64) < 1e-5
+
+
 def test_gpu_gmres_direct_config1_matches_oracle(lib, oracle):
     """Device GMRES (CGS2 Arnoldi + Givens) vs the oracle's Householder GMRES.
 
