@@ -3,7 +3,7 @@
 
 Workload (the configuration the headline metric is quoted on): Colton-Kress kite
 x(t) = (cos t + 0.65 cos 2t - 0.65, 1.5 sin t), k = 500, 512 equal-parameter patches x 16
-Fejer nodes (N = 8192), single-layer operator, IFGF with 5 x 5 Chebyshev nodes per cone,
+Fejer nodes (N = 8192), combined-field operator (1/2 I + K - i k S), IFGF with 5 x 5 Chebyshev nodes per cone,
 the deepest tree that keeps singular points in the leaf neighbourhood, FP64 (plain form).
 A step is one forward map y = A x (singular correction + IFGF far field) on a seeded
 mt19937(0) density.  Synthetic geometry, no dataset.
@@ -33,9 +33,10 @@ sys.path.insert(0, ROOT)
 
 K_WAVE = 500.0
 NPATCH, NP, DELTA = 512, 16, 0.01
-METRIC = "IFGF matvecs/s (kite k=500, N=8192, FP64 single layer)"
+METRIC = "IFGF matvecs/s (kite k=500, N=8192, FP64 combined field)"
 UNIT = "matvec/s"
-WORKLOAD = "kite k=500, 512 equal patches x 16 Fejer nodes (N=8192), IFGF 5x5 cones, FP64"
+WORKLOAD = ("kite k=500, 512 equal patches x 16 Fejer nodes (N=8192), combined field (1/2 I + K - i k S), "
+            "IFGF 5x5 cones, FP64")
 
 
 def parse():
@@ -110,7 +111,7 @@ class ClockSampler:
 # ---------------------------------------------------------------- workload
 def make_ours():
     import ifgf2d_gb300 as G
-    fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, K_WAVE, Np=NP, patches_per_curve=NPATCH)
+    fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, K_WAVE, Np=NP, patches_per_curve=NPATCH, formulation="combined")
     fm.precomps_and_setup(K_WAVE, 0)
     return G, fm
 
@@ -275,7 +276,7 @@ def time_oracle(budget_s=12.0, max_steps=None):
     """CPU oracle (single-threaded restatement of the reference path) on the same workload."""
     from oracle import oracle as O
     O.build()
-    om = O.OracleForwardMap([O.curve_kite()], NP, DELTA, 1.0, K_WAVE, patches_per_curve=NPATCH)
+    om = O.OracleForwardMap([O.curve_kite()], NP, DELTA, 1.0, K_WAVE, patches_per_curve=NPATCH, formulation="combined")
     om.precompute(K_WAVE)
     import ifgf2d_gb300 as G
     # same tree depth rule as the product: deepest nlevels passing the neighbourhood check

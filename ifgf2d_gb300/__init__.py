@@ -138,10 +138,13 @@ class ForwardMap:
     ForwardMap(delta, curves, curve_touch_tracker, wavelengths_per_patch, patch_split_wavenumber, p=4)
     with ``Np``, ``Ps``, ``Pang`` given as keyword arguments (template parameters in C++).
     ``patches_per_curve > 0`` selects an equal-parameter split instead of the arc-length rule.
+    ``formulation="combined"`` selects the sound-soft combined field operator (1/2 I + K - i eta S)
+    with eta = ``coupling`` (eta = k when coupling <= 0); the default is the reference's single layer.
     """
 
     def __init__(self, delta, curves, curve_touch_tracker=(), wavelengths_per_patch=1.0,
-                 patch_split_wavenumber=1.0, p=4.0, *, Np=10, Ps=5, Pang=5, patches_per_curve=0):
+                 patch_split_wavenumber=1.0, p=4.0, *, Np=10, Ps=5, Pang=5, patches_per_curve=0,
+                 formulation="single_layer", coupling=0.0):
         L = _lib.load()
         curves = list(curves)
         if not curves:
@@ -149,7 +152,12 @@ class ForwardMap:
         carr = (_lib.Curve * len(curves))(*curves)
         jl = list(curve_touch_tracker)
         jarr = (_lib.Junction * max(len(jl), 1))(*jl) if jl else None
-        opt = _lib.Options(Np, delta, wavelengths_per_patch, patch_split_wavenumber, p, patches_per_curve, Ps, Pang)
+        forms = {"single_layer": _lib.SINGLE_LAYER, "combined": _lib.COMBINED}
+        if formulation not in forms:
+            raise ValueError(f"formulation must be one of {sorted(forms)}")
+        opt = _lib.Options(Np, delta, wavelengths_per_patch, patch_split_wavenumber, p, patches_per_curve, Ps, Pang,
+                           forms[formulation], float(coupling))
+        self.formulation = formulation
         h = ctypes.c_void_p()
         rc = L.ifgf2d_create(carr, len(curves), jarr, len(jl), ctypes.byref(opt), ctypes.byref(h))
         self._h = h.value

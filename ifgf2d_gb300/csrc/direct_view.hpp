@@ -22,6 +22,10 @@ struct DirectView {
     const int* patch_of = nullptr;
     const int* nsp_ptr = nullptr;        // per point: patches it is near-singular to
     const int* nsp = nullptr;
+    const double* nx = nullptr;          // unit normals (original order)
+    const double* ny = nullptr;
+    int form = 0;                        // IFGF2D_SINGLE_LAYER or IFGF2D_COMBINED
+    double eta = 0.0, half = 0.0;        // coupling and jump-term factor
 };
 
 // Fills `v` once the rectangular-polar weights are on the device; returns an IFGF2D status

@@ -75,6 +75,22 @@ __device__ __forceinline__ double2 green_sl(double dx, double dy, double k) {
     return make_double2(-0.25 * h.y, 0.25 * h.x);
 }
 
+// Combined-field kernel without the jump term, target minus source d = x - y, unit normal n
+// at the source y:  dPhi/dn_y - i eta Phi = (ik/4) H1(kr) (d.n)/r + (eta/4) H0(kr); 0 for r < 1e-14.
+__device__ __forceinline__ double2 green_cfie(double dx, double dy, double nx, double ny, double k, double eta) {
+    const double r = sqrt(dx * dx + dy * dy);
+    if (r < 1e-14) return make_double2(0.0, 0.0);
+    const double2 h0 = hankel1<0>(k * r);
+    const double2 h1 = hankel1<1>(k * r);
+    const double c = 0.25 * k * (dx * nx + dy * ny) / r;   // (ik/4)(d.n)/r = i c
+    return make_double2(-c * h1.y + 0.25 * eta * h0.x, c * h1.x + 0.25 * eta * h0.y);
+}
+
+// kernel of the chosen formulation (eta unused for the single layer)
+__device__ __forceinline__ double2 green_form(int form, double dx, double dy, double nx, double ny, double k, double eta) {
+    return form == 2 ? green_cfie(dx, dy, nx, ny, k, eta) : green_sl(dx, dy, k);
+}
+
 // e^{ikr}/sqrt(r) (GreenFunctions.hpp:125-131)
 __device__ __forceinline__ double2 factorization(double r, double k) {
     double s, c;

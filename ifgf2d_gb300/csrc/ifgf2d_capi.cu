@@ -53,8 +53,10 @@ struct ifgf2d_ctx {
     bool device_ready = false, precomputed = false, ifgf_ready = false;
     std::vector<int> h_nsp_ptr, h_nsp, h_srow_ptr, h_srow_col;
     int nlevels = 0;
+    int form = IFGF2D_SINGLE_LAYER;
+    double eta = 0.0;               // coupling of the combined formulation, resolved at precompute
     // geometry (original order)
-    DBuf<double> x, y, wq, edge;
+    DBuf<double> x, y, nx, ny, wq, edge;
     DBuf<int> patch_of;
     DBuf<DevCurve> curves;
     DBuf<DevPatch> patches;
@@ -69,7 +71,7 @@ struct ifgf2d_ctx {
     // IFGF tree
     Tree T;
     DBuf<long long> sorting;
-    DBuf<double> xs_s, ys_s;
+    DBuf<double> xs_s, ys_s, nxs_s, nys_s;
     DBuf<int> patch_s, nsp_ptr_s, nsp_s;
     DBuf<int> leaf_start, leaf_count, point_leaf, nbr_ptr, nbr_box;
     DBuf<long long> near_off;
@@ -122,6 +124,10 @@ extern "C" int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf
         const bool ok = (ps == 5 && pa == 5) || (ps == 5 && pa == 7) || (ps == 3 && pa == 5) || (ps == 3 && pa == 3) ||
                         (ps == 7 && pa == 7) || (ps == 4 && pa == 4) || (ps == 6 && pa == 6);
         if (!ok) { *out = ctx; ctx->err = "(Ps, Pang) must be one of (3,3) (3,5) (4,4) (5,5) (5,7) (6,6) (7,7)"; return IFGF2D_ERR_ARG; }
+        if (ctx->opt.formulation != IFGF2D_SINGLE_LAYER && ctx->opt.formulation != IFGF2D_COMBINED) {
+            *out = ctx; ctx->err = "formulation must be IFGF2D_SINGLE_LAYER or IFGF2D_COMBINED"; return IFGF2D_ERR_ARG;
+        }
+        ctx->form = ctx->opt.formulation;
     }
     std::string msg = discretise(curves, ncurves, junctions, njunctions, ctx->opt, ctx->D);
     if (!msg.empty()) {
@@ -180,6 +186,7 @@ static int ensure_device(ifgf2d_ctx* ctx) {
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     const Discretisation& D = ctx->D;
     CK(ctx->x.upload(D.x)); CK(ctx->y.upload(D.y)); CK(ctx->wq.upload(D.wq)); CK(ctx->edge.upload(D.edge_jac));
+    CK(ctx->nx.upload(D.nx)); CK(ctx->ny.upload(D.ny));
     CK(ctx->patch_of.upload(D.patch_of));
     std::vector<DevCurve> dc(D.curves.size());
     for (size_t c = 0; c < D.curves.size(); ++c) { dc[c].type = D.curves[c].type; dc[c].pad = 0; std::memcpy(dc[c].p, D.curves[c].p, sizeof(dc[c].p)); }
@@ -241,7 +248,9 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     const int ncols = (int)ctx->hcols.size();
     CK(ctx->M.alloc((size_t)ncols * D.Np));
     CK(ctx->W.alloc((size_t)ncols * D.Np));
-    launch_rp_precompute(ctx->cols.p, ncols, ctx->patches.p, ctx->curves.p, ctx->nsn.p, ctx->nsw.p, D.Np, D.p, k, ctx->M.p, ctx->stream);
+    ctx->eta = ctx->opt.coupling > 0 ? ctx->opt.coupling : k;
+    launch_rp_precompute(ctx->cols.p, ncols, ctx->patches.p, ctx->curves.p, ctx->nsn.p, ctx->nsw.p, D.Np, D.p, k, ctx->form,
+                         ctx->eta, ctx->M.p, ctx->stream);
     CK(cudaGetLastError());
     launch_rp_fold(ctx->M.p, ctx->cols.p, ncols, ctx->edge.p, ctx->patches.p, D.Np, ctx->W.p, ctx->stream);
     CK(cudaGetLastError());
@@ -320,6 +329,11 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         for (long long i = 0; i < N; ++i) { for (int p : per[i]) nl.push_back(p); nptr[i + 1] = (int)nl.size(); }
     }
     CK(ctx->sorting.upload(T.sorting)); CK(ctx->xs_s.upload(T.xs)); CK(ctx->ys_s.upload(T.ys));
+    {
+        std::vector<double> snx(N), sny(N);
+        for (long long i = 0; i < N; ++i) { snx[i] = D.nx[T.sorting[i]]; sny[i] = D.ny[T.sorting[i]]; }
+        CK(ctx->nxs_s.upload(snx)); CK(ctx->nys_s.upload(sny));
+    }
     CK(ctx->patch_s.upload(patch_s)); CK(ctx->nsp_ptr_s.upload(nptr)); CK(ctx->nsp_s.upload(nl));
     CK(ctx->leaf_start.upload(T.leaf_start)); CK(ctx->leaf_count.upload(T.leaf_count)); CK(ctx->point_leaf.upload(T.point_leaf));
     CK(ctx->nbr_ptr.upload(T.nbr_ptr)); CK(ctx->nbr_box.upload(T.nbr_box));
@@ -339,7 +353,8 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     }
     CK(ctx->near.alloc(noff[nleaf]));
     launch_near_setup(ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p, ctx->near_off.p, nleaf,
-                      ctx->xs_s.p, ctx->ys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k, ctx->near.p, ctx->stream);
+                      ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k,
+                      ctx->form, ctx->eta, ctx->near.p, ctx->stream);
     CK(cudaGetLastError());
     // values-to-coefficients matrix of the cone interpolant (Interpolator.h:81-120)
     {
@@ -382,7 +397,8 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     CK(ctx->leaf_cone_box.upload(LD.cone_box)); CK(ctx->leaf_off.upload(loff));
     CK(ctx->leafL.alloc(loff[ncl]));
     launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,
-                      ctx->xs_s.p, ctx->ys_s.p, P, k, ctx->Gm.p, ctx->leafL.p, ctx->stream);
+                      ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, P, k, ctx->form, ctx->eta, ctx->Gm.p,
+                      ctx->leafL.p, ctx->stream);
     CK(cudaGetLastError());
     // propagation and interpolation plans
     {
@@ -484,11 +500,12 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
-    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, ctx->stream);
+    const double half = ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0;
+    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, half, y, ctx->stream);
     if (mode != IFGF2D_APPLY_DIRECT) return far_apply(ctx, x, ctx->wq.p, y, mode, nullptr);
     launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
-    launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->patch_of.p,
-                      ctx->rho.p, N, ctx->k, y, 1, ctx->stream);
+    launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->nx.p, ctx->ny.p,
+                      ctx->patch_of.p, ctx->rho.p, N, ctx->k, ctx->form, ctx->eta, y, 1, ctx->stream);
     CK(cudaGetLastError());
     return IFGF2D_OK;
 }
@@ -507,7 +524,8 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
     for (int i = 0; i < 6; ++i) CK(cudaEventCreate(&ev[i]));
     cudaStream_t s = ctx->stream;
     CK(cudaEventRecord(ev[0], s));
-    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, y, s);
+    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np,
+                      ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0, y, s);
     CK(cudaEventRecord(ev[1], s));
     if (mode != IFGF2D_APPLY_DIRECT) {
         int rc = far_apply(ctx, x, ctx->wq.p, y, mode, ev + 2);
@@ -517,8 +535,8 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
         CK(cudaEventRecord(ev[2], s));
         CK(cudaEventRecord(ev[3], s));
         CK(cudaEventRecord(ev[4], s));
-        launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->patch_of.p,
-                          ctx->rho.p, N, ctx->k, y, 1, s);
+        launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->nx.p,
+                          ctx->ny.p, ctx->patch_of.p, ctx->rho.p, N, ctx->k, ctx->form, ctx->eta, y, 1, s);
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[5], s));
@@ -575,7 +593,8 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
     CK(tx.upload(xp, m)); CK(ty.upload(yp, m)); CK(o.alloc(m));
     CK(cudaMemcpyAsync(ctx->vin.p, dens, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
     launch_intensities(ctx->vin.p, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
-    launch_direct_far(tx.p, ty.p, (int)m, nullptr, nullptr, nullptr, ctx->x.p, ctx->y.p, nullptr, ctx->rho.p, N, ctx->k, o.p, 0, ctx->stream);
+    launch_direct_far(tx.p, ty.p, (int)m, nullptr, nullptr, nullptr, ctx->x.p, ctx->y.p, ctx->nx.p, ctx->ny.p, nullptr, ctx->rho.p, N,
+                      ctx->k, ctx->form, ctx->eta, o.p, 0, ctx->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, o.p, sizeof(double2) * m, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -794,6 +813,8 @@ int ifgf::direct_view(ifgf2d_ctx* ctx, ifgf::DirectView* v) {
     v->W = ctx->W.p; v->srow_ptr = ctx->srow_ptr.p; v->srow_col = ctx->srow_col.p; v->cols = ctx->cols.p;
     v->wq = ctx->wq.p; v->x = ctx->x.p; v->y = ctx->y.p; v->patch_of = ctx->patch_of.p;
     v->nsp_ptr = ctx->nsp_ptr.p; v->nsp = ctx->nsp.p;
+    v->nx = ctx->nx.p; v->ny = ctx->ny.p; v->form = ctx->form; v->eta = ctx->eta;
+    v->half = ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0;
     return IFGF2D_OK;
 }
 

@@ -35,9 +35,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr_box,
                              const long long* __restrict__ near_off, const double* __restrict__ xs,
-                             const double* __restrict__ ys, const int* __restrict__ patch_s,
-                             const int* __restrict__ nsp_ptr, const int* __restrict__ nsp, double k,
-                             double2* __restrict__ near) {
+                             const double* __restrict__ ys, const double* __restrict__ nxs, const double* __restrict__ nys,
+                             const int* __restrict__ patch_s, const int* __restrict__ nsp_ptr, const int* __restrict__ nsp,
+                             double k, int form, double eta, double2* __restrict__ near) {
     const int b = blockIdx.x;
     const int nB = leaf_count[b], t0 = leaf_start[b];
     const int n0 = nbr_ptr[b], n1 = nbr_ptr[b + 1];
@@ -56,7 +56,7 @@ __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __re
         double2 v = make_double2(0.0, 0.0);
         bool skip = (j == i) || (patch_s[j] == patch_s[i]);
         for (int q = nsp_ptr[i]; q < nsp_ptr[i + 1] && !skip; ++q) skip = (nsp[q] == patch_s[j]);
-        if (!skip) v = green_sl(xs[i] - xs[j], ys[i] - ys[j], k);
+        if (!skip) v = green_form(form, xs[i] - xs[j], ys[i] - ys[j], nxs[j], nys[j], k, eta);
         near[near_off[b] + e] = v;
     }
 }
@@ -68,7 +68,8 @@ __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __re
 __global__ void k_leaf_setup(const int* __restrict__ cone_box, int ncones, const int* __restrict__ leaf_start,
                              const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
                              const LeafNode* __restrict__ nodes, const double* __restrict__ xs,
-                             const double* __restrict__ ys, int P, double k, const double* __restrict__ Gm,
+                             const double* __restrict__ ys, const double* __restrict__ nxs, const double* __restrict__ nys,
+                             int P, double k, int form, double eta, const double* __restrict__ Gm,
                              double2* __restrict__ L) {
     extern __shared__ double sG[];
     for (int i = threadIdx.x; i < P * P; i += blockDim.x) sG[i] = Gm[i];
@@ -82,7 +83,7 @@ __global__ void k_leaf_setup(const int* __restrict__ cone_box, int ncones, const
     for (int s = warp; s < n; s += nw) {
         const int j = s0 + s;
         double2 h = make_double2(0.0, 0.0);
-        if (lane < P) h = cmul(green_sl(nd.x - xs[j], nd.y - ys[j], k), make_double2(nd.ir, nd.ii));
+        if (lane < P) h = cmul(green_form(form, nd.x - xs[j], nd.y - ys[j], nxs[j], nys[j], k, eta), make_double2(nd.ir, nd.ii));
         double2 acc = make_double2(0.0, 0.0);
         for (int q = 0; q < P; ++q) {
             const double hx = __shfl_sync(0xffffffffu, h.x, q), hy = __shfl_sync(0xffffffffu, h.y, q);
@@ -95,7 +96,7 @@ __global__ void k_leaf_setup(const int* __restrict__ cone_box, int ncones, const
 // ------------------------------------------------------------------ apply: singular part
 __global__ void k_sing_apply(const double2* __restrict__ x, const double2* __restrict__ W, const int* __restrict__ row_ptr,
                              const int* __restrict__ row_col, const RPColumn* __restrict__ cols, int N, int Np,
-                             double2* __restrict__ y) {
+                             double half, double2* __restrict__ y) {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= N) return;
     double2 acc = make_double2(0.0, 0.0);
@@ -107,6 +108,7 @@ __global__ void k_sing_apply(const double2* __restrict__ x, const double2* __res
         for (int kk = 0; kk < Np; ++kk) cfma(s, d[kk], w[kk]);
         acc = cadd(acc, s);
     }
+    if (half != 0.0) { const double2 v = x[o]; acc.x += half * v.x; acc.y += half * v.y; }   // jump term
     y[o] = acc;
 }
 
@@ -117,9 +119,11 @@ __global__ void k_sing_apply(const double2* __restrict__ x, const double2* __res
 constexpr int kTile = 128;
 __global__ void __launch_bounds__(kTile) k_direct_far(const double* __restrict__ tx, const double* __restrict__ ty, int nt,
                              const int* __restrict__ t_patch, const int* __restrict__ t_nsp_ptr, const int* __restrict__ t_nsp,
-                             const double* __restrict__ sx, const double* __restrict__ sy, const int* __restrict__ s_patch,
-                             const double2* __restrict__ rho, int ns, double k, double2* __restrict__ y, int accumulate) {
-    __shared__ double shx[kTile], shy[kTile];
+                             const double* __restrict__ sx, const double* __restrict__ sy, const double* __restrict__ snx,
+                             const double* __restrict__ sny, const int* __restrict__ s_patch,
+                             const double2* __restrict__ rho, int ns, double k, int form, double eta,
+                             double2* __restrict__ y, int accumulate) {
+    __shared__ double shx[kTile], shy[kTile], shnx[kTile], shny[kTile];
     __shared__ double2 shr[kTile];
     __shared__ int shp[kTile];
     const int i = blockIdx.x * kTile + threadIdx.x;
@@ -135,6 +139,7 @@ __global__ void __launch_bounds__(kTile) k_direct_far(const double* __restrict__
         if (threadIdx.x < n) {
             const int j = s0 + threadIdx.x;
             shx[threadIdx.x] = sx[j]; shy[threadIdx.x] = sy[j]; shr[threadIdx.x] = rho[j];
+            shnx[threadIdx.x] = snx ? snx[j] : 0.0; shny[threadIdx.x] = sny ? sny[j] : 0.0;
             shp[threadIdx.x] = s_patch ? s_patch[j] : -2;
         }
         __syncthreads();
@@ -143,13 +148,13 @@ __global__ void __launch_bounds__(kTile) k_direct_far(const double* __restrict__
         bool check = s_patch && (pi >= pa && pi <= pb);
         for (int q = 0; q < nex; ++q) check |= (ex[q] >= pa && ex[q] <= pb);
         if (!check) {
-            for (int j = 0; j < n; ++j) cfma(acc, green_sl(xi - shx[j], yi - shy[j], k), shr[j]);
+            for (int j = 0; j < n; ++j) cfma(acc, green_form(form, xi - shx[j], yi - shy[j], shnx[j], shny[j], k, eta), shr[j]);
         } else {
             for (int j = 0; j < n; ++j) {
                 const int pj = shp[j];
                 bool skip = (pj == pi);
                 for (int q = 0; q < nex; ++q) skip |= (ex[q] == pj);
-                if (!skip) cfma(acc, green_sl(xi - shx[j], yi - shy[j], k), shr[j]);
+                if (!skip) cfma(acc, green_form(form, xi - shx[j], yi - shy[j], shnx[j], shny[j], k, eta), shr[j]);
             }
         }
     }
@@ -230,26 +235,30 @@ __global__ void k_fp64_peak(double* out, int iters, double a, double b) {
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* nbr_ptr, const int* nbr_box,
-                       const long long* near_off, int nleaf, const double* xs, const double* ys, const int* patch_s,
-                       const int* nsp_ptr, const int* nsp, double k, double2* near, cudaStream_t s) {
+                       const long long* near_off, int nleaf, const double* xs, const double* ys, const double* nxs,
+                       const double* nys, const int* patch_s, const int* nsp_ptr, const int* nsp, double k, int form,
+                       double eta, double2* near, cudaStream_t s) {
     if (nleaf <= 0) return;
-    k_near_setup<<<nleaf, 256, 0, s>>>(leaf_start, leaf_count, nbr_ptr, nbr_box, near_off, xs, ys, patch_s, nsp_ptr, nsp, k, near);
+    k_near_setup<<<nleaf, 256, 0, s>>>(leaf_start, leaf_count, nbr_ptr, nbr_box, near_off, xs, ys, nxs, nys, patch_s, nsp_ptr,
+                                       nsp, k, form, eta, near);
 }
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
-                       const LeafNode* nodes, const double* xs, const double* ys, int P, double k, const double* Gm, double2* L,
-                       cudaStream_t s) {
+                       const LeafNode* nodes, const double* xs, const double* ys, const double* nxs, const double* nys, int P,
+                       double k, int form, double eta, const double* Gm, double2* L, cudaStream_t s) {
     if (ncones <= 0) return;
-    k_leaf_setup<<<ncones, 256, P * P * sizeof(double), s>>>(cone_box, ncones, leaf_start, leaf_count, leaf_off, nodes, xs, ys, P, k, Gm, L);
+    k_leaf_setup<<<ncones, 256, P * P * sizeof(double), s>>>(cone_box, ncones, leaf_start, leaf_count, leaf_off, nodes, xs, ys,
+                                                             nxs, nys, P, k, form, eta, Gm, L);
 }
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols,
-                       int N, int Np, double2* y, cudaStream_t s) {
-    k_sing_apply<<<nblk(N, 128), 128, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, y);
+                       int N, int Np, double half, double2* y, cudaStream_t s) {
+    k_sing_apply<<<nblk(N, 128), 128, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, half, y);
 }
 void launch_direct_far(const double* tx, const double* ty, int nt, const int* t_patch, const int* t_nsp_ptr, const int* t_nsp,
-                       const double* sx, const double* sy, const int* s_patch, const double2* rho, int ns, double k,
-                       double2* y, int accumulate, cudaStream_t s) {
+                       const double* sx, const double* sy, const double* snx, const double* sny, const int* s_patch,
+                       const double2* rho, int ns, double k, int form, double eta, double2* y, int accumulate, cudaStream_t s) {
     if (nt <= 0) return;
-    k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, s_patch, rho, ns, k, y, accumulate);
+    k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, snx, sny, s_patch, rho, ns, k,
+                                                   form, eta, y, accumulate);
 }
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s) {
     if (n <= 0) return;

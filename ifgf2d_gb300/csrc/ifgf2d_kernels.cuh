@@ -52,23 +52,27 @@ constexpr int kMaxP = 64;          // Ps * Pang limit of the device interpolator
 // ---------------- setup kernels ----------------
 void launch_rp_precompute(const RPColumn* cols, int ncols, const DevPatch* patches, const DevCurve* curves,
                           const double* ns_nodes, const double* ns_weights, int Np, double p, double k,
-                          double2* M, cudaStream_t s);
+                          int form, double eta, double2* M, cudaStream_t s);
 void launch_rp_fold(const double2* M, const RPColumn* cols, int ncols, const double* edge_jac, const DevPatch* patches,
                     int Np, double2* W, cudaStream_t s);
 void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* nbr_ptr, const int* nbr_box,
                        const long long* near_off, int nleaf, const double* xs, const double* ys,
-                       const int* patch_s, const int* nsp_ptr, const int* nsp, double k, double2* near,
-                       cudaStream_t s);
+                       const double* nxs, const double* nys, const int* patch_s, const int* nsp_ptr,
+                       const int* nsp, double k, int form, double eta, double2* near, cudaStream_t s);
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count,
-                       const long long* leaf_off, const LeafNode* nodes, const double* xs, const double* ys, int P,
-                       double k, const double* Gm, double2* L, cudaStream_t s);
+                       const long long* leaf_off, const LeafNode* nodes, const double* xs, const double* ys,
+                       const double* nxs, const double* nys, int P, double k, int form, double eta,
+                       const double* Gm, double2* L, cudaStream_t s);
 
 // ---------------- per-apply kernels ----------------
+// y = singular correction (+ half * x: the jump term of the combined formulation)
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col,
-                       const RPColumn* cols, int N, int Np, double2* y, cudaStream_t s);
+                       const RPColumn* cols, int N, int Np, double half, double2* y, cudaStream_t s);
+// sources with unit normals snx, sny (NULL for the single layer); form 0 single layer, 2 combined
 void launch_direct_far(const double* tx, const double* ty, int ntarget, const int* t_patch, const int* t_nsp_ptr,
-                       const int* t_nsp, const double* sx, const double* sy, const int* s_patch,
-                       const double2* rho, int nsource, double k, double2* y, int accumulate, cudaStream_t s);
+                       const int* t_nsp, const double* sx, const double* sy, const double* snx, const double* sny,
+                       const int* s_patch, const double2* rho, int nsource, double k, int form, double eta, double2* y,
+                       int accumulate, cudaStream_t s);
 
 // precision-templated IFGF apply (ifgf_apply.cu); R = double (plain) or float (mixed)
 template <typename R>

@@ -61,10 +61,10 @@ extern "C" int ifgf2d_apply_direct_noalloc(ifgf2d_ctx* ctx, const void* d_x, voi
     const double2* x = static_cast<const double2*>(d_x);
     double2* y = static_cast<double2*>(d_y);
     // every entry of the scratch is rewritten by the intensities kernel before it is read
-    ifgf::launch_sing_apply(x, v.W, v.srow_ptr, v.srow_col, v.cols, v.N, v.Np, y, v.stream);
+    ifgf::launch_sing_apply(x, v.W, v.srow_ptr, v.srow_col, v.cols, v.N, v.Np, v.half, y, v.stream);
     ifgf::launch_intensities(x, v.wq, nullptr, v.N, rho, v.stream);
-    ifgf::launch_direct_far(v.x, v.y, v.N, v.patch_of, v.nsp_ptr, v.nsp, v.x, v.y, v.patch_of, rho, v.N, v.k, y, 1,
-                            v.stream);
+    ifgf::launch_direct_far(v.x, v.y, v.N, v.patch_of, v.nsp_ptr, v.nsp, v.x, v.y, v.nx, v.ny, v.patch_of, rho, v.N, v.k,
+                            v.form, v.eta, y, 1, v.stream);
     if (cudaGetLastError() != cudaSuccess) { ifgf::set_error(ctx, "kernel launch failed"); return IFGF2D_ERR_CUDA; }
     return IFGF2D_OK;
 }

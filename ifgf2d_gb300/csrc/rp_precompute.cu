@@ -56,7 +56,8 @@ __device__ __forceinline__ int d_sgn(double v) { return (0.0 < v) - (v < 0.0); }
 // the Green function at each node, then the Np Chebyshev moments (ForwardMap.tpp:287-389).
 __global__ void k_rp_precompute(const RPColumn* __restrict__ cols, int ncols, const DevPatch* __restrict__ patches,
                                 const DevCurve* __restrict__ curves, const double* __restrict__ nsn,
-                                const double* __restrict__ nsw, int Np, double p, double k, double2* __restrict__ M) {
+                                const double* __restrict__ nsw, int Np, double p, double k, int form, double eta,
+                                double2* __restrict__ M) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= ncols) return;
@@ -93,7 +94,8 @@ __global__ void k_rp_precompute(const RPColumn* __restrict__ cols, int ncols, co
         double px, py, pxp, pyp;
         curve_eval(cv, g, px, py, pxp, pyp);
         const double cj = sqrt(pyp * pyp + pxp * pxp);
-        const double2 G = green_sl(px - c.xs, py - c.ys, k);
+        // target: the (near-)singular point; source: x(g) with its unit normal (y', -x') / |x'|
+        const double2 G = green_form(form, c.xs - px, c.ys - py, pyp / cj, -pxp / cj, k, eta);
         const double f = ((P.t2 - P.t1) / 2.0);
         double2 v = make_double2(f * G.x, f * G.y);
         v.x *= cj; v.y *= cj; v.x *= dx; v.y *= dx; v.x *= nsw[i]; v.y *= nsw[i];
@@ -142,9 +144,10 @@ __global__ void k_rp_fold(const double2* __restrict__ M, const RPColumn* __restr
 static inline unsigned nblk_rp(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 void launch_rp_precompute(const RPColumn* cols, int ncols, const DevPatch* patches, const DevCurve* curves,
-                          const double* nsn, const double* nsw, int Np, double p, double k, double2* M, cudaStream_t s) {
+                          const double* nsn, const double* nsw, int Np, double p, double k, int form, double eta, double2* M,
+                          cudaStream_t s) {
     if (ncols <= 0) return;
-    k_rp_precompute<<<nblk_rp((long long)ncols * 32, 128), 128, 0, s>>>(cols, ncols, patches, curves, nsn, nsw, Np, p, k, M);
+    k_rp_precompute<<<nblk_rp((long long)ncols * 32, 128), 128, 0, s>>>(cols, ncols, patches, curves, nsn, nsw, Np, p, k, form, eta, M);
 }
 void launch_rp_fold(const double2* M, const RPColumn* cols, int ncols, const double* edge, const DevPatch* patches,
                     int Np, double2* W, cudaStream_t s) {

@@ -32,6 +32,13 @@ extern "C" {
 #define IFGF2D_ERR_NONFINITE 7    /* non-finite value in an output */
 #define IFGF2D_ERR_NOCONV 8       /* GMRES did not reach the tolerance */
 
+/* formulations (FormulationType, ForwardMap/GreenFunctions.hpp:15-20) */
+#define IFGF2D_SINGLE_LAYER 0 /* S phi, kernel (i/4) H0(k r) (the reference's working formulation) */
+#define IFGF2D_COMBINED 2     /* (1/2 I + K - i eta S) phi: sound-soft combined field equation, with
+                               * K the double layer (normal derivative at the source).  The
+                               * reference's Combined is commented out (GreenFunctions.hpp:68-75);
+                               * this one is written from the Colton-Kress formulation. */
+
 /* apply modes */
 #define IFGF2D_APPLY_DIRECT 0 /* ForwardMap::compute_Ax_unacc  (ForwardMap/ForwardMap.tpp:517-540) */
 #define IFGF2D_APPLY_IFGF 1   /* ForwardMap::compute_Ax_acc    (ForwardMap/ForwardMap.tpp:609-655) */
@@ -64,6 +71,8 @@ typedef struct ifgf2d_options {
     int patches_per_curve;         /* > 0: equal-parameter split instead (extension) */
     int Ps;                        /* IFGF radial Chebyshev nodes (template Ps, default 5) */
     int Pang;                      /* IFGF angular Chebyshev nodes (template Pang, default 5) */
+    int formulation;               /* IFGF2D_SINGLE_LAYER (template Formulation) or IFGF2D_COMBINED */
+    double coupling;               /* eta of IFGF2D_COMBINED; <= 0 means eta = wavenumber */
 } ifgf2d_options;
 
 typedef struct ifgf2d_ctx ifgf2d_ctx;

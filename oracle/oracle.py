@@ -43,7 +43,7 @@ def lib():
         L.orc_fm_create.restype = P
         L.orc_fm_create.argtypes = [ctypes.c_int, I32, I32, D, D, ctypes.c_int, I32, ctypes.c_int,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                                    ctypes.c_int]
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_double]
         L.orc_fm_destroy.argtypes = [P]
         L.orc_fm_N.argtypes = [P]; L.orc_fm_N.restype = ctypes.c_longlong
         L.orc_fm_num_patches.argtypes = [P]; L.orc_fm_num_patches.restype = ctypes.c_longlong
@@ -130,13 +130,14 @@ class OracleForwardMap:
     """CPU restatement of ForwardMap<Np, SingleLayer, Ps, Pang> (ForwardMap/ForwardMap.hpp:49-177)."""
 
     def __init__(self, curves, Np, delta, wavelengths_per_patch, split_k, p=4.0,
-                 patches_per_curve=0, junctions=()):
+                 patches_per_curve=0, junctions=(), formulation="single_layer", coupling=0.0):
         L = lib()
         types, closed, tl, params = pack_curves(curves)
         j = np.array(junctions, dtype=np.int32).ravel() if junctions else np.zeros(3, np.int32)
         self.h = L.orc_fm_create(len(curves), _i32(types), _i32(closed), _d(tl), _d(params),
                                  len(junctions), _i32(j), Np, delta, wavelengths_per_patch,
-                                 split_k, p, patches_per_curve)
+                                 split_k, p, patches_per_curve,
+                                 {"single_layer": 0, "combined": 2}[formulation], coupling)
         self.Np = Np
         self.N = L.orc_fm_N(self.h)
         self.num_patches = L.orc_fm_num_patches(self.h)

@@ -35,7 +35,7 @@ void orc_hankel(int order, long long n, const double* x, double* out) {
 // curves: types[c], closed[c], tlims[2c..2c+1], params[16c..16c+15]; junctions: triples
 void* orc_fm_create(int ncurves, const int* types, const int* closed, const double* tlims, const double* params,
                     int njunc, const int* junc, int Np, double delta, double wl_per_patch, double split_k,
-                    double p, int patches_per_curve) {
+                    double p, int patches_per_curve, int form, double coupling) {
     std::vector<Curve> cs(ncurves);
     for (int c = 0; c < ncurves; ++c) {
         cs[c].type = types[c]; cs[c].is_closed = closed[c] != 0;
@@ -49,6 +49,7 @@ void* orc_fm_create(int ncurves, const int* types, const int* closed, const doub
     }
     OracleFM* h = new OracleFM;
     h->fm.reset(new ForwardMap(Np, delta, cs, touch, wl_per_patch, split_k, p, patches_per_curve));
+    h->fm->form = form; h->fm->coupling = coupling;
     return h;
 }
 void orc_fm_destroy(void* h) { delete (OracleFM*)h; }
@@ -100,7 +101,7 @@ int orc_fm_setup_ifgf(void* hh, double k, int nlevels, int Ps, int Pang) {
     OracleFM* h = (OracleFM*)hh; ForwardMap& F = *h->fm;
     try {
         h->tree.reset(new BoxTree(Ps, Pang));
-        h->tree->Reinitialize(F.xs, F.ys, nlevels, k);
+        h->tree->Reinitialize(F.xs, F.ys, F.nxs, F.nys, nlevels, k, F.form, F.coupling > 0 ? F.coupling : k);
         h->tree->CheckIfSingandNearSingInNeighborhood(F.xs, F.ys, F.patches, F.Np);
     } catch (std::logic_error& e) {
         h->err = e.what();
@@ -139,6 +140,7 @@ void orc_fm_apply_acc(void* hh, const double* in, double* out) {
     F.compute_intensities(d);
     h->tree->Solve(d, &h->sort_sing);
     for (long long i = 0; i < F.N; ++i) sns[i] += d[i];
+    F.add_jump(to_c(in, F.N), sns);
     from_c(sns, out);
 }
 // BoxTree::Solve on given intensities (original order in and out), with the exclusion sets
@@ -158,7 +160,7 @@ void orc_fm_direct_excluded(void* hh, const double* in, double* out, long long r
         cd s = 0.0;
         for (long long j = 0; j < F.N; ++j) {
             if (j == t || h->sort_sing[inv[t]].count(inv[j])) continue;
-            s += GF_SL(F.xs[j], F.ys[j], F.xs[t], F.ys[t], F.wavenumber) * d[j];
+            s += GF_form(F.form, F.xs[t], F.ys[t], F.xs[j], F.ys[j], F.nxs[j], F.nys[j], F.wavenumber, F.eta) * d[j];
         }
         out[2 * (t - row0)] = s.real(); out[2 * (t - row0) + 1] = s.imag();
     }
@@ -175,6 +177,7 @@ int orc_fm_solve(void* hh, const double* rhs, double* x, int accelerated, double
             F.compute_intensities(d);
             h->tree->Solve(d, &h->sort_sing);
             for (long long i = 0; i < F.N; ++i) sns[i] += d[i];
+            F.add_jump(in, sns);
             o = sns;
         } else {
             o = F.apply_unacc(in);

@@ -165,6 +165,20 @@ static inline cd GF_SL(double p1x, double p1y, double p2x, double p2y, double k)
     if (r < 1e-14) return cd(0.0, 0.0);
     return cd(0.0, 0.25) * hankel1(0, k * r);
 }
+// Sound-soft combined field kernel without the jump term (not working in the reference,
+// GreenFunctions.hpp:51-75; written from the Colton-Kress formulation): target t, source s with
+// unit normal n_s,  dPhi/dn_s - i eta Phi = (ik/4) H1(kr) ((t - s).n_s)/r + (eta/4) H0(kr).
+static inline cd GF_CF(double tx, double ty, double sx, double sy, double snx, double sny, double k, double eta) {
+    const double dx = tx - sx, dy = ty - sy;
+    const double r = std::sqrt(dx * dx + dy * dy);
+    if (r < 1e-14) return cd(0.0, 0.0);
+    return cd(0.0, 0.25 * k) * hankel1(1, k * r) * ((dx * snx + dy * sny) / r) + (0.25 * eta) * hankel1(0, k * r);
+}
+enum Formulation { FORM_SINGLE_LAYER = 0, FORM_COMBINED = 2 };
+static inline cd GF_form(int form, double tx, double ty, double sx, double sy, double snx, double sny, double k, double eta) {
+    return form == FORM_COMBINED ? GF_CF(tx, ty, sx, sy, snx, sny, k, eta) : GF_SL(tx, ty, sx, sy, k);
+}
+
 // GreenFunctions.hpp:125-131
 static inline cd factorization(double r, double k) {
     return std::exp(cd(0.0, 1.0) * k * r) / std::sqrt(r);
@@ -182,6 +196,8 @@ struct ForwardMap {
     std::vector<double> fej_n, fej_w, fej_ns_n, fej_ns_w;
     std::vector<std::vector<double>> chebT;         // T_n at the Np Chebyshev points
     double wavenumber = 0.0;
+    int form = FORM_SINGLE_LAYER;
+    double coupling = 0.0, eta = 0.0;               // eta = coupling, or k when coupling <= 0
 
     // ForwardMap.tpp:15-35
     ForwardMap(int Np_, double delta_, std::vector<Curve> curves_, std::vector<std::vector<Junction>> touch_,
@@ -323,7 +339,7 @@ struct ForwardMap {
             const double xt = P.curve->xt(g), yt = P.curve->yt(g);
             double nx, ny; P.curve->normal_t(g, nx, ny);
             cj[i] = std::sqrt(nx * nx + ny * ny);
-            green[i] = GF_SL(xsing, ysing, xt, yt, k);
+            green[i] = GF_form(form, xsing, ysing, xt, yt, nx / cj[i], ny / cj[i], k, eta);
         }
         std::vector<cd> integ(M);
         for (int i = 0; i < M; ++i)
@@ -343,6 +359,7 @@ struct ForwardMap {
     // ForwardMap.tpp:391-423
     void compute_precomputations(double k) {
         wavenumber = k;
+        eta = coupling > 0 ? coupling : k;
         for (long long ii = 0; ii < num_patches; ++ii) {
             Patch& P = patches[ii];
             const size_t ncol = Np + P.ns_t.size();
@@ -372,8 +389,10 @@ struct ForwardMap {
                 for (long long p2 = 0; p2 < num_patches; ++p2) {
                     if (p1 == p2 || patches[p2].ns_lookup.count(xi)) continue;
                     cd s = 0.0;
-                    for (int j = 0; j < Np; ++j)
-                        s += GF_SL(xt, yt, xs[Np * p2 + j], ys[Np * p2 + j], k) * d[Np * p2 + j];
+                    for (int j = 0; j < Np; ++j) {
+                        const long long q = Np * p2 + j;
+                        s += GF_form(form, xt, yt, xs[q], ys[q], nxs[q], nys[q], k, eta) * d[q];
+                    }
                     acc += s;
                 }
                 out[xi] += acc;
@@ -410,7 +429,14 @@ struct ForwardMap {
         compute_intensities(d);
         std::vector<cd> ns = non_singular_unacc(d, wavenumber);
         for (long long i = 0; i < N; ++i) sns[i] += ns[i];
+        add_jump(density, sns);
         return sns;
+    }
+
+    // 1/2 I of the combined formulation (exterior limit of the double layer)
+    void add_jump(const std::vector<cd>& density, std::vector<cd>& y) const {
+        if (form != FORM_COMBINED) return;
+        for (long long i = 0; i < N; ++i) y[i] += 0.5 * density[i];
     }
 
     // ForwardMap.tpp:701-727
@@ -420,7 +446,7 @@ struct ForwardMap {
         std::vector<cd> out(xp.size());
         for (size_t i = 0; i < xp.size(); ++i) {
             cd s = 0.0;
-            for (size_t j = 0; j < xs.size(); ++j) s += d[j] * GF_SL(xp[i], yp[i], xs[j], ys[j], k);
+            for (size_t j = 0; j < xs.size(); ++j) s += d[j] * GF_form(form, xp[i], yp[i], xs[j], ys[j], nxs[j], nys[j], k, eta);
             out[i] = s;
         }
         return out;

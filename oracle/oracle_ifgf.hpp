@@ -242,7 +242,9 @@ struct Level {
 struct WorkCounts { long long near_pairs = 0, leaf_evals = 0, prop_evals = 0, interp_evals = 0, cones = 0, cone_levels = 0; };
 
 struct BoxTree {
-    std::vector<double> x, y;
+    std::vector<double> x, y, nx, ny;
+    int form = FORM_SINGLE_LAYER;
+    double eta = 0.0;
     std::vector<long long> sorting, inverse;
     int nlevels = 0;
     double k = 0.0;
@@ -255,8 +257,9 @@ struct BoxTree {
     BoxTree(int Ps, int Pang) : ip(Ps, Pang) {}
 
     // BoxTree.h:995-1008
-    void Reinitialize(const std::vector<double>& xx, const std::vector<double>& yy, int nl, double kk) {
-        x = xx; y = yy; N = (long long)x.size(); nlevels = nl; k = kk;
+    void Reinitialize(const std::vector<double>& xx, const std::vector<double>& yy, const std::vector<double>& nxx,
+                      const std::vector<double>& nyy, int nl, double kk, int form_, double eta_) {
+        x = xx; y = yy; nx = nxx; ny = nyy; N = (long long)x.size(); nlevels = nl; k = kk; form = form_; eta = eta_;
         inverse.assign(N, 0); sorting.clear(); levels.clear();
         InitializeBoxesAndLevels();
         InitializeRelevantConeSegments();
@@ -283,9 +286,9 @@ struct BoxTree {
         sorting.resize(N);
         for (long long i = 0; i < N; ++i) sorting[i] = i;
         std::stable_sort(sorting.begin(), sorting.end(), [&](long long a, long long b) { return code[a] < code[b]; });
-        std::vector<double> tx(N), ty(N);
-        for (long long i = 0; i < N; ++i) { tx[i] = x[sorting[i]]; ty[i] = y[sorting[i]]; }
-        x = tx; y = ty;
+        std::vector<double> tx(N), ty(N), tnx(N), tny(N);
+        for (long long i = 0; i < N; ++i) { tx[i] = x[sorting[i]]; ty[i] = y[sorting[i]]; tnx[i] = nx[sorting[i]]; tny[i] = ny[sorting[i]]; }
+        x = tx; y = ty; nx = tnx; ny = tny;
         for (long long i = 0; i < N; ++i) inverse[sorting[i]] = i;
         levels.resize(nlevels);
         for (int i = 1; i < nlevels; ++i)
@@ -395,7 +398,7 @@ struct BoxTree {
                     const long long j = pd[0] + s;
                     if (j == i) continue;
                     if (excl && (*excl)[i].count(j)) continue;
-                    res += GF_SL(x[j], y[j], x[i], y[i], k) * dens[j];
+                    res += GF_form(form, x[i], y[i], x[j], y[j], nx[j], ny[j], k, eta) * dens[j];
                 }
             }
             solution[i] = res;
@@ -414,7 +417,10 @@ struct BoxTree {
                 const double rad = D.Cheb2Radius(nonrel, px);
                 D.Cheb2Cart(box, nonrel, px, py);
                 cd res = 0.0;
-                for (long long s = 0; s < pd[1]; ++s) res += GF_SL(x[pd[0] + s], y[pd[0] + s], px, py, k) * dens[pd[0] + s];
+                for (long long s = 0; s < pd[1]; ++s) {
+                    const long long j = pd[0] + s;
+                    res += GF_form(form, px, py, x[j], y[j], nx[j], ny[j], k, eta) * dens[j];
+                }
                 co[j] = res / factorization(rad, k);
             }
             ip.generate(co);

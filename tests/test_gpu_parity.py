@@ -34,11 +34,11 @@ def test_gpu_hankel_dense_sweep(lib, oracle):
         assert r.max() < 5e-15, (order, r.max(), x[r.argmax()])
 
 
-def _pair(lib, oracle, kind, Np, delta, wl, k, p=4.0, ppc=0):
+def _pair(lib, oracle, kind, Np, delta, wl, k, p=4.0, ppc=0, form="single_layer"):
     gc = {"circle": lib.Circle(), "kite": lib.Kite(), "line": lib.Line(-1, -0.2, 1, -0.2)}[kind]
     oc = {"circle": oracle.curve_circle(), "kite": oracle.curve_kite(), "line": oracle.curve_line(-1, -0.2, 1, -0.2)}[kind]
-    fm = lib.ForwardMap(delta, [gc], (), wl, k, p, Np=Np, patches_per_curve=ppc)
-    om = oracle.OracleForwardMap([oc], Np, delta, wl, k, p, patches_per_curve=ppc)
+    fm = lib.ForwardMap(delta, [gc], (), wl, k, p, Np=Np, patches_per_curve=ppc, formulation=form)
+    om = oracle.OracleForwardMap([oc], Np, delta, wl, k, p, patches_per_curve=ppc, formulation=form)
     return fm, om
 
 
@@ -194,3 +194,65 @@ def test_gpu_error_paths(lib):
     fm.precomps_and_setup(20.0, 0)
     with pytest.raises(ValueError):
         fm.compute_Ax_acc(np.ones(3, complex))
+
+
+# ---------------------------------------------------------------- combined field formulation
+@pytest.mark.parametrize("kind,Np,delta,wl,k,p,ppc", [
+    ("circle", 10, 0.01, 1.0, 10.0, 4.0, 20),
+    ("kite", 16, 0.01, 1.0, 100.0, 4.0, 128),
+    ("line", 20, 0.1, 0.5, 3.0, 6.0, 0),
+])
+def test_gpu_combined_direct_matches_oracle(lib, oracle, kind, Np, delta, wl, k, p, ppc):
+    fm, om = _pair(lib, oracle, kind, Np, delta, wl, k, p, ppc, form="combined")
+    fm.compute_precomputations(k)
+    om.precompute(k)
+    for patch in (0, fm.num_patches_ - 1):
+        a, b = fm.precomputations(patch), om.precomp_matrix(patch)
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    assert rel(fm.compute_Ax_unacc(d), om.compute_Ax_unacc(d)) < 1e-12
+
+
+def test_gpu_combined_ifgf_matches_oracle(lib, oracle):
+    k = 100.0
+    fm, om = _pair(lib, oracle, "kite", 16, 0.01, 1.0, k, 4.0, 128, form="combined")
+    fm.precomps_and_setup(k, 0)
+    om.precompute(k)
+    om.setup_ifgf(k, fm.nlevels)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    y = fm.compute_Ax_acc(d)
+    assert rel(y, om.compute_Ax_acc(d)) < 1e-11
+    assert rel(y, fm.compute_Ax_unacc(d)) < 1e-3
+    assert rel(fm.compute_Ax_acc(d, mixed=True), y) < 2e-6
+
+
+def test_gpu_combined_mie_and_iterations(lib):
+    """Config 1: unit circle, k = 10, CFIE eta = k, 20 patches x 10 nodes, GMRES to 1e-10,
+    checked against the exact circle series."""
+    import scipy.special as sp
+    k = 10.0
+    fm = lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, k, Np=10, patches_per_curve=20, formulation="combined")
+    x = fm.solve(-np.exp(1j * k * fm.xs_), k, accelerated=False, tol=1e-10)
+    assert fm.last_solve["converged"] and fm.last_solve["iters"] < 40
+    th = np.linspace(0, 2 * np.pi, 13)[:-1]
+    r = 2.0 * np.ones_like(th)
+    n = np.arange(-60, 61)
+    c = -(1j ** n) * sp.jv(n, k) / sp.hankel1(n, k)
+    ue = (c[None, :] * sp.hankel1(n[None, :], k * r[:, None]) * np.exp(1j * n[None, :] * th[:, None])).sum(1)
+    u = fm.propagate_unacc(r * np.cos(th), r * np.sin(th), x)
+    assert np.abs(u - ue).max() / np.abs(ue).max() < 3e-5
+
+
+def test_gpu_combined_kite_k500_solve_converges(lib):
+    """Config 2 size with the combined formulation: the second-kind equation converges fast,
+    in the FP64 form and through FP64 refinement around complex64 inner solves."""
+    k = 500.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=512, formulation="combined")
+    fm.precomps_and_setup(k, 0)
+    b = -np.exp(1j * k * fm.xs_)
+    x = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=1000)
+    assert fm.last_solve["converged"] and fm.last_solve["iters"] < 300
+    assert rel(fm.compute_Ax_acc(x), b) < 1e-6
+    xm = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=1000, mixed=True)
+    assert fm.last_solve["converged"]
+    assert rel(fm.compute_Ax_acc(xm), b) < 1e-6

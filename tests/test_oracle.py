@@ -91,3 +91,29 @@ def test_oracle_gmres_direct_solve_residual(oracle):
     x, info = fm.solve(b, False, tol=1e-10)
     r = fm.compute_Ax_unacc(x) - b
     assert info["rc"] == 0 and np.linalg.norm(r) / np.linalg.norm(b) < 1e-9
+
+
+def _mie_scattered(k, r, th, M=None):
+    """Exact sound-soft circle (radius 1) scattered field of the plane wave e^{ikx}."""
+    import scipy.special as sp
+    M = M or int(k + 40)
+    n = np.arange(-M, M + 1)
+    c = -(1j ** n) * sp.jv(n, k) / sp.hankel1(n, k)
+    return (c[None, :] * sp.hankel1(n[None, :], k * r[:, None]) * np.exp(1j * n[None, :] * th[:, None])).sum(1)
+
+
+def test_oracle_combined_field_mie(oracle):
+    """(1/2 I + K - i k S) phi = -u_inc on the unit circle, k = 10 (20 patches x 10 nodes):
+    the field D phi - i k S phi at r = 2 matches the exact series to the method's accuracy
+    (the reference's fixed 40-node rectangular-polar rule limits both formulations to ~1e-5)."""
+    k = 10.0
+    fm = oracle.OracleForwardMap([oracle.curve_circle()], 10, 0.01, 1.0, k, patches_per_curve=20, formulation="combined")
+    fm.precompute(k)
+    xs, _, _, _ = fm.points()
+    x, info = fm.solve(-np.exp(1j * k * xs), False, tol=1e-12)
+    assert info["rc"] == 0 and info["iters"] < 40
+    th = np.linspace(0, 2 * np.pi, 13)[:-1]
+    r = 2.0 * np.ones_like(th)
+    u = fm.propagate_unacc(r * np.cos(th), r * np.sin(th), x)
+    ue = _mie_scattered(k, r, th)
+    assert np.abs(u - ue).max() / np.abs(ue).max() < 3e-5
