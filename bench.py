@@ -213,6 +213,12 @@ def run_ours(args, rank, local_rank, world):
         assert rc == 0
         acc += np.array(buf[:])
     acc /= nrep
+    acc_mixed = np.zeros(5)
+    for _ in range(nrep):
+        rc = L.ifgf2d_apply_timed(fm.handle, x.data_ptr(), y.data_ptr(), 2, buf)
+        assert rc == 0
+        acc_mixed += np.array(buf[:])
+    acc_mixed /= nrep
     P = fm.Ps * fm.Pang
     nl = fm.nlevels
     # coefficient writes are bounded by the total cone count (a small term)
@@ -244,12 +250,16 @@ def run_ours(args, rank, local_rank, world):
         b = -np.exp(1j * K_WAVE * fm.xs_)
         solve = {}
         for name, mixed in (("plain_fp64", False), ("chosen_mixed", True)):
-            t0 = time.perf_counter()
-            xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
-            solve_s = time.perf_counter() - t0
+            times = []
+            for _ in range(3):   # first call: Krylov workspace + graph capture; then warm solves
+                t0 = time.perf_counter()
+                xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
+                times.append(time.perf_counter() - t0)
             true_res = float(np.linalg.norm(fm.compute_Ax_acc(xs) - b) / np.linalg.norm(b))
-            solve[name] = {"seconds": solve_s, "iters": fm.last_solve["iters"], "converged": fm.last_solve["converged"],
-                           "true_rel_residual_fp64": true_res, "tol": 1e-6, "restart": 300}
+            solve[name] = {"seconds": min(times[1:]), "seconds_first_call": times[0], "iters": fm.last_solve["iters"],
+                           "converged": fm.last_solve["converged"], "true_rel_residual_fp64": true_res, "tol": 1e-6,
+                           "restart": 300}
+        solve["speedup_chosen_vs_plain"] = solve["plain_fp64"]["seconds"] / solve["chosen_mixed"]["seconds"]
     launches_per_apply = 3 + (nl - 3) + 1
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -266,7 +276,8 @@ def run_ours(args, rank, local_rank, world):
         "solve": solve,
         "chosen": {"form": "IFGF far field complex64 (FP32 arithmetic, FP64-computed tables), FP64 singular correction",
                    "value": world * args.steps / (ms_mixed * 1e-3), "unit": UNIT, "ms_per_step": ms_mixed / args.steps,
-                   "rel_err_vs_fp64": mixed_err},
+                   "rel_err_vs_fp64": mixed_err,
+                   "phase_ms": dict(zip(phases, [float(v) for v in acc_mixed]))},
         "work": wc,
     }
     return out

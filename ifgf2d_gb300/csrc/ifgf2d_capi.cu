@@ -13,6 +13,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <memory>
 
 using namespace ifgf;
 
@@ -43,6 +44,25 @@ struct DBuf {
 
 }  // namespace
 
+// GMRES workspace of a context: Krylov basis, Arnoldi state and one captured iteration graph
+// per apply mode.  Kept across solves; rebuilt when the restart length or the tables change.
+struct GmresWork {
+    DBuf<double2> V, w, h, t, H, g, cs, sn, y, vin;
+    DBuf<double> scal, ring;
+    DBuf<int> jdev;
+    double* ring_host = nullptr;     // pinned copy of the (estimate, h_{j+1,j}) ring
+    long long n = 0;
+    int m = 0;
+    cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+    void drop_graphs() {
+        for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+    }
+    ~GmresWork() {
+        drop_graphs();
+        if (ring_host) cudaFreeHost(ring_host);
+    }
+};
+
 struct ifgf2d_ctx {
     Discretisation D;
     ifgf2d_options opt{};
@@ -70,7 +90,7 @@ struct ifgf2d_ctx {
     DBuf<int> srow_ptr, srow_col;
     // IFGF tree
     Tree T;
-    DBuf<long long> sorting;
+    DBuf<long long> sorting, inverse;
     DBuf<double> xs_s, ys_s, nxs_s, nys_s;
     DBuf<int> patch_s, nsp_ptr_s, nsp_s;
     DBuf<int> leaf_start, leaf_count, point_leaf, nbr_ptr, nbr_box;
@@ -95,6 +115,7 @@ struct ifgf2d_ctx {
     DBuf<float> Gsep32;
     // work vectors
     DBuf<double2> rho, vin, vout;
+    std::unique_ptr<GmresWork> gw;
     long long counts[8] = {0};
 };
 
@@ -258,6 +279,7 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     ctx->k = k;
     ctx->precomputed = true;
     ctx->ifgf_ready = false;
+    if (ctx->gw) ctx->gw->drop_graphs();
     ctx->counts[6] = (long long)ncols * D.Np;
     return IFGF2D_OK;
 }
@@ -328,7 +350,8 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
             for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) per[T.inverse[D.ns_idx[q]]].push_back((int)p);
         for (long long i = 0; i < N; ++i) { for (int p : per[i]) nl.push_back(p); nptr[i + 1] = (int)nl.size(); }
     }
-    CK(ctx->sorting.upload(T.sorting)); CK(ctx->xs_s.upload(T.xs)); CK(ctx->ys_s.upload(T.ys));
+    CK(ctx->sorting.upload(T.sorting)); CK(ctx->inverse.upload(T.inverse));
+    CK(ctx->xs_s.upload(T.xs)); CK(ctx->ys_s.upload(T.ys));
     {
         std::vector<double> snx(N), sny(N);
         for (long long i = 0; i < N; ++i) { snx[i] = D.nx[T.sorting[i]]; sny[i] = D.ny[T.sorting[i]]; }
@@ -438,6 +461,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     ctx->counts[7] = (long long)(ctx->near.n + ctx->leafL.n + ctx->coef.n + ctx->W.n) * 16 + (long long)ctx->pp.n * sizeof(PropEntryD) +
                      (long long)ctx->ip.n * sizeof(InterpEntryD);
     ctx->ifgf_ready = true;
+    if (ctx->gw) ctx->gw->drop_graphs();
     return IFGF2D_OK;
 }
 
@@ -475,16 +499,18 @@ static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, con
                       ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p, y, s);
 }
 
-// the IFGF far field in the precision of `mode`; x in original order, y += result
-static int far_apply(ifgf2d_ctx* ctx, const double2* x, const double* wq, double2* y, int mode, cudaEvent_t* ev) {
+// the IFGF far field in the precision of `mode`; x in original order, y += result.  With
+// rho_ready the Morton-ordered intensities were already written (by the fused singular pass).
+static int far_apply(ifgf2d_ctx* ctx, const double2* x, const double* wq, double2* y, int mode, cudaEvent_t* ev,
+                     bool rho_ready = false) {
     const int N = (int)ctx->D.N;
     if (mode == IFGF2D_APPLY_IFGF_MIXED) {
-        launch_intensities_t<float>(x, wq, ctx->sorting.p, N, ctx->rho32.p, ctx->stream);
+        if (!rho_ready) launch_intensities_t<float>(x, wq, ctx->sorting.p, N, ctx->rho32.p, ctx->stream);
         if (ev) cudaEventRecord(ev[0], ctx->stream);
         far_ifgf_t<float>(ctx, ctx->rho32.p, ctx->near32.p, ctx->leafL32.p, ctx->pp32.p, ctx->ip32.p, ctx->Gsep32.p,
                           ctx->coef32.p, y, ev ? ev + 1 : nullptr);
     } else {
-        launch_intensities_t<double>(x, wq, ctx->sorting.p, N, ctx->rho.p, ctx->stream);
+        if (!rho_ready) launch_intensities_t<double>(x, wq, ctx->sorting.p, N, ctx->rho.p, ctx->stream);
         if (ev) cudaEventRecord(ev[0], ctx->stream);
         far_ifgf_t<double>(ctx, ctx->rho.p, ctx->near.p, ctx->leafL.p, ctx->pp.p, ctx->ip.p, ctx->Gsep.p, ctx->coef.p, y,
                            ev ? ev + 1 : nullptr);
@@ -501,9 +527,14 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
         return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
     const double half = ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0;
-    launch_sing_apply(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, half, y, ctx->stream);
-    if (mode != IFGF2D_APPLY_DIRECT) return far_apply(ctx, x, ctx->wq.p, y, mode, nullptr);
-    launch_intensities(x, ctx->wq.p, nullptr, N, ctx->rho.p, ctx->stream);
+    if (mode != IFGF2D_APPLY_DIRECT) {
+        launch_sing_intens(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, half, y, ctx->wq.p,
+                           ctx->inverse.p, mode == IFGF2D_APPLY_IFGF_MIXED ? nullptr : ctx->rho.p,
+                           mode == IFGF2D_APPLY_IFGF_MIXED ? ctx->rho32.p : nullptr, ctx->stream);
+        return far_apply(ctx, x, ctx->wq.p, y, mode, nullptr, true);
+    }
+    launch_sing_intens(x, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, N, D.Np, half, y, ctx->wq.p, nullptr,
+                       ctx->rho.p, nullptr, ctx->stream);
     launch_direct_far(ctx->x.p, ctx->y.p, N, ctx->patch_of.p, ctx->nsp_ptr.p, ctx->nsp.p, ctx->x.p, ctx->y.p, ctx->nx.p, ctx->ny.p,
                       ctx->patch_of.p, ctx->rho.p, N, ctx->k, ctx->form, ctx->eta, y, 1, ctx->stream);
     CK(cudaGetLastError());
@@ -602,55 +633,40 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
 }
 
 // ------------------------------------------------------------------ GMRES on the device
-// Arnoldi with classical Gram-Schmidt and one re-orthogonalisation pass (CGS2); the Krylov
-// basis lives on the device; the (restart+1) x restart Hessenberg least-squares problem is
-// reduced with Givens rotations on the host.  Same iterates as the reference's Householder
-// Arnoldi (ForwardMap/opGMRES.hpp:68-269) in exact arithmetic; the stopping test is the same
-// residual estimate |w_k| / ||r_0||.
-namespace {
-struct Giv { std::complex<double> c, s; };
-Giv make_giv(std::complex<double> p, std::complex<double> q) {
-    Giv g;
-    if (q == 0.0) { g.c = p.real() < 0 ? -1.0 : 1.0; g.s = 0.0; return g; }
-    if (p == 0.0) { g.c = 0.0; g.s = -q / std::abs(q); return g; }
-    const double p1 = std::fabs(p.real()) + std::fabs(p.imag()), q1 = std::fabs(q.real()) + std::fabs(q.imag());
-    if (p1 >= q1) {
-        std::complex<double> ps = p / p1, qs = q / p1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = std::sqrt(1.0 + q2 / p2); if (p.real() < 0) u = -u;
-        g.c = 1.0 / u; g.s = -qs * std::conj(ps) * (g.c.real() / p2);
-    } else {
-        std::complex<double> ps = p / q1, qs = q / q1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = q1 * std::sqrt(p2 + q2); if (p.real() < 0) u = -u;
-        const double pa = std::abs(p); ps = p / pa;
-        g.c = pa / u; g.s = -std::conj(ps) * (q / u);
-    }
-    return g;
-}
-// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]: G^* [p; q] = [r; 0]
-void rot(const Giv& g, std::complex<double>& x, std::complex<double>& y) {
-    const std::complex<double> nx = std::conj(g.c) * x - std::conj(g.s) * y, ny = g.s * x + g.c * y;
-    x = nx; y = ny;
-}
-}  // namespace
-
-struct GmresWork {
-    DBuf<double2> V, w, h, t;
-    long long n = 0;
-    int m = 0;
-};
-
 // GMRES core on device vectors: x = A^{-1} b from the initial guess 0 (the reference's guess,
-// opGMRES.hpp:383-392).  Stops when |g_{j+1}| / ||r0|| < tol or after max_iters iterations.
-static int gmres_core(ifgf2d_ctx* ctx, GmresWork& G, const double2* b, double2* x, int mode, double tol, int restart,
+// opGMRES.hpp:383-392).  Arnoldi with classical Gram-Schmidt twice (CGS2).  One iteration --
+// copy of v_j, the whole apply, CGS2, Hessenberg column, Givens update, normalisation -- is a
+// captured CUDA graph whose kernels read j from device memory, so the same graph serves every
+// iteration; the host launches it in batches of four and reads the estimates back once per
+// batch.  Stops when |g_{j+1}| / ||r0|| < tol (the first ||r0||, opGMRES.hpp:207) or after
+// max_iters iterations; iterations run past the stop inside a batch are discarded.
+static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, double tol, int restart,
                       int max_iters, int& iters, double& est) {
     const long long N = ctx->D.N;
-    const int m = restart;
+    const int m = restart, ldh = m + 1;
     cudaStream_t s = ctx->stream;
-    if (G.n != N || G.m < m) {
-        CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N));
+    if (!ctx->gw) ctx->gw.reset(new GmresWork);
+    GmresWork& G = *ctx->gw;
+    if (G.n != N || G.m != m) {
+        G.drop_graphs();
+        CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N)); CK(G.vin.alloc(N));
+        CK(G.H.alloc((size_t)ldh * m)); CK(G.g.alloc(m + 1)); CK(G.cs.alloc(m)); CK(G.sn.alloc(m)); CK(G.y.alloc(m));
+        CK(G.scal.alloc(4)); CK(G.ring.alloc(2 * (size_t)m)); CK(G.jdev.alloc(1));
+        if (G.ring_host) { cudaFreeHost(G.ring_host); G.ring_host = nullptr; }
+        CK(cudaMallocHost((void**)&G.ring_host, 2 * (size_t)m * sizeof(double)));
         G.n = N; G.m = m;
+    }
+    if (!G.exec[mode]) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        launch_copy_col(G.V.p, N, G.jdev.p, G.vin.p, s);
+        int rc = apply_dev(ctx, G.vin.p, G.w.p, mode);
+        launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.vin.p, G.w.p, G.h.p, G.H.p, G.g.p, G.cs.p, G.sn.p, G.scal.p, G.ring.p, s);
+        cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (rc != IFGF2D_OK) return rc;
+        CK(ec);
+        CK(cudaGraphInstantiate(&G.exec[mode], graph, 0));
+        cudaGraphDestroy(graph);
     }
     double2 *V = G.V.p, *w = G.w.p, *h = G.h.p, *t = G.t.p;
     CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, s));
@@ -672,55 +688,34 @@ static int gmres_core(ifgf2d_ctx* ctx, GmresWork& G, const double2* b, double2* 
     const double r0n = beta;
     est = 1.0;
     if (beta == 0.0) { est = 0.0; return IFGF2D_OK; }
-    std::vector<std::complex<double>> H((size_t)(m + 1) * m), g(m + 1), hv(m + 1);
-    std::vector<Giv> Gr(m);
-    std::vector<double2> hh(m + 1), yv(m);
+    const double scal_init[4] = {0.0, 0.0, 0.0, r0n};
+    CK(cudaMemcpyAsync(G.scal.p, scal_init, sizeof(scal_init), cudaMemcpyHostToDevice, s));
     for (;;) {
         launch_scale(w, make_double2(1.0 / beta, 0.0), N, V, s);
-        std::fill(H.begin(), H.end(), 0.0); std::fill(g.begin(), g.end(), 0.0);
-        g[0] = beta;
-        int j = 0;
+        CK(cudaMemsetAsync(G.H.p, 0, sizeof(double2) * ldh * m, s));
+        CK(cudaMemsetAsync(G.g.p, 0, sizeof(double2) * (m + 1), s));
+        const double2 b0 = make_double2(beta, 0.0);
+        CK(cudaMemcpyAsync(G.g.p, &b0, sizeof(double2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(G.jdev.p, 0, sizeof(int), s));
+        int j = 0, jcols = 0;
         bool stop = false;
-        for (; j < m; ++j) {
-            double2* vj = V + (size_t)j * N;
-            if ((rc = apply_dev(ctx, vj, w, mode))) return rc;
-            std::fill(hv.begin(), hv.end(), 0.0);
-            for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice (CGS2)
-                launch_multidot(V, N, j + 1, w, N, h, s);
-                launch_multi_axpy(V, N, j + 1, h, -1.0, N, w, s);
-                CK(cudaMemcpyAsync(hh.data(), h, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                for (int i = 0; i <= j; ++i) hv[i] += std::complex<double>(hh[i].x, hh[i].y);
+        while (j < m && !stop) {
+            const int nb = std::min(4, m - j);
+            for (int q = 0; q < nb; ++q) CK(cudaGraphLaunch(G.exec[mode], s));
+            CK(cudaMemcpyAsync(G.ring_host + 2 * j, G.ring.p + 2 * j, 2 * nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            CK(cudaGetLastError());
+            for (int q = 0; q < nb; ++q) {
+                ++iters;
+                est = G.ring_host[2 * (j + q)];
+                const double hn = G.ring_host[2 * (j + q) + 1];
+                if (iters >= N || est < tol || iters >= max_iters || hn == 0.0) { stop = true; jcols = j + q + 1; break; }
             }
-            double hn; if ((rc = dnorm(w, hn))) return rc;
-            ++iters;
-            std::complex<double>* col = &H[(size_t)j * (m + 1)];
-            for (int i = 0; i <= j; ++i) col[i] = hv[i];
-            col[j + 1] = hn;
-            for (int i = 0; i < j; ++i) rot(Gr[i], col[i], col[i + 1]);
-            if (col[j + 1] != 0.0) {
-                Gr[j] = make_giv(col[j], col[j + 1]);
-                rot(Gr[j], col[j], col[j + 1]);
-                rot(Gr[j], g[j], g[j + 1]);
-            } else {
-                Gr[j] = Giv{1.0, 0.0};
-            }
-            est = std::abs(g[j + 1]) / r0n;
-            stop = (iters >= N || est < tol || iters >= max_iters || hn == 0.0);
-            if (stop) { ++j; break; }
-            if (j + 1 < m) launch_scale(w, make_double2(1.0 / hn, 0.0), N, V + (size_t)(j + 1) * N, s);
+            if (!stop) { j += nb; jcols = j; }
         }
-        if (j > m) j = m;
         // y = R^{-1} g, x += V y
-        std::vector<std::complex<double>> y(j);
-        for (int i = j - 1; i >= 0; --i) {
-            std::complex<double> acc = g[i];
-            for (int q = i + 1; q < j; ++q) acc -= H[(size_t)q * (m + 1) + i] * y[q];
-            y[i] = acc / H[(size_t)i * (m + 1) + i];
-        }
-        for (int i = 0; i < j; ++i) yv[i] = make_double2(y[i].real(), y[i].imag());
-        CK(cudaMemcpyAsync(h, yv.data(), sizeof(double2) * j, cudaMemcpyHostToDevice, s));
-        launch_multi_axpy(V, N, j, h, 1.0, N, x, s);
+        launch_backsolve(G.H.p, ldh, jcols, G.g.p, G.y.p, s);
+        launch_multi_axpy(V, N, jcols, G.y.p, 1.0, N, x, s);
         if (stop) break;
         // restart: r = b - A x (the residual estimate keeps the first ||r0||, opGMRES.hpp:207)
         if ((rc = apply_dev(ctx, x, t, mode))) return rc;
@@ -729,6 +724,7 @@ static int gmres_core(ifgf2d_ctx* ctx, GmresWork& G, const double2* b, double2* 
         if (beta == 0.0) { est = 0.0; break; }
     }
     CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
     return IFGF2D_OK;
 }
 
@@ -741,14 +737,13 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
     const long long N = ctx->D.N;
     cudaStream_t s = ctx->stream;
-    GmresWork G;
     DBuf<double2> b, x;
     CK(b.alloc(N)); CK(x.alloc(N));
     CK(cudaMemcpyAsync(b.p, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
     int iters = 0, rc;
     double est = 0.0;
     if (mode != IFGF2D_APPLY_IFGF_MIXED) {
-        if ((rc = gmres_core(ctx, G, b.p, x.p, mode, tol, restart, max_iters, iters, est))) return rc;
+        if ((rc = gmres_core(ctx, b.p, x.p, mode, tol, restart, max_iters, iters, est))) return rc;
     } else {
         // FP64 iterative refinement: r = b - A x with the FP64 IFGF operator, inner GMRES on the
         // complex64 operator for the correction, x += d, until ||r|| / ||b|| < tol
@@ -770,7 +765,7 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
             // the inner solve only has to beat the complex64 operator's own accuracy
             const double inner_tol = std::max(1e-5, 0.5 * tol * bn / rn);
             int it = 0; double e = 0.0;
-            if ((rc = gmres_core(ctx, G, r.p, d.p, IFGF2D_APPLY_IFGF_MIXED, inner_tol, restart, max_iters - iters, it, e))) return rc;
+            if ((rc = gmres_core(ctx, r.p, d.p, IFGF2D_APPLY_IFGF_MIXED, inner_tol, restart, max_iters - iters, it, e))) return rc;
             iters += it;
             {
                 double2 one = make_double2(1.0, 0.0);

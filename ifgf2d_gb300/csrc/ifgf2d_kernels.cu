@@ -94,22 +94,42 @@ __global__ void k_leaf_setup(const int* __restrict__ cone_box, int ncones, const
 }
 
 // ------------------------------------------------------------------ apply: singular part
+// Eight lanes per output row: lane k8 takes the nodes k = k8, k8+8, ... of every weight column of
+// the row, then the row's eight partial sums are reduced with shuffles.  Optionally also writes
+// the row's quadrature-weighted density into rho64 / rho32 at inv[o] (the Morton position) or
+// at o, which fuses ForwardMap::compute_intensities into the same pass.
+template <typename RhoT>
 __global__ void k_sing_apply(const double2* __restrict__ x, const double2* __restrict__ W, const int* __restrict__ row_ptr,
                              const int* __restrict__ row_col, const RPColumn* __restrict__ cols, int N, int Np,
-                             double half, double2* __restrict__ y) {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= N) return;
+                             double half, double2* __restrict__ y, const double* __restrict__ wq,
+                             const long long* __restrict__ inv, RhoT* __restrict__ rho) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int o = (int)(t >> 3), k8 = (int)(t & 7);
+    const bool active = o < N;
     double2 acc = make_double2(0.0, 0.0);
-    for (int q = row_ptr[o]; q < row_ptr[o + 1]; ++q) {
-        const int col = row_col[q];
-        const double2* w = W + (long long)col * Np;
-        const double2* d = x + (long long)cols[col].patch * Np;
-        double2 s = make_double2(0.0, 0.0);
-        for (int kk = 0; kk < Np; ++kk) cfma(s, d[kk], w[kk]);
-        acc = cadd(acc, s);
+    if (active) {
+        for (int q = row_ptr[o]; q < row_ptr[o + 1]; ++q) {
+            const int col = row_col[q];
+            const double2* w = W + (long long)col * Np;
+            const double2* d = x + (long long)cols[col].patch * Np;
+            for (int kk = k8; kk < Np; kk += 8) cfma(acc, d[kk], w[kk]);
+        }
     }
-    if (half != 0.0) { const double2 v = x[o]; acc.x += half * v.x; acc.y += half * v.y; }   // jump term
-    y[o] = acc;
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+    }
+    if (active && k8 == 0) {
+        const double2 v = x[o];
+        if (half != 0.0) { acc.x += half * v.x; acc.y += half * v.y; }   // jump term
+        y[o] = acc;
+        if (rho) {
+            const double wv = wq[o];
+            RhoT r; r.x = v.x * wv; r.y = v.y * wv;
+            rho[inv ? inv[o] : o] = r;
+        }
+    }
 }
 
 // ------------------------------------------------------------------ apply: direct far sum
@@ -216,6 +236,168 @@ __global__ void k_nonfinite(const double2* __restrict__ v, long long n, int* __r
     if (i < n && !(isfinite(v[i].x) && isfinite(v[i].y))) atomicOr(flag, 1);
 }
 
+// ------------------------------------------------------------------ device-side Arnoldi bookkeeping
+// H column j (leading dimension ldh = m + 1) := h (mode 0) or += h (mode 1), rows 0..j
+__global__ void k_hcol(double2* __restrict__ H, int ldh, int j, const double2* __restrict__ h, int add) {
+    const int i = threadIdx.x + blockIdx.x * blockDim.x;
+    if (i > j) return;
+    double2* c = H + (long long)j * ldh;
+    if (add) { c[i].x += h[i].x; c[i].y += h[i].y; } else c[i] = h[i];
+}
+
+// Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)
+__device__ void make_givens_d(double2 p, double2 q, double2& c, double2& s) {
+    const double q1 = fabs(q.x) + fabs(q.y), p1 = fabs(p.x) + fabs(p.y);
+    if (q.x == 0.0 && q.y == 0.0) { c = make_double2(p.x < 0 ? -1.0 : 1.0, 0.0); s = make_double2(0.0, 0.0); return; }
+    if (p.x == 0.0 && p.y == 0.0) { const double a = hypot(q.x, q.y); c = make_double2(0.0, 0.0); s = make_double2(-q.x / a, -q.y / a); return; }
+    if (p1 >= q1) {
+        const double2 ps = make_double2(p.x / p1, p.y / p1), qs = make_double2(q.x / p1, q.y / p1);
+        const double p2 = ps.x * ps.x + ps.y * ps.y, q2 = qs.x * qs.x + qs.y * qs.y;
+        double u = sqrt(1.0 + q2 / p2); if (p.x < 0) u = -u;
+        const double cr = 1.0 / u;
+        // s = -qs * conj(ps) * (c / p2)
+        const double2 t = make_double2(qs.x * ps.x + qs.y * ps.y, qs.y * ps.x - qs.x * ps.y);
+        c = make_double2(cr, 0.0); s = make_double2(-t.x * (cr / p2), -t.y * (cr / p2));
+    } else {
+        const double2 ps0 = make_double2(p.x / q1, p.y / q1), qs = make_double2(q.x / q1, q.y / q1);
+        const double p2 = ps0.x * ps0.x + ps0.y * ps0.y, q2 = qs.x * qs.x + qs.y * qs.y;
+        double u = q1 * sqrt(p2 + q2); if (p.x < 0) u = -u;
+        const double pa = hypot(p.x, p.y);
+        const double2 ps = make_double2(p.x / pa, p.y / pa);
+        // s = -conj(ps) * (q / u)
+        const double2 qu = make_double2(q.x / u, q.y / u);
+        c = make_double2(pa / u, 0.0);
+        s = make_double2(-(ps.x * qu.x + ps.y * qu.y), -(ps.x * qu.y - ps.y * qu.x));
+    }
+}
+// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]
+__device__ void rot_d(double2 c, double2 s, double2& x, double2& y) {
+    const double2 nx = make_double2(c.x * x.x + c.y * x.y - (s.x * y.x + s.y * y.y), c.x * x.y - c.y * x.x - (s.x * y.y - s.y * y.x));
+    const double2 ny = make_double2(s.x * x.x - s.y * x.y + c.x * y.x - c.y * y.y, s.x * x.y + s.y * x.x + c.x * y.y + c.y * y.x);
+    x = nx; y = ny;
+}
+// column j of the Hessenberg matrix is complete up to row j; nrm2 holds ||w||^2 (in .x):
+// finish the column, rotate it, extend the rotation to g, publish 1/h_{j+1,j} and the estimate
+__global__ void k_givens_step(double2* __restrict__ H, int ldh, int j, double2* __restrict__ g, double2* __restrict__ cs,
+                              double2* __restrict__ sn, const double2* __restrict__ nrm2, double r0n, double* __restrict__ scal) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double2* col = H + (long long)j * ldh;
+    const double hn = sqrt(fmax(nrm2->x, 0.0));
+    col[j + 1] = make_double2(hn, 0.0);
+    for (int i = 0; i < j; ++i) rot_d(cs[i], sn[i], col[i], col[i + 1]);
+    if (hn != 0.0) {
+        double2 c, s;
+        make_givens_d(col[j], col[j + 1], c, s);
+        cs[j] = c; sn[j] = s;
+        rot_d(c, s, col[j], col[j + 1]);
+        rot_d(c, s, g[j], g[j + 1]);
+    } else {
+        cs[j] = make_double2(1.0, 0.0); sn[j] = make_double2(0.0, 0.0);
+    }
+    scal[0] = hn != 0.0 ? 1.0 / hn : 0.0;
+    scal[1] = hypot(g[j + 1].x, g[j + 1].y) / r0n;
+    scal[2] = hn;
+}
+// v = w * scal[0]
+__global__ void k_scale_by(const double2* __restrict__ w, const double* __restrict__ scal, long long n, double2* __restrict__ v) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { const double a = scal[0]; v[i] = make_double2(w[i].x * a, w[i].y * a); }
+}
+// y = R^{-1} g (upper triangular, j x j) by back substitution, one thread
+__global__ void k_backsolve(const double2* __restrict__ H, int ldh, int j, const double2* __restrict__ g, double2* __restrict__ y) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int i = j - 1; i >= 0; --i) {
+        double2 a = g[i];
+        for (int q = i + 1; q < j; ++q) {
+            const double2 h = H[(long long)q * ldh + i], v = y[q];
+            a.x -= h.x * v.x - h.y * v.y; a.y -= h.x * v.y + h.y * v.x;
+        }
+        const double2 d = H[(long long)i * ldh + i];
+        const double den = d.x * d.x + d.y * d.y;
+        y[i] = make_double2((a.x * d.x + a.y * d.y) / den, (a.y * d.x - a.x * d.y) / den);
+    }
+}
+
+// ---- variants that read the Arnoldi index j from device memory, for a captured iteration graph
+__global__ void k_copy_col(const double2* __restrict__ V, long long n, const int* __restrict__ jp, double2* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = V[(long long)(*jp) * n + i];
+}
+__global__ void k_multidot_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                               const double2* __restrict__ w, long long n, double2* __restrict__ h) {
+    const int j = blockIdx.x;
+    if (j > *jp) return;
+    const double2* v = V + (long long)j * ldv;
+    double re = 0.0, im = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 a = v[i], b = w[i];
+        re = fma(a.x, b.x, fma(a.y, b.y, re));
+        im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+    __shared__ double sr[32], si[32];
+    re = warp_sum(re); im = warp_sum(im);
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = re; si[threadIdx.x >> 5] = im; }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x >> 5;
+        re = threadIdx.x < nw ? sr[threadIdx.x] : 0.0; im = threadIdx.x < nw ? si[threadIdx.x] : 0.0;
+        re = warp_sum(re); im = warp_sum(im);
+        if (threadIdx.x == 0) h[j] = make_double2(re, im);
+    }
+}
+__global__ void k_multi_axpy_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                                 const double2* __restrict__ h, double sign, long long n, double2* __restrict__ w) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nc = *jp + 1;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = 0; j < nc; ++j) cfma(acc, V[(long long)j * ldv + i], h[j]);
+    double2 v = w[i];
+    v.x += sign * acc.x; v.y += sign * acc.y;
+    w[i] = v;
+}
+__global__ void k_hcol_dyn(double2* __restrict__ H, int ldh, const int* __restrict__ jp, const double2* __restrict__ h, int add) {
+    const int j = *jp;
+    const int i = threadIdx.x + blockIdx.x * blockDim.x;
+    if (i > j) return;
+    double2* c = H + (long long)j * ldh;
+    if (add) { c[i].x += h[i].x; c[i].y += h[i].y; } else c[i] = h[i];
+}
+// as k_givens_step with j from memory; scal[3] holds ||r0||; records the estimate and
+// h_{j+1,j} in est_ring[2j], est_ring[2j+1]
+__global__ void k_givens_step_dyn(double2* __restrict__ H, int ldh, const int* __restrict__ jp, double2* __restrict__ g,
+                                  double2* __restrict__ cs, double2* __restrict__ sn, const double2* __restrict__ nrm2,
+                                  double* __restrict__ scal, double* __restrict__ est_ring) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int j = *jp;
+    double2* col = H + (long long)j * ldh;
+    const double hn = sqrt(fmax(nrm2->x, 0.0));
+    col[j + 1] = make_double2(hn, 0.0);
+    for (int i = 0; i < j; ++i) rot_d(cs[i], sn[i], col[i], col[i + 1]);
+    if (hn != 0.0) {
+        double2 c, s;
+        make_givens_d(col[j], col[j + 1], c, s);
+        cs[j] = c; sn[j] = s;
+        rot_d(c, s, col[j], col[j + 1]);
+        rot_d(c, s, g[j], g[j + 1]);
+    } else {
+        cs[j] = make_double2(1.0, 0.0); sn[j] = make_double2(0.0, 0.0);
+    }
+    const double est = hypot(g[j + 1].x, g[j + 1].y) / scal[3];
+    scal[0] = hn != 0.0 ? 1.0 / hn : 0.0;
+    scal[1] = est;
+    scal[2] = hn;
+    est_ring[2 * j] = est;
+    est_ring[2 * j + 1] = hn;
+}
+// V[:, j+1] = w * scal[0], then j += 1 (the last block to finish advances j)
+__global__ void k_scale_next(const double2* __restrict__ w, const double* __restrict__ scal, long long n,
+                             double2* __restrict__ V, const int* __restrict__ jp) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { const double a = scal[0]; V[(long long)(*jp + 1) * n + i] = make_double2(w[i].x * a, w[i].y * a); }
+}
+__global__ void k_advance(int* __restrict__ jp) { if (threadIdx.x == 0 && blockIdx.x == 0) *jp += 1; }
+
 // dependent FP64 FMA chains, 8 independent chains per thread
 __global__ void k_fp64_peak(double* out, int iters, double a, double b) {
     double x[8];
@@ -251,7 +433,16 @@ void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, c
 }
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols,
                        int N, int Np, double half, double2* y, cudaStream_t s) {
-    k_sing_apply<<<nblk(N, 128), 128, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, half, y);
+    k_sing_apply<double2><<<nblk((long long)N * 8, 256), 256, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, half, y, nullptr,
+                                                                       nullptr, (double2*)nullptr);
+}
+void launch_sing_intens(const double2* x, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols,
+                        int N, int Np, double half, double2* y, const double* wq, const long long* inv, double2* rho64,
+                        float2* rho32, cudaStream_t s) {
+    if (rho32)
+        k_sing_apply<float2><<<nblk((long long)N * 8, 256), 256, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, half, y, wq, inv, rho32);
+    else
+        k_sing_apply<double2><<<nblk((long long)N * 8, 256), 256, 0, s>>>(x, W, row_ptr, row_col, cols, N, Np, half, y, wq, inv, rho64);
 }
 void launch_direct_far(const double* tx, const double* ty, int nt, const int* t_patch, const int* t_nsp_ptr, const int* t_nsp,
                        const double* sx, const double* sy, const double* snx, const double* sny, const int* s_patch,
@@ -276,6 +467,37 @@ void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaSt
 }
 void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s) {
     k_sub<<<nblk(n, 256), 256, 0, s>>>(a, b, n, out);
+}
+void launch_hcol(double2* H, int ldh, int j, const double2* h, int add, cudaStream_t s) {
+    k_hcol<<<nblk(j + 1, 256), 256, 0, s>>>(H, ldh, j, h, add);
+}
+void launch_givens_step(double2* H, int ldh, int j, double2* g, double2* cs, double2* sn, const double2* nrm2, double r0n,
+                        double* scal, cudaStream_t s) {
+    k_givens_step<<<1, 32, 0, s>>>(H, ldh, j, g, cs, sn, nrm2, r0n, scal);
+}
+void launch_scale_by(const double2* w, const double* scal, long long n, double2* v, cudaStream_t s) {
+    k_scale_by<<<nblk(n, 256), 256, 0, s>>>(w, scal, n, v);
+}
+void launch_backsolve(const double2* H, int ldh, int j, const double2* g, double2* y, cudaStream_t s) {
+    k_backsolve<<<1, 32, 0, s>>>(H, ldh, j, g, y);
+}
+void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* vin, double2* w, double2* h, double2* H,
+                         double2* g, double2* cs, double2* sn, double* scal, double* est_ring, cudaStream_t s) {
+    // w holds A v_j on entry (the apply ran between k_copy_col and this call)
+    const int ldh = m + 1;
+    for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice
+        k_multidot_dyn<<<m + 1, 256, 0, s>>>(V, n, jp, w, n, h);
+        k_multi_axpy_dyn<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, h, -1.0, n, w);
+        k_hcol_dyn<<<nblk(m + 1, 256), 256, 0, s>>>(H, ldh, jp, h, pass);
+    }
+    k_multidot<<<1, 256, 0, s>>>(w, n, w, n, h + m + 1);
+    k_givens_step_dyn<<<1, 32, 0, s>>>(H, ldh, jp, g, cs, sn, h + m + 1, scal, est_ring);
+    k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, scal, n, V, jp);
+    k_advance<<<1, 32, 0, s>>>(jp);
+    (void)vin;
+}
+void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, cudaStream_t s) {
+    k_copy_col<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, out);
 }
 bool launch_fp64_peak(double* tflops) {
     int dev = 0, sms = 0;

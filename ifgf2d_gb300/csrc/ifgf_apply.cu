@@ -78,14 +78,27 @@ __global__ void k_leaf_apply_t(const int* __restrict__ cone_box, int ncones, int
     const int n = leaf_count[b], s0 = leaf_start[b];
     const V2<R>* Lc = L + leaf_off[c] + m;
     const V2<R>* rh = rho + s0;
-    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    V2<R> a0, a1, a2, a3;
+    a0.x = a0.y = a1.x = a1.y = a2.x = a2.y = a3.x = a3.y = R(0);
     int s = 0;
-    for (; s + 1 < n; s += 2) {
-        const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
-        const V2<R> r0 = rh[s], r1 = rh[s + 1];
-        cmac<R>(acc, l0, r0); cmac<R>(acc, l1, r1);
+    if (sizeof(R) == 4) {
+        for (; s + 3 < n; s += 4) {   // FP32: four independent chains, eight loads in flight per thread
+            const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
+            const V2<R> l2 = Lc[(long long)(s + 2) * P], l3 = Lc[(long long)(s + 3) * P];
+            const V2<R> r0 = rh[s], r1 = rh[s + 1], r2 = rh[s + 2], r3 = rh[s + 3];
+            cmac<R>(a0, l0, r0); cmac<R>(a1, l1, r1); cmac<R>(a2, l2, r2); cmac<R>(a3, l3, r3);
+        }
+    } else {
+        for (; s + 1 < n; s += 2) {   // FP64 is pipe-bound: two chains suffice
+            const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
+            const V2<R> r0 = rh[s], r1 = rh[s + 1];
+            cmac<R>(a0, l0, r0); cmac<R>(a1, l1, r1);
+        }
     }
-    if (s < n) cmac<R>(acc, Lc[(long long)s * P], rh[s]);
+    for (; s < n; ++s) cmac<R>(a0, Lc[(long long)s * P], rh[s]);
+    V2<R> acc;
+    acc.x = (a0.x + a1.x) + (a2.x + a3.x);
+    acc.y = (a0.y + a1.y) + (a2.y + a3.y);
     coef[(long long)(cone_base + c) * P + m] = acc;
 }
 
