@@ -237,91 +237,12 @@ __global__ void k_nonfinite(const double2* __restrict__ v, long long n, int* __r
 }
 
 // ------------------------------------------------------------------ device-side Arnoldi bookkeeping
-// H column j (leading dimension ldh = m + 1) := h (mode 0) or += h (mode 1), rows 0..j
-__global__ void k_hcol(double2* __restrict__ H, int ldh, int j, const double2* __restrict__ h, int add) {
-    const int i = threadIdx.x + blockIdx.x * blockDim.x;
-    if (i > j) return;
-    double2* c = H + (long long)j * ldh;
-    if (add) { c[i].x += h[i].x; c[i].y += h[i].y; } else c[i] = h[i];
-}
-
-// Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)
-__device__ void make_givens_d(double2 p, double2 q, double2& c, double2& s) {
-    const double q1 = fabs(q.x) + fabs(q.y), p1 = fabs(p.x) + fabs(p.y);
-    if (q.x == 0.0 && q.y == 0.0) { c = make_double2(p.x < 0 ? -1.0 : 1.0, 0.0); s = make_double2(0.0, 0.0); return; }
-    if (p.x == 0.0 && p.y == 0.0) { const double a = hypot(q.x, q.y); c = make_double2(0.0, 0.0); s = make_double2(-q.x / a, -q.y / a); return; }
-    if (p1 >= q1) {
-        const double2 ps = make_double2(p.x / p1, p.y / p1), qs = make_double2(q.x / p1, q.y / p1);
-        const double p2 = ps.x * ps.x + ps.y * ps.y, q2 = qs.x * qs.x + qs.y * qs.y;
-        double u = sqrt(1.0 + q2 / p2); if (p.x < 0) u = -u;
-        const double cr = 1.0 / u;
-        // s = -qs * conj(ps) * (c / p2)
-        const double2 t = make_double2(qs.x * ps.x + qs.y * ps.y, qs.y * ps.x - qs.x * ps.y);
-        c = make_double2(cr, 0.0); s = make_double2(-t.x * (cr / p2), -t.y * (cr / p2));
-    } else {
-        const double2 ps0 = make_double2(p.x / q1, p.y / q1), qs = make_double2(q.x / q1, q.y / q1);
-        const double p2 = ps0.x * ps0.x + ps0.y * ps0.y, q2 = qs.x * qs.x + qs.y * qs.y;
-        double u = q1 * sqrt(p2 + q2); if (p.x < 0) u = -u;
-        const double pa = hypot(p.x, p.y);
-        const double2 ps = make_double2(p.x / pa, p.y / pa);
-        // s = -conj(ps) * (q / u)
-        const double2 qu = make_double2(q.x / u, q.y / u);
-        c = make_double2(pa / u, 0.0);
-        s = make_double2(-(ps.x * qu.x + ps.y * qu.y), -(ps.x * qu.y - ps.y * qu.x));
-    }
-}
-// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]
-__device__ void rot_d(double2 c, double2 s, double2& x, double2& y) {
-    const double2 nx = make_double2(c.x * x.x + c.y * x.y - (s.x * y.x + s.y * y.y), c.x * x.y - c.y * x.x - (s.x * y.y - s.y * y.x));
-    const double2 ny = make_double2(s.x * x.x - s.y * x.y + c.x * y.x - c.y * y.y, s.x * x.y + s.y * x.x + c.x * y.y + c.y * y.x);
-    x = nx; y = ny;
-}
-// column j of the Hessenberg matrix is complete up to row j; nrm2 holds ||w||^2 (in .x):
-// finish the column, rotate it, extend the rotation to g, publish 1/h_{j+1,j} and the estimate
-__global__ void k_givens_step(double2* __restrict__ H, int ldh, int j, double2* __restrict__ g, double2* __restrict__ cs,
-                              double2* __restrict__ sn, const double2* __restrict__ nrm2, double r0n, double* __restrict__ scal) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double2* col = H + (long long)j * ldh;
-    const double hn = sqrt(fmax(nrm2->x, 0.0));
-    col[j + 1] = make_double2(hn, 0.0);
-    for (int i = 0; i < j; ++i) rot_d(cs[i], sn[i], col[i], col[i + 1]);
-    if (hn != 0.0) {
-        double2 c, s;
-        make_givens_d(col[j], col[j + 1], c, s);
-        cs[j] = c; sn[j] = s;
-        rot_d(c, s, col[j], col[j + 1]);
-        rot_d(c, s, g[j], g[j + 1]);
-    } else {
-        cs[j] = make_double2(1.0, 0.0); sn[j] = make_double2(0.0, 0.0);
-    }
-    scal[0] = hn != 0.0 ? 1.0 / hn : 0.0;
-    scal[1] = hypot(g[j + 1].x, g[j + 1].y) / r0n;
-    scal[2] = hn;
-}
-// v = w * scal[0]
-__global__ void k_scale_by(const double2* __restrict__ w, const double* __restrict__ scal, long long n, double2* __restrict__ v) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) { const double a = scal[0]; v[i] = make_double2(w[i].x * a, w[i].y * a); }
-}
-// y = R^{-1} g (upper triangular, j x j) by back substitution, one thread
-__global__ void k_backsolve(const double2* __restrict__ H, int ldh, int j, const double2* __restrict__ g, double2* __restrict__ y) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int i = j - 1; i >= 0; --i) {
-        double2 a = g[i];
-        for (int q = i + 1; q < j; ++q) {
-            const double2 h = H[(long long)q * ldh + i], v = y[q];
-            a.x -= h.x * v.x - h.y * v.y; a.y -= h.x * v.y + h.y * v.x;
-        }
-        const double2 d = H[(long long)i * ldh + i];
-        const double den = d.x * d.x + d.y * d.y;
-        y[i] = make_double2((a.x * d.x + a.y * d.y) / den, (a.y * d.x - a.x * d.y) / den);
-    }
-}
-
 // ---- variants that read the Arnoldi index j from device memory, for a captured iteration graph
-__global__ void k_copy_col(const double2* __restrict__ V, long long n, const int* __restrict__ jp, double2* __restrict__ out) {
+__global__ void k_copy_col(const double2* __restrict__ V, long long n, const int* __restrict__ jp, double2* __restrict__ out,
+                           double* __restrict__ nrm2) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = V[(long long)(*jp) * n + i];
+    if (i == 0 && nrm2) *nrm2 = 0.0;
 }
 __global__ void k_multidot_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
                                const double2* __restrict__ w, long long n, double2* __restrict__ h) {
@@ -345,56 +266,51 @@ __global__ void k_multidot_dyn(const double2* __restrict__ V, long long ldv, con
         if (threadIdx.x == 0) h[j] = make_double2(re, im);
     }
 }
-__global__ void k_multi_axpy_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
-                                 const double2* __restrict__ h, double sign, long long n, double2* __restrict__ w) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int nc = *jp + 1;
+// w -= V[:, 0..j] h: 64 rows per block, four threads per row split the columns (j = part mod 4);
+// block 0 also writes (add = 0) or adds (add = 1) h into the Hessenberg column j.
+__global__ void __launch_bounds__(256) k_cgs_update_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                                                        const double2* __restrict__ h, long long n, double2* __restrict__ w,
+                                                        double2* __restrict__ H, int ldh, int add, double* __restrict__ nrm2) {
+    __shared__ double2 part[4][64];
+    __shared__ double npart[2];
+    const int r = threadIdx.x & 63, q = threadIdx.x >> 6;
+    const long long i = (long long)blockIdx.x * 64 + r;
+    const int j = *jp;
     double2 acc = make_double2(0.0, 0.0);
-    for (int j = 0; j < nc; ++j) cfma(acc, V[(long long)j * ldv + i], h[j]);
-    double2 v = w[i];
-    v.x += sign * acc.x; v.y += sign * acc.y;
-    w[i] = v;
-}
-__global__ void k_hcol_dyn(double2* __restrict__ H, int ldh, const int* __restrict__ jp, const double2* __restrict__ h, int add) {
-    const int j = *jp;
-    const int i = threadIdx.x + blockIdx.x * blockDim.x;
-    if (i > j) return;
-    double2* c = H + (long long)j * ldh;
-    if (add) { c[i].x += h[i].x; c[i].y += h[i].y; } else c[i] = h[i];
-}
-// as k_givens_step with j from memory; scal[3] holds ||r0||; records the estimate and
-// h_{j+1,j} in est_ring[2j], est_ring[2j+1]
-__global__ void k_givens_step_dyn(double2* __restrict__ H, int ldh, const int* __restrict__ jp, double2* __restrict__ g,
-                                  double2* __restrict__ cs, double2* __restrict__ sn, const double2* __restrict__ nrm2,
-                                  double* __restrict__ scal, double* __restrict__ est_ring) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int j = *jp;
-    double2* col = H + (long long)j * ldh;
-    const double hn = sqrt(fmax(nrm2->x, 0.0));
-    col[j + 1] = make_double2(hn, 0.0);
-    for (int i = 0; i < j; ++i) rot_d(cs[i], sn[i], col[i], col[i + 1]);
-    if (hn != 0.0) {
-        double2 c, s;
-        make_givens_d(col[j], col[j + 1], c, s);
-        cs[j] = c; sn[j] = s;
-        rot_d(c, s, col[j], col[j + 1]);
-        rot_d(c, s, g[j], g[j + 1]);
-    } else {
-        cs[j] = make_double2(1.0, 0.0); sn[j] = make_double2(0.0, 0.0);
+    if (i < n)
+        for (int c = q; c <= j; c += 4) cfma(acc, V[(long long)c * ldv + i], h[c]);
+    part[q][r] = acc;
+    __syncthreads();
+    double sq = 0.0;
+    if (q == 0 && i < n) {
+        double2 v = w[i];
+        v.x -= part[0][r].x + part[1][r].x + part[2][r].x + part[3][r].x;
+        v.y -= part[0][r].y + part[1][r].y + part[2][r].y + part[3][r].y;
+        w[i] = v;
+        sq = v.x * v.x + v.y * v.y;
     }
-    const double est = hypot(g[j + 1].x, g[j + 1].y) / scal[3];
-    scal[0] = hn != 0.0 ? 1.0 / hn : 0.0;
-    scal[1] = est;
-    scal[2] = hn;
-    est_ring[2 * j] = est;
-    est_ring[2 * j + 1] = hn;
+    if (nrm2 && q == 0) {   // ||w||^2 of the updated vector: warps 0 and 1 hold the 64 rows
+        sq = warp_sum(sq);
+        if ((threadIdx.x & 31) == 0) npart[threadIdx.x >> 5] = sq;
+    }
+    __syncthreads();
+    if (nrm2 && threadIdx.x == 0) atomicAdd(nrm2, npart[0] + npart[1]);
+    if (blockIdx.x == 0)
+        for (int c = threadIdx.x; c <= j; c += blockDim.x) {
+            double2* col = H + (long long)j * ldh;
+            if (add) { col[c].x += h[c].x; col[c].y += h[c].y; } else col[c] = h[c];
+        }
 }
-// V[:, j+1] = w * scal[0], then j += 1 (the last block to finish advances j)
-__global__ void k_scale_next(const double2* __restrict__ w, const double* __restrict__ scal, long long n,
-                             double2* __restrict__ V, const int* __restrict__ jp) {
+// h_{j+1,j} = ||w|| from the accumulated square; V[:, j+1] = w / h_{j+1,j}; block 0 stores
+// h_{j+1,j} in the Hessenberg matrix (j is advanced by the next kernel)
+__global__ void k_scale_next(const double2* __restrict__ w, const double* __restrict__ nrm2, long long n,
+                             double2* __restrict__ V, const int* __restrict__ jp, double2* __restrict__ H, int ldh) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) { const double a = scal[0]; V[(long long)(*jp + 1) * n + i] = make_double2(w[i].x * a, w[i].y * a); }
+    const int j = *jp;
+    const double hn = sqrt(fmax(*nrm2, 0.0));
+    const double a = hn != 0.0 ? 1.0 / hn : 0.0;
+    if (i < n) V[(long long)(j + 1) * n + i] = make_double2(w[i].x * a, w[i].y * a);
+    if (i == 0) H[(long long)j * ldh + j + 1] = make_double2(hn, 0.0);
 }
 __global__ void k_advance(int* __restrict__ jp) { if (threadIdx.x == 0 && blockIdx.x == 0) *jp += 1; }
 
@@ -468,36 +384,19 @@ void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaSt
 void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s) {
     k_sub<<<nblk(n, 256), 256, 0, s>>>(a, b, n, out);
 }
-void launch_hcol(double2* H, int ldh, int j, const double2* h, int add, cudaStream_t s) {
-    k_hcol<<<nblk(j + 1, 256), 256, 0, s>>>(H, ldh, j, h, add);
-}
-void launch_givens_step(double2* H, int ldh, int j, double2* g, double2* cs, double2* sn, const double2* nrm2, double r0n,
-                        double* scal, cudaStream_t s) {
-    k_givens_step<<<1, 32, 0, s>>>(H, ldh, j, g, cs, sn, nrm2, r0n, scal);
-}
-void launch_scale_by(const double2* w, const double* scal, long long n, double2* v, cudaStream_t s) {
-    k_scale_by<<<nblk(n, 256), 256, 0, s>>>(w, scal, n, v);
-}
-void launch_backsolve(const double2* H, int ldh, int j, const double2* g, double2* y, cudaStream_t s) {
-    k_backsolve<<<1, 32, 0, s>>>(H, ldh, j, g, y);
-}
-void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* vin, double2* w, double2* h, double2* H,
-                         double2* g, double2* cs, double2* sn, double* scal, double* est_ring, cudaStream_t s) {
+void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
+                         cudaStream_t s) {
     // w holds A v_j on entry (the apply ran between k_copy_col and this call)
     const int ldh = m + 1;
-    for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice
+    for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice; the second pass sums ||w||^2
         k_multidot_dyn<<<m + 1, 256, 0, s>>>(V, n, jp, w, n, h);
-        k_multi_axpy_dyn<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, h, -1.0, n, w);
-        k_hcol_dyn<<<nblk(m + 1, 256), 256, 0, s>>>(H, ldh, jp, h, pass);
+        k_cgs_update_dyn<<<nblk(n, 64), 256, 0, s>>>(V, n, jp, h, n, w, H, ldh, pass, pass ? nrm2 : nullptr);
     }
-    k_multidot<<<1, 256, 0, s>>>(w, n, w, n, h + m + 1);
-    k_givens_step_dyn<<<1, 32, 0, s>>>(H, ldh, jp, g, cs, sn, h + m + 1, scal, est_ring);
-    k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, scal, n, V, jp);
+    k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, nrm2, n, V, jp, H, ldh);
     k_advance<<<1, 32, 0, s>>>(jp);
-    (void)vin;
 }
-void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, cudaStream_t s) {
-    k_copy_col<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, out);
+void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, double* nrm2, cudaStream_t s) {
+    k_copy_col<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, out, nrm2);
 }
 bool launch_fp64_peak(double* tflops) {
     int dev = 0, sms = 0;

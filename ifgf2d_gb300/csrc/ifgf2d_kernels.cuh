@@ -105,18 +105,13 @@ void launch_multi_axpy(const double2* V, long long ldv, int ncols, const double2
 void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaStream_t s);
 void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s);
 void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream_t s);
-// device-side Arnoldi bookkeeping of the GMRES core (Hessenberg column, Givens, back-solve)
-void launch_hcol(double2* H, int ldh, int j, const double2* h, int add, cudaStream_t s);
-void launch_givens_step(double2* H, int ldh, int j, double2* g, double2* cs, double2* sn, const double2* nrm2, double r0n,
-                        double* scal, cudaStream_t s);
-void launch_scale_by(const double2* w, const double* scal, long long n, double2* v, cudaStream_t s);
-void launch_backsolve(const double2* H, int ldh, int j, const double2* g, double2* y, cudaStream_t s);
 // one Arnoldi step after w = A v_j, with j read from *jp (for a captured iteration graph):
-// CGS2 against V[:, 0..j], Hessenberg column, Givens update, V[:, j+1] = w / h_{j+1,j}, j += 1;
-// records (estimate, h_{j+1,j}) in est_ring[2j], est_ring[2j+1]; scal[3] must hold ||r0||
-void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* vin, double2* w, double2* h, double2* H,
-                         double2* g, double2* cs, double2* sn, double* scal, double* est_ring, cudaStream_t s);
-void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, cudaStream_t s);
+// CGS2 against V[:, 0..j] into the Hessenberg column j, ||w||^2 into *nrm2 (zeroed by
+// launch_copy_col), h_{j+1,j} and V[:, j+1] = w / h_{j+1,j}, then j += 1
+void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
+                         cudaStream_t s);
+// out = V[:, *jp]; zeroes *nrm2 when given
+void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, double* nrm2, cudaStream_t s);
 // FP64 FMA throughput (TFLOP/s) of the current device; false on a CUDA error
 bool launch_fp64_peak(double* tflops);
 

@@ -65,41 +65,45 @@ __global__ void k_intensities_t(const double2* __restrict__ x, const double* __r
     rho[i] = r;
 }
 
-// thread = (leaf cone, coefficient); 256/P cones per block
-template <typename R>
-__global__ void k_leaf_apply_t(const int* __restrict__ cone_box, int ncones, int cone_base, const int* __restrict__ leaf_start,
-                               const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
-                               const V2<R>* __restrict__ L, const V2<R>* __restrict__ rho, int P, V2<R>* __restrict__ coef) {
-    const int cpb = blockDim.x / P;
-    const int local = threadIdx.x / P, m = threadIdx.x - local * P;
+// thread = (leaf cone, source chunk, coefficient).  CH threads share one (cone, coefficient):
+// chunk ch takes the sources s = ch, ch + CH, ...; the CH partial sums meet in shared memory.
+// Boxes hold 10-100 points, so splitting the source walk shortens the latency chain of the
+// longest boxes by CH.
+template <typename R, int CH>
+__global__ void __launch_bounds__(256) k_leaf_apply_t(const int* __restrict__ cone_box, int ncones, int cone_base,
+                                                      const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
+                                                      const long long* __restrict__ leaf_off, const V2<R>* __restrict__ L,
+                                                      const V2<R>* __restrict__ rho, int P, V2<R>* __restrict__ coef) {
+    __shared__ V2<R> part[256];
+    const int per_cone = P * CH;
+    const int cpb = blockDim.x / per_cone;
+    const int local = threadIdx.x / per_cone, r = threadIdx.x - local * per_cone;
+    const int ch = r / P, m = r - ch * P;
     const int c = blockIdx.x * cpb + local;
-    if (local >= cpb || c >= ncones) return;
-    const int b = cone_box[c];
-    const int n = leaf_count[b], s0 = leaf_start[b];
-    const V2<R>* Lc = L + leaf_off[c] + m;
-    const V2<R>* rh = rho + s0;
-    V2<R> a0, a1, a2, a3;
-    a0.x = a0.y = a1.x = a1.y = a2.x = a2.y = a3.x = a3.y = R(0);
-    int s = 0;
-    if (sizeof(R) == 4) {
-        for (; s + 3 < n; s += 4) {   // FP32: four independent chains, eight loads in flight per thread
-            const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
-            const V2<R> l2 = Lc[(long long)(s + 2) * P], l3 = Lc[(long long)(s + 3) * P];
-            const V2<R> r0 = rh[s], r1 = rh[s + 1], r2 = rh[s + 2], r3 = rh[s + 3];
-            cmac<R>(a0, l0, r0); cmac<R>(a1, l1, r1); cmac<R>(a2, l2, r2); cmac<R>(a3, l3, r3);
-        }
-    } else {
-        for (; s + 1 < n; s += 2) {   // FP64 is pipe-bound: two chains suffice
-            const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + 1) * P];
-            const V2<R> r0 = rh[s], r1 = rh[s + 1];
+    const bool active = local < cpb && c < ncones;
+    V2<R> a0, a1;
+    a0.x = a0.y = a1.x = a1.y = R(0);
+    if (active) {
+        const int b = cone_box[c];
+        const int n = leaf_count[b], s0 = leaf_start[b];
+        const V2<R>* Lc = L + leaf_off[c] + m;
+        const V2<R>* rh = rho + s0;
+        int s = ch;
+        for (; s + CH < n; s += 2 * CH) {
+            const V2<R> l0 = Lc[(long long)s * P], l1 = Lc[(long long)(s + CH) * P];
+            const V2<R> r0 = rh[s], r1 = rh[s + CH];
             cmac<R>(a0, l0, r0); cmac<R>(a1, l1, r1);
         }
+        if (s < n) cmac<R>(a0, Lc[(long long)s * P], rh[s]);
+        a0.x += a1.x; a0.y += a1.y;
     }
-    for (; s < n; ++s) cmac<R>(a0, Lc[(long long)s * P], rh[s]);
-    V2<R> acc;
-    acc.x = (a0.x + a1.x) + (a2.x + a3.x);
-    acc.y = (a0.y + a1.y) + (a2.y + a3.y);
-    coef[(long long)(cone_base + c) * P + m] = acc;
+    part[threadIdx.x] = a0;
+    __syncthreads();
+    if (active && ch == 0) {
+        V2<R> acc = a0;
+        for (int q = 1; q < CH; ++q) { const V2<R> v = part[local * per_cone + q * P + m]; acc.x += v.x; acc.y += v.y; }
+        coef[(long long)(cone_base + c) * P + m] = acc;
+    }
 }
 
 // thread = (parent cone, interpolation node); CPB cones per block.  Gsep = [PS x PS radial
@@ -121,11 +125,35 @@ __global__ void __launch_bounds__(256) k_propagate_t(int pbegin, int pend, const
         const long long e0 = pp_ptr[pc];
         const int nch = pp_nchild[pc];
         V2<R> v; v.x = R(0); v.y = R(0);
-        for (int ch = 0; ch < nch; ++ch) {
-            const PropE<R> E = pp[e0 + (long long)ch * P + pt];
-            const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.child_cone * P, E.s, E.th);
-            V2<R> w; w.x = E.wr; w.y = E.wi;
-            cmac<R>(v, it, w);
+        if (sizeof(R) == 4) {
+            // all plan entries first, then two children's coefficient gathers before any arithmetic
+            PropE<R> E[4];
+#pragma unroll
+            for (int ch = 0; ch < 4; ++ch) if (ch < nch) E[ch] = pp[e0 + (long long)ch * P + pt];
+#pragma unroll
+            for (int c0 = 0; c0 < 4; c0 += 2) {
+                if (c0 >= nch) break;
+                V2<R> ca[P], cb[P];
+                const V2<R>* pa = coef + (long long)E[c0].child_cone * P;
+                const bool two = c0 + 1 < nch;
+                const int cb_cone = two ? E[c0 + 1].child_cone : E[c0].child_cone;
+                const V2<R>* pb = coef + (long long)cb_cone * P;
+#pragma unroll
+                for (int q = 0; q < P; ++q) { ca[q] = pa[q]; cb[q] = pb[q]; }
+                V2<R> w; w.x = E[c0].wr; w.y = E[c0].wi;
+                cmac<R>(v, interp_eval<R, PS, PA>(ca, E[c0].s, E[c0].th), w);
+                if (two) {
+                    w.x = E[c0 + 1].wr; w.y = E[c0 + 1].wi;
+                    cmac<R>(v, interp_eval<R, PS, PA>(cb, E[c0 + 1].s, E[c0 + 1].th), w);
+                }
+            }
+        } else {
+            for (int ch = 0; ch < nch; ++ch) {
+                const PropE<R> E = pp[e0 + (long long)ch * P + pt];
+                const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.child_cone * P, E.s, E.th);
+                V2<R> w; w.x = E.wr; w.y = E.wi;
+                cmac<R>(v, it, w);
+            }
         }
         sv[local][pt] = v;
     }
@@ -220,8 +248,15 @@ template <typename R>
 void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
                          const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s) {
     if (ncones <= 0) return;
-    const int cpb = 256 / P;
-    k_leaf_apply_t<R><<<nblk_a(ncones, cpb), cpb * P, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count, leaf_off, L, rho, P, coef);
+    constexpr int CH = 5;
+    const int cpb = 256 / (P * CH);
+    if (cpb >= 1) {
+        k_leaf_apply_t<R, CH><<<nblk_a(ncones, cpb), cpb * P * CH, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count,
+                                                                          leaf_off, L, rho, P, coef);
+    } else {   // P > 51: one chunk per coefficient
+        k_leaf_apply_t<R, 1><<<nblk_a(ncones, 256 / P), (256 / P) * P, 0, s>>>(cone_box, ncones, cone_base, leaf_start,
+                                                                              leaf_count, leaf_off, L, rho, P, coef);
+    }
 }
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps, int Pang,
