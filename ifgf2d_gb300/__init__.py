@@ -292,6 +292,56 @@ class ForwardMap:
     def stream(self):
         return _lib.load().ifgf2d_stream(self._h)
 
+    # -- many right-hand sides
+    def _batch_in(self, X):
+        n = self.total_num_unknowns_
+        X = np.asarray(X, dtype=np.complex128)
+        if X.ndim == 1:
+            X = X[:, None]
+        if X.shape[0] != n:
+            raise ValueError(f"expected an ({n}, nrhs) matrix, got {X.shape}")
+        return np.asfortranarray(X)
+
+    def apply_batch(self, X, accelerated=True, mixed=False):
+        """Y = A X for the columns of an (N, nrhs) matrix in one pass over the operator's tables
+        (the reference applies LinearOperator::operator* once per column)."""
+        Xf = self._batch_in(X)
+        Y = np.empty_like(Xf, order="F")
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        _check(_lib.load().ifgf2d_apply_batch(self._h, _dp(Xf), _dp(Y), Xf.shape[1], mode),
+               self._h)
+        return Y
+
+    def apply_batch_device(self, d_x, d_y, nrhs, accelerated=True, mixed=False):
+        """Batched apply on device pointers: column-major N x nrhs complex128 matrices."""
+        px = d_x.data_ptr() if hasattr(d_x, "data_ptr") else int(d_x)
+        py = d_y.data_ptr() if hasattr(d_y, "data_ptr") else int(d_y)
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        _check(_lib.load().ifgf2d_apply_batch_device(self._h, px, py, int(nrhs), mode), self._h)
+
+    def gmres_batch(self, B, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False, mixed=False):
+        """GMRES for every column of an (N, nrhs) matrix, all columns in lock step on the batched
+        operator; ``self.last_solve`` holds per-column iterations and errors."""
+        Bf = self._batch_in(B)
+        X = np.empty_like(Bf, order="F")
+        nrhs = Bf.shape[1]
+        it = np.zeros(nrhs, dtype=np.int32)
+        err = np.zeros(nrhs, dtype=np.float64)
+        tol = self.GMRES_TOLERANCE_ if tol is None else tol
+        restart = self.GMRES_MAX_ITER_ if restart is None else restart
+        max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        rc = _lib.load().ifgf2d_solve_batch(self._h, _dp(Bf), _dp(X), nrhs, mode,
+                                            float(tol), int(restart), int(max_iters),
+                                            it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0))
+        if rc == 8:
+            if raise_on_noconv:
+                raise NoConvergence(f"GMRES: iterations {it.tolist()}, estimated errors {err.tolist()}")
+        else:
+            _check(rc, self._h)
+        return X
+
     # -- solver
     def solve(self, rhs, wavenumber, nlevels=0, accelerated=True, tol=None, restart=None, max_iters=None,
               raise_on_noconv=False, mixed=False):

@@ -29,7 +29,7 @@ EXPORTS = [
     "ifgf2d_get_precomputations", "ifgf2d_setup", "ifgf2d_get_nlevels", "ifgf2d_get_sorting", "ifgf2d_apply",
     "ifgf2d_apply_device", "ifgf2d_ifgf_far", "ifgf2d_solve", "ifgf2d_propagate", "ifgf2d_hankel",
     "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
-    "ifgf2d_apply_direct_noalloc",
+    "ifgf2d_apply_direct_noalloc", "ifgf2d_apply_batch", "ifgf2d_apply_batch_device", "ifgf2d_solve_batch",
 ]
 
 
@@ -95,5 +95,9 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_apply_timed.argtypes = [P, P, P, ctypes.c_int, D]
         L.ifgf2d_measure_fp64_peak.argtypes = [D]
         L.ifgf2d_apply_direct_noalloc.argtypes = [P, P, P]
+        L.ifgf2d_apply_batch.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int]
+        L.ifgf2d_apply_batch_device.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
+        L.ifgf2d_solve_batch.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int), D]
         _lib = L
         return L

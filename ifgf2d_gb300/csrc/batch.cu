@@ -1,0 +1,413 @@
+// batch.cu -- batched apply and solve of the C ABI (include/ifgf2d.h): many right-hand sides
+// (incidence angles) with one geometry and wavenumber.
+//
+// The reference solves one right-hand side per ForwardMap::solve call (ForwardMap.tpp:658-697);
+// every call re-reads the same operator.  Here up to kMaxBatch right-hand sides share one pass
+// over the tables (ifgf_batch.cu), and GMRES runs for all of them in lock step: one batched
+// apply per iteration, per-RHS Gram-Schmidt coefficients from batched reductions, and each
+// right-hand side's own Givens rotations, residual estimate and stop test on the host.
+#include "context.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+struct BatchWork {
+    int cap = 0;                               // right-hand sides the apply buffers hold
+    DBuf<double2> xt, yt;                      // interleaved [N][cap]
+    DBuf<double2> rho64, coef64;
+    DBuf<float2> rho32, coef32;
+    DBuf<PropB<double>> pb64;
+    DBuf<PropB<float>> pb32;
+    DBuf<double2> xcm, ycm;                    // column-major staging of the host entry points
+    // GMRES
+    int m = 0, scap = 0;
+    DBuf<double2> V, w, t, h, H, part, Y, hn, b, x, r, d, ones;
+};
+
+void ifgf::free_batch(ifgf2d_ctx* ctx) {
+    delete ctx->bw;
+    ctx->bw = nullptr;
+}
+
+namespace {
+
+// a parent's propagation terms sorted by child cone (stable), with the parent node recorded
+template <typename R>
+std::vector<PropB<R>> sorted_plan(const Tree& T) {
+    std::vector<PropB<R>> out(T.pp.size());
+    const int P = T.P;
+    std::vector<int> idx;
+    for (int pc = 0; pc < T.total_cones; ++pc) {
+        const long long e0 = T.pp_ptr[pc];
+        const int ne = (int)(T.pp_ptr[pc + 1] - e0);
+        idx.resize(ne);
+        for (int i = 0; i < ne; ++i) idx[i] = i;
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](int a, int b) { return T.pp[e0 + a].child_cone < T.pp[e0 + b].child_cone; });
+        for (int q = 0; q < ne; ++q) {
+            const PropEntry& e = T.pp[e0 + idx[q]];
+            out[e0 + q] = PropB<R>{e.child_cone, idx[q] % P, (R)e.s, (R)e.th, (R)e.wr, (R)e.wi};
+        }
+    }
+    return out;
+}
+
+int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
+    if (!ctx->bw) ctx->bw = new BatchWork;
+    BatchWork& W = *ctx->bw;
+    const long long N = ctx->D.N;
+    const size_t ncoef = (size_t)ctx->T.total_cones * ctx->T.P;
+    if (W.cap < B) {
+        W.xt.release(); W.yt.release(); W.rho64.release(); W.coef64.release(); W.rho32.release(); W.coef32.release();
+        CK(W.xt.alloc((size_t)N * B)); CK(W.yt.alloc((size_t)N * B));
+        W.cap = B;
+    }
+    if (mixed) {
+        if (!W.rho32.p) { CK(W.rho32.alloc((size_t)N * W.cap)); CK(W.coef32.alloc(ncoef * W.cap)); }
+        if (!W.pb32.p) CK(W.pb32.upload(sorted_plan<float>(ctx->T)));
+    } else {
+        if (!W.rho64.p) { CK(W.rho64.alloc((size_t)N * W.cap)); CK(W.coef64.alloc(ncoef * W.cap)); }
+        if (!W.pb64.p) CK(W.pb64.upload(sorted_plan<double>(ctx->T)));
+    }
+    return IFGF2D_OK;
+}
+
+template <typename R>
+void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* leafL, const PropB<R>* pb,
+           const InterpE<R>* ip, const R* Gsep, V2<R>* coef, int B, double2* yt) {
+    const Tree& T = ctx->T;
+    const int Dl = ctx->nlevels - 1;
+    const TreeLevel& LD = T.L[Dl];
+    cudaStream_t s = ctx->stream;
+    launch_leaf_b<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                     ctx->leaf_off.p, leafL, rho, T.Ps, T.Pang, B, coef, s);
+    for (int l = Dl; l >= 3; --l) {
+        const TreeLevel& Lp = T.L[l - 1];
+        launch_prop_b<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps,
+                         T.Pang, Gsep, B, coef, s);
+    }
+    launch_final_b<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
+                      ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p,
+                      B, yt, s);
+}
+
+// yt = A xt for B <= kMaxBatch interleaved right-hand sides (IFGF modes)
+int apply_il(ifgf2d_ctx* ctx, const double2* xt, double2* yt, int B, int mode) {
+    const bool mixed = mode == IFGF2D_APPLY_IFGF_MIXED;
+    int rc = ensure_apply(ctx, B, mixed);
+    if (rc != IFGF2D_OK) return rc;
+    BatchWork& W = *ctx->bw;
+    const Discretisation& D = ctx->D;
+    const double half = ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0;
+    launch_sing_b(xt, ctx->W.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, (int)D.N, D.Np, B, half, yt, ctx->wq.p,
+                  ctx->inverse.p, mixed ? nullptr : W.rho64.p, mixed ? W.rho32.p : nullptr, ctx->stream);
+    if (mixed)
+        far_b<float>(ctx, W.rho32.p, ctx->near32.p, ctx->leafL32.p, W.pb32.p, ctx->ip32.p, ctx->Gsep32.p, W.coef32.p, B, yt);
+    else
+        far_b<double>(ctx, W.rho64.p, ctx->near.p, ctx->leafL.p, W.pb64.p, ctx->ip.p, ctx->Gsep.p, W.coef64.p, B, yt);
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+int check_mode(ifgf2d_ctx* ctx, int mode) {
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
+    return IFGF2D_OK;
+}
+
+// column-major device matrices, any nrhs
+int apply_cm(ifgf2d_ctx* ctx, const double2* x, double2* y, int nrhs, int mode) {
+    const long long N = ctx->D.N;
+    if (mode == IFGF2D_APPLY_DIRECT) {
+        for (int r = 0; r < nrhs; ++r) {
+            int rc = apply_single(ctx, x + (long long)r * N, y + (long long)r * N, mode);
+            if (rc != IFGF2D_OK) return rc;
+        }
+        return IFGF2D_OK;
+    }
+    for (int r0 = 0; r0 < nrhs; r0 += kMaxBatch) {
+        const int B = std::min(kMaxBatch, nrhs - r0);
+        int rc = ensure_apply(ctx, B, mode == IFGF2D_APPLY_IFGF_MIXED);
+        if (rc != IFGF2D_OK) return rc;
+        BatchWork& W = *ctx->bw;
+        launch_interleave(x + (long long)r0 * N, N, B, W.xt.p, ctx->stream);
+        if ((rc = apply_il(ctx, W.xt.p, W.yt.p, B, mode))) return rc;
+        launch_deinterleave(W.yt.p, N, B, y + (long long)r0 * N, ctx->stream);
+    }
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+// ---------------------------------------------------------------- batched GMRES
+int ensure_solve(ifgf2d_ctx* ctx, int B, int m) {
+    if (!ctx->bw) ctx->bw = new BatchWork;
+    BatchWork& W = *ctx->bw;
+    const long long N = ctx->D.N;
+    if (W.scap < B || W.m != m) {
+        const size_t nb = (size_t)N * B;
+        CK(W.V.alloc(nb * (m + 1))); CK(W.w.alloc(nb)); CK(W.t.alloc(nb));
+        CK(W.b.alloc(nb)); CK(W.x.alloc(nb)); CK(W.r.alloc(nb)); CK(W.d.alloc(nb));
+        CK(W.h.alloc((size_t)(m + 1) * B)); CK(W.H.alloc((size_t)m * (m + 1) * B));
+        CK(W.part.alloc((size_t)bdot_chunks(N) * (m + 1) * B)); CK(W.Y.alloc((size_t)m * B)); CK(W.hn.alloc(B));
+        std::vector<double2> one(B, make_double2(1.0, 0.0));
+        CK(W.ones.upload(one));
+        W.scap = B; W.m = m;
+    }
+    return IFGF2D_OK;
+}
+
+// per-RHS 2-norms of interleaved vectors into W.hn, copied to host
+int bnorms(ifgf2d_ctx* ctx, const double2* v, int B, std::vector<double>& out) {
+    BatchWork& W = *ctx->bw;
+    const long long N = ctx->D.N;
+    launch_bdot(v, 0, 1, v, N, B, W.part.p, nullptr, W.hn.p, 0, 0, ctx->stream);
+    std::vector<double2> hv(B);
+    CK(cudaMemcpyAsync(hv.data(), W.hn.p, sizeof(double2) * B, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    out.resize(B);
+    for (int r = 0; r < B; ++r) out[r] = hv[r].x;
+    return IFGF2D_OK;
+}
+
+// x = A^{-1} b for B interleaved right-hand sides, initial guess 0 (opGMRES.hpp:383-392).
+// Right-hand side r stops when |g_{j+1}| / ||r0|| < tol[r] (opGMRES.hpp:207), after max_iters
+// iterations, or at the start when skip[r]; a stopped right-hand side keeps its x.
+int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, const std::vector<double>& tol, int restart,
+                int max_iters, const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est) {
+    const long long N = ctx->D.N;
+    const int m = (int)std::min<long long>(restart, N);
+    int rc = ensure_solve(ctx, B, m);
+    if (rc != IFGF2D_OK) return rc;
+    BatchWork& W = *ctx->bw;
+    cudaStream_t s = ctx->stream;
+    const long long nb = N * B;
+    const int ldh = m + 1;
+    CK(cudaMemsetAsync(x, 0, sizeof(double2) * nb, s));
+    iters.assign(B, 0);
+    est.assign(B, 0.0);
+    std::vector<double> beta, r0n;
+    if ((rc = bnorms(ctx, b, B, beta))) return rc;
+    r0n = beta;
+    std::vector<char> done(B, 0);
+    for (int r = 0; r < B; ++r) {
+        done[r] = skip[r] || beta[r] == 0.0;
+        est[r] = done[r] ? 0.0 : 1.0;
+    }
+    CK(cudaMemcpyAsync(W.w.p, b, sizeof(double2) * nb, cudaMemcpyDeviceToDevice, s));
+    using C = std::complex<double>;
+    std::vector<std::vector<C>> R(B), g(B);
+    std::vector<std::vector<Giv>> G(B);
+    std::vector<int> jcols(B);
+    std::vector<char> active(B);
+    std::vector<double2> Hh((size_t)(m + 1) * B), Yh((size_t)m * B);
+    auto all_done = [&]() { for (int r = 0; r < B; ++r) if (!done[r]) return false; return true; };
+    while (!all_done()) {
+        // v_0 = r / ||r|| (W.hn holds ||r|| per RHS; 0 gives a zero vector)
+        launch_bscale(W.w.p, W.hn.p, N, B, W.V.p, s);
+        CK(cudaMemsetAsync(W.H.p, 0, sizeof(double2) * (size_t)m * ldh * B, s));
+        for (int r = 0; r < B; ++r) {
+            R[r].clear();
+            g[r].assign(m + 1, C(0.0));
+            g[r][0] = beta[r];
+            G[r].assign(m, Giv{1.0, 0.0});
+            jcols[r] = 0;
+            active[r] = !done[r];
+        }
+        int ncols = 0;
+        for (int j = 0; j < m; ++j) {
+            double2* vj = W.V.p + (long long)j * nb;
+            double2* Hcol = W.H.p + (long long)j * ldh * B;
+            if ((rc = apply_il(ctx, vj, W.w.p, B, mode))) return rc;
+            for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice
+                launch_bdot(W.V.p, nb, j + 1, W.w.p, N, B, W.part.p, W.h.p, Hcol, pass, -1, s);
+                launch_bupdate(W.V.p, nb, j + 1, W.h.p, -1.0, N, B, W.w.p, s);
+            }
+            launch_bdot(W.w.p, 0, 1, W.w.p, N, B, W.part.p, nullptr, Hcol, 0, j + 1, s);
+            launch_bscale(W.w.p, Hcol + (long long)(j + 1) * B, N, B, W.V.p + (long long)(j + 1) * nb, s);
+            CK(cudaMemcpyAsync(Hh.data(), Hcol, sizeof(double2) * (size_t)(j + 2) * B, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            CK(cudaGetLastError());
+            ncols = j + 1;
+            bool any = false;
+            for (int r = 0; r < B; ++r) {
+                if (!active[r]) continue;
+                R[r].resize((size_t)(j + 1) * ldh);
+                C* col = &R[r][(size_t)j * ldh];
+                for (int i = 0; i <= j + 1; ++i) col[i] = C(Hh[(size_t)i * B + r].x, Hh[(size_t)i * B + r].y);
+                const double hnv = std::abs(col[j + 1]);
+                for (int i = 0; i < j; ++i) rot(G[r][i], col[i], col[i + 1]);
+                if (col[j + 1] != 0.0) {
+                    G[r][j] = make_giv(col[j], col[j + 1]);
+                    rot(G[r][j], col[j], col[j + 1]);
+                    rot(G[r][j], g[r][j], g[r][j + 1]);
+                }
+                ++iters[r];
+                jcols[r] = j + 1;
+                est[r] = std::abs(g[r][j + 1]) / r0n[r];
+                if (est[r] < tol[r] || iters[r] >= max_iters || iters[r] >= N || hnv == 0.0) {
+                    active[r] = 0;
+                    done[r] = 1;
+                } else {
+                    any = true;
+                }
+            }
+            if (!any) break;
+        }
+        // y_r = R_r^{-1} g_r over its own column count, x += V Y
+        std::fill(Yh.begin(), Yh.end(), make_double2(0.0, 0.0));
+        for (int r = 0; r < B; ++r) {
+            const int jc = jcols[r];
+            std::vector<C> yv(jc);
+            for (int i = jc - 1; i >= 0; --i) {
+                C acc = g[r][i];
+                for (int q = i + 1; q < jc; ++q) acc -= R[r][(size_t)q * ldh + i] * yv[q];
+                yv[i] = acc / R[r][(size_t)i * ldh + i];
+                Yh[(size_t)i * B + r] = make_double2(yv[i].real(), yv[i].imag());
+            }
+        }
+        CK(cudaMemcpyAsync(W.Y.p, Yh.data(), sizeof(double2) * (size_t)ncols * B, cudaMemcpyHostToDevice, s));
+        launch_bupdate(W.V.p, nb, ncols, W.Y.p, 1.0, N, B, x, s);
+        if (all_done()) break;
+        // restart: r = b - A x; the estimate keeps the first ||r0|| (opGMRES.hpp:207)
+        if ((rc = apply_il(ctx, x, W.t.p, B, mode))) return rc;
+        launch_sub(b, W.t.p, nb, W.w.p, s);
+        if ((rc = bnorms(ctx, W.w.p, B, beta))) return rc;
+        for (int r = 0; r < B; ++r) if (!done[r] && beta[r] == 0.0) { done[r] = 1; est[r] = 0.0; }
+    }
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+// solve B <= kMaxBatch interleaved right-hand sides W.b into W.x
+int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_iters, std::vector<int>& iters,
+             std::vector<double>& est) {
+    BatchWork& W = *ctx->bw;
+    const long long N = ctx->D.N;
+    const long long nb = N * B;
+    cudaStream_t s = ctx->stream;
+    int rc;
+    if (mode != IFGF2D_APPLY_IFGF_MIXED) {
+        std::vector<double> tv(B, tol);
+        std::vector<char> skip(B, 0);
+        return gmres_batch(ctx, W.b.p, W.x.p, B, mode, tv, restart, max_iters, skip, iters, est);
+    }
+    // FP64 iterative refinement per right-hand side, as ifgf2d_solve: residual with the FP64
+    // operator, correction from GMRES on the complex64 operator
+    std::vector<double> bn, rn;
+    if ((rc = bnorms(ctx, W.b.p, B, bn))) return rc;
+    rn = bn;
+    iters.assign(B, 0);
+    est.assign(B, 0.0);
+    std::vector<char> done(B, 0);
+    for (int r = 0; r < B; ++r) { est[r] = bn[r] > 0 ? 1.0 : 0.0; done[r] = est[r] < tol; }
+    CK(cudaMemsetAsync(W.x.p, 0, sizeof(double2) * nb, s));
+    CK(cudaMemcpyAsync(W.r.p, W.b.p, sizeof(double2) * nb, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> itol(B);
+    std::vector<int> it;
+    std::vector<double> e;
+    for (int outer = 0; outer < 30; ++outer) {
+        bool left = false;
+        int most = 0;
+        for (int r = 0; r < B; ++r) {
+            if (!done[r] && iters[r] < max_iters) left = true;
+            most = std::max(most, iters[r]);
+            itol[r] = std::max(2e-7, 0.3 * tol * bn[r] / std::max(rn[r], 1e-300));
+        }
+        if (!left) break;
+        std::vector<char> skip(B);
+        for (int r = 0; r < B; ++r) skip[r] = done[r] || iters[r] >= max_iters;
+        if ((rc = gmres_batch(ctx, W.r.p, W.d.p, B, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most), skip,
+                              it, e)))
+            return rc;
+        for (int r = 0; r < B; ++r) iters[r] += it[r];
+        launch_bupdate(W.d.p, 0, 1, W.ones.p, 1.0, N, B, W.x.p, s);   // x += d (d is 0 where skipped)
+        if ((rc = apply_il(ctx, W.x.p, W.t.p, B, IFGF2D_APPLY_IFGF))) return rc;
+        launch_sub(W.b.p, W.t.p, nb, W.r.p, s);
+        if ((rc = bnorms(ctx, W.r.p, B, rn))) return rc;
+        for (int r = 0; r < B; ++r) {
+            est[r] = bn[r] > 0 ? rn[r] / bn[r] : 0.0;
+            if (est[r] < tol) done[r] = 1;
+        }
+    }
+    return IFGF2D_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" int ifgf2d_apply_batch_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int nrhs, int mode) {
+    if (!ctx || nrhs < 0 || (nrhs > 0 && (!d_x || !d_y))) return IFGF2D_ERR_ARG;
+    int rc = check_mode(ctx, mode);
+    if (rc != IFGF2D_OK || nrhs == 0) return rc;
+    return apply_cm(ctx, (const double2*)d_x, (double2*)d_y, nrhs, mode);
+}
+
+extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, int nrhs, int mode) {
+    if (!ctx || nrhs < 0 || (nrhs > 0 && (!x || !y))) return IFGF2D_ERR_ARG;
+    int rc = check_mode(ctx, mode);
+    if (rc != IFGF2D_OK || nrhs == 0) return rc;
+    const long long N = ctx->D.N;
+    const int chunk = std::min(nrhs, kMaxBatch);
+    if (!ctx->bw) ctx->bw = new BatchWork;
+    BatchWork& W = *ctx->bw;
+    if (W.xcm.n < (size_t)N * chunk) { CK(W.xcm.alloc((size_t)N * chunk)); CK(W.ycm.alloc((size_t)N * chunk)); }
+    for (int r0 = 0; r0 < nrhs; r0 += chunk) {
+        const int B = std::min(chunk, nrhs - r0);
+        const size_t bytes = sizeof(double2) * (size_t)N * B;
+        CK(cudaMemcpyAsync(W.xcm.p, x + 2 * (size_t)N * r0, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        if ((rc = apply_cm(ctx, W.xcm.p, W.ycm.p, B, mode))) return rc;
+        CK(cudaMemcpyAsync(y + 2 * (size_t)N * r0, W.ycm.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
+                                  int max_iters, int* iters, double* est_error) {
+    if (!ctx || nrhs < 0 || (nrhs > 0 && (!rhs || !x)) || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    int rc = check_mode(ctx, mode);
+    if (rc != IFGF2D_OK || nrhs == 0) return rc;
+    const long long N = ctx->D.N;
+    bool all_ok = true;
+    if (mode == IFGF2D_APPLY_DIRECT) {   // one right-hand side at a time
+        for (int r = 0; r < nrhs; ++r) {
+            int it = 0; double e = 0.0;
+            rc = ifgf2d_solve(ctx, rhs + 2 * (size_t)N * r, x + 2 * (size_t)N * r, mode, tol, restart, max_iters, &it, &e);
+            if (rc != IFGF2D_OK && rc != IFGF2D_ERR_NOCONV) return rc;
+            all_ok = all_ok && rc == IFGF2D_OK;
+            if (iters) iters[r] = it;
+            if (est_error) est_error[r] = e;
+        }
+        return all_ok ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+    }
+    const int chunk = std::min(nrhs, kMaxBatch);
+    if ((rc = ensure_apply(ctx, chunk, mode == IFGF2D_APPLY_IFGF_MIXED))) return rc;
+    if (mode == IFGF2D_APPLY_IFGF_MIXED && (rc = ensure_apply(ctx, chunk, false))) return rc;
+    if ((rc = ensure_solve(ctx, chunk, (int)std::min<long long>(restart, N)))) return rc;
+    BatchWork& W = *ctx->bw;
+    if (W.xcm.n < (size_t)N * chunk) { CK(W.xcm.alloc((size_t)N * chunk)); CK(W.ycm.alloc((size_t)N * chunk)); }
+    cudaStream_t s = ctx->stream;
+    for (int r0 = 0; r0 < nrhs; r0 += chunk) {
+        const int B = std::min(chunk, nrhs - r0);
+        const size_t bytes = sizeof(double2) * (size_t)N * B;
+        CK(cudaMemcpyAsync(W.xcm.p, rhs + 2 * (size_t)N * r0, bytes, cudaMemcpyHostToDevice, s));
+        launch_interleave(W.xcm.p, N, B, W.b.p, s);
+        std::vector<int> it;
+        std::vector<double> e;
+        if ((rc = solve_il(ctx, B, mode, tol, restart, max_iters, it, e))) return rc;
+        launch_deinterleave(W.x.p, N, B, W.ycm.p, s);
+        CK(cudaMemcpyAsync(x + 2 * (size_t)N * r0, W.ycm.p, bytes, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int r = 0; r < B; ++r) {
+            if (iters) iters[r0 + r] = it[r];
+            if (est_error) est_error[r0 + r] = e[r];
+            all_ok = all_ok && e[r] < tol;
+        }
+    }
+    return all_ok ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}

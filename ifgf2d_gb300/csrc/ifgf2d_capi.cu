@@ -2,11 +2,6 @@
 //
 // Host orchestration of the GB300 forward map.  The context owns every device buffer; set-up
 // sizes them once, so an apply or a GMRES iteration allocates nothing.
-#include "../../include/ifgf2d.h"
-#include "geometry.hpp"
-#include "tree.hpp"
-#include "ifgf2d_kernels.cuh"
-
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <complex>
@@ -15,120 +10,10 @@
 #include <vector>
 #include <memory>
 
+#include "context.hpp"
+
 using namespace ifgf;
 
-namespace {
-
-template <class T>
-struct DBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    DBuf() = default;
-    DBuf(const DBuf&) = delete;
-    DBuf& operator=(const DBuf&) = delete;
-    ~DBuf() { release(); }
-    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
-    cudaError_t alloc(size_t cnt) {
-        release();
-        n = cnt;
-        if (cnt == 0) return cudaSuccess;
-        return cudaMalloc((void**)&p, cnt * sizeof(T));
-    }
-    cudaError_t upload(const T* src, size_t cnt) {
-        cudaError_t e = alloc(cnt);
-        if (e != cudaSuccess || cnt == 0) return e;
-        return cudaMemcpy(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice);
-    }
-    cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
-};
-
-}  // namespace
-
-// GMRES workspace of a context: Krylov basis, Arnoldi state and one captured iteration graph
-// per apply mode.  Kept across solves; rebuilt when the restart length or the tables change.
-struct GmresWork {
-    DBuf<double2> V, w, h, t, H, y, vin;
-    DBuf<double> nrm2;
-    DBuf<int> jdev;
-    double2* H_host = nullptr;       // pinned copy of the Hessenberg columns read back per batch
-    long long n = 0;
-    int m = 0;
-    cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
-    void drop_graphs() {
-        for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
-    }
-    ~GmresWork() {
-        drop_graphs();
-        if (H_host) cudaFreeHost(H_host);
-    }
-};
-
-struct ifgf2d_ctx {
-    Discretisation D;
-    ifgf2d_options opt{};
-    std::string err;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    double k = 0.0;
-    bool device_ready = false, precomputed = false, ifgf_ready = false;
-    std::vector<int> h_nsp_ptr, h_nsp, h_srow_ptr, h_srow_col;
-    int nlevels = 0;
-    int form = IFGF2D_SINGLE_LAYER;
-    double eta = 0.0;               // coupling of the combined formulation, resolved at precompute
-    // geometry (original order)
-    DBuf<double> x, y, nx, ny, wq, edge;
-    DBuf<int> patch_of;
-    DBuf<DevCurve> curves;
-    DBuf<DevPatch> patches;
-    DBuf<double> nsn, nsw;
-    DBuf<int> nsp_ptr, nsp;        // per point: patches it is near-singular to
-    // rectangular-polar correction
-    std::vector<RPColumn> hcols;
-    std::vector<int> col_ptr;      // per patch: first column
-    DBuf<RPColumn> cols;
-    DBuf<double2> M, W;
-    DBuf<int> srow_ptr, srow_col;
-    // IFGF tree
-    Tree T;
-    DBuf<long long> sorting, inverse;
-    DBuf<double> xs_s, ys_s, nxs_s, nys_s;
-    DBuf<int> patch_s, nsp_ptr_s, nsp_s;
-    DBuf<int> leaf_start, leaf_count, point_leaf, nbr_ptr, nbr_box;
-    DBuf<long long> near_off;
-    DBuf<double2> near;
-    DBuf<int> leaf_cone_box;
-    DBuf<long long> leaf_off;
-    DBuf<LeafNode> leaf_nodes_d;
-    DBuf<double2> leafL;
-    DBuf<long long> pp_ptr;
-    DBuf<int> pp_nchild;
-    DBuf<PropEntryD> pp;
-    DBuf<int> ip_ptr;
-    DBuf<InterpEntryD> ip;
-    DBuf<double2> coef;
-    DBuf<double> Gm, Gsep;          // full and separable values->coefficients maps
-    DBuf<int> near_rowlen;          // per leaf box: sources in its 3x3 neighbourhood
-    // complex64 copies of the IFGF tables (mixed form)
-    DBuf<float2> near32, leafL32, coef32, rho32;
-    DBuf<PropE<float>> pp32;
-    DBuf<InterpE<float>> ip32;
-    DBuf<float> Gsep32;
-    // work vectors
-    DBuf<double2> rho, vin, vout;
-    std::unique_ptr<GmresWork> gw;
-    long long counts[8] = {0};
-};
-
-#define CK(call)                                                                          \
-    do {                                                                                  \
-        cudaError_t e_ = (call);                                                          \
-        if (e_ != cudaSuccess) {                                                          \
-            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                \
-            return IFGF2D_ERR_CUDA;                                                       \
-        }                                                                                 \
-    } while (0)
-
-static int fail(ifgf2d_ctx* ctx, int code, const std::string& msg) { ctx->err = msg; return code; }
 
 // ------------------------------------------------------------------ create / destroy
 extern "C" int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf2d_junction* junctions, int njunctions,
@@ -226,7 +111,9 @@ static int ensure_device(ifgf2d_ctx* ctx) {
 
 extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
     if (!ctx) return IFGF2D_ERR_ARG;
-    if (ctx->stream) { cudaStreamSynchronize(ctx->stream); cudaStreamDestroy(ctx->stream); }
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch(ctx);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return IFGF2D_OK;
 }
@@ -280,6 +167,7 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     ctx->precomputed = true;
     ctx->ifgf_ready = false;
     if (ctx->gw) ctx->gw->drop_graphs();
+    free_batch(ctx);
     ctx->counts[6] = (long long)ncols * D.Np;
     return IFGF2D_OK;
 }
@@ -332,6 +220,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         if (!neighbourhood_ok(D, nlevels)) return fail(ctx, IFGF2D_ERR_NEIGHBORHOOD, "Singular point not in neighborhood");
     }
     ctx->ifgf_ready = false;
+    free_batch(ctx);
     Tree& T = ctx->T;
     std::string msg = build_tree(D.x, D.y, nlevels, k, ctx->opt.Ps, ctx->opt.Pang, T);
     if (!msg.empty()) return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
@@ -541,6 +430,8 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
     return IFGF2D_OK;
 }
 
+int ifgf::apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) { return apply_dev(ctx, x, y, mode); }
+
 extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]) {
     if (!ctx || !d_x || !d_y || !ms) return IFGF2D_ERR_ARG;
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
@@ -633,34 +524,6 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
 }
 
 // ------------------------------------------------------------------ GMRES on the device
-// Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)
-namespace {
-struct Giv { std::complex<double> c, s; };
-Giv make_giv(std::complex<double> p, std::complex<double> q) {
-    Giv g;
-    if (q == 0.0) { g.c = p.real() < 0 ? -1.0 : 1.0; g.s = 0.0; return g; }
-    if (p == 0.0) { g.c = 0.0; g.s = -q / std::abs(q); return g; }
-    const double p1 = std::fabs(p.real()) + std::fabs(p.imag()), q1 = std::fabs(q.real()) + std::fabs(q.imag());
-    if (p1 >= q1) {
-        std::complex<double> ps = p / p1, qs = q / p1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = std::sqrt(1.0 + q2 / p2); if (p.real() < 0) u = -u;
-        g.c = 1.0 / u; g.s = -qs * std::conj(ps) * (g.c.real() / p2);
-    } else {
-        std::complex<double> ps = p / q1, qs = q / q1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = q1 * std::sqrt(p2 + q2); if (p.real() < 0) u = -u;
-        const double pa = std::abs(p); ps = p / pa;
-        g.c = pa / u; g.s = -std::conj(ps) * (q / u);
-    }
-    return g;
-}
-// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]
-void rot(const Giv& g, std::complex<double>& x, std::complex<double>& y) {
-    const std::complex<double> nx = std::conj(g.c) * x - std::conj(g.s) * y, ny = g.s * x + g.c * y;
-    x = nx; y = ny;
-}
-}  // namespace
 
 // GMRES core on device vectors: x = A^{-1} b from the initial guess 0 (the reference's guess,
 // opGMRES.hpp:383-392).  Arnoldi with classical Gram-Schmidt twice (CGS2).  One iteration --

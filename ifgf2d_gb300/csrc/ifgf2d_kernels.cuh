@@ -44,6 +44,11 @@ template <> struct InterpE<float> { int cone; float s, th, fr, fi; };
 template <typename R> struct PropE;
 template <> struct PropE<double> { int child_cone; int pad; double s, th, wr, wi; };
 template <> struct PropE<float> { int child_cone; float s, th, wr, wi; };
+// batched propagation term: the parent node pt it feeds, then as PropE.  A parent's terms are
+// sorted by child cone, so a warp loads each child cone's coefficients once per parent.
+template <typename R> struct PropB;
+template <> struct PropB<double> { int child_cone; int pt; double s, th, wr, wi; };
+template <> struct PropB<float> { int child_cone; int pt; float s, th, wr, wi; };
 using InterpEntryD = InterpE<double>;
 using PropEntryD = PropE<double>;
 
@@ -97,6 +102,40 @@ void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s);
 inline void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s) {
     launch_intensities_t<double>(x, wq, perm, N, rho, s);
 }
+
+// ---------------- batched apply (ifgf_batch.cu) ----------------
+// A batch of B right-hand sides is held interleaved, [N][B] (RHS index fastest); cone
+// coefficients likewise [cone][P][B].  One warp serves 32 right-hand sides of one row, cone or
+// target, so every table entry is read once per 32 right-hand sides.
+constexpr int kMaxBatch = 64;      // right-hand sides per batched apply (larger batches are chunked)
+void launch_interleave(const double2* x, long long N, int B, double2* xt, cudaStream_t s);     // [B][N] -> [N][B]
+void launch_deinterleave(const double2* xt, long long N, int B, double2* x, cudaStream_t s);   // [N][B] -> [B][N]
+void launch_sing_b(const double2* xt, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols, int N,
+                   int Np, int B, double half, double2* yt, const double* wq, const long long* inv, double2* rho64,
+                   float2* rho32, cudaStream_t s);
+template <typename R>
+void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                   const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int Ps, int Pang, int B, V2<R>* coef,
+                   cudaStream_t s);
+template <typename R>
+void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
+                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s);
+template <typename R>
+void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
+                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,
+                    const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
+                    const long long* sorting, int B, double2* yt, cudaStream_t s);
+// batched GMRES helpers on interleaved [N][B] vectors; column c of a basis starts at V + c * ldc
+int bdot_chunks(long long N);
+// h[c][r] = sum_i conj(V_c[i][r]) w[i][r] for c < ncols; Hcol[c][r] = h (add: +=).  With
+// sqrt_row >= 0 (ncols = 1, V = w): Hcol[sqrt_row][r] = sqrt(sum_i |w[i][r]|^2) instead.
+void launch_bdot(const double2* V, long long ldc, int ncols, const double2* w, long long N, int B, double2* part,
+                 double2* h, double2* Hcol, int add, int sqrt_row, cudaStream_t s);
+// w[i][r] += sign * sum_{c < ncols} V_c[i][r] h[c][r]
+void launch_bupdate(const double2* V, long long ldc, int ncols, const double2* h, double sign, long long N, int B, double2* w,
+                    cudaStream_t s);
+// out[i][r] = w[i][r] / hn[r].x, 0 where hn[r] = 0
+void launch_bscale(const double2* w, const double2* hn, long long N, int B, double2* out, cudaStream_t s);
 
 // ---------------- tests / GMRES helpers ----------------
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s);

@@ -10,48 +10,9 @@
 //                  separable values->coefficients map                             BoxTree.h:767-868, Interpolator.h:81-120
 //   k_final        near field + every level's cousin interpolants, one warp per target,
 //                  result added to y at the target's original index               BoxTree.h:614-683, 876-937, 1063-1069
-#include "ifgf2d_kernels.cuh"
+#include "ifgf_device.cuh"
 
 namespace ifgf {
-
-__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
-
-template <typename R>
-__device__ __forceinline__ void cmac(V2<R>& acc, V2<R> a, V2<R> b) {
-    acc.x = rfma(a.x, b.x, rfma(-a.y, b.y, acc.x));
-    acc.y = rfma(a.x, b.y, rfma(a.y, b.x, acc.y));
-}
-template <typename R>
-__device__ __forceinline__ R warp_sum_r(R v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// sum_a T_a(th) sum_q T_q(s) c[a*PS + q]  (Interpolator.h:55-77, evaluated separably)
-template <typename R, int PS, int PA>
-__device__ __forceinline__ V2<R> interp_eval(const V2<R>* __restrict__ c, R s, R th) {
-    R Ts[PS], Tt[PA];
-    Ts[0] = R(1); if (PS > 1) Ts[1] = s;
-#pragma unroll
-    for (int i = 2; i < PS; ++i) Ts[i] = R(2) * s * Ts[i - 1] - Ts[i - 2];
-    Tt[0] = R(1); if (PA > 1) Tt[1] = th;
-#pragma unroll
-    for (int i = 2; i < PA; ++i) Tt[i] = R(2) * th * Tt[i - 1] - Tt[i - 2];
-    V2<R> r; r.x = R(0); r.y = R(0);
-#pragma unroll
-    for (int a = 0; a < PA; ++a) {
-        V2<R> u; u.x = R(0); u.y = R(0);
-#pragma unroll
-        for (int q = 0; q < PS; ++q) {
-            const V2<R> v = c[a * PS + q];
-            u.x = rfma(Ts[q], v.x, u.x); u.y = rfma(Ts[q], v.y, u.y);
-        }
-        r.x = rfma(Tt[a], u.x, r.x); r.y = rfma(Tt[a], u.y, r.y);
-    }
-    return r;
-}
 
 template <typename R>
 __global__ void k_intensities_t(const double2* __restrict__ x, const double* __restrict__ wq, const long long* __restrict__ perm,
@@ -230,15 +191,6 @@ __global__ void k_d2f(const double2* __restrict__ a, long long n, float2* __rest
 
 // ------------------------------------------------------------------ launchers
 static inline unsigned nblk_a(long long n, int b) { return (unsigned)((n + b - 1) / b); }
-
-#define IFGF_DISPATCH_P(PS_, PA_, ...)                                              \
-    if (PS_ == 5 && PA_ == 5) { constexpr int PS = 5, PA = 5; __VA_ARGS__; }        \
-    else if (PS_ == 5 && PA_ == 7) { constexpr int PS = 5, PA = 7; __VA_ARGS__; }   \
-    else if (PS_ == 3 && PA_ == 5) { constexpr int PS = 3, PA = 5; __VA_ARGS__; }   \
-    else if (PS_ == 3 && PA_ == 3) { constexpr int PS = 3, PA = 3; __VA_ARGS__; }   \
-    else if (PS_ == 7 && PA_ == 7) { constexpr int PS = 7, PA = 7; __VA_ARGS__; }   \
-    else if (PS_ == 4 && PA_ == 4) { constexpr int PS = 4, PA = 4; __VA_ARGS__; }   \
-    else if (PS_ == 6 && PA_ == 6) { constexpr int PS = 6, PA = 6; __VA_ARGS__; }
 
 template <typename R>
 void launch_intensities_t(const double2* x, const double* wq, const long long* perm, int N, V2<R>* rho, cudaStream_t s) {

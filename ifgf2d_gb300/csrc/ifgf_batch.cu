@@ -1,0 +1,391 @@
+// ifgf_batch.cu -- the IFGF forward map applied to a batch of right-hand sides at once.
+//
+// Every table of the single-vector apply (near-field Green values, leaf-cone values,
+// propagation and interpolation plans) depends on the geometry and k only, so B right-hand
+// sides (plane waves of different incidence, ForwardMap::solve called B times) can share one
+// pass over them.  The batch lives interleaved, [N][B] with the RHS index fastest, and one warp
+// serves 32 right-hand sides: table entries become warp-uniform broadcast loads and the
+// density / coefficient accesses are 256-byte coalesced rows.
+//
+//   k_sing_b   singular correction + jump term + intensities     ForwardMap.tpp:425-435, 481-515
+//   k_leaf_b   leaf cone coefficients, 25 accumulators per lane    BoxTree.h:685-762
+//   k_prop_b   child -> parent, per parent cone one warp; the
+//              parent's terms sorted by child cone so each child
+//              cone's coefficients are loaded once                 BoxTree.h:767-868, Interpolator.h:81-120
+//   k_final_b  near field + cousin interpolation per target       BoxTree.h:614-683, 876-937
+//
+// plus the batched GMRES vector kernels (per-RHS dot products, CGS updates, scaling).
+#include "ifgf_device.cuh"
+
+namespace ifgf {
+
+static inline unsigned nblk_b(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// ------------------------------------------------------------------ layout changes
+__global__ void k_interleave(const double2* __restrict__ x, long long N, int B, double2* __restrict__ xt) {
+    __shared__ double2 t[32][33];
+    const long long i0 = (long long)blockIdx.x * 32;
+    const int r0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int r = r0 + k;
+        const long long i = i0 + threadIdx.x;
+        if (r < B && i < N) t[k][threadIdx.x] = x[(long long)r * N + i];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const long long i = i0 + k;
+        const int r = r0 + threadIdx.x;
+        if (r < B && i < N) xt[i * B + r] = t[threadIdx.x][k];
+    }
+}
+__global__ void k_deinterleave(const double2* __restrict__ xt, long long N, int B, double2* __restrict__ x) {
+    __shared__ double2 t[32][33];
+    const long long i0 = (long long)blockIdx.x * 32;
+    const int r0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const long long i = i0 + k;
+        const int r = r0 + threadIdx.x;
+        if (r < B && i < N) t[k][threadIdx.x] = xt[i * B + r];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int r = r0 + k;
+        const long long i = i0 + threadIdx.x;
+        if (r < B && i < N) x[(long long)r * N + i] = t[threadIdx.x][k];
+    }
+}
+
+// ------------------------------------------------------------------ singular correction
+// warp = one output row, lane = one right-hand side; FP64 as in the single-vector path
+template <typename RhoT>
+__global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, const double2* __restrict__ W,
+                                                const int* __restrict__ row_ptr, const int* __restrict__ row_col,
+                                                const RPColumn* __restrict__ cols, int N, int Np, int B, double half,
+                                                double2* __restrict__ yt, const double* __restrict__ wq,
+                                                const long long* __restrict__ inv, RhoT* __restrict__ rho) {
+    const int o = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int r = blockIdx.y * 32 + (threadIdx.x & 31);
+    if (o >= N || r >= B) return;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int q = row_ptr[o]; q < row_ptr[o + 1]; ++q) {
+        const int col = row_col[q];
+        const double2* w = W + (long long)col * Np;
+        const double2* d = xt + (long long)cols[col].patch * Np * B + r;
+        for (int kk = 0; kk < Np; ++kk) {
+            const double2 a = d[(long long)kk * B], b = w[kk];
+            acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+            acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+        }
+    }
+    const double2 v = xt[(long long)o * B + r];
+    if (half != 0.0) { acc.x += half * v.x; acc.y += half * v.y; }   // jump term
+    yt[(long long)o * B + r] = acc;
+    if (rho) {
+        const double wv = wq[o];
+        RhoT q; q.x = v.x * wv; q.y = v.y * wv;
+        rho[inv[o] * B + r] = q;
+    }
+}
+
+// ------------------------------------------------------------------ leaf cones
+// warp = one leaf cone, lane = one right-hand side, P accumulators per lane
+template <typename R, int P>
+__global__ void __launch_bounds__(256) k_leaf_b(const int* __restrict__ cone_box, int ncones, int cone_base,
+                                                const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
+                                                const long long* __restrict__ leaf_off, const V2<R>* __restrict__ L,
+                                                const V2<R>* __restrict__ rho, int B, V2<R>* __restrict__ coef) {
+    const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int r = blockIdx.y * 32 + (threadIdx.x & 31);
+    if (c >= ncones) return;
+    const bool act = r < B;
+    const int rr = act ? r : 0;
+    const int b = cone_box[c];
+    const int n = leaf_count[b], s0 = leaf_start[b];
+    const V2<R>* Lc = L + leaf_off[c];
+    const V2<R>* rh = rho + (long long)s0 * B + rr;
+    V2<R> acc[P];
+#pragma unroll
+    for (int m = 0; m < P; ++m) { acc[m].x = R(0); acc[m].y = R(0); }
+    for (int s = 0; s < n; ++s) {
+        const V2<R> v = rh[(long long)s * B];
+        const V2<R>* l = Lc + (long long)s * P;
+#pragma unroll
+        for (int m = 0; m < P; ++m) cmac<R>(acc[m], l[m], v);
+    }
+    if (act) {
+        V2<R>* out = coef + (long long)(cone_base + c) * P * B + r;
+#pragma unroll
+        for (int m = 0; m < P; ++m) out[(long long)m * B] = acc[m];
+    }
+}
+
+// ------------------------------------------------------------------ propagation
+// warp = one parent cone, lane = one right-hand side.  Node values accumulate in the lane's own
+// shared-memory column; the values -> coefficients map then runs in the lane's registers.
+template <typename R, int P>
+struct PropBlock {
+    static constexpr int bytes_per_warp = P * 32 * (int)sizeof(V2<R>);
+    static constexpr int W = 32768 / bytes_per_warp >= 4 ? 4 : (32768 / bytes_per_warp >= 2 ? 2 : 1);
+};
+template <typename R, int PS, int PA, int WPB>
+__global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const long long* __restrict__ pp_ptr,
+                                                     const int* __restrict__ pp_nchild, const PropB<R>* __restrict__ pb,
+                                                     const R* __restrict__ Gsep, int B, V2<R>* __restrict__ coef) {
+    constexpr int P = PS * PA;
+    __shared__ V2<R> sv[WPB][P][32];
+    __shared__ R sG[PS * PS + PA * PA];
+    for (int i = threadIdx.x; i < PS * PS + PA * PA; i += blockDim.x) sG[i] = Gsep[i];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pc = pbegin + blockIdx.x * WPB + w;
+    if (pc >= pend) return;
+    const int r = blockIdx.y * 32 + lane;
+    const bool act = r < B;
+    const int rr = act ? r : 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) { sv[w][q][lane].x = R(0); sv[w][q][lane].y = R(0); }
+    const long long e0 = pp_ptr[pc];
+    const int ne = pp_nchild[pc] * P;
+    V2<R> cc[P];
+    int cur = -1;
+    for (int e = 0; e < ne; ++e) {
+        const PropB<R> E = pb[e0 + e];
+        if (E.child_cone != cur) {             // warp-uniform: E is the same for every lane
+            cur = E.child_cone;
+            const V2<R>* src = coef + (long long)cur * P * B + rr;
+#pragma unroll
+            for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B];
+        }
+        const V2<R> it = interp_eval<R, PS, PA>(cc, E.s, E.th);
+        V2<R> wv; wv.x = E.wr; wv.y = E.wi;
+        V2<R> a = sv[w][E.pt][lane];
+        cmac<R>(a, it, wv);
+        sv[w][E.pt][lane] = a;
+    }
+    // u[l][m] = sum_k Gs[m][k] v[l][k];  c[n][m] = sum_l Ga[n][l] u[l][m], stored at n*PS + m
+    V2<R> u[P];
+#pragma unroll
+    for (int l = 0; l < PA; ++l) {
+        V2<R> v[PS];
+#pragma unroll
+        for (int k = 0; k < PS; ++k) v[k] = sv[w][l * PS + k][lane];
+#pragma unroll
+        for (int m = 0; m < PS; ++m) {
+            V2<R> a; a.x = R(0); a.y = R(0);
+#pragma unroll
+            for (int k = 0; k < PS; ++k) { const R g = sG[m * PS + k]; a.x = rfma(g, v[k].x, a.x); a.y = rfma(g, v[k].y, a.y); }
+            u[l * PS + m] = a;
+        }
+    }
+    if (!act) return;
+    V2<R>* out = coef + (long long)pc * P * B + r;
+#pragma unroll
+    for (int n = 0; n < PA; ++n)
+#pragma unroll
+        for (int m = 0; m < PS; ++m) {
+            V2<R> a; a.x = R(0); a.y = R(0);
+#pragma unroll
+            for (int l = 0; l < PA; ++l) {
+                const R g = sG[PS * PS + n * PA + l];
+                a.x = rfma(g, u[l * PS + m].x, a.x); a.y = rfma(g, u[l * PS + m].y, a.y);
+            }
+            out[(long long)(n * PS + m) * B] = a;
+        }
+}
+
+// ------------------------------------------------------------------ near field + interpolation
+// warp = one Morton-sorted target, lane = one right-hand side; y accumulated at the original index
+template <typename R, int PS, int PA>
+__global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
+                                                 const int* __restrict__ leaf_count, const int* __restrict__ nbr_ptr,
+                                                 const int* __restrict__ nbr_box, const int* __restrict__ near_rowlen,
+                                                 const long long* __restrict__ near_off, const V2<R>* __restrict__ near,
+                                                 const V2<R>* __restrict__ rho, const int* __restrict__ ip_ptr,
+                                                 const InterpE<R>* __restrict__ ip, const V2<R>* __restrict__ coef,
+                                                 const long long* __restrict__ sorting, int B, double2* __restrict__ yt) {
+    constexpr int P = PS * PA;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int r = blockIdx.y * 32 + (threadIdx.x & 31);
+    if (i >= N) return;
+    const bool act = r < B;
+    const int rr = act ? r : 0;
+    const int b = point_leaf[i];
+    const int t = i - leaf_start[b];
+    const V2<R>* row = near + near_off[b] + (long long)t * near_rowlen[b];
+    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    int sg = 0;
+    for (int q = nbr_ptr[b]; q < nbr_ptr[b + 1]; ++q) {
+        const int bb = nbr_box[q];
+        const int c = leaf_count[bb];
+        const V2<R>* rh = rho + (long long)leaf_start[bb] * B + rr;
+        for (int s = 0; s < c; ++s) cmac<R>(acc, row[sg + s], rh[(long long)s * B]);
+        sg += c;
+    }
+    for (int e = ip_ptr[i]; e < ip_ptr[i + 1]; ++e) {
+        const InterpE<R> E = ip[e];
+        const V2<R>* src = coef + (long long)E.cone * P * B + rr;
+        V2<R> cc[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B];
+        const V2<R> it = interp_eval<R, PS, PA>(cc, E.s, E.th);
+        V2<R> f; f.x = E.fr; f.y = E.fi;
+        cmac<R>(acc, it, f);
+    }
+    if (act) {
+        double2* yo = yt + sorting[i] * B + r;
+        double2 v = *yo;
+        v.x += (double)acc.x; v.y += (double)acc.y;
+        *yo = v;
+    }
+}
+
+// ------------------------------------------------------------------ batched GMRES vector kernels
+constexpr int kRowsPerChunk = 512;
+int bdot_chunks(long long N) { return (int)((N + kRowsPerChunk - 1) / kRowsPerChunk); }
+
+// block (chunk, column c): partial sums of conj(V_c) w over the chunk's rows, per RHS
+__global__ void __launch_bounds__(256) k_bdot_part(const double2* __restrict__ V, long long ldc, const double2* __restrict__ w,
+                                                   long long N, int B, double2* __restrict__ part) {
+    __shared__ double2 sm[256];
+    const int c = blockIdx.y, chunk = blockIdx.x, nchunk = gridDim.x;
+    const int RP = 256 / B;
+    const int t = threadIdx.x, g = t / B, r = t - g * B;
+    double2 acc = make_double2(0.0, 0.0);
+    if (g < RP) {
+        const long long i0 = (long long)chunk * kRowsPerChunk;
+        const long long i1 = i0 + kRowsPerChunk < N ? i0 + kRowsPerChunk : N;
+        const double2* v = V + (long long)c * ldc;
+        for (long long i = i0 + g; i < i1; i += RP) {
+            const double2 a = v[i * B + r], b = w[i * B + r];
+            acc.x = fma(a.x, b.x, fma(a.y, b.y, acc.x));
+            acc.y = fma(a.x, b.y, fma(-a.y, b.x, acc.y));
+        }
+    }
+    sm[t] = acc;
+    __syncthreads();
+    if (t < B) {
+        double2 s = sm[t];
+        for (int q = 1; q < RP; ++q) { s.x += sm[q * B + t].x; s.y += sm[q * B + t].y; }
+        part[((long long)c * nchunk + chunk) * B + t] = s;
+    }
+}
+__global__ void k_bdot_reduce(const double2* __restrict__ part, int nchunk, int ncols, int B, double2* __restrict__ h,
+                              double2* __restrict__ Hcol, int add, int sqrt_row) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncols * B) return;
+    const int c = idx / B, r = idx - c * B;
+    double2 s = make_double2(0.0, 0.0);
+    const double2* p = part + (long long)c * nchunk * B + r;
+    for (int q = 0; q < nchunk; ++q) { s.x += p[(long long)q * B].x; s.y += p[(long long)q * B].y; }
+    if (sqrt_row >= 0) {
+        Hcol[(long long)sqrt_row * B + r] = make_double2(sqrt(s.x > 0.0 ? s.x : 0.0), 0.0);
+        return;
+    }
+    if (h) h[idx] = s;
+    if (Hcol) {
+        double2 v = s;
+        if (add) { v.x += Hcol[idx].x; v.y += Hcol[idx].y; }
+        Hcol[idx] = v;
+    }
+}
+__global__ void __launch_bounds__(256) k_bupdate(const double2* __restrict__ V, long long ldc, int ncols,
+                                                 const double2* __restrict__ h, double sign, long long n, int B,
+                                                 double2* __restrict__ w) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int r = (int)(e % B);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int c = 0; c < ncols; ++c) {
+        const double2 a = V[(long long)c * ldc + e], b = h[c * B + r];
+        acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+        acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+    }
+    double2 v = w[e];
+    v.x = fma(sign, acc.x, v.x); v.y = fma(sign, acc.y, v.y);
+    w[e] = v;
+}
+__global__ void k_bscale(const double2* __restrict__ w, const double2* __restrict__ hn, long long n, int B,
+                         double2* __restrict__ out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const double h = hn[e % B].x;
+    const double s = h > 0.0 ? 1.0 / h : 0.0;
+    const double2 v = w[e];
+    out[e] = make_double2(v.x * s, v.y * s);
+}
+
+// ------------------------------------------------------------------ launchers
+void launch_interleave(const double2* x, long long N, int B, double2* xt, cudaStream_t s) {
+    if (N <= 0 || B <= 0) return;
+    k_interleave<<<dim3(nblk_b(N, 32), nblk_b(B, 32)), dim3(32, 8), 0, s>>>(x, N, B, xt);
+}
+void launch_deinterleave(const double2* xt, long long N, int B, double2* x, cudaStream_t s) {
+    if (N <= 0 || B <= 0) return;
+    k_deinterleave<<<dim3(nblk_b(N, 32), nblk_b(B, 32)), dim3(32, 8), 0, s>>>(xt, N, B, x);
+}
+void launch_sing_b(const double2* xt, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols, int N,
+                   int Np, int B, double half, double2* yt, const double* wq, const long long* inv, double2* rho64,
+                   float2* rho32, cudaStream_t s) {
+    const dim3 grid(nblk_b(N, 8), nblk_b(B, 32));
+    if (rho32)
+        k_sing_b<float2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho32);
+    else
+        k_sing_b<double2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho64);
+}
+template <typename R>
+void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                   const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int Ps, int Pang, int B, V2<R>* coef,
+                   cudaStream_t s) {
+    if (ncones <= 0) return;
+    const dim3 grid(nblk_b(ncones, 8), nblk_b(B, 32));
+    IFGF_DISPATCH_P(Ps, Pang, (k_leaf_b<R, PS * PA><<<grid, 256, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count,
+                                                                        leaf_off, L, rho, B, coef)));
+}
+template <typename R>
+void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
+                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s) {
+    if (pend <= pbegin) return;
+    IFGF_DISPATCH_P(Ps, Pang, {
+        constexpr int WPB = PropBlock<R, PS * PA>::W;
+        k_prop_b<R, PS, PA, WPB><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32)), WPB * 32, 0, s>>>(
+            pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
+    });
+}
+template <typename R>
+void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
+                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,
+                    const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
+                    const long long* sorting, int B, double2* yt, cudaStream_t s) {
+    const dim3 grid(nblk_b(N, 8), nblk_b(B, 32));
+    IFGF_DISPATCH_P(Ps, Pang, (k_final_b<R, PS, PA><<<grid, 256, 0, s>>>(N, point_leaf, leaf_start, leaf_count, nbr_ptr,
+                                                                        nbr_box, near_rowlen, near_off, near, rho, ip_ptr,
+                                                                        ip, coef, sorting, B, yt)));
+}
+void launch_bdot(const double2* V, long long ldc, int ncols, const double2* w, long long N, int B, double2* part,
+                 double2* h, double2* Hcol, int add, int sqrt_row, cudaStream_t s) {
+    if (ncols <= 0) return;
+    const int nchunk = bdot_chunks(N);
+    k_bdot_part<<<dim3(nchunk, ncols), 256, 0, s>>>(V, ldc, w, N, B, part);
+    k_bdot_reduce<<<nblk_b((long long)ncols * B, 256), 256, 0, s>>>(part, nchunk, ncols, B, h, Hcol, add, sqrt_row);
+}
+void launch_bupdate(const double2* V, long long ldc, int ncols, const double2* h, double sign, long long N, int B, double2* w,
+                    cudaStream_t s) {
+    if (ncols <= 0) return;
+    k_bupdate<<<nblk_b(N * B, 256), 256, 0, s>>>(V, ldc, ncols, h, sign, N * B, B, w);
+}
+void launch_bscale(const double2* w, const double2* hn, long long N, int B, double2* out, cudaStream_t s) {
+    k_bscale<<<nblk_b(N * B, 256), 256, 0, s>>>(w, hn, N * B, B, out);
+}
+
+#define IFGF_BATCH_INSTANTIATE(R)                                                                                       \
+    template void launch_leaf_b<R>(const int*, int, int, const int*, const int*, const long long*, const V2<R>*,        \
+                                   const V2<R>*, int, int, int, V2<R>*, cudaStream_t);                                  \
+    template void launch_prop_b<R>(int, int, const long long*, const int*, const PropB<R>*, int, int, const R*, int,    \
+                                   V2<R>*, cudaStream_t);                                                               \
+    template void launch_final_b<R>(int, const int*, const int*, const int*, const int*, const int*, const int*,        \
+                                    const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,        \
+                                    const V2<R>*, int, int, const long long*, int, double2*, cudaStream_t);
+IFGF_BATCH_INSTANTIATE(double)
+IFGF_BATCH_INSTANTIATE(float)
+
+}  // namespace ifgf

@@ -125,6 +125,25 @@ int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intensities, double* y);
 int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* x, int mode, double tol, int restart,
                  int max_iters, int* iters, double* est_error);
 
+/* Batched forms for nrhs right-hand sides with one geometry and wavenumber (the reference
+ * calls LinearOperator::operator* / ForwardMap::solve once per right-hand side,
+ * ForwardMap.tpp:658-697).  x, y, rhs are column-major N x nrhs complex matrices (right-hand
+ * side r at offset 2*N*r doubles, interleaved re/im), as an Eigen::MatrixXcd stores them.  The
+ * IFGF modes process up to IFGF2D_MAX_BATCH right-hand sides per pass over the tables (larger
+ * batches run in chunks); IFGF2D_APPLY_DIRECT runs one right-hand side at a time. */
+#define IFGF2D_MAX_BATCH 64
+int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, int nrhs, int mode);
+/* the same on device-resident matrices (cudaMalloc'ed, N * nrhs complex each); asynchronous on
+ * the context's stream */
+int ifgf2d_apply_batch_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int nrhs, int mode);
+/* ifgf2d_solve for every column of rhs: GMRES runs for all right-hand sides in lock step with
+ * the batched operator, each with its own Krylov basis, Hessenberg matrix, rotations and stop
+ * test (a converged right-hand side is frozen).  iters[r] and est_error[r] as in ifgf2d_solve
+ * (either may be NULL).  Returns IFGF2D_ERR_NOCONV when some right-hand side reached max_iters
+ * first. */
+int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
+                       int max_iters, int* iters, double* est_error);
+
 /* ForwardMap::propagate_unacc (ForwardMap/ForwardMap.tpp:701-727): direct off-surface field */
 int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp,
                      const double* density, double* out);
