@@ -34,7 +34,7 @@ def nvcc() -> str:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-ffp-contract=off",
+           "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread",
            "-c", os.path.join(CSRC, src), "-o", obj]
     if src in NO_FMAD:
         cmd[1:1] = ["-fmad=false"]
@@ -59,7 +59,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             return LIB
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", LIB, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

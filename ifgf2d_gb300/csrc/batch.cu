@@ -7,6 +7,7 @@
 // apply per iteration, per-RHS Gram-Schmidt coefficients from batched reductions, and each
 // right-hand side's own Givens rotations, residual estimate and stop test on the host.
 #include "context.hpp"
+#include "host_threads.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -38,19 +39,21 @@ template <typename R>
 std::vector<PropB<R>> sorted_plan(const Tree& T) {
     std::vector<PropB<R>> out(T.pp.size());
     const int P = T.P;
-    std::vector<int> idx;
-    for (int pc = 0; pc < T.total_cones; ++pc) {
-        const long long e0 = T.pp_ptr[pc];
-        const int ne = (int)(T.pp_ptr[pc + 1] - e0);
-        idx.resize(ne);
-        for (int i = 0; i < ne; ++i) idx[i] = i;
-        std::stable_sort(idx.begin(), idx.end(),
-                         [&](int a, int b) { return T.pp[e0 + a].child_cone < T.pp[e0 + b].child_cone; });
-        for (int q = 0; q < ne; ++q) {
-            const PropEntry& e = T.pp[e0 + idx[q]];
-            out[e0 + q] = PropB<R>{e.child_cone, idx[q] % P, (R)e.s, (R)e.th, (R)e.wr, (R)e.wi};
+    parallel_for(T.total_cones, [&](long long p0, long long p1) {
+        std::vector<int> idx;
+        for (long long pc = p0; pc < p1; ++pc) {
+            const long long e0 = T.pp_ptr[pc];
+            const int ne = (int)(T.pp_ptr[pc + 1] - e0);
+            idx.resize(ne);
+            for (int i = 0; i < ne; ++i) idx[i] = i;
+            std::stable_sort(idx.begin(), idx.end(),
+                             [&](int a, int b) { return T.pp[e0 + a].child_cone < T.pp[e0 + b].child_cone; });
+            for (int q = 0; q < ne; ++q) {
+                const PropEntry& e = T.pp[e0 + idx[q]];
+                out[e0 + q] = PropB<R>{e.child_cone, idx[q] % P, (R)e.s, (R)e.th, (R)e.wr, (R)e.wi};
+            }
         }
-    }
+    }, 256);
     return out;
 }
 

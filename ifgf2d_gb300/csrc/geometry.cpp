@@ -1,5 +1,6 @@
 // geometry.cpp -- host discretisation of the boundary (see geometry.hpp for the reference map).
 #include "geometry.hpp"
+#include "host_threads.hpp"
 #include <algorithm>
 #include <cstring>
 
@@ -248,7 +249,6 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
         }
     }
     std::vector<int> per(ncurves), first(ncurves), past(ncurves);
-    std::vector<Box4> boxes;
     for (int c = 0; c < ncurves; ++c) {
         const HostCurve& cv = D.curves[c];
         std::vector<double> lims = patch_limits(cv, opt.wavelengths_per_patch, opt.patch_split_wavenumber, opt.patches_per_curve);
@@ -262,7 +262,6 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
             const bool open = !cv.closed;
             const int s1 = open && (np == 1 || pi == 0), s2 = open && (np == 1 || pi == np - 1);
             D.ist1sing.push_back(s1); D.ist2sing.push_back(s2);
-            boxes.push_back(patch_box(cv, a, b, D.delta));
             for (int j = 0; j < Np; ++j) {
                 const double z = D.fej_n[j];
                 double tm = z, ej = 0.0;
@@ -284,6 +283,11 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
         }
     }
     D.N = D.num_patches * Np;
+    // patch bounding boxes (Patch.tpp:36-64), one per patch, independent of each other
+    std::vector<Box4> boxes(D.num_patches);
+    parallel_for(D.num_patches, [&](long long p0, long long p1) {
+        for (long long pi = p0; pi < p1; ++pi) boxes[pi] = patch_box(D.curves[D.curve_of[pi]], D.t1[pi], D.t2[pi], D.delta);
+    }, 16);
     // candidate patches (ForwardMap.tpp:164-219); junction entries keep the reference's
     // `curve_patches_end` index, which names the patch after the touching curve
     std::vector<std::vector<long long>> cand(D.num_patches);
@@ -303,27 +307,33 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
             } else { e.push_back(s + pi - 1); e.push_back(s + pi + 1); }
         }
     }
-    // near-singular points (ForwardMap.tpp:224-285)
-    D.ns_ptr.assign(D.num_patches + 1, 0);
-    for (long long pi = 0; pi < D.num_patches; ++pi) {
-        const HostCurve& cv = D.curves[D.curve_of[pi]];
-        const double a = D.t1[pi], b = D.t2[pi];
-        for (long long tp : cand[pi]) {
-            if (tp < 0 || tp >= D.num_patches) continue;
-            for (long long kk = tp * Np; kk < tp * Np + Np; ++kk) {
-                const double xp = D.x[kk], yp = D.y[kk];
-                if (!box_contains(boxes[pi], xp, yp)) continue;
-                auto dist = [&](double t) {
-                    const double dx = cv.x(t) - xp, dy = cv.y(t) - yp;
-                    return std::sqrt(std::fabs(dx * dx + dy * dy));
-                };
-                double tsing, dmin;
-                if (dist(a) < D.delta) tsing = a;
-                else if (dist(b) < D.delta) tsing = b;
-                else { brent_min(dist, a, b, tsing, dmin); if (!(dmin < D.delta)) continue; }
-                D.ns_idx.push_back(kk); D.ns_t.push_back(tsing);
+    // near-singular points (ForwardMap.tpp:224-285), per patch in parallel, then concatenated
+    std::vector<std::vector<std::pair<long long, double>>> found(D.num_patches);
+    parallel_for(D.num_patches, [&](long long p0, long long p1) {
+        for (long long pi = p0; pi < p1; ++pi) {
+            const HostCurve& cv = D.curves[D.curve_of[pi]];
+            const double a = D.t1[pi], b = D.t2[pi];
+            for (long long tp : cand[pi]) {
+                if (tp < 0 || tp >= D.num_patches) continue;
+                for (long long kk = tp * Np; kk < tp * Np + Np; ++kk) {
+                    const double xp = D.x[kk], yp = D.y[kk];
+                    if (!box_contains(boxes[pi], xp, yp)) continue;
+                    auto dist = [&](double t) {
+                        const double dx = cv.x(t) - xp, dy = cv.y(t) - yp;
+                        return std::sqrt(std::fabs(dx * dx + dy * dy));
+                    };
+                    double tsing, dmin;
+                    if (dist(a) < D.delta) tsing = a;
+                    else if (dist(b) < D.delta) tsing = b;
+                    else { brent_min(dist, a, b, tsing, dmin); if (!(dmin < D.delta)) continue; }
+                    found[pi].push_back({kk, tsing});
+                }
             }
         }
+    }, 16);
+    D.ns_ptr.assign(D.num_patches + 1, 0);
+    for (long long pi = 0; pi < D.num_patches; ++pi) {
+        for (auto& f : found[pi]) { D.ns_idx.push_back(f.first); D.ns_t.push_back(f.second); }
         D.ns_ptr[pi + 1] = (int)D.ns_idx.size();
     }
     return "";

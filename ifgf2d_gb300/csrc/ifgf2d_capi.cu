@@ -11,6 +11,7 @@
 #include <memory>
 
 #include "context.hpp"
+#include "host_threads.hpp"
 
 using namespace ifgf;
 
@@ -314,26 +315,29 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     CK(cudaGetLastError());
     // propagation and interpolation plans
     {
-        std::vector<PropEntryD> pe(T.pp.size());
-        for (size_t i = 0; i < T.pp.size(); ++i) { const PropEntry& e = T.pp[i]; pe[i] = PropEntryD{e.child_cone, 0, e.s, e.th, e.wr, e.wi}; }
-        CK(ctx->pp.upload(pe));
+        // the host plan entries have the device layout of the FP64 form
+        static_assert(sizeof(PropEntry) == sizeof(PropEntryD) && sizeof(InterpEntry) == sizeof(InterpEntryD),
+                      "host and device plan layouts differ");
+        CK(ctx->pp.upload(reinterpret_cast<const PropEntryD*>(T.pp.data()), T.pp.size()));
         CK(ctx->pp_ptr.upload(T.pp_ptr)); CK(ctx->pp_nchild.upload(T.pp_nchild));
-        std::vector<InterpEntryD> ie(T.ip.size());
-        for (size_t i = 0; i < T.ip.size(); ++i) { const InterpEntry& e = T.ip[i]; ie[i] = InterpEntryD{e.cone, 0, e.s, e.th, e.fr, e.fi}; }
-        CK(ctx->ip.upload(ie));
+        CK(ctx->ip.upload(reinterpret_cast<const InterpEntryD*>(T.ip.data()), T.ip.size()));
         CK(ctx->ip_ptr.upload(T.ip_ptr));
         // complex64 copies for the mixed form (values computed in FP64, rounded once)
         std::vector<PropE<float>> pf(T.pp.size());
-        for (size_t i = 0; i < T.pp.size(); ++i) {
-            const PropEntry& e = T.pp[i];
-            pf[i] = PropE<float>{e.child_cone, (float)e.s, (float)e.th, (float)e.wr, (float)e.wi};
-        }
+        parallel_for((long long)T.pp.size(), [&](long long i0, long long i1) {
+            for (long long i = i0; i < i1; ++i) {
+                const PropEntry& e = T.pp[i];
+                pf[i] = PropE<float>{e.child_cone, (float)e.s, (float)e.th, (float)e.wr, (float)e.wi};
+            }
+        }, 1 << 16);
         CK(ctx->pp32.upload(pf));
         std::vector<InterpE<float>> jf(T.ip.size());
-        for (size_t i = 0; i < T.ip.size(); ++i) {
-            const InterpEntry& e = T.ip[i];
-            jf[i] = InterpE<float>{e.cone, (float)e.s, (float)e.th, (float)e.fr, (float)e.fi};
-        }
+        parallel_for((long long)T.ip.size(), [&](long long i0, long long i1) {
+            for (long long i = i0; i < i1; ++i) {
+                const InterpEntry& e = T.ip[i];
+                jf[i] = InterpE<float>{e.cone, (float)e.s, (float)e.th, (float)e.fr, (float)e.fi};
+            }
+        }, 1 << 16);
         CK(ctx->ip32.upload(jf));
     }
     CK(ctx->coef.alloc((size_t)T.total_cones * P));

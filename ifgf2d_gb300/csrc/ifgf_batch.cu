@@ -8,7 +8,8 @@
 // density / coefficient accesses are 256-byte coalesced rows.
 //
 //   k_sing_b   singular correction + jump term + intensities     ForwardMap.tpp:425-435, 481-515
-//   k_leaf_b   leaf cone coefficients, 25 accumulators per lane    BoxTree.h:685-762
+//   k_leaf_b   leaf cone coefficients, table rows staged in shared
+//              memory by cp.async, 25 accumulators per RHS          BoxTree.h:685-762
 //   k_prop_b   child -> parent, per parent cone one warp; the
 //              parent's terms sorted by child cone so each child
 //              cone's coefficients are loaded once                 BoxTree.h:767-868, Interpolator.h:81-120
@@ -87,115 +88,202 @@ __global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, 
     }
 }
 
+// ------------------------------------------------------------------ asynchronous copies
+// cp.async (global -> shared without a register round trip) of one 8- or 16-byte element
+template <int BYTES>
+__device__ __forceinline__ void cp_async_el(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
+
+// right-hand sides per lane: two for the complex64 form (a warp covers a 64-wide batch, so
+// every table entry is read once per batch), one for FP64 (register budget)
+template <typename R> struct Rpl { static constexpr int v = sizeof(R) == 4 ? 2 : 1; };
+
 // ------------------------------------------------------------------ leaf cones
-// warp = one leaf cone, lane = one right-hand side, P accumulators per lane
-template <typename R, int P>
-__global__ void __launch_bounds__(256) k_leaf_b(const int* __restrict__ cone_box, int ncones, int cone_base,
-                                                const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
-                                                const long long* __restrict__ leaf_off, const V2<R>* __restrict__ L,
-                                                const V2<R>* __restrict__ rho, int B, V2<R>* __restrict__ coef) {
-    const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
-    const int r = blockIdx.y * 32 + (threadIdx.x & 31);
-    if (c >= ncones) return;
-    const bool act = r < B;
-    const int rr = act ? r : 0;
+// warp = one leaf cone x 32*RPL right-hand sides, P accumulators per (lane, RHS).  The cone's
+// table rows stream through shared memory in tiles of TS sources (cp.async, double-buffered)
+// and every lane reads them as broadcasts; densities are prefetched one source ahead.
+constexpr int kLeafWarps = 4;
+template <typename R, int P, int RPL>
+__global__ void __launch_bounds__(kLeafWarps * 32) k_leaf_b(const int* __restrict__ cone_box, int ncones, int cone_base,
+                                                            const int* __restrict__ leaf_start,
+                                                            const int* __restrict__ leaf_count,
+                                                            const long long* __restrict__ leaf_off,
+                                                            const V2<R>* __restrict__ L, const V2<R>* __restrict__ rho, int B,
+                                                            V2<R>* __restrict__ coef) {
+    constexpr int TS = sizeof(R) == 4 ? 16 : 8;
+    __shared__ V2<R> tile[kLeafWarps][2][TS * P];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kLeafWarps + w;
+    if (c >= ncones) return;                 // warps are independent: no block-wide barrier below
+    int rr[RPL];
+    bool act[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+        const int r = blockIdx.y * 32 * RPL + 32 * k + lane;
+        act[k] = r < B;
+        rr[k] = act[k] ? r : 0;
+    }
     const int b = cone_box[c];
     const int n = leaf_count[b], s0 = leaf_start[b];
     const V2<R>* Lc = L + leaf_off[c];
-    const V2<R>* rh = rho + (long long)s0 * B + rr;
-    V2<R> acc[P];
+    auto load_tile = [&](int t) {
+        const int sb = t * TS;
+        const int cnt = (n - sb < TS ? n - sb : TS) * P;
+        const V2<R>* src = Lc + (long long)sb * P;
+        V2<R>* dst = tile[w][t & 1];
+        for (int q = lane; q < cnt; q += 32) cp_async_el<(int)sizeof(V2<R>)>(dst + q, src + q);
+        cp_async_commit();
+    };
+    V2<R> acc[RPL][P];
 #pragma unroll
-    for (int m = 0; m < P; ++m) { acc[m].x = R(0); acc[m].y = R(0); }
-    for (int s = 0; s < n; ++s) {
-        const V2<R> v = rh[(long long)s * B];
-        const V2<R>* l = Lc + (long long)s * P;
+    for (int k = 0; k < RPL; ++k)
 #pragma unroll
-        for (int m = 0; m < P; ++m) cmac<R>(acc[m], l[m], v);
+        for (int m = 0; m < P; ++m) { acc[k][m].x = R(0); acc[k][m].y = R(0); }
+    const V2<R>* rh = rho + (long long)s0 * B;
+    V2<R> vn[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) vn[k] = rh[rr[k]];
+    const int nt = (n + TS - 1) / TS;
+    load_tile(0);
+    for (int t = 0; t < nt; ++t) {
+        if (t + 1 < nt) { load_tile(t + 1); cp_async_wait<1>(); }
+        else cp_async_wait<0>();
+        __syncwarp();
+        const V2<R>* Lt = tile[w][t & 1];
+        const int sb = t * TS;
+        const int cnt = n - sb < TS ? n - sb : TS;
+        for (int s = 0; s < cnt; ++s) {
+            V2<R> v[RPL];
+#pragma unroll
+            for (int k = 0; k < RPL; ++k) v[k] = vn[k];
+            if (sb + s + 1 < n) {
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) vn[k] = rh[(long long)(sb + s + 1) * B + rr[k]];
+            }
+#pragma unroll
+            for (int m = 0; m < P; ++m) {
+                const V2<R> l = Lt[s * P + m];
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) cmac<R>(acc[k][m], l, v[k]);
+            }
+        }
+        __syncwarp();                        // the buffer is refilled two tiles later
     }
-    if (act) {
-        V2<R>* out = coef + (long long)(cone_base + c) * P * B + r;
 #pragma unroll
-        for (int m = 0; m < P; ++m) out[(long long)m * B] = acc[m];
+    for (int k = 0; k < RPL; ++k) {
+        if (!act[k]) continue;
+        V2<R>* out = coef + (long long)(cone_base + c) * P * B + rr[k];
+#pragma unroll
+        for (int m = 0; m < P; ++m) out[(long long)m * B] = acc[k][m];
     }
 }
 
 // ------------------------------------------------------------------ propagation
-// warp = one parent cone, lane = one right-hand side.  Node values accumulate in the lane's own
-// shared-memory column; the values -> coefficients map then runs in the lane's registers.
-template <typename R, int P>
+// warp = one parent cone x 32*RPL right-hand sides.  Node values accumulate in the lane's own
+// shared-memory columns; the values -> coefficients map then runs in the lane's registers.
+template <typename R, int P, int RPL>
 struct PropBlock {
-    static constexpr int bytes_per_warp = P * 32 * (int)sizeof(V2<R>);
+    static constexpr int bytes_per_warp = P * 32 * RPL * (int)sizeof(V2<R>);
     static constexpr int W = 32768 / bytes_per_warp >= 4 ? 4 : (32768 / bytes_per_warp >= 2 ? 2 : 1);
 };
-template <typename R, int PS, int PA, int WPB>
+template <typename R, int PS, int PA, int WPB, int RPL>
 __global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const long long* __restrict__ pp_ptr,
                                                      const int* __restrict__ pp_nchild, const PropB<R>* __restrict__ pb,
                                                      const R* __restrict__ Gsep, int B, V2<R>* __restrict__ coef) {
     constexpr int P = PS * PA;
-    __shared__ V2<R> sv[WPB][P][32];
+    __shared__ V2<R> sv[WPB][P][32 * RPL];
     __shared__ R sG[PS * PS + PA * PA];
     for (int i = threadIdx.x; i < PS * PS + PA * PA; i += blockDim.x) sG[i] = Gsep[i];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pc = pbegin + blockIdx.x * WPB + w;
     if (pc >= pend) return;
-    const int r = blockIdx.y * 32 + lane;
-    const bool act = r < B;
-    const int rr = act ? r : 0;
+    int rr[RPL];
+    bool act[RPL];
 #pragma unroll
-    for (int q = 0; q < P; ++q) { sv[w][q][lane].x = R(0); sv[w][q][lane].y = R(0); }
+    for (int k = 0; k < RPL; ++k) {
+        const int r = blockIdx.y * 32 * RPL + 32 * k + lane;
+        act[k] = r < B;
+        rr[k] = act[k] ? r : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) { sv[w][q][32 * k + lane].x = R(0); sv[w][q][32 * k + lane].y = R(0); }
     const long long e0 = pp_ptr[pc];
     const int ne = pp_nchild[pc] * P;
-    V2<R> cc[P];
+    V2<R> cc[RPL][P];
     int cur = -1;
+    PropB<R> En{};
+    if (ne > 0) En = pb[e0];
     for (int e = 0; e < ne; ++e) {
-        const PropB<R> E = pb[e0 + e];
+        const PropB<R> E = En;
+        if (e + 1 < ne) En = pb[e0 + e + 1];   // next term in flight during this one
         if (E.child_cone != cur) {             // warp-uniform: E is the same for every lane
             cur = E.child_cone;
-            const V2<R>* src = coef + (long long)cur * P * B + rr;
+            const V2<R>* src = coef + (long long)cur * P * B;
 #pragma unroll
-            for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B];
+            for (int k = 0; k < RPL; ++k)
+#pragma unroll
+                for (int q = 0; q < P; ++q) cc[k][q] = src[(long long)q * B + rr[k]];
         }
-        const V2<R> it = interp_eval<R, PS, PA>(cc, E.s, E.th);
+        R Ts[PS], Tt[PA];
+        cheb_row<R, PS>(E.s, Ts);
+        cheb_row<R, PA>(E.th, Tt);
         V2<R> wv; wv.x = E.wr; wv.y = E.wi;
-        V2<R> a = sv[w][E.pt][lane];
-        cmac<R>(a, it, wv);
-        sv[w][E.pt][lane] = a;
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) {
+            const V2<R> it = interp_eval_tt<R, PS, PA>(cc[k], Ts, Tt);
+            V2<R> a = sv[w][E.pt][32 * k + lane];
+            cmac<R>(a, it, wv);
+            sv[w][E.pt][32 * k + lane] = a;
+        }
     }
     // u[l][m] = sum_k Gs[m][k] v[l][k];  c[n][m] = sum_l Ga[n][l] u[l][m], stored at n*PS + m
-    V2<R> u[P];
 #pragma unroll
-    for (int l = 0; l < PA; ++l) {
-        V2<R> v[PS];
+    for (int k = 0; k < RPL; ++k) {
+        V2<R> u[P];
 #pragma unroll
-        for (int k = 0; k < PS; ++k) v[k] = sv[w][l * PS + k][lane];
+        for (int l = 0; l < PA; ++l) {
+            V2<R> v[PS];
 #pragma unroll
-        for (int m = 0; m < PS; ++m) {
-            V2<R> a; a.x = R(0); a.y = R(0);
+            for (int q = 0; q < PS; ++q) v[q] = sv[w][l * PS + q][32 * k + lane];
 #pragma unroll
-            for (int k = 0; k < PS; ++k) { const R g = sG[m * PS + k]; a.x = rfma(g, v[k].x, a.x); a.y = rfma(g, v[k].y, a.y); }
-            u[l * PS + m] = a;
-        }
-    }
-    if (!act) return;
-    V2<R>* out = coef + (long long)pc * P * B + r;
+            for (int m = 0; m < PS; ++m) {
+                V2<R> a; a.x = R(0); a.y = R(0);
 #pragma unroll
-    for (int n = 0; n < PA; ++n)
-#pragma unroll
-        for (int m = 0; m < PS; ++m) {
-            V2<R> a; a.x = R(0); a.y = R(0);
-#pragma unroll
-            for (int l = 0; l < PA; ++l) {
-                const R g = sG[PS * PS + n * PA + l];
-                a.x = rfma(g, u[l * PS + m].x, a.x); a.y = rfma(g, u[l * PS + m].y, a.y);
+                for (int q = 0; q < PS; ++q) { const R g = sG[m * PS + q]; a.x = rfma(g, v[q].x, a.x); a.y = rfma(g, v[q].y, a.y); }
+                u[l * PS + m] = a;
             }
-            out[(long long)(n * PS + m) * B] = a;
         }
+        if (!act[k]) continue;
+        V2<R>* out = coef + (long long)pc * P * B + rr[k];
+#pragma unroll
+        for (int n = 0; n < PA; ++n)
+#pragma unroll
+            for (int m = 0; m < PS; ++m) {
+                V2<R> a; a.x = R(0); a.y = R(0);
+#pragma unroll
+                for (int l = 0; l < PA; ++l) {
+                    const R g = sG[PS * PS + n * PA + l];
+                    a.x = rfma(g, u[l * PS + m].x, a.x); a.y = rfma(g, u[l * PS + m].y, a.y);
+                }
+                out[(long long)(n * PS + m) * B] = a;
+            }
+    }
 }
 
 // ------------------------------------------------------------------ near field + interpolation
-// warp = one Morton-sorted target, lane = one right-hand side; y accumulated at the original index
-template <typename R, int PS, int PA>
+// warp = one Morton-sorted target x 32*RPL right-hand sides; y accumulated at the original index
+template <typename R, int PS, int PA, int RPL>
 __global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
                                                  const int* __restrict__ leaf_count, const int* __restrict__ nbr_ptr,
                                                  const int* __restrict__ nbr_box, const int* __restrict__ near_rowlen,
@@ -205,36 +293,70 @@ __global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ 
                                                  const long long* __restrict__ sorting, int B, double2* __restrict__ yt) {
     constexpr int P = PS * PA;
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-    const int r = blockIdx.y * 32 + (threadIdx.x & 31);
+    const int lane = threadIdx.x & 31;
     if (i >= N) return;
-    const bool act = r < B;
-    const int rr = act ? r : 0;
+    int rr[RPL];
+    bool act[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+        const int r = blockIdx.y * 32 * RPL + 32 * k + lane;
+        act[k] = r < B;
+        rr[k] = act[k] ? r : 0;
+    }
     const int b = point_leaf[i];
     const int t = i - leaf_start[b];
     const V2<R>* row = near + near_off[b] + (long long)t * near_rowlen[b];
-    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    V2<R> acc[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) { acc[k].x = R(0); acc[k].y = R(0); }
     int sg = 0;
     for (int q = nbr_ptr[b]; q < nbr_ptr[b + 1]; ++q) {
         const int bb = nbr_box[q];
         const int c = leaf_count[bb];
-        const V2<R>* rh = rho + (long long)leaf_start[bb] * B + rr;
-        for (int s = 0; s < c; ++s) cmac<R>(acc, row[sg + s], rh[(long long)s * B]);
+        const V2<R>* rh = rho + (long long)leaf_start[bb] * B;
+        int s = 0;
+        for (; s + 4 <= c; s += 4) {           // four sources' loads in flight at once
+            V2<R> nv[4], rv[4][RPL];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                nv[u] = row[sg + s + u];
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) rv[u][k] = rh[(long long)(s + u) * B + rr[k]];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int k = 0; k < RPL; ++k) cmac<R>(acc[k], nv[u], rv[u][k]);
+        }
+        for (; s < c; ++s) {
+            const V2<R> nv = row[sg + s];
+#pragma unroll
+            for (int k = 0; k < RPL; ++k) cmac<R>(acc[k], nv, rh[(long long)s * B + rr[k]]);
+        }
         sg += c;
     }
     for (int e = ip_ptr[i]; e < ip_ptr[i + 1]; ++e) {
         const InterpE<R> E = ip[e];
-        const V2<R>* src = coef + (long long)E.cone * P * B + rr;
-        V2<R> cc[P];
-#pragma unroll
-        for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B];
-        const V2<R> it = interp_eval<R, PS, PA>(cc, E.s, E.th);
+        R Ts[PS], Tt[PA];
+        cheb_row<R, PS>(E.s, Ts);
+        cheb_row<R, PA>(E.th, Tt);
         V2<R> f; f.x = E.fr; f.y = E.fi;
-        cmac<R>(acc, it, f);
+        const V2<R>* src = coef + (long long)E.cone * P * B;
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) {
+            V2<R> cc[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B + rr[k]];
+            cmac<R>(acc[k], interp_eval_tt<R, PS, PA>(cc, Ts, Tt), f);
+        }
     }
-    if (act) {
-        double2* yo = yt + sorting[i] * B + r;
+    const long long o = sorting[i];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+        if (!act[k]) continue;
+        double2* yo = yt + o * B + rr[k];
         double2 v = *yo;
-        v.x += (double)acc.x; v.y += (double)acc.y;
+        v.x += (double)acc[k].x; v.y += (double)acc[k].y;
         *yo = v;
     }
 }
@@ -337,17 +459,19 @@ void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* le
                    const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int Ps, int Pang, int B, V2<R>* coef,
                    cudaStream_t s) {
     if (ncones <= 0) return;
-    const dim3 grid(nblk_b(ncones, 8), nblk_b(B, 32));
-    IFGF_DISPATCH_P(Ps, Pang, (k_leaf_b<R, PS * PA><<<grid, 256, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count,
-                                                                        leaf_off, L, rho, B, coef)));
+    constexpr int RPL = Rpl<R>::v;
+    const dim3 grid(nblk_b(ncones, kLeafWarps), nblk_b(B, 32 * RPL));
+    IFGF_DISPATCH_P(Ps, Pang, (k_leaf_b<R, PS * PA, RPL><<<grid, kLeafWarps * 32, 0, s>>>(
+                                   cone_box, ncones, cone_base, leaf_start, leaf_count, leaf_off, L, rho, B, coef)));
 }
 template <typename R>
 void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
                    const R* Gsep, int B, V2<R>* coef, cudaStream_t s) {
     if (pend <= pbegin) return;
+    constexpr int RPL = Rpl<R>::v;
     IFGF_DISPATCH_P(Ps, Pang, {
-        constexpr int WPB = PropBlock<R, PS * PA>::W;
-        k_prop_b<R, PS, PA, WPB><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32)), WPB * 32, 0, s>>>(
+        constexpr int WPB = PropBlock<R, PS * PA, RPL>::W;
+        k_prop_b<R, PS, PA, WPB, RPL><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32 * RPL)), WPB * 32, 0, s>>>(
             pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
     });
 }
@@ -356,10 +480,11 @@ void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const i
                     const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,
                     const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
                     const long long* sorting, int B, double2* yt, cudaStream_t s) {
-    const dim3 grid(nblk_b(N, 8), nblk_b(B, 32));
-    IFGF_DISPATCH_P(Ps, Pang, (k_final_b<R, PS, PA><<<grid, 256, 0, s>>>(N, point_leaf, leaf_start, leaf_count, nbr_ptr,
-                                                                        nbr_box, near_rowlen, near_off, near, rho, ip_ptr,
-                                                                        ip, coef, sorting, B, yt)));
+    constexpr int RPL = Rpl<R>::v;
+    const dim3 grid(nblk_b(N, 8), nblk_b(B, 32 * RPL));
+    IFGF_DISPATCH_P(Ps, Pang, (k_final_b<R, PS, PA, RPL><<<grid, 256, 0, s>>>(N, point_leaf, leaf_start, leaf_count,
+                                                                             nbr_ptr, nbr_box, near_rowlen, near_off, near,
+                                                                             rho, ip_ptr, ip, coef, sorting, B, yt)));
 }
 void launch_bdot(const double2* V, long long ldc, int ncols, const double2* w, long long N, int B, double2* part,
                  double2* h, double2* Hcol, int add, int sqrt_row, cudaStream_t s) {

@@ -45,6 +45,31 @@ __device__ __forceinline__ V2<R> interp_eval(const V2<R>* __restrict__ c, R s, R
     return r;
 }
 
+// T_0..T_{n-1} at x (Chebyshev.h:38-68)
+template <typename R, int NT>
+__device__ __forceinline__ void cheb_row(R x, R* T) {
+    T[0] = R(1);
+    if (NT > 1) T[1] = x;
+#pragma unroll
+    for (int i = 2; i < NT; ++i) T[i] = R(2) * x * T[i - 1] - T[i - 2];
+}
+// interp_eval with the Chebyshev rows precomputed (shared by several right-hand sides)
+template <typename R, int PS, int PA>
+__device__ __forceinline__ V2<R> interp_eval_tt(const V2<R>* __restrict__ c, const R* Ts, const R* Tt) {
+    V2<R> r; r.x = R(0); r.y = R(0);
+#pragma unroll
+    for (int a = 0; a < PA; ++a) {
+        V2<R> u; u.x = R(0); u.y = R(0);
+#pragma unroll
+        for (int q = 0; q < PS; ++q) {
+            const V2<R> v = c[a * PS + q];
+            u.x = rfma(Ts[q], v.x, u.x); u.y = rfma(Ts[q], v.y, u.y);
+        }
+        r.x = rfma(Tt[a], u.x, r.x); r.y = rfma(Tt[a], u.y, r.y);
+    }
+    return r;
+}
+
 #define IFGF_DISPATCH_P(PS_, PA_, ...)                                              \
     if (PS_ == 5 && PA_ == 5) { constexpr int PS = 5, PA = 5; __VA_ARGS__; }        \
     else if (PS_ == 5 && PA_ == 7) { constexpr int PS = 5, PA = 7; __VA_ARGS__; }   \

@@ -5,6 +5,7 @@
 #include <numeric>
 #include <unordered_map>
 #include <array>
+#include "host_threads.hpp"
 
 namespace ifgf {
 
@@ -54,6 +55,36 @@ int TreeLevel::find_cone(int b, long long nonrel) const {
     auto it = std::lower_bound(first, last, nonrel);
     return (it != last && *it == nonrel) ? (int)(it - cone_nonrel.begin()) : -1;
 }
+
+// ---------------------------------------------------------------- host threads
+namespace {
+void sort_unique(std::vector<unsigned long long>& v) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+}
+// union of sorted, duplicate-free lists: pairwise merges, in parallel per round
+std::vector<unsigned long long> merge_unique(std::vector<std::vector<unsigned long long>>& parts) {
+    if (parts.empty()) return {};
+    while (parts.size() > 1) {
+        const long long np = (long long)(parts.size() + 1) / 2;
+        std::vector<std::vector<unsigned long long>> next(np);
+        parallel_for(np, [&](long long q0, long long q1) {
+            for (long long q = q0; q < q1; ++q) {
+                if (2 * q + 1 >= (long long)parts.size()) { next[q].swap(parts[2 * q]); continue; }
+                auto& a = parts[2 * q];
+                auto& b = parts[2 * q + 1];
+                next[q].resize(a.size() + b.size());
+                auto e = std::set_union(a.begin(), a.end(), b.begin(), b.end(), next[q].begin());
+                next[q].resize(e - next[q].begin());
+                std::vector<unsigned long long>().swap(a);
+                std::vector<unsigned long long>().swap(b);
+            }
+        }, 1);
+        parts.swap(next);
+    }
+    return std::move(parts[0]);
+}
+}  // namespace
 
 // ---------------------------------------------------------------- per-level geometry
 namespace {
@@ -239,78 +270,131 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     for (int i = 0; i < Pang; ++i) na[Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Pang));
     const int P = T.P;
 
-    // relevant cones, level by level (BoxTree.h:553-583)
-    std::vector<int> cous;
+    // relevant cones, level by level (BoxTree.h:553-583).  A wanted cone is the key
+    // (box index << 32 | nonrel cone); each level's keys are collected per thread, then sorted
+    // and deduplicated, which gives the cones in (box, nonrel) order.
+    std::vector<std::vector<PropEntry>> level_pp(nlevels);
     for (int l = 2; l < nlevels; ++l) {
         TreeLevel& L = T.L[l];
         LevelGeo G{&L, T.min_x, T.min_y};
-        std::vector<std::pair<int, long long>> want;   // (box index, nonrel cone)
-        // cones seen by the cousins' points (BoxTree.h:235-277)
-        long long old = -1;
         const int shift = 2 * (D - l);
-        for (long long i = 0; i < N; ++i) {
-            const long long m = scode[i] >> shift;
-            if (m != old) { cousins_of(L, m, cous); old = m; }
-            for (int c : cous) want.push_back({c, G.nonrel_of(L.boxes[c], T.xs[i], T.ys[i])});
+        auto key = [](long long b, long long nonrel) { return ((unsigned long long)b << 32) | (unsigned long long)nonrel; };
+        std::vector<std::vector<unsigned long long>> part;
+        // cones seen by the cousins' points (BoxTree.h:235-277)
+        {
+            const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, N / 1024));
+            part.resize(nchunk);
+            parallel_for(nchunk, [&](long long c0, long long c1) {
+                std::vector<int> cs;
+                for (long long c = c0; c < c1; ++c) {
+                    const long long i0 = N * c / nchunk, i1 = N * (c + 1) / nchunk;
+                    long long old = -1;
+                    auto& w = part[c];
+                    for (long long i = i0; i < i1; ++i) {
+                        const long long m = scode[i] >> shift;
+                        if (m != old) { cousins_of(L, m, cs); old = m; }
+                        for (int cb : cs) w.push_back(key(cb, G.nonrel_of(L.boxes[cb], T.xs[i], T.ys[i])));
+                    }
+                    sort_unique(w);
+                }
+            }, 1);
         }
         // cones needed by the parents' interpolation nodes, through the protobox routing
         // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
         // routing is computed once, from the first parent box (in cone order) that has it.
-        if (l > 2) {
-            const TreeLevel& Lp = T.L[l - 1];
+        struct Route { long long pnc; int pos; int first_pc; std::vector<std::pair<long long, int>> e; };
+        std::vector<Route> routes;
+        std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
+        const TreeLevel* Lpp = l > 2 ? &T.L[l - 1] : nullptr;
+        if (Lpp) {
+            const TreeLevel& Lp = *Lpp;
             LevelGeo Gp{&Lp, T.min_x, T.min_y};
-            std::unordered_map<long long, std::array<std::vector<std::pair<long long, int>>, 4>> proto;  // nonrel -> pos -> (child nonrel, node)
-            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
-                const int pb = Lp.cone_box[pc];
-                const long long pm = Lp.boxes[pb], pnc = Lp.cone_nonrel[pc];
-                auto& entry = proto[pnc];
-                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
-                    const int cb = L.find_box(cm);
-                    if (cb < 0) continue;
-                    auto& v = entry[cm % 4];
-                    if (!v.empty()) continue;
+            const size_t npar = Lp.cone_nonrel.size();
+            route_of.assign(npar * 4, -1);
+            std::unordered_map<long long, int> seen;   // pnc * 4 + pos -> route
+            for (size_t pc = 0; pc < npar; ++pc) {
+                const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
+                for (int pos = 0; pos < 4; ++pos) {
+                    if (L.find_box(pm * 4 + pos) < 0) continue;
+                    auto it = seen.find(pnc * 4 + pos);
+                    if (it == seen.end()) {
+                        it = seen.emplace(pnc * 4 + pos, (int)routes.size()).first;
+                        routes.push_back(Route{pnc, pos, (int)pc, {}});
+                    }
+                    route_of[pc * 4 + pos] = it->second;
+                }
+            }
+            parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
+                for (long long r = r0; r < r1; ++r) {
+                    Route& R = routes[r];
+                    const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
                     for (int it = 0; it < P; ++it) {
                         double px = ns[it % Ps], py = na[it / Ps];
-                        Gp.cheb_to_cart(pm, pnc, px, py);
-                        v.push_back({G.nonrel_of(cm, px, py), it});
+                        Gp.cheb_to_cart(pm, R.pnc, px, py);
+                        R.e.push_back({G.nonrel_of(pm * 4 + R.pos, px, py), it});
                     }
                 }
-            }
-            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
-                const long long pm = Lp.boxes[Lp.cone_box[pc]];
-                const auto& entry = proto.at(Lp.cone_nonrel[pc]);
-                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
-                    const int cb = L.find_box(cm);
-                    if (cb < 0) continue;
-                    for (auto& e : entry[cm % 4]) want.push_back({cb, e.first});
+            });
+            const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, (long long)npar / 256));
+            const size_t base = part.size();
+            part.resize(base + nchunk);
+            parallel_for(nchunk, [&](long long c0, long long c1) {
+                for (long long c = c0; c < c1; ++c) {
+                    const size_t p0 = npar * c / nchunk, p1 = npar * (c + 1) / nchunk;
+                    auto& w = part[base + c];
+                    for (size_t pc = p0; pc < p1; ++pc) {
+                        const long long pm = Lp.boxes[Lp.cone_box[pc]];
+                        for (int pos = 0; pos < 4; ++pos) {
+                            const int r = route_of[pc * 4 + pos];
+                            if (r < 0) continue;
+                            const int cb = L.find_box(pm * 4 + pos);
+                            for (auto& e : routes[r].e) w.push_back(key(cb, e.first));
+                        }
+                    }
+                    sort_unique(w);
                 }
-            }
-            // merged cone list first (sorted by box, then nonrel cone), then the plan,
-            // which needs the child cone ids
-            std::sort(want.begin(), want.end());
-            want.erase(std::unique(want.begin(), want.end()), want.end());
-            if (want.empty()) return "The number of cone segments on any level cannot be 0";
-            L.cone_ptr.assign(L.boxes.size() + 1, 0);
-            for (auto& w : want) { L.cone_box.push_back(w.first); L.cone_nonrel.push_back(w.second); L.cone_ptr[w.first + 1]++; }
-            for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
-            L.cone_base = T.total_cones;
-            T.total_cones += (int)L.cone_nonrel.size();
-            // propagation plan of this level: parents are the cones of level l-1
-            if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
-            // parent cones of level l-1 get their entries in global-id order; levels are
-            // built upwards, so level l-1's entries are appended now (its id range is final)
-            const int pbase = Lp.cone_base;
-            if ((long long)T.pp_ptr.size() - 1 != pbase) return "internal: propagation plan out of order";
-            for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) {
+            }, 1);
+        }
+        // merged cone list, sorted by box, then nonrel cone
+        std::vector<unsigned long long> want = merge_unique(part);
+        if (want.empty()) return "The number of cone segments on any level cannot be 0";
+        L.cone_ptr.assign(L.boxes.size() + 1, 0);
+        L.cone_box.resize(want.size()); L.cone_nonrel.resize(want.size());
+        for (size_t q = 0; q < want.size(); ++q) {
+            const int b = (int)(want[q] >> 32);
+            L.cone_box[q] = b; L.cone_nonrel[q] = (long long)(want[q] & 0xFFFFFFFFull); L.cone_ptr[b + 1]++;
+        }
+        for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
+        L.cone_base = T.total_cones;
+        T.total_cones += (int)L.cone_nonrel.size();
+        if (!Lpp) continue;
+        // propagation plan of this level: parents are the cones of level l-1, entries in
+        // global parent-id order (levels are built upwards, so level l-1's id range is final)
+        const TreeLevel& Lp = *Lpp;
+        LevelGeo Gp{&Lp, T.min_x, T.min_y};
+        if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
+        if ((long long)T.pp_ptr.size() - 1 != Lp.cone_base) return "internal: propagation plan out of order";
+        const size_t npar = Lp.cone_nonrel.size();
+        std::vector<int> nchv(npar, 0);
+        for (size_t pc = 0; pc < npar; ++pc)
+            for (int pos = 0; pos < 4; ++pos) nchv[pc] += route_of[pc * 4 + pos] >= 0;
+        std::vector<size_t> off(npar + 1, 0);
+        for (size_t pc = 0; pc < npar; ++pc) off[pc + 1] = off[pc] + (size_t)nchv[pc] * P;
+        std::vector<PropEntry>& lp = level_pp[l];
+        lp.resize(off[npar]);
+        std::vector<char> bad(npar, 0);
+        parallel_for((long long)npar, [&](long long p0, long long p1) {
+            for (long long pc = p0; pc < p1; ++pc) {
                 const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
-                const auto& entry = proto.at(pnc);
-                int nch = 0;
-                for (long long cm = pm * 4; cm < pm * 4 + 4; ++cm) {
+                size_t o = off[pc];
+                for (int pos = 0; pos < 4; ++pos) {
+                    const int r = route_of[pc * 4 + pos];
+                    if (r < 0) continue;
+                    const long long cm = pm * 4 + pos;
                     const int cb = L.find_box(cm);
-                    if (cb < 0) continue;
-                    ++nch;
-                    std::vector<PropEntry> slot(P);
-                    for (auto& e : entry[cm % 4]) {
+                    PropEntry* slot = &lp[o];
+                    for (int it = 0; it < P; ++it) slot[it] = PropEntry{0, 0, 0.0, 0.0, 0.0, 0.0};
+                    for (auto& e : routes[r].e) {
                         const int it = e.second;
                         double px = ns[it % Ps], py = na[it / Ps];
                         const double rp = Gp.cheb_to_radius(pnc % Lp.nrad, px);
@@ -319,28 +403,29 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                         G.cart_to_cheb(cm, e.first, lx, ly);
                         const double rc = G.cheb_to_radius(e.first % L.nrad, lx);
                         const int cc = L.find_cone(cb, e.first);
-                        if (cc < 0) return "internal: child cone missing";
+                        if (cc < 0) { bad[pc] = 1; continue; }
                         const std::complex<double> fc = std::complex<double>(std::cos(k * rc), std::sin(k * rc)) / std::sqrt(rc);
                         const std::complex<double> fp = std::complex<double>(std::cos(k * rp), std::sin(k * rp)) / std::sqrt(rp);
                         const std::complex<double> w = fc / fp;
                         slot[it] = PropEntry{L.cone_base + cc, it, lx, ly, w.real(), w.imag()};
                     }
-                    T.pp.insert(T.pp.end(), slot.begin(), slot.end());
+                    o += P;
                 }
-                T.pp_nchild.push_back(nch);
-                T.pp_ptr.push_back((long long)T.pp.size());
-                T.prop_evals += (long long)nch * P;
             }
-            continue;
+        });
+        long long done = T.pp_ptr.back();
+        for (size_t pc = 0; pc < npar; ++pc) {
+            if (bad[pc]) return "internal: child cone missing";
+            T.pp_nchild.push_back(nchv[pc]);
+            T.pp_ptr.push_back(done + (long long)off[pc + 1]);
+            T.prop_evals += (long long)nchv[pc] * P;
         }
-        std::sort(want.begin(), want.end());
-        want.erase(std::unique(want.begin(), want.end()), want.end());
-        if (want.empty()) return "The number of cone segments on any level cannot be 0";
-        L.cone_ptr.assign(L.boxes.size() + 1, 0);
-        for (auto& w : want) { L.cone_box.push_back(w.first); L.cone_nonrel.push_back(w.second); L.cone_ptr[w.first + 1]++; }
-        for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
-        L.cone_base = T.total_cones;
-        T.total_cones += (int)L.cone_nonrel.size();
+    }
+    {
+        size_t tot = 0;
+        for (auto& v : level_pp) tot += v.size();
+        T.pp.reserve(tot);
+        for (auto& v : level_pp) { T.pp.insert(T.pp.end(), v.begin(), v.end()); std::vector<PropEntry>().swap(v); }
     }
     // leaf-level cones have no children: close the propagation CSR for them
     if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
@@ -351,25 +436,30 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     T.ip_ptr.assign(N + 1, 0);
     {
         std::vector<std::vector<InterpEntry>> per(N);
-        for (int l = D; l >= 2; --l) {   // the reference interpolates level D first (BoxTree.h:1049-1061)
-            const TreeLevel& L = T.L[l];
-            LevelGeo G{&L, T.min_x, T.min_y};
-            const int shift = 2 * (D - l);
-            long long old = -1;
-            for (long long i = 0; i < N; ++i) {
-                const long long m = scode[i] >> shift;
-                if (m != old) { cousins_of(L, m, cous); old = m; }
-                for (int c : cous) {
-                    double lx = T.xs[i], ly = T.ys[i];
-                    const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
-                    const int cc = L.find_cone(c, nonrel);
-                    if (cc < 0) return "internal: interpolation cone missing";
-                    const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
-                    const double sr = std::sqrt(r);
-                    per[i].push_back(InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(k * r) / sr, std::sin(k * r) / sr});
+        std::vector<char> bad(N, 0);
+        parallel_for(N, [&](long long i0, long long i1) {
+            std::vector<int> cs;
+            for (int l = D; l >= 2; --l) {   // the reference interpolates level D first (BoxTree.h:1049-1061)
+                const TreeLevel& L = T.L[l];
+                LevelGeo G{&L, T.min_x, T.min_y};
+                const int shift = 2 * (D - l);
+                long long old = -1;
+                for (long long i = i0; i < i1; ++i) {
+                    const long long m = scode[i] >> shift;
+                    if (m != old) { cousins_of(L, m, cs); old = m; }
+                    for (int c : cs) {
+                        double lx = T.xs[i], ly = T.ys[i];
+                        const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
+                        const int cc = L.find_cone(c, nonrel);
+                        if (cc < 0) { bad[i] = 1; continue; }
+                        const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
+                        const double sr = std::sqrt(r);
+                        per[i].push_back(InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(k * r) / sr, std::sin(k * r) / sr});
+                    }
                 }
             }
-        }
+        });
+        for (long long i = 0; i < N; ++i) if (bad[i]) return "internal: interpolation cone missing";
         for (long long i = 0; i < N; ++i) T.ip_ptr[i + 1] = T.ip_ptr[i] + (int)per[i].size();
         T.ip.reserve(T.ip_ptr[N]);
         for (long long i = 0; i < N; ++i) T.ip.insert(T.ip.end(), per[i].begin(), per[i].end());
