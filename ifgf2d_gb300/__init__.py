@@ -54,6 +54,17 @@ def _check(rc, ctx=None):
     raise IFGF2DError(f"ifgf2d: {name}: {msg}")
 
 
+def seeded_density(n, seed=0):
+    """Seeded benchmark density rho_j = u_{2j} + i u_{2j+1}, u = w / 2^32 from the raw words w
+    of std::mt19937(seed) (the reference's benchmark densities, IFGF_Source/main.cpp:150-160,
+    with an independent imaginary part).  numpy's MT19937 with legacy seeding is std::mt19937."""
+    bg = np.random.MT19937(0)
+    bg._legacy_seeding(seed)
+    w = bg.random_raw(2 * n).astype(np.uint64) & 0xFFFFFFFF
+    u = w.astype(np.float64) / 4294967296.0
+    return u[0::2] + 1j * u[1::2]
+
+
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 

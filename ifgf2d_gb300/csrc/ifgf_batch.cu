@@ -8,6 +8,7 @@
 // density / coefficient accesses are 256-byte coalesced rows.
 //
 //   k_sing_b   singular correction + jump term + intensities     ForwardMap.tpp:425-435, 481-515
+//              (FP32 weights in the mixed form)
 //   k_leaf_b   leaf cone coefficients, table rows staged in shared
 //              memory by cp.async, 25 accumulators per RHS          BoxTree.h:685-762
 //   k_prop_b   child -> parent, per parent cone one warp; the
@@ -57,28 +58,47 @@ __global__ void k_deinterleave(const double2* __restrict__ xt, long long N, int 
 }
 
 // ------------------------------------------------------------------ singular correction
-// warp = one output row, lane = one right-hand side; FP64 as in the single-vector path
-template <typename RhoT>
-__global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, const double2* __restrict__ W,
+// warp = one output row, lane = one right-hand side.  WT = double2: FP64 weights and arithmetic
+// (the plain form); WT = float2: the complex64 copy of the FP64-computed weights with FP32
+// accumulation (the mixed form).  The jump term and the intensities stay FP64.
+template <typename WT, typename RhoT>
+__global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, const WT* __restrict__ W,
                                                 const int* __restrict__ row_ptr, const int* __restrict__ row_col,
                                                 const RPColumn* __restrict__ cols, int N, int Np, int B, double half,
                                                 double2* __restrict__ yt, const double* __restrict__ wq,
                                                 const long long* __restrict__ inv, RhoT* __restrict__ rho) {
+    using A = decltype(WT{}.x);
     const int o = blockIdx.x * 8 + (threadIdx.x >> 5);
     const int r = blockIdx.y * 32 + (threadIdx.x & 31);
     if (o >= N || r >= B) return;
-    double2 acc = make_double2(0.0, 0.0);
+    A ax = A(0), ay = A(0);
     for (int q = row_ptr[o]; q < row_ptr[o + 1]; ++q) {
         const int col = row_col[q];
-        const double2* w = W + (long long)col * Np;
+        const WT* w = W + (long long)col * Np;
         const double2* d = xt + (long long)cols[col].patch * Np * B + r;
-        for (int kk = 0; kk < Np; ++kk) {
-            const double2 a = d[(long long)kk * B], b = w[kk];
-            acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
-            acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+        int kk = 0;
+        for (; kk + 4 <= Np; kk += 4) {         // four nodes' loads in flight at once
+            double2 a[4];
+            WT bw[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { a[u] = d[(long long)(kk + u) * B]; bw[u] = w[kk + u]; }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const A x = (A)a[u].x, y = (A)a[u].y;
+                ax = fma(x, bw[u].x, fma(-y, bw[u].y, ax));
+                ay = fma(x, bw[u].y, fma(y, bw[u].x, ay));
+            }
+        }
+        for (; kk < Np; ++kk) {
+            const double2 a = d[(long long)kk * B];
+            const WT b = w[kk];
+            const A x = (A)a.x, y = (A)a.y;
+            ax = fma(x, b.x, fma(-y, b.y, ax));
+            ay = fma(x, b.y, fma(y, b.x, ay));
         }
     }
     const double2 v = xt[(long long)o * B + r];
+    double2 acc = make_double2((double)ax, (double)ay);
     if (half != 0.0) { acc.x += half * v.x; acc.y += half * v.y; }   // jump term
     yt[(long long)o * B + r] = acc;
     if (rho) {
@@ -445,14 +465,14 @@ void launch_deinterleave(const double2* xt, long long N, int B, double2* x, cuda
     if (N <= 0 || B <= 0) return;
     k_deinterleave<<<dim3(nblk_b(N, 32), nblk_b(B, 32)), dim3(32, 8), 0, s>>>(xt, N, B, x);
 }
-void launch_sing_b(const double2* xt, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols, int N,
-                   int Np, int B, double half, double2* yt, const double* wq, const long long* inv, double2* rho64,
-                   float2* rho32, cudaStream_t s) {
+void launch_sing_b(const double2* xt, const double2* W, const float2* W32, const int* row_ptr, const int* row_col,
+                   const RPColumn* cols, int N, int Np, int B, double half, double2* yt, const double* wq,
+                   const long long* inv, double2* rho64, float2* rho32, cudaStream_t s) {
     const dim3 grid(nblk_b(N, 8), nblk_b(B, 32));
     if (rho32)
-        k_sing_b<float2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho32);
+        k_sing_b<float2, float2><<<grid, 256, 0, s>>>(xt, W32, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho32);
     else
-        k_sing_b<double2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho64);
+        k_sing_b<double2, double2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho64);
 }
 template <typename R>
 void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
