@@ -230,6 +230,7 @@ class ForwardMap:
         """ForwardMap.tpp:391-423 (rectangular-polar weights, computed on the GPU)."""
         _check(_lib.load().ifgf2d_precompute(self._h, float(wavenumber)), self._h)
         self.wavenumber = float(wavenumber)
+        self._setup_serial = getattr(self, "_setup_serial", 0) + 1   # invalidates evaluation plans
 
     def precomputations(self, patch):
         """Patch.hpp:55 precomputations_: Np x (Np + n_ns) complex matrix of one patch."""
@@ -243,6 +244,7 @@ class ForwardMap:
         """ForwardMap.tpp:542-565; nlevels <= 0 picks the deepest tree that passes the neighbourhood check."""
         _check(_lib.load().ifgf2d_setup(self._h, float(wavenumber), int(nlevels)), self._h)
         self.wavenumber = float(wavenumber)
+        self._setup_serial = getattr(self, "_setup_serial", 0) + 1   # invalidates evaluation plans
         self.nlevels = int(_lib.load().ifgf2d_get_nlevels(self._h))
 
     def getSorting(self):
@@ -393,6 +395,30 @@ class ForwardMap:
         """LinearOperator wrapping compute_Ax_acc / compute_Ax_unacc, as ForwardMap::solve builds it."""
         f = self.compute_Ax_acc if accelerated else self.compute_Ax_unacc
         return LinearOperator(self.total_num_unknowns_, self.total_num_unknowns_, lambda x, out: f(x, out))
+
+    def propagate_acc(self, x_prop, y_prop, density):
+        """The off-surface field of ``density`` at (x_prop, y_prop) with the IFGF: the accelerated
+        counterpart of propagate_unacc (ForwardMap.tpp:701-727), within the IFGF tolerance of it.
+        Needs precomps_and_setup; the evaluation plan is kept for repeated calls on the same
+        points."""
+        xp = np.ascontiguousarray(x_prop, dtype=np.float64).ravel()
+        yp = np.ascontiguousarray(y_prop, dtype=np.float64).ravel()
+        if xp.shape != yp.shape:
+            raise ValueError("x_prop and y_prop must have the same length")
+        L = _lib.load()
+        key = (getattr(self, "_setup_serial", 0), xp.tobytes(), yp.tobytes())
+        if getattr(self, "_eval_key", None) != key:
+            _check(L.ifgf2d_eval_offsurface_setup(self._h, xp.size, _dp(xp), _dp(yp)), self._h)
+            self._eval_key = key
+        d = _cview(density, self.total_num_unknowns_)
+        out = np.empty(xp.size, dtype=np.complex128)
+        _check(L.ifgf2d_eval_offsurface(self._h, _dp(d.view(np.float64)), _dp(out.view(np.float64))), self._h)
+        return out
+
+    def propagate_acc_counts(self):
+        c = np.zeros(4, dtype=np.int64)
+        _check(_lib.load().ifgf2d_eval_offsurface_counts(self._h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)
+        return dict(zip(["near_pairs", "leaf_evals", "prop_evals", "interp_evals"], (int(v) for v in c)))
 
     def propagate_unacc(self, x_prop, y_prop, density, wavenumber=None):
         """ForwardMap.tpp:701-727: direct evaluation of the layer potential off the surface."""

@@ -15,6 +15,7 @@
 #include <vector>
 
 struct BatchWork;
+struct EvalWork;
 
 namespace ifgf {
 
@@ -118,6 +119,7 @@ struct ifgf2d_ctx {
     DBuf<double2> rho, vin, vout;
     std::unique_ptr<GmresWork> gw;
     BatchWork* bw = nullptr;        // batched apply / solve workspace (batch.cu), freed by destroy
+    EvalWork* ew = nullptr;         // off-surface evaluation plan (offsurface.cu), freed by destroy
     long long counts[8] = {0};
 };
 
@@ -137,6 +139,8 @@ namespace ifgf {
 int apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode);
 // batched workspace release (batch.cu)
 void free_batch(ifgf2d_ctx* ctx);
+// off-surface evaluation plan release (offsurface.cu)
+void free_eval(ifgf2d_ctx* ctx);
 }  // namespace ifgf
 
 // Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)

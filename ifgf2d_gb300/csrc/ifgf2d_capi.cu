@@ -114,6 +114,7 @@ extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
     if (!ctx) return IFGF2D_ERR_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_batch(ctx);
+    free_eval(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return IFGF2D_OK;
@@ -169,6 +170,7 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     ctx->ifgf_ready = false;
     if (ctx->gw) ctx->gw->drop_graphs();
     free_batch(ctx);
+    free_eval(ctx);
     ctx->counts[6] = (long long)ncols * D.Np;
     return IFGF2D_OK;
 }
@@ -222,6 +224,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     }
     ctx->ifgf_ready = false;
     free_batch(ctx);
+    free_eval(ctx);
     Tree& T = ctx->T;
     std::string msg = build_tree(D.x, D.y, nlevels, k, ctx->opt.Ps, ctx->opt.Pang, T);
     if (!msg.empty()) return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);

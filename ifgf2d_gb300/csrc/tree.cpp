@@ -153,10 +153,12 @@ struct LevelGeo {
     }
 };
 
-// Level.h:88-142 (Helmholtz cone refinement)
-void init_cones(TreeLevel& L, double k) {
+// Level.h:88-142 (Helmholtz cone refinement).  The cone segments cover box-centre distances
+// from 1.5 box sizes to the farthest point of the root box; `reach` (> 0 for off-surface
+// targets) extends the outer radius to cover targets outside it.
+void init_cones(TreeLevel& L, double k, double reach = 0.0) {
     const double minsize = (3.0 / 2.0 * L.boxsize) * (1.0 - 1e-10);
-    const double maxsize = (std::sqrt(2.0) * L.boxsize * L.nside - std::sqrt(2.0) / 2.0 * L.boxsize) * (1.0 + 1e-10);
+    const double maxsize = std::max(reach, (std::sqrt(2.0) * L.boxsize * L.nside - std::sqrt(2.0) / 2.0 * L.boxsize) * (1.0 + 1e-10));
     long long scal = 1;
     if (L.level > 1) scal = std::max<long long>(1, (long long)std::ceil(k * L.boxsize * (1.0 / kPiT) * 1.2));
     L.ntheta = 2 * scal;
@@ -192,6 +194,167 @@ void cousins_of(const TreeLevel& L, long long m, std::vector<int>& out) {
 }
 }  // namespace
 
+// Cones of level l and the propagation plan of its parents.  `part` holds the wanted cones
+// (box index << 32 | nonrel cone, each list sorted and unique) that the targets see; the cones
+// needed by the parents' interpolation nodes are added here through the protobox routing table
+// (BoxTree.h:299-428).  Fills T.L[l]'s cone lists and appends, for every parent cone of level
+// l-1 in global-id order, its plan entries to `lp` and its CSR row to T.pp_ptr / pp_nchild.
+std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long long>>& part, const std::vector<double>& ns,
+                     const std::vector<double>& na, std::vector<PropEntry>& lp) {
+    TreeLevel& L = T.L[l];
+    LevelGeo G{&L, T.min_x, T.min_y};
+    const int P = T.P, Ps = T.Ps;
+    const double k = T.k;
+    auto key = [](long long b, long long nonrel) { return ((unsigned long long)b << 32) | (unsigned long long)nonrel; };
+    // cones needed by the parents' interpolation nodes, through the protobox routing
+    // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
+    // routing is computed once, from the first parent box (in cone order) that has it.
+    struct Route { long long pnc; int pos; int first_pc; std::vector<std::pair<long long, int>> e; };
+    std::vector<Route> routes;
+    std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
+    const TreeLevel* Lpp = l > 2 ? &T.L[l - 1] : nullptr;
+    if (Lpp) {
+        const TreeLevel& Lp = *Lpp;
+        LevelGeo Gp{&Lp, T.min_x, T.min_y};
+        const size_t npar = Lp.cone_nonrel.size();
+        route_of.assign(npar * 4, -1);
+        std::unordered_map<long long, int> seen;   // pnc * 4 + pos -> route
+        for (size_t pc = 0; pc < npar; ++pc) {
+            const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
+            for (int pos = 0; pos < 4; ++pos) {
+                if (L.find_box(pm * 4 + pos) < 0) continue;
+                auto it = seen.find(pnc * 4 + pos);
+                if (it == seen.end()) {
+                    it = seen.emplace(pnc * 4 + pos, (int)routes.size()).first;
+                    routes.push_back(Route{pnc, pos, (int)pc, {}});
+                }
+                route_of[pc * 4 + pos] = it->second;
+            }
+        }
+        parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
+            for (long long r = r0; r < r1; ++r) {
+                Route& R = routes[r];
+                const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
+                for (int it = 0; it < P; ++it) {
+                    double px = ns[it % Ps], py = na[it / Ps];
+                    Gp.cheb_to_cart(pm, R.pnc, px, py);
+                    R.e.push_back({G.nonrel_of(pm * 4 + R.pos, px, py), it});
+                }
+            }
+        });
+        const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, (long long)npar / 256));
+        const size_t base = part.size();
+        part.resize(base + nchunk);
+        parallel_for(nchunk, [&](long long c0, long long c1) {
+            for (long long c = c0; c < c1; ++c) {
+                const size_t p0 = npar * c / nchunk, p1 = npar * (c + 1) / nchunk;
+                auto& w = part[base + c];
+                for (size_t pc = p0; pc < p1; ++pc) {
+                    const long long pm = Lp.boxes[Lp.cone_box[pc]];
+                    for (int pos = 0; pos < 4; ++pos) {
+                        const int r = route_of[pc * 4 + pos];
+                        if (r < 0) continue;
+                        const int cb = L.find_box(pm * 4 + pos);
+                        for (auto& e : routes[r].e) w.push_back(key(cb, e.first));
+                    }
+                }
+                sort_unique(w);
+            }
+        }, 1);
+    }
+    // merged cone list, sorted by box, then nonrel cone
+    std::vector<unsigned long long> want = merge_unique(part);
+    if (want.empty()) return "The number of cone segments on any level cannot be 0";
+    L.cone_ptr.assign(L.boxes.size() + 1, 0);
+    L.cone_box.resize(want.size()); L.cone_nonrel.resize(want.size());
+    for (size_t q = 0; q < want.size(); ++q) {
+        const int b = (int)(want[q] >> 32);
+        L.cone_box[q] = b; L.cone_nonrel[q] = (long long)(want[q] & 0xFFFFFFFFull); L.cone_ptr[b + 1]++;
+    }
+    for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
+    L.cone_base = T.total_cones;
+    T.total_cones += (int)L.cone_nonrel.size();
+    if (!Lpp) return "";
+    // propagation plan of this level: parents are the cones of level l-1, entries in
+    // global parent-id order (levels are built upwards, so level l-1's id range is final)
+    const TreeLevel& Lp = *Lpp;
+    LevelGeo Gp{&Lp, T.min_x, T.min_y};
+    if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
+    if ((long long)T.pp_ptr.size() - 1 != Lp.cone_base) return "internal: propagation plan out of order";
+    const size_t npar = Lp.cone_nonrel.size();
+    std::vector<int> nchv(npar, 0);
+    for (size_t pc = 0; pc < npar; ++pc)
+        for (int pos = 0; pos < 4; ++pos) nchv[pc] += route_of[pc * 4 + pos] >= 0;
+    std::vector<size_t> off(npar + 1, 0);
+    for (size_t pc = 0; pc < npar; ++pc) off[pc + 1] = off[pc] + (size_t)nchv[pc] * P;
+    lp.resize(off[npar]);
+    std::vector<char> bad(npar, 0);
+    parallel_for((long long)npar, [&](long long p0, long long p1) {
+        for (long long pc = p0; pc < p1; ++pc) {
+            const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
+            size_t o = off[pc];
+            for (int pos = 0; pos < 4; ++pos) {
+                const int r = route_of[pc * 4 + pos];
+                if (r < 0) continue;
+                const long long cm = pm * 4 + pos;
+                const int cb = L.find_box(cm);
+                PropEntry* slot = &lp[o];
+                for (int it = 0; it < P; ++it) slot[it] = PropEntry{0, 0, 0.0, 0.0, 0.0, 0.0};
+                for (auto& e : routes[r].e) {
+                    const int it = e.second;
+                    double px = ns[it % Ps], py = na[it / Ps];
+                    const double rp = Gp.cheb_to_radius(pnc % Lp.nrad, px);
+                    Gp.cheb_to_cart(pm, pnc, px, py);
+                    double lx = px, ly = py;
+                    G.cart_to_cheb(cm, e.first, lx, ly);
+                    const double rc = G.cheb_to_radius(e.first % L.nrad, lx);
+                    const int cc = L.find_cone(cb, e.first);
+                    if (cc < 0) { bad[pc] = 1; continue; }
+                    const std::complex<double> fc = std::complex<double>(std::cos(k * rc), std::sin(k * rc)) / std::sqrt(rc);
+                    const std::complex<double> fp = std::complex<double>(std::cos(k * rp), std::sin(k * rp)) / std::sqrt(rp);
+                    const std::complex<double> w = fc / fp;
+                    slot[it] = PropEntry{L.cone_base + cc, it, lx, ly, w.real(), w.imag()};
+                }
+                o += P;
+            }
+        }
+    });
+    long long done = T.pp_ptr.back();
+    for (size_t pc = 0; pc < npar; ++pc) {
+        if (bad[pc]) return "internal: child cone missing";
+        T.pp_nchild.push_back(nchv[pc]);
+        T.pp_ptr.push_back(done + (long long)off[pc + 1]);
+        T.prop_evals += (long long)nchv[pc] * P;
+    }
+    return "";
+}
+
+// relevant boxes of level l that a target in the (possibly virtual, outside the root box) box
+// (bx, by) interpolates from: at level 2 every box not adjacent to it; deeper, the children of
+// the boxes adjacent to its parent box that are not adjacent to it.  For a target inside the
+// root box this is the cousin list above; with the adjacent leaf boxes (the direct near
+// field) every source is counted once.
+void target_list(const TreeLevel& L, int l, long long bx, long long by, std::vector<int>& out) {
+    out.clear();
+    std::vector<std::pair<long long, int>> tmp;
+    auto consider = [&](long long i, long long j) {
+        if (i < 0 || j < 0 || i >= L.nside || j >= L.nside) return;
+        if (std::llabs(i - bx) <= 1 && std::llabs(j - by) <= 1) return;
+        const long long cm = morton_of(i, j);
+        const int b = L.find_box(cm);
+        if (b >= 0) tmp.push_back({cm, b});
+    };
+    if (l == 2) {
+        for (long long j = 0; j < L.nside; ++j)
+            for (long long i = 0; i < L.nside; ++i) consider(i, j);
+    } else {
+        const long long px = bx >> 1, py = by >> 1;   // arithmetic shift: floor for negative boxes
+        for (long long j = 2 * (py - 1); j <= 2 * (py + 1) + 1; ++j)
+            for (long long i = 2 * (px - 1); i <= 2 * (px + 1) + 1; ++i) consider(i, j);
+    }
+    std::sort(tmp.begin(), tmp.end());
+    for (auto& t : tmp) out.push_back(t.second);
+}
 // ---------------------------------------------------------------- build
 std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
                        int Ps, int Pang, Tree& T) {
@@ -299,127 +462,8 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                 }
             }, 1);
         }
-        // cones needed by the parents' interpolation nodes, through the protobox routing
-        // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
-        // routing is computed once, from the first parent box (in cone order) that has it.
-        struct Route { long long pnc; int pos; int first_pc; std::vector<std::pair<long long, int>> e; };
-        std::vector<Route> routes;
-        std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
-        const TreeLevel* Lpp = l > 2 ? &T.L[l - 1] : nullptr;
-        if (Lpp) {
-            const TreeLevel& Lp = *Lpp;
-            LevelGeo Gp{&Lp, T.min_x, T.min_y};
-            const size_t npar = Lp.cone_nonrel.size();
-            route_of.assign(npar * 4, -1);
-            std::unordered_map<long long, int> seen;   // pnc * 4 + pos -> route
-            for (size_t pc = 0; pc < npar; ++pc) {
-                const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
-                for (int pos = 0; pos < 4; ++pos) {
-                    if (L.find_box(pm * 4 + pos) < 0) continue;
-                    auto it = seen.find(pnc * 4 + pos);
-                    if (it == seen.end()) {
-                        it = seen.emplace(pnc * 4 + pos, (int)routes.size()).first;
-                        routes.push_back(Route{pnc, pos, (int)pc, {}});
-                    }
-                    route_of[pc * 4 + pos] = it->second;
-                }
-            }
-            parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
-                for (long long r = r0; r < r1; ++r) {
-                    Route& R = routes[r];
-                    const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
-                    for (int it = 0; it < P; ++it) {
-                        double px = ns[it % Ps], py = na[it / Ps];
-                        Gp.cheb_to_cart(pm, R.pnc, px, py);
-                        R.e.push_back({G.nonrel_of(pm * 4 + R.pos, px, py), it});
-                    }
-                }
-            });
-            const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, (long long)npar / 256));
-            const size_t base = part.size();
-            part.resize(base + nchunk);
-            parallel_for(nchunk, [&](long long c0, long long c1) {
-                for (long long c = c0; c < c1; ++c) {
-                    const size_t p0 = npar * c / nchunk, p1 = npar * (c + 1) / nchunk;
-                    auto& w = part[base + c];
-                    for (size_t pc = p0; pc < p1; ++pc) {
-                        const long long pm = Lp.boxes[Lp.cone_box[pc]];
-                        for (int pos = 0; pos < 4; ++pos) {
-                            const int r = route_of[pc * 4 + pos];
-                            if (r < 0) continue;
-                            const int cb = L.find_box(pm * 4 + pos);
-                            for (auto& e : routes[r].e) w.push_back(key(cb, e.first));
-                        }
-                    }
-                    sort_unique(w);
-                }
-            }, 1);
-        }
-        // merged cone list, sorted by box, then nonrel cone
-        std::vector<unsigned long long> want = merge_unique(part);
-        if (want.empty()) return "The number of cone segments on any level cannot be 0";
-        L.cone_ptr.assign(L.boxes.size() + 1, 0);
-        L.cone_box.resize(want.size()); L.cone_nonrel.resize(want.size());
-        for (size_t q = 0; q < want.size(); ++q) {
-            const int b = (int)(want[q] >> 32);
-            L.cone_box[q] = b; L.cone_nonrel[q] = (long long)(want[q] & 0xFFFFFFFFull); L.cone_ptr[b + 1]++;
-        }
-        for (size_t b = 0; b < L.boxes.size(); ++b) L.cone_ptr[b + 1] += L.cone_ptr[b];
-        L.cone_base = T.total_cones;
-        T.total_cones += (int)L.cone_nonrel.size();
-        if (!Lpp) continue;
-        // propagation plan of this level: parents are the cones of level l-1, entries in
-        // global parent-id order (levels are built upwards, so level l-1's id range is final)
-        const TreeLevel& Lp = *Lpp;
-        LevelGeo Gp{&Lp, T.min_x, T.min_y};
-        if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
-        if ((long long)T.pp_ptr.size() - 1 != Lp.cone_base) return "internal: propagation plan out of order";
-        const size_t npar = Lp.cone_nonrel.size();
-        std::vector<int> nchv(npar, 0);
-        for (size_t pc = 0; pc < npar; ++pc)
-            for (int pos = 0; pos < 4; ++pos) nchv[pc] += route_of[pc * 4 + pos] >= 0;
-        std::vector<size_t> off(npar + 1, 0);
-        for (size_t pc = 0; pc < npar; ++pc) off[pc + 1] = off[pc] + (size_t)nchv[pc] * P;
-        std::vector<PropEntry>& lp = level_pp[l];
-        lp.resize(off[npar]);
-        std::vector<char> bad(npar, 0);
-        parallel_for((long long)npar, [&](long long p0, long long p1) {
-            for (long long pc = p0; pc < p1; ++pc) {
-                const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
-                size_t o = off[pc];
-                for (int pos = 0; pos < 4; ++pos) {
-                    const int r = route_of[pc * 4 + pos];
-                    if (r < 0) continue;
-                    const long long cm = pm * 4 + pos;
-                    const int cb = L.find_box(cm);
-                    PropEntry* slot = &lp[o];
-                    for (int it = 0; it < P; ++it) slot[it] = PropEntry{0, 0, 0.0, 0.0, 0.0, 0.0};
-                    for (auto& e : routes[r].e) {
-                        const int it = e.second;
-                        double px = ns[it % Ps], py = na[it / Ps];
-                        const double rp = Gp.cheb_to_radius(pnc % Lp.nrad, px);
-                        Gp.cheb_to_cart(pm, pnc, px, py);
-                        double lx = px, ly = py;
-                        G.cart_to_cheb(cm, e.first, lx, ly);
-                        const double rc = G.cheb_to_radius(e.first % L.nrad, lx);
-                        const int cc = L.find_cone(cb, e.first);
-                        if (cc < 0) { bad[pc] = 1; continue; }
-                        const std::complex<double> fc = std::complex<double>(std::cos(k * rc), std::sin(k * rc)) / std::sqrt(rc);
-                        const std::complex<double> fp = std::complex<double>(std::cos(k * rp), std::sin(k * rp)) / std::sqrt(rp);
-                        const std::complex<double> w = fc / fp;
-                        slot[it] = PropEntry{L.cone_base + cc, it, lx, ly, w.real(), w.imag()};
-                    }
-                    o += P;
-                }
-            }
-        });
-        long long done = T.pp_ptr.back();
-        for (size_t pc = 0; pc < npar; ++pc) {
-            if (bad[pc]) return "internal: child cone missing";
-            T.pp_nchild.push_back(nchv[pc]);
-            T.pp_ptr.push_back(done + (long long)off[pc + 1]);
-            T.prop_evals += (long long)nchv[pc] * P;
-        }
+        std::string msg = finish_level(T, l, part, ns, na, level_pp[l]);
+        if (!msg.empty()) return msg;
     }
     {
         size_t tot = 0;
@@ -488,6 +532,144 @@ void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, s
             x[c * T.P + it] = px; y[c * T.P + it] = py; ir[c * T.P + it] = inv.real(); ii[c * T.P + it] = inv.imag();
         }
     }
+}
+
+}  // namespace ifgf
+
+namespace ifgf {
+
+// ---------------------------------------------------------------- off-surface targets
+std::string build_target_tree(const Tree& S, const std::vector<double>& tx, const std::vector<double>& ty, Tree& E) {
+    if (tx.size() != ty.size()) return "target coordinate arrays differ in length";
+    const int nlevels = S.nlevels, D = nlevels - 1;
+    E = Tree();
+    E.nlevels = nlevels; E.k = S.k; E.Ps = S.Ps; E.Pang = S.Pang; E.P = S.P; E.N = S.N;
+    E.min_x = S.min_x; E.min_y = S.min_y; E.boxsize0 = S.boxsize0;
+    E.leaf_start = S.leaf_start; E.leaf_count = S.leaf_count;
+    const long long M = (long long)tx.size();
+    // cone segments out to the farthest target: a box centre is within R of any target, and a
+    // parent's interpolation node is within the parent's reach plus half a child diagonal of
+    // the child's centre, hence the growth with the level
+    const double cx0 = S.min_x + 0.5 * S.boxsize0, cy0 = S.min_y + 0.5 * S.boxsize0;
+    double R = std::sqrt(2.0) * S.boxsize0;
+    for (long long t = 0; t < M; ++t)
+        R = std::max(R, std::hypot(tx[t] - cx0, ty[t] - cy0) + std::sqrt(2.0) / 2.0 * S.boxsize0);
+    E.L.resize(nlevels);
+    for (int l = 1; l < nlevels; ++l) {
+        TreeLevel& L = E.L[l];
+        L.level = l; L.nside = 1LL << l; L.boxsize = S.L[l].boxsize;
+        L.boxes = S.L[l].boxes;
+        const double reach = (R + std::sqrt(2.0) * S.boxsize0 * (1.0 - std::ldexp(1.0, -l))) * (1.0 + 1e-10);
+        init_cones(L, E.k, reach);
+    }
+    // virtual leaf boxes of the targets (may lie outside [0, 2^D))
+    const double bsD = E.L[D].boxsize;
+    std::vector<long long> tbx(M), tby(M);
+    for (long long t = 0; t < M; ++t) {
+        tbx[t] = (long long)std::floor((tx[t] - E.min_x) / bsD);
+        tby[t] = (long long)std::floor((ty[t] - E.min_y) / bsD);
+    }
+    std::vector<double> ns(E.Ps), na(E.Pang);
+    for (int i = 0; i < E.Ps; ++i) ns[E.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Ps));
+    for (int i = 0; i < E.Pang; ++i) na[E.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Pang));
+    const int P = E.P;
+    std::vector<std::vector<PropEntry>> level_pp(nlevels);
+    for (int l = 2; l < nlevels; ++l) {
+        TreeLevel& L = E.L[l];
+        LevelGeo G{&L, E.min_x, E.min_y};
+        const int sh = D - l;
+        const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, M / 256));
+        std::vector<std::vector<unsigned long long>> part(nchunk);
+        parallel_for(nchunk, [&](long long c0, long long c1) {
+            std::vector<int> cs;
+            for (long long c = c0; c < c1; ++c) {
+                auto& w = part[c];
+                for (long long t = M * c / nchunk; t < M * (c + 1) / nchunk; ++t) {
+                    target_list(L, l, tbx[t] >> sh, tby[t] >> sh, cs);
+                    for (int cb : cs)
+                        w.push_back(((unsigned long long)cb << 32) | (unsigned long long)G.nonrel_of(L.boxes[cb], tx[t], ty[t]));
+                }
+                sort_unique(w);
+            }
+        }, 1);
+        // a level whose targets see no box still needs the cones its parents route to
+        bool any = false;
+        for (auto& w : part) any = any || !w.empty();
+        if (!any && l == 2) part.assign(1, std::vector<unsigned long long>{});
+        std::string msg = finish_level(E, l, part, ns, na, level_pp[l]);
+        if (!msg.empty() && msg != "The number of cone segments on any level cannot be 0") return msg;
+        if (!msg.empty()) {   // no cone at this level: empty lists, nothing below needs it either
+            TreeLevel& Le = E.L[l];
+            Le.cone_ptr.assign(Le.boxes.size() + 1, 0);
+            Le.cone_box.clear(); Le.cone_nonrel.clear();
+            Le.cone_base = E.total_cones;
+            if (l > 2) {
+                const TreeLevel& Lp = E.L[l - 1];
+                if (E.pp_ptr.empty()) E.pp_ptr.assign(1, 0);
+                for (size_t pc = 0; pc < Lp.cone_nonrel.size(); ++pc) { E.pp_nchild.push_back(0); E.pp_ptr.push_back(E.pp_ptr.back()); }
+            }
+        }
+    }
+    {
+        size_t tot = 0;
+        for (auto& v : level_pp) tot += v.size();
+        E.pp.reserve(tot);
+        for (auto& v : level_pp) { E.pp.insert(E.pp.end(), v.begin(), v.end()); std::vector<PropEntry>().swap(v); }
+    }
+    if (E.pp_ptr.empty()) E.pp_ptr.assign(1, 0);
+    while ((long long)E.pp_ptr.size() - 1 < E.total_cones) { E.pp_ptr.push_back((long long)E.pp.size()); E.pp_nchild.push_back(0); }
+    for (size_t c = 0; c < E.L[D].cone_nonrel.size(); ++c) E.leaf_evals += (long long)P * E.leaf_count[E.L[D].cone_box[c]];
+    // per target: interpolation entries, level D first (BoxTree.h:1049-1061), and the
+    // adjacent leaf boxes of the direct near field
+    std::vector<std::vector<InterpEntry>> per(M);
+    std::vector<std::vector<int>> nb(M);
+    std::vector<char> bad(M, 0);
+    parallel_for(M, [&](long long t0, long long t1) {
+        std::vector<int> cs;
+        for (long long t = t0; t < t1; ++t) {
+            for (int l = D; l >= 2; --l) {
+                const TreeLevel& L = E.L[l];
+                LevelGeo G{&L, E.min_x, E.min_y};
+                target_list(L, l, tbx[t] >> (D - l), tby[t] >> (D - l), cs);
+                for (int c : cs) {
+                    double lx = tx[t], ly = ty[t];
+                    const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
+                    const int cc = L.find_cone(c, nonrel);
+                    if (cc < 0) { bad[t] = 1; continue; }
+                    const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
+                    const double sr = std::sqrt(r);
+                    per[t].push_back(InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(E.k * r) / sr, std::sin(E.k * r) / sr});
+                }
+            }
+            const TreeLevel& LD = E.L[D];
+            std::vector<std::pair<long long, int>> tmp;
+            for (long long j = tby[t] - 1; j <= tby[t] + 1; ++j)
+                for (long long i = tbx[t] - 1; i <= tbx[t] + 1; ++i) {
+                    if (i < 0 || j < 0 || i >= LD.nside || j >= LD.nside) continue;
+                    const long long m = morton_of(i, j);
+                    const int q = LD.find_box(m);
+                    if (q >= 0) tmp.push_back({m, q});
+                }
+            std::sort(tmp.begin(), tmp.end());
+            for (auto& e : tmp) nb[t].push_back(e.second);
+        }
+    });
+    for (long long t = 0; t < M; ++t) if (bad[t]) return "internal: target interpolation cone missing";
+    E.ip_ptr.assign(M + 1, 0);
+    E.nbr_ptr.assign(M + 1, 0);
+    for (long long t = 0; t < M; ++t) {
+        E.ip_ptr[t + 1] = E.ip_ptr[t] + (int)per[t].size();
+        E.nbr_ptr[t + 1] = E.nbr_ptr[t] + (int)nb[t].size();
+        for (int q : nb[t]) E.near_pairs += E.leaf_count[q];
+    }
+    E.ip.reserve(E.ip_ptr[M]);
+    E.nbr_box.reserve(E.nbr_ptr[M]);
+    for (long long t = 0; t < M; ++t) {
+        E.ip.insert(E.ip.end(), per[t].begin(), per[t].end());
+        E.nbr_box.insert(E.nbr_box.end(), nb[t].begin(), nb[t].end());
+    }
+    E.interp_evals = E.ip_ptr[M];
+    return "";
 }
 
 }  // namespace ifgf

@@ -76,6 +76,13 @@ struct Tree {
 std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
                        int Ps, int Pang, Tree& T);
 
+// Evaluation plan for off-surface targets (the accelerated form of ForwardMap::propagate_unacc,
+// ForwardMap.tpp:701-727).  E keeps the source boxes of S (sources, leaf ranges, Morton order)
+// and gets the cones and propagation plan the targets need, with cone segments reaching the
+// farthest target.  Per target, in input order: interpolation entries (E.ip_ptr / E.ip) and
+// the adjacent leaf boxes of the direct near field (E.nbr_ptr / E.nbr_box).
+std::string build_target_tree(const Tree& S, const std::vector<double>& tx, const std::vector<double>& ty, Tree& E);
+
 // Morton code of (x, y) at `level` for a root box [min_x, min_x + size] (Level.h:145-161);
 // returns -1 when the point is outside.
 long long point_morton(double x, double y, double min_x, double min_y, double boxsize, int level);

@@ -148,6 +148,19 @@ int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, 
 int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp,
                      const double* density, double* out);
 
+/* The off-surface field with the IFGF (no counterpart in the reference, which sums directly:
+ * ForwardMap::propagate_unacc, ForwardMap.tpp:701-727).  setup builds the evaluation plan for
+ * m targets (anywhere, also outside the tree's box) on a context that ifgf2d_setup prepared;
+ * it stays valid until the next setup or precompute.  eval then takes a density (N complex,
+ * patch order) and writes the field at the m targets (m complex): direct sums over the
+ * sources of each target's adjacent leaf boxes plus cone interpolation for the rest, within
+ * the IFGF tolerance of ifgf2d_propagate. */
+int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp);
+int ifgf2d_eval_offsurface(ifgf2d_ctx* ctx, const double* density, double* out);
+/* work of one evaluation: near pairs, leaf evaluations, propagation evaluations, interpolation
+ * evaluations */
+int ifgf2d_eval_offsurface_counts(const ifgf2d_ctx* ctx, long long out[4]);
+
 /* Device Hankel evaluator (replaces sp_bessel::hankelH1, complex_bessel
  * besselFunctions.h:313-341, for real arguments): out[i] = H_order^(1)(x[i]), order 0 or 1. */
 int ifgf2d_hankel(int order, long long n, const double* x, double* out);
