@@ -22,6 +22,7 @@ struct BatchWork {
     DBuf<PropB<double>> pb64;
     DBuf<PropB<float>> pb32;
     DBuf<float2> W32;                          // complex64 copy of the singular-correction weights
+    DBuf<float2> xt32;                         // complex64 copy of the interleaved input (mixed form)
     DBuf<double2> xcm, ycm;                    // column-major staging of the host entry points
     // GMRES
     int m = 0, scap = 0;
@@ -65,11 +66,14 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
     const size_t ncoef = (size_t)ctx->T.total_cones * ctx->T.P;
     if (W.cap < B) {
         W.xt.release(); W.yt.release(); W.rho64.release(); W.coef64.release(); W.rho32.release(); W.coef32.release();
+        W.xt32.release();
         CK(W.xt.alloc((size_t)N * B)); CK(W.yt.alloc((size_t)N * B));
         W.cap = B;
     }
     if (mixed) {
-        if (!W.rho32.p) { CK(W.rho32.alloc((size_t)N * W.cap)); CK(W.coef32.alloc(ncoef * W.cap)); }
+        if (!W.rho32.p) {
+            CK(W.rho32.alloc((size_t)N * W.cap)); CK(W.coef32.alloc(ncoef * W.cap)); CK(W.xt32.alloc((size_t)N * W.cap));
+        }
         if (!W.pb32.p) CK(W.pb32.upload(sorted_plan<float>(ctx->T)));
         if (!W.W32.p) {
             CK(W.W32.alloc(ctx->W.n));
@@ -109,7 +113,8 @@ int apply_il(ifgf2d_ctx* ctx, const double2* xt, double2* yt, int B, int mode) {
     BatchWork& W = *ctx->bw;
     const Discretisation& D = ctx->D;
     const double half = ctx->form == IFGF2D_COMBINED ? 0.5 : 0.0;
-    launch_sing_b(xt, ctx->W.p, W.W32.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, (int)D.N, D.Np, B, half, yt, ctx->wq.p,
+    if (mixed) launch_d2f(xt, (long long)D.N * B, W.xt32.p, ctx->stream);
+    launch_sing_b(xt, W.xt32.p, ctx->W.p, W.W32.p, ctx->srow_ptr.p, ctx->srow_col.p, ctx->cols.p, (int)D.N, D.Np, B, half, yt, ctx->wq.p,
                   ctx->inverse.p, mixed ? nullptr : W.rho64.p, mixed ? W.rho32.p : nullptr, ctx->stream);
     if (mixed)
         far_b<float>(ctx, W.rho32.p, ctx->near32.p, ctx->leafL32.p, W.pb32.p, ctx->ip32.p, ctx->Gsep32.p, W.coef32.p, B, yt);

@@ -110,10 +110,11 @@ inline void launch_intensities(const double2* x, const double* wq, const long lo
 constexpr int kMaxBatch = 64;      // right-hand sides per batched apply (larger batches are chunked)
 void launch_interleave(const double2* x, long long N, int B, double2* xt, cudaStream_t s);     // [B][N] -> [N][B]
 void launch_deinterleave(const double2* xt, long long N, int B, double2* x, cudaStream_t s);   // [N][B] -> [B][N]
-// rho32 given: the mixed form (W32 weights, FP32 sums); else FP64 with W
-void launch_sing_b(const double2* xt, const double2* W, const float2* W32, const int* row_ptr, const int* row_col,
-                   const RPColumn* cols, int N, int Np, int B, double half, double2* yt, const double* wq,
-                   const long long* inv, double2* rho64, float2* rho32, cudaStream_t s);
+// rho32 given: the mixed form (complex64 densities xt32 and weights W32, FP32 sums); else FP64
+// with xt and W.  The jump term and the intensities use xt.
+void launch_sing_b(const double2* xt, const float2* xt32, const double2* W, const float2* W32, const int* row_ptr,
+                   const int* row_col, const RPColumn* cols, int N, int Np, int B, double half, double2* yt,
+                   const double* wq, const long long* inv, double2* rho64, float2* rho32, cudaStream_t s);
 template <typename R>
 void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
                    const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int Ps, int Pang, int B, V2<R>* coef,

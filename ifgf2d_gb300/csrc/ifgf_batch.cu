@@ -58,15 +58,17 @@ __global__ void k_deinterleave(const double2* __restrict__ xt, long long N, int 
 }
 
 // ------------------------------------------------------------------ singular correction
-// warp = one output row, lane = one right-hand side.  WT = double2: FP64 weights and arithmetic
-// (the plain form); WT = float2: the complex64 copy of the FP64-computed weights with FP32
-// accumulation (the mixed form).  The jump term and the intensities stay FP64.
+// warp = one output row, lane = one right-hand side.  WT = double2: FP64 weights, densities and
+// arithmetic (the plain form; xw = xt); WT = float2: complex64 copies of the FP64-computed
+// weights and of the densities (xw), FP32 sums (the mixed form).  The jump term and the
+// intensities take the FP64 densities xt.
 template <typename WT, typename RhoT>
-__global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, const WT* __restrict__ W,
-                                                const int* __restrict__ row_ptr, const int* __restrict__ row_col,
-                                                const RPColumn* __restrict__ cols, int N, int Np, int B, double half,
-                                                double2* __restrict__ yt, const double* __restrict__ wq,
-                                                const long long* __restrict__ inv, RhoT* __restrict__ rho) {
+__global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, const WT* __restrict__ xw,
+                                                const WT* __restrict__ W, const int* __restrict__ row_ptr,
+                                                const int* __restrict__ row_col, const RPColumn* __restrict__ cols, int N,
+                                                int Np, int B, double half, double2* __restrict__ yt,
+                                                const double* __restrict__ wq, const long long* __restrict__ inv,
+                                                RhoT* __restrict__ rho) {
     using A = decltype(WT{}.x);
     const int o = blockIdx.x * 8 + (threadIdx.x >> 5);
     const int r = blockIdx.y * 32 + (threadIdx.x & 31);
@@ -75,26 +77,22 @@ __global__ void __launch_bounds__(256) k_sing_b(const double2* __restrict__ xt, 
     for (int q = row_ptr[o]; q < row_ptr[o + 1]; ++q) {
         const int col = row_col[q];
         const WT* w = W + (long long)col * Np;
-        const double2* d = xt + (long long)cols[col].patch * Np * B + r;
+        const WT* d = xw + (long long)cols[col].patch * Np * B + r;
         int kk = 0;
         for (; kk + 4 <= Np; kk += 4) {         // four nodes' loads in flight at once
-            double2 a[4];
-            WT bw[4];
+            WT a[4], bw[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) { a[u] = d[(long long)(kk + u) * B]; bw[u] = w[kk + u]; }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const A x = (A)a[u].x, y = (A)a[u].y;
-                ax = fma(x, bw[u].x, fma(-y, bw[u].y, ax));
-                ay = fma(x, bw[u].y, fma(y, bw[u].x, ay));
+                ax = fma(a[u].x, bw[u].x, fma(-a[u].y, bw[u].y, ax));
+                ay = fma(a[u].x, bw[u].y, fma(a[u].y, bw[u].x, ay));
             }
         }
         for (; kk < Np; ++kk) {
-            const double2 a = d[(long long)kk * B];
-            const WT b = w[kk];
-            const A x = (A)a.x, y = (A)a.y;
-            ax = fma(x, b.x, fma(-y, b.y, ax));
-            ay = fma(x, b.y, fma(y, b.x, ay));
+            const WT a = d[(long long)kk * B], b = w[kk];
+            ax = fma(a.x, b.x, fma(-a.y, b.y, ax));
+            ay = fma(a.x, b.y, fma(a.y, b.x, ay));
         }
     }
     const double2 v = xt[(long long)o * B + r];
@@ -465,14 +463,14 @@ void launch_deinterleave(const double2* xt, long long N, int B, double2* x, cuda
     if (N <= 0 || B <= 0) return;
     k_deinterleave<<<dim3(nblk_b(N, 32), nblk_b(B, 32)), dim3(32, 8), 0, s>>>(xt, N, B, x);
 }
-void launch_sing_b(const double2* xt, const double2* W, const float2* W32, const int* row_ptr, const int* row_col,
-                   const RPColumn* cols, int N, int Np, int B, double half, double2* yt, const double* wq,
-                   const long long* inv, double2* rho64, float2* rho32, cudaStream_t s) {
+void launch_sing_b(const double2* xt, const float2* xt32, const double2* W, const float2* W32, const int* row_ptr,
+                   const int* row_col, const RPColumn* cols, int N, int Np, int B, double half, double2* yt,
+                   const double* wq, const long long* inv, double2* rho64, float2* rho32, cudaStream_t s) {
     const dim3 grid(nblk_b(N, 8), nblk_b(B, 32));
     if (rho32)
-        k_sing_b<float2, float2><<<grid, 256, 0, s>>>(xt, W32, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho32);
+        k_sing_b<float2, float2><<<grid, 256, 0, s>>>(xt, xt32, W32, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho32);
     else
-        k_sing_b<double2, double2><<<grid, 256, 0, s>>>(xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho64);
+        k_sing_b<double2, double2><<<grid, 256, 0, s>>>(xt, xt, W, row_ptr, row_col, cols, N, Np, B, half, yt, wq, inv, rho64);
 }
 template <typename R>
 void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
