@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the GMRES solve (for profiler runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-angle batch (kite k=2000, N=32768)")
+    ap.add_argument("--no-obstacles", action="store_true", help="skip the 256-obstacle workload")
+    ap.add_argument("--no-large", action="store_true", help="skip the kite k=8000, N=131072 solve")
     ap.add_argument("--batch-k", type=float, default=2000.0, help="wavenumber of the batch workload (profiling)")
     ap.add_argument("--batch-patches", type=int, default=2048, help="patches of the batch workload (profiling)")
     return ap.parse_args()
@@ -290,7 +292,78 @@ def run_ours(args, rank, local_rank, world):
         del fm
         torch.cuda.synchronize()
         out["batch"] = run_batch(G, k=args.batch_k, npatch=args.batch_patches, solve=not args.no_solve)
+    if not args.no_large and not args.no_solve:
+        out["large"] = run_large(G)
+    if not args.no_obstacles and not args.no_solve:
+        out["obstacles"] = run_obstacles()
     return out
+
+
+def run_large(G, k=8000.0, npatch=8192):
+    """Kite k=8000, 8192 patches x 16 (N=131072), plane wave at angle 0: plain FP64 GMRES
+    against FP64 refinement around complex64 inner solves, both to a 1e-6 FP64 residual."""
+    import torch
+    t0 = time.perf_counter()
+    fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, k, Np=NP, patches_per_curve=npatch, formulation="combined")
+    fm.precomps_and_setup(k, 0)
+    torch.cuda.synchronize()
+    res = {"workload": f"kite k={k:g}, {npatch} patches x {NP} (N={fm.total_num_unknowns_}), combined field, plane wave",
+           "N": fm.total_num_unknowns_, "nlevels": fm.nlevels, "setup_s": time.perf_counter() - t0}
+    N = fm.total_num_unknowns_
+    x = torch.from_numpy(G.seeded_density(N)).cuda()
+    y = torch.empty_like(x)
+    ext = torch.cuda.ExternalStream(fm.stream())
+    for mixed in (False, True):
+        for _ in range(3):
+            fm.apply_device(x, y, mixed=mixed)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(10):
+            fm.apply_device(x, y, mixed=mixed)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        res["apply_" + ("mixed" if mixed else "fp64") + "_ms"] = e0.elapsed_time(e1) / 10
+    b = -np.exp(1j * k * fm.xs_)
+    for name, mixed in (("plain_fp64", False), ("chosen_mixed", True)):
+        times = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
+            times.append(time.perf_counter() - t0)
+        tr = float(np.linalg.norm(fm.compute_Ax_acc(xs) - b) / np.linalg.norm(b))
+        res[name] = {"seconds": times[1], "seconds_first_call": times[0], "iters": fm.last_solve["iters"],
+                     "converged": fm.last_solve["converged"], "true_rel_residual_fp64": tr}
+    res["speedup_chosen_vs_plain"] = res["plain_fp64"]["seconds"] / res["chosen_mixed"]["seconds"]
+    return res
+
+
+def run_obstacles(n=256, plain_sample=256):
+    """256 seeded star obstacles (k ~ U(10, 400), 10 points per wavelength, plane waves),
+    each solved to a 1e-6 FP64 residual.  Chosen: host set-up of the next obstacles on 15
+    host threads while one thread runs each obstacle's device work, complex64 inner solves.
+    Plain: one obstacle after another, FP64 GMRES, on the first `plain_sample` obstacles."""
+    from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles
+    obs = star_obstacles(n)
+    t0 = time.perf_counter()
+    solve_obstacles(obs, tol=1e-6, workers=15, mixed=True)
+    dt = time.perf_counter() - t0
+    r = [o.result for o in obs]
+    sub = star_obstacles(n)[:plain_sample]
+    t0 = time.perf_counter()
+    solve_obstacles(sub, tol=1e-6, workers=0, mixed=False)
+    dtp = time.perf_counter() - t0
+    rp = [o.result for o in sub]
+    return {"workload": f"{n} star obstacles r = 1 + sum_m a_m cos mt + b_m sin mt (m <= 5, |a|,|b| < 0.05), "
+                        "k ~ U(10, 400), N_i = 16 ceil(10 k L / 2 pi / 16), plane wave at a random angle; numpy default_rng(0)",
+            "n": n, "unknowns_total": int(sum(o.npoints for o in obs)),
+            "chosen": {"seconds": dt, "ms_per_obstacle": dt / n * 1e3, "all_converged": all(x["converged"] for x in r),
+                       "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in r),
+                       "ifgf": int(sum(x["accelerated"] for x in r)), "direct": int(sum(not x["accelerated"] for x in r))},
+            "plain": {"ms_per_obstacle": dtp / plain_sample * 1e3, "sample": f"the first {plain_sample} obstacles, one at a time",
+                      "all_converged": all(x["converged"] for x in rp),
+                      "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in rp)},
+            "speedup_chosen_vs_plain_per_obstacle": (dtp / plain_sample) / (dt / n)}
 
 
 def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):

@@ -247,6 +247,11 @@ class ForwardMap:
         self._setup_serial = getattr(self, "_setup_serial", 0) + 1   # invalidates evaluation plans
         self.nlevels = int(_lib.load().ifgf2d_get_nlevels(self._h))
 
+    def prepare(self, wavenumber, nlevels=0):
+        """The host part of precomps_and_setup (tree depth, tree, plans) with no GPU call, for
+        a host thread that prepares contexts while the GPU serves others."""
+        _check(_lib.load().ifgf2d_prepare(self._h, float(wavenumber), int(nlevels)), self._h)
+
     def getSorting(self):
         s = np.empty(self.total_num_unknowns_, dtype=np.int64)
         _check(_lib.load().ifgf2d_get_sorting(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)

@@ -30,7 +30,7 @@ EXPORTS = [
     "ifgf2d_apply_device", "ifgf2d_ifgf_far", "ifgf2d_solve", "ifgf2d_propagate", "ifgf2d_hankel",
     "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
     "ifgf2d_apply_direct_noalloc", "ifgf2d_apply_batch", "ifgf2d_apply_batch_device", "ifgf2d_solve_batch",
-    "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
+    "ifgf2d_set_host_threads", "ifgf2d_prepare", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
 ]
 
 
@@ -96,6 +96,8 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_apply_timed.argtypes = [P, P, P, ctypes.c_int, D]
         L.ifgf2d_measure_fp64_peak.argtypes = [D]
         L.ifgf2d_apply_direct_noalloc.argtypes = [P, P, P]
+        L.ifgf2d_set_host_threads.argtypes = [ctypes.c_int]
+        L.ifgf2d_prepare.argtypes = [P, ctypes.c_double, ctypes.c_int]
         L.ifgf2d_eval_offsurface_setup.argtypes = [P, ctypes.c_longlong, D, D]
         L.ifgf2d_eval_offsurface.argtypes = [P, D, D]
         L.ifgf2d_eval_offsurface_counts.argtypes = [P, I64]

@@ -50,6 +50,11 @@ using namespace ifgf;
 // per apply mode.  Kept across solves; rebuilt when the restart length or the tables change.
 struct GmresWork {
     DBuf<double2> V, w, h, t, H, y, vin;
+    // the solve's own vectors (right-hand side, solution, refinement residual, correction,
+    // product, one scalar), kept so that a solve after the first allocates and frees nothing:
+    // cudaFree synchronises the device, which would serialise contexts solving concurrently
+    DBuf<double2> sb, sx, sr, sd, st, shb;
+    long long sn = 0;
     DBuf<double> nrm2;
     DBuf<int> jdev;
     double2* H_host = nullptr;       // pinned copy of the Hessenberg columns read back per batch
@@ -75,6 +80,10 @@ struct ifgf2d_ctx {
     bool device_ready = false, precomputed = false, ifgf_ready = false;
     std::vector<int> h_nsp_ptr, h_nsp, h_srow_ptr, h_srow_col;
     int nlevels = 0;
+    // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
+    bool prep_ready = false;
+    double prep_k = 0.0;
+    int prep_request = 0, prep_nlevels = 0;
     int form = IFGF2D_SINGLE_LAYER;
     double eta = 0.0;               // coupling of the combined formulation, resolved at precompute
     // geometry (original order)

@@ -119,6 +119,11 @@ extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
     delete ctx;
     return IFGF2D_OK;
 }
+extern "C" int ifgf2d_set_host_threads(int n) {
+    if (n < 0) return IFGF2D_ERR_ARG;
+    host_thread_limit().store(n);
+    return IFGF2D_OK;
+}
 extern "C" const char* ifgf2d_last_error(const ifgf2d_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 extern "C" long long ifgf2d_num_unknowns(const ifgf2d_ctx* ctx) { return ctx ? ctx->D.N : -1; }
 extern "C" long long ifgf2d_num_patches(const ifgf2d_ctx* ctx) { return ctx ? ctx->D.num_patches : -1; }
@@ -206,12 +211,11 @@ static bool neighbourhood_ok(const Discretisation& D, int nlevels) {
     return true;
 }
 
-extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
+// the host part of the set-up: tree depth, neighbourhood check, tree and plans (no CUDA call)
+extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
     if (!ctx) return IFGF2D_ERR_ARG;
-    if (!ctx->precomputed || ctx->k != k) {
-        int rc = ifgf2d_precompute(ctx, k);
-        if (rc != IFGF2D_OK) return rc;
-    }
+    if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
+    const int request = nlevels;
     const Discretisation& D = ctx->D;
     if (nlevels <= 0) {
         nlevels = 0;
@@ -222,12 +226,34 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         if (nlevels > 20) return fail(ctx, IFGF2D_ERR_NLEVELS, "nlevels too large");
         if (!neighbourhood_ok(D, nlevels)) return fail(ctx, IFGF2D_ERR_NEIGHBORHOOD, "Singular point not in neighborhood");
     }
+    // the device tables no longer match the host tree from here until ifgf2d_setup completes
     ctx->ifgf_ready = false;
+    ctx->prep_ready = false;
+    std::string msg = build_tree(D.x, D.y, nlevels, k, ctx->opt.Ps, ctx->opt.Pang, ctx->T);
+    if (!msg.empty()) return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
+    ctx->prep_ready = true;
+    ctx->prep_k = k;
+    ctx->prep_request = request;
+    ctx->prep_nlevels = nlevels;
+    return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed || ctx->k != k) {
+        int rc = ifgf2d_precompute(ctx, k);
+        if (rc != IFGF2D_OK) return rc;
+    }
+    const Discretisation& D = ctx->D;
+    if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) {
+        int rc = ifgf2d_prepare(ctx, k, nlevels);
+        if (rc != IFGF2D_OK) return rc;
+    }
+    ctx->prep_ready = false;
+    nlevels = ctx->prep_nlevels;
     free_batch(ctx);
     free_eval(ctx);
     Tree& T = ctx->T;
-    std::string msg = build_tree(D.x, D.y, nlevels, k, ctx->opt.Ps, ctx->opt.Pang, T);
-    if (!msg.empty()) return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
     ctx->nlevels = nlevels;
     const long long N = D.N;
     const int P = T.P, Dl = nlevels - 1;
@@ -656,8 +682,14 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
     const long long N = ctx->D.N;
     cudaStream_t s = ctx->stream;
-    DBuf<double2> b, x;
-    CK(b.alloc(N)); CK(x.alloc(N));
+    if (!ctx->gw) ctx->gw.reset(new GmresWork);
+    GmresWork& GW = *ctx->gw;
+    if (GW.sn != N) {
+        CK(GW.sb.alloc(N)); CK(GW.sx.alloc(N)); CK(GW.sr.alloc(N)); CK(GW.sd.alloc(N)); CK(GW.st.alloc(N)); CK(GW.shb.alloc(1));
+        GW.sn = N;
+    }
+    DBuf<double2>& b = GW.sb;
+    DBuf<double2>& x = GW.sx;
     CK(cudaMemcpyAsync(b.p, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
     int iters = 0, rc;
     double est = 0.0;
@@ -666,8 +698,10 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
     } else {
         // FP64 iterative refinement: r = b - A x with the FP64 IFGF operator, inner GMRES on the
         // complex64 operator for the correction, x += d, until ||r|| / ||b|| < tol
-        DBuf<double2> r, d, t, hb;
-        CK(r.alloc(N)); CK(d.alloc(N)); CK(t.alloc(N)); CK(hb.alloc(1));
+        DBuf<double2>& r = GW.sr;
+        DBuf<double2>& d = GW.sd;
+        DBuf<double2>& t = GW.st;
+        DBuf<double2>& hb = GW.shb;
         CK(cudaMemsetAsync(x.p, 0, sizeof(double2) * N, s));
         auto nrm = [&](const double2* v, double& out) -> int {
             launch_multidot(v, N, 1, v, N, hb.p, s);

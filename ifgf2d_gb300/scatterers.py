@@ -1,0 +1,121 @@
+"""Many independent obstacles, each solved to a tolerance on its own context.
+
+The reference solves one obstacle per ForwardMap (ForwardMap.tpp:658-697).  Here the work of
+an obstacle is split at the host/device line: a pool of host threads runs the host part
+(discretisation, tree depth, tree and plans: ifgf2d_create + ifgf2d_prepare, no CUDA calls)
+a bounded number of obstacles ahead, while one thread runs the device part of each obstacle
+in turn (precomputation, device tables, GMRES, residual).  Host set-up thus overlaps GPU work
+without CUDA calls contending from many threads.  Set-up calls run single-threaded inside
+(ifgf2d_set_host_threads(1)); the pool supplies the host parallelism.  Obstacles below
+`direct_below` unknowns, and those whose points no tree depth keeps in the leaf
+neighbourhood, use the direct operator, which needs no tree.
+
+The seeded configuration of `star_obstacles` is the multi-obstacle benchmark: star curves
+r(t) = 1 + sum_{m=1..5} a_m cos mt + b_m sin mt with a_m, b_m ~ U(-0.05, 0.05), k ~ U(10, 400),
+N_i = 16 * ceil(10 k L / (2 pi) / 16) points (10 per wavelength, L the perimeter) and a plane
+wave at an angle ~ U(0, 2 pi), drawn from numpy's default_rng(seed).
+"""
+from __future__ import annotations
+
+import math
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Obstacle:
+    a: np.ndarray                  # cosine coefficients a_1..a_M of the star radius
+    b: np.ndarray                  # sine coefficients b_1..b_M
+    k: float                       # wavenumber
+    angle: float                   # incidence angle of the plane wave
+    npoints: int                   # unknowns (a multiple of 16)
+    result: dict = field(default_factory=dict)
+
+
+def star_perimeter(a, b, nt=4000):
+    t = np.linspace(0.0, 2 * np.pi, nt, endpoint=False)
+    m = np.arange(1, len(a) + 1)
+    r = 1.0 + (np.asarray(a)[None, :] * np.cos(m[None, :] * t[:, None]) + np.asarray(b)[None, :] * np.sin(m[None, :] * t[:, None])).sum(1)
+    dr = (m[None, :] * (-np.asarray(a)[None, :] * np.sin(m[None, :] * t[:, None])
+                        + np.asarray(b)[None, :] * np.cos(m[None, :] * t[:, None]))).sum(1)
+    return float(np.sum(np.sqrt(r * r + dr * dr)) * (2 * np.pi / nt))
+
+
+def star_obstacles(n=256, seed=0, kmin=10.0, kmax=400.0, modes=5, amp=0.05, ppw=10.0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a = rng.uniform(-amp, amp, modes)
+        b = rng.uniform(-amp, amp, modes)
+        k = float(rng.uniform(kmin, kmax))
+        ang = float(rng.uniform(0.0, 2 * np.pi))
+        L = star_perimeter(a, b)
+        npts = 16 * int(math.ceil(ppw * k * L / (2 * np.pi) / 16))
+        out.append(Obstacle(a, b, k, ang, npts))
+    return out
+
+
+def _prepare_one(G, ob, direct_below):
+    fm = G.ForwardMap(0.01, [G.Star(ob.a, ob.b)], (), 1.0, ob.k, Np=16, patches_per_curve=max(ob.npoints // 16, 4),
+                      formulation="combined")
+    accel = fm.total_num_unknowns_ >= direct_below
+    if accel:
+        try:
+            fm.prepare(ob.k, 0)
+        except G.NeighbourhoodError:
+            accel = False
+    return fm, accel
+
+
+def _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters):
+    rhs = -np.exp(1j * ob.k * (math.cos(ob.angle) * fm.xs_ + math.sin(ob.angle) * fm.ys_))
+    if accel:
+        fm.precomps_and_setup(ob.k, 0)
+    else:
+        fm.compute_precomputations(ob.k)
+    x = fm.gmres(rhs, accelerated=accel, tol=tol, restart=restart, max_iters=max_iters, mixed=mixed and accel)
+    st = dict(fm.last_solve)
+    y = fm.compute_Ax_acc(x) if accel else fm.compute_Ax_unacc(x)
+    st["true_rel_residual"] = float(np.linalg.norm(y - rhs) / np.linalg.norm(rhs))
+    st["accelerated"] = accel
+    st["N"] = fm.total_num_unknowns_
+    ob.result = st
+    return x
+
+
+def solve_obstacles(obstacles, tol=1e-6, workers=15, mixed=True, direct_below=0, restart=300, max_iters=1000,
+                    keep_solutions=False, lookahead=None):
+    """Solve every obstacle (plane-wave scattering, combined field) to `tol`.  Returns the
+    densities when keep_solutions, else None; each obstacle's `result` holds iterations,
+    convergence, the true FP64 relative residual and the operator used.  workers = 0 runs
+    everything on the calling thread."""
+    from . import _lib
+    import ifgf2d_gb300 as G
+    L = _lib.load()
+    xs = []
+    if workers <= 0:
+        for ob in obstacles:
+            fm, accel = _prepare_one(G, ob, direct_below)
+            x = _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters)
+            del fm
+            xs.append(x if keep_solutions else None)
+        return xs if keep_solutions else None
+    ahead = lookahead or 2 * workers
+    L.ifgf2d_set_host_threads(1)
+    try:
+        with ThreadPoolExecutor(workers) as ex:
+            futs = {}
+            nxt = 0
+            for i, ob in enumerate(obstacles):
+                while nxt < len(obstacles) and nxt < i + ahead:
+                    futs[nxt] = ex.submit(_prepare_one, G, obstacles[nxt], direct_below)
+                    nxt += 1
+                fm, accel = futs.pop(i).result()
+                x = _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters)
+                del fm
+                xs.append(x if keep_solutions else None)
+    finally:
+        L.ifgf2d_set_host_threads(0)
+    return xs if keep_solutions else None

@@ -83,6 +83,11 @@ int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf2d_junction
 int ifgf2d_destroy(ifgf2d_ctx* ctx);
 const char* ifgf2d_last_error(const ifgf2d_ctx* ctx);
 
+/* Host threads one set-up call may use (tree, plans, discretisation; process-wide): 0 = all
+ * cores (the default), 1 = serial.  A caller that sets up many contexts concurrently from its
+ * own threads (independent obstacles) sets 1 and keeps its own threads busy instead. */
+int ifgf2d_set_host_threads(int n);
+
 /* ForwardMap::total_num_unknowns_, num_patches_ (ForwardMap/ForwardMap.hpp:52-53) */
 long long ifgf2d_num_unknowns(const ifgf2d_ctx* ctx);
 long long ifgf2d_num_patches(const ifgf2d_ctx* ctx);
@@ -103,6 +108,11 @@ int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, double* out);
  * (BoxTree.h:1079-1161) and the exclusion sets (ForwardMap.tpp:567-607), all flattened into
  * device tables.  nlevels <= 0 picks the deepest tree that passes the neighbourhood check. */
 int ifgf2d_setup(ifgf2d_ctx* ctx, double wavenumber, int nlevels);
+/* The host part of ifgf2d_setup alone: tree depth, neighbourhood check, tree and plans.  It
+ * makes no CUDA call, so it may run on any host thread while the GPU works on other contexts;
+ * a following ifgf2d_setup with the same wavenumber and nlevels does only the device part.
+ * Until that setup the context's IFGF applies return IFGF2D_ERR_STATE. */
+int ifgf2d_prepare(ifgf2d_ctx* ctx, double wavenumber, int nlevels);
 int ifgf2d_get_nlevels(const ifgf2d_ctx* ctx);
 /* BoxTree::getSorting (IFGF_Source/BoxTree.h:1163-1165) */
 int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* sorting);

@@ -79,3 +79,19 @@ def test_rectangle_junctions_discretise(lib, oracle):
     _, i_g, _ = fm.near_singular()
     _, i_o, _ = om.near_singular()
     assert np.array_equal(i_g, i_o)
+
+
+def test_star_obstacle_configuration():
+    """The seeded multi-obstacle configuration: 256 stars, k in [10, 400], 10 points per
+    wavelength rounded up to whole 16-point patches, reproducible from the seed."""
+    from ifgf2d_gb300.scatterers import star_obstacles, star_perimeter
+    a = star_obstacles(256)
+    b = star_obstacles(256)
+    assert len(a) == 256
+    for o, p in zip(a, b):
+        assert o.k == p.k and o.angle == p.angle and np.array_equal(o.a, p.a)
+        assert 10.0 <= o.k <= 400.0 and np.all(np.abs(o.a) <= 0.05) and np.all(np.abs(o.b) <= 0.05)
+        L = star_perimeter(o.a, o.b)
+        assert o.npoints % 16 == 0 and o.npoints >= 10 * o.k * L / (2 * np.pi) > o.npoints - 16
+    # the unperturbed star is the unit circle
+    assert abs(star_perimeter(np.zeros(5), np.zeros(5)) - 2 * np.pi) < 1e-12
