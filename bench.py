@@ -142,6 +142,23 @@ def phase_model(wc, N, P, ncones_leaf, nparent):
     }
 
 
+def max_over_ranks(v, world, device):
+    """The slowest rank's value (a barrier follows): the whole job is as fast as its slowest replica."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_value(world, steps, ms):
+    """Whole-job matvecs/s: every replica did `steps` applies in at most `ms` milliseconds."""
+    return world * steps / (ms * 1e-3)
+
+
 def run_ours(args, rank, local_rank, world):
     import torch
     torch.cuda.set_device(local_rank)
@@ -169,13 +186,8 @@ def run_ours(args, rank, local_rank, world):
             fm.apply_device(x, y)
         e1.record(ext)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
-    value = world * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    value = replica_value(world, args.steps, ms)
     # the chosen form: IFGF far field in complex64 (FP32 arithmetic), FP64 singular correction
     for _ in range(max(args.warmup, 3)):
         fm.apply_device(x, y, mixed=True)
@@ -288,6 +300,8 @@ def run_ours(args, rank, local_rank, world):
                    "phase_ms": dict(zip(phases, [float(v) for v in acc_mixed]))},
         "work": wc,
     }
+    if world > 1:   # the extra workloads are single-GPU measurements, reported at N = 1
+        return out
     if not args.no_batch:
         del fm
         torch.cuda.synchronize()

@@ -235,6 +235,10 @@ extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
     ctx->prep_k = k;
     ctx->prep_request = request;
     ctx->prep_nlevels = nlevels;
+    ctx->nlevels = nlevels;
+    const Tree& T = ctx->T;
+    ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
+    ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
     return IFGF2D_OK;
 }
 
@@ -389,7 +393,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
 
 extern "C" int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* s) {
     if (!ctx || !s) return IFGF2D_ERR_ARG;
-    if (!ctx->ifgf_ready) return IFGF2D_ERR_STATE;
+    if (!ctx->ifgf_ready && !ctx->prep_ready) return IFGF2D_ERR_STATE;
     std::copy(ctx->T.sorting.begin(), ctx->T.sorting.end(), s);
     return IFGF2D_OK;
 }
@@ -513,6 +517,11 @@ extern "C" int ifgf2d_apply_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, 
 
 extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mode) {
     if (!ctx || !x || !y) return IFGF2D_ERR_ARG;
+    // state and mode before any copy (apply_dev repeats the checks for the device entry point)
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
     const size_t bytes = sizeof(double2) * ctx->D.N;
     CK(cudaMemcpyAsync(ctx->vin.p, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
     int rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, mode);

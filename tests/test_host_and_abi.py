@@ -95,3 +95,32 @@ def test_star_obstacle_configuration():
         assert o.npoints % 16 == 0 and o.npoints >= 10 * o.k * L / (2 * np.pi) > o.npoints - 16
     # the unperturbed star is the unit circle
     assert abs(star_perimeter(np.zeros(5), np.zeros(5)) - 2 * np.pi) < 1e-12
+
+
+def test_prepare_builds_the_oracle_tree_without_a_gpu(lib, oracle):
+    """ifgf2d_prepare is host-only: on a machine without a GPU it builds the tree, whose Morton
+    sorting and work counts equal the oracle's (BoxTree.h:61-600, Level.h), with one set-up
+    thread or all of them."""
+    k = 40.0
+    L = lib._lib.load()
+    om = oracle.OracleForwardMap([oracle.curve_kite()], 16, 0.01, 1.0, k, patches_per_curve=64)
+    seen = []
+    for threads in (1, 0):
+        assert L.ifgf2d_set_host_threads(threads) == 0
+        fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
+        fm.prepare(k, 0)
+        nl = int(L.ifgf2d_get_nlevels(fm.handle))
+        om.setup_ifgf(k, nl)
+        assert np.array_equal(fm.getSorting(), om.sorting())
+        wc, ow = fm.work_counts(), om.work()
+        for key in ("near_pairs", "leaf_evals", "prop_evals", "interp_evals", "cones"):
+            assert wc[key] == ow[key], key
+        seen.append((nl, fm.getSorting().tobytes(), tuple(sorted(wc.items()))))
+        # the device tables do not exist yet: applies report the state, before any copy
+        with pytest.raises(lib.IFGF2DError):
+            fm.compute_Ax_acc(np.ones(fm.total_num_unknowns_, dtype=complex))
+    assert seen[0] == seen[1]
+    assert L.ifgf2d_set_host_threads(-1) == 1
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
+    assert L.ifgf2d_prepare(fm.handle, k, 2) == 4          # IFGF2D_ERR_NLEVELS, BoxTree.h:1117
+    assert L.ifgf2d_prepare(fm.handle, -1.0, 0) == 1
