@@ -453,35 +453,62 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
     return res
 
 
-def time_oracle(budget_s=12.0, max_steps=None):
-    """CPU oracle (single-threaded restatement of the reference path) on the same workload."""
+def time_oracle(budget_s=12.0, max_steps=None, threads=None):
+    """The CPU oracle (restatement of the reference path, which is single-threaded) on the same
+    workload, on every host thread: one oracle context per thread, each running whole IFGF
+    matvecs until the common deadline; the value is all threads' matvecs over the wall time."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle as O
     O.build()
-    om = O.OracleForwardMap([O.curve_kite()], NP, DELTA, 1.0, K_WAVE, patches_per_curve=NPATCH, formulation="combined")
-    om.precompute(K_WAVE)
-    import ifgf2d_gb300 as G
-    # same tree depth rule as the product: deepest nlevels passing the neighbourhood check
-    for nl in range(16, 2, -1):
-        try:
-            om.setup_ifgf(K_WAVE, nl)
-            break
-        except RuntimeError:
-            continue
-    d = O.seeded_density(om.N)
-    steps, t_total = 0, 0.0
-    while t_total < budget_s and (max_steps is None or steps < max_steps):
-        t0 = time.perf_counter()
-        om.compute_Ax_acc(d)
-        t_total += time.perf_counter() - t0
-        steps += 1
-    return {"value": steps / t_total, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} full IFGF matvecs of the same workload (nlevels {nl}), {t_total:.1f} s, 1 thread"}
+    nt = threads or max(1, min(32, os.cpu_count() or 1))
+
+    def make():
+        om = O.OracleForwardMap([O.curve_kite()], NP, DELTA, 1.0, K_WAVE, patches_per_curve=NPATCH, formulation="combined")
+        om.precompute(K_WAVE)
+        # same tree depth rule as the product: deepest nlevels passing the neighbourhood check
+        for nl in range(16, 2, -1):
+            try:
+                om.setup_ifgf(K_WAVE, nl)
+                return om, nl
+            except RuntimeError:
+                continue
+        raise RuntimeError("oracle: no valid tree depth")
+
+    with ThreadPoolExecutor(nt) as ex:
+        ctxs = list(ex.map(lambda _: make(), range(nt)))
+    d = O.seeded_density(ctxs[0][0].N)
+    counts = [0] * nt
+    ends = [0.0] * nt
+    per_thread_cap = None if max_steps is None else max(1, -(-max_steps // nt))
+    t_start = time.perf_counter()
+    deadline = t_start + budget_s
+
+    def run(i):
+        om = ctxs[i][0]
+        while True:
+            om.compute_Ax_acc(d)
+            counts[i] += 1
+            ends[i] = time.perf_counter()
+            if ends[i] >= deadline or (per_thread_cap is not None and counts[i] >= per_thread_cap):
+                return
+
+    ths = [threading.Thread(target=run, args=(i,)) for i in range(nt)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = max(ends) - t_start
+    steps = sum(counts)
+    return {"value": steps / wall, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"{steps} full IFGF matvecs of the same workload (nlevels {ctxs[0][1]}) on {nt} threads, "
+                      f"one oracle context each, {wall:.1f} s wall"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    r = time_oracle(budget_s=float(os.environ.get("IFGF2D_REF_BUDGET_S", "60")),
+    r = time_oracle(budget_s=float(os.environ.get("IFGF2D_REF_BUDGET_S", "30")),
                     max_steps=max(1, args.steps))
     return {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
