@@ -396,6 +396,36 @@ class ForwardMap:
             _check(rc, self._h)
         return x
 
+    def geometry_features(self):
+        """(N, 4): curvature, unit tangent x, y and quadrature weight per point (patch order), the
+        geometry the learned preconditioner reads"""
+        g = np.empty((self.total_num_unknowns_, 4))
+        _check(_lib.load().ifgf2d_get_geometry_features(self._h, _dp(g)), self._h)
+        return g
+
+    def solve_precond(self, net, rhs, accelerated=True, tol=None, restart=None, max_iters=None, mixed=False,
+                      raise_on_noconv=False):
+        """GMRES with the learned right preconditioner (flexible GMRES inside FP64 iterative
+        refinement, plain GMRES after a stall); ``net`` is a learned.PreconditionerNet."""
+        n = self.total_num_unknowns_
+        b = _cview(rhs, n)
+        x = np.empty(n, dtype=np.complex128)
+        it = ctypes.c_int(0)
+        err = ctypes.c_double(0.0)
+        tol = self.GMRES_TOLERANCE_ if tol is None else tol
+        restart = self.GMRES_MAX_ITER_ if restart is None else restart
+        max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        rc = _lib.load().ifgf2d_solve_precond(self._h, net.handle, _dp(b.view(np.float64)), _dp(x.view(np.float64)), mode,
+                                              float(tol), int(restart), int(max_iters), ctypes.byref(it), ctypes.byref(err))
+        self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0))
+        if rc == 8:
+            if raise_on_noconv:
+                raise NoConvergence(f"FGMRES: {it.value} iterations, error {err.value:.3e}")
+        else:
+            _check(rc, self._h)
+        return x
+
     def linear_operator(self, accelerated=True):
         """LinearOperator wrapping compute_Ax_acc / compute_Ax_unacc, as ForwardMap::solve builds it."""
         f = self.compute_Ax_acc if accelerated else self.compute_Ax_unacc

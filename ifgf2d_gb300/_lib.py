@@ -30,7 +30,9 @@ EXPORTS = [
     "ifgf2d_apply_device", "ifgf2d_ifgf_far", "ifgf2d_solve", "ifgf2d_propagate", "ifgf2d_hankel",
     "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
     "ifgf2d_apply_direct_noalloc", "ifgf2d_apply_batch", "ifgf2d_apply_batch_device", "ifgf2d_solve_batch",
-    "ifgf2d_set_host_threads", "ifgf2d_prepare", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
+    "ifgf2d_set_host_threads", "ifgf2d_prepare", "ifgf2d_net_num_params", "ifgf2d_net_create", "ifgf2d_net_destroy",
+    "ifgf2d_net_last_error", "ifgf2d_net_get_params", "ifgf2d_net_set_params", "ifgf2d_net_gradient",
+    "ifgf2d_net_train_step", "ifgf2d_net_apply", "ifgf2d_get_geometry_features", "ifgf2d_solve_precond", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
 ]
 
 
@@ -98,6 +100,20 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_apply_direct_noalloc.argtypes = [P, P, P]
         L.ifgf2d_set_host_threads.argtypes = [ctypes.c_int]
         L.ifgf2d_prepare.argtypes = [P, ctypes.c_double, ctypes.c_int]
+        F = ctypes.POINTER(ctypes.c_float)
+        IP = ctypes.POINTER(ctypes.c_int)
+        L.ifgf2d_net_num_params.restype = ctypes.c_longlong
+        L.ifgf2d_net_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(P)]
+        L.ifgf2d_net_destroy.argtypes = [P]
+        L.ifgf2d_net_last_error.argtypes = [P]; L.ifgf2d_net_last_error.restype = ctypes.c_char_p
+        L.ifgf2d_net_get_params.argtypes = [P, F]
+        L.ifgf2d_net_set_params.argtypes = [P, F]
+        L.ifgf2d_net_gradient.argtypes = [P, ctypes.c_int, IP, D, D, D, D, D, F]
+        L.ifgf2d_net_train_step.argtypes = [P, ctypes.c_int, IP, D, D, D, D, ctypes.c_float, ctypes.c_float, D]
+        L.ifgf2d_net_apply.argtypes = [P, ctypes.c_int, IP, D, D, D, D, F]
+        L.ifgf2d_get_geometry_features.argtypes = [P, D]
+        L.ifgf2d_solve_precond.argtypes = [P, P, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int), D]
         L.ifgf2d_eval_offsurface_setup.argtypes = [P, ctypes.c_longlong, D, D]
         L.ifgf2d_eval_offsurface.argtypes = [P, D, D]
         L.ifgf2d_eval_offsurface_counts.argtypes = [P, I64]

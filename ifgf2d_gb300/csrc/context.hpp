@@ -49,18 +49,21 @@ using namespace ifgf;
 // GMRES workspace of a context: Krylov basis, Arnoldi state and one captured iteration graph
 // per apply mode.  Kept across solves; rebuilt when the restart length or the tables change.
 struct GmresWork {
-    DBuf<double2> V, w, h, t, H, y, vin;
+    DBuf<double2> V, w, h, t, H, y, vin, part;
     // the solve's own vectors (right-hand side, solution, refinement residual, correction,
     // product, one scalar), kept so that a solve after the first allocates and frees nothing:
     // cudaFree synchronises the device, which would serialise contexts solving concurrently
     DBuf<double2> sb, sx, sr, sd, st, shb;
     long long sn = 0;
+    // flexible GMRES with the learned preconditioner: z_j = M(v_j) for every column, and the
+    // preconditioner's output buffer the captured iteration writes before copying it into Z
+    DBuf<double2> Z, zt;
     DBuf<double> nrm2;
     DBuf<int> jdev;
     double2* H_host = nullptr;       // pinned copy of the Hessenberg columns read back per batch
     long long n = 0;
     int m = 0;
-    cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // mode x (plain, preconditioned)
     void drop_graphs() {
         for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
     }
@@ -150,6 +153,11 @@ int apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode);
 void free_batch(ifgf2d_ctx* ctx);
 // off-surface evaluation plan release (offsurface.cu)
 void free_eval(ifgf2d_ctx* ctx);
+// the learned preconditioner on one curve of N points (precond_capi.cu): prepare lays the
+// network out for N points with the curve's geometry (host call, synchronous, not capturable);
+// launch queues z = M(r) on stream s (capturable; the buffers stay fixed until the next prepare)
+int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, double k, std::string& err);
+void net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cudaStream_t s);
 }  // namespace ifgf
 
 // Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)

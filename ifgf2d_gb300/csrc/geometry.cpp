@@ -54,6 +54,31 @@ double HostCurve::yp(double t) const {
     }
 }
 
+double HostCurve::curvature(double t) const {
+    double xpp = 0.0, ypp = 0.0;
+    switch (type) {
+        case IFGF2D_CURVE_CIRCLE: xpp = -p[2] * std::cos(t); ypp = -p[2] * std::sin(t); break;
+        case IFGF2D_CURVE_KITE: xpp = -p[0] * std::cos(t) - 4.0 * p[1] * std::cos(2.0 * t); ypp = -p[3] * std::sin(t); break;
+        case IFGF2D_CURVE_LINE: return 0.0;
+        default: {
+            const int M = (int)p[2];
+            double r = 1.0, dr = 0.0, ddr = 0.0;
+            for (int m = 1; m <= M; ++m) {
+                const double c = std::cos(m * t), s = std::sin(m * t);
+                r += p[2 + m] * c + p[2 + M + m] * s;
+                dr += -m * p[2 + m] * s + m * p[2 + M + m] * c;
+                ddr += -m * m * (p[2 + m] * c + p[2 + M + m] * s);
+            }
+            const double c = std::cos(t), s = std::sin(t);
+            xpp = ddr * c - 2.0 * dr * s - r * c;
+            ypp = ddr * s + 2.0 * dr * c - r * s;
+        }
+    }
+    const double a = xp(t), b = yp(t);
+    const double sp = std::sqrt(a * a + b * b);
+    return (a * ypp - b * xpp) / (sp * sp * sp);
+}
+
 // ---------------------------------------------------------------- quadrature (Quadrature.hpp)
 static inline double lin_map(double x, double a, double b, double c, double d) { return ((d - c) / (b - a)) * (x - a) + c; }
 
@@ -274,6 +299,7 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
                 double cj = nn;
                 if (s1 || s2) cj *= ej;
                 D.x.push_back(cv.x(t)); D.y.push_back(cv.y(t));
+                D.kappa.push_back(cv.curvature(t));
                 D.nx.push_back(nx / nn); D.ny.push_back(ny / nn);
                 D.t.push_back(t);
                 D.wq.push_back(((b - a) / 2.0) * D.fej_w[j] * cj);

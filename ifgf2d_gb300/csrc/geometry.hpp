@@ -31,6 +31,8 @@ struct HostCurve {
     double y(double t) const;
     double xp(double t) const;
     double yp(double t) const;
+    // signed curvature (x' y'' - y' x'') / |x'|^3 (for the learned preconditioner's features)
+    double curvature(double t) const;
 };
 
 // Everything the constructor of ForwardMap computes (ForwardMap.tpp:15-285)
@@ -40,7 +42,7 @@ struct Discretisation {
     long long N = 0, num_patches = 0;
     std::vector<HostCurve> curves;
     // per point (patch-major order, as in ForwardMap::xs_)
-    std::vector<double> x, y, nx, ny, t, wq, edge_jac;
+    std::vector<double> x, y, nx, ny, t, wq, edge_jac, kappa;
     std::vector<int> patch_of;
     // per patch
     std::vector<double> t1, t2;

@@ -577,7 +577,7 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
 // thread.  Stops when |g_{j+1}| / ||r0|| < tol (the first ||r0||, opGMRES.hpp:207) or after
 // max_iters iterations; iterations run past the stop inside a batch are discarded.
 static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, double tol, int restart,
-                      int max_iters, int& iters, double& est) {
+                      int max_iters, int& iters, double& est, ifgf2d_net* net = nullptr) {
     const long long N = ctx->D.N;
     const int m = restart, ldh = m + 1;
     cudaStream_t s = ctx->stream;
@@ -587,20 +587,32 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         G.drop_graphs();
         CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N)); CK(G.vin.alloc(N));
         CK(G.H.alloc((size_t)ldh * m)); CK(G.y.alloc(m)); CK(G.nrm2.alloc(1)); CK(G.jdev.alloc(1));
+        CK(G.part.alloc((size_t)arnoldi_part_size(N, m)));
         if (G.H_host) { cudaFreeHost(G.H_host); G.H_host = nullptr; }
         CK(cudaMallocHost((void**)&G.H_host, (size_t)ldh * m * sizeof(double2)));
+        G.Z.release(); G.zt.release();
         G.n = N; G.m = m;
     }
-    if (!G.exec[mode]) {
+    if (net && !G.Z.p) { CK(G.Z.alloc((size_t)N * m)); CK(G.zt.alloc(N)); }
+    const int gi = mode + (net ? 3 : 0);
+    if (!G.exec[gi]) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         launch_copy_col(G.V.p, N, G.jdev.p, G.vin.p, G.nrm2.p, s);
-        int rc = apply_dev(ctx, G.vin.p, G.w.p, mode);
-        launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.w.p, G.h.p, G.H.p, G.nrm2.p, s);
+        int rc;
+        if (net) {
+            // flexible GMRES: z_j = M(v_j) into Z[:, j], then w = A z_j
+            net_precondition_launch(net, G.vin.p, G.zt.p, s);
+            launch_store_col(G.zt.p, N, G.jdev.p, G.Z.p, s);
+            rc = apply_dev(ctx, G.zt.p, G.w.p, mode);
+        } else {
+            rc = apply_dev(ctx, G.vin.p, G.w.p, mode);
+        }
+        launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.w.p, G.h.p, G.H.p, G.nrm2.p, G.part.p, s);
         cudaError_t ec = cudaStreamEndCapture(s, &graph);
         if (rc != IFGF2D_OK) return rc;
         CK(ec);
-        CK(cudaGraphInstantiate(&G.exec[mode], graph, 0));
+        CK(cudaGraphInstantiate(&G.exec[gi], graph, 0));
         cudaGraphDestroy(graph);
     }
     double2 *V = G.V.p, *w = G.w.p, *h = G.h.p, *t = G.t.p;
@@ -616,9 +628,9 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
     iters = 0; est = 0.0;
     double bn; if ((rc = dnorm(b, bn))) return rc;
     if (bn <= 2.2250738585072014e-308) return IFGF2D_OK;
-    // r0 = b - A x0 with x0 = 0 (the reference applies the operator to the zero guess too)
-    if ((rc = apply_dev(ctx, x, t, mode))) return rc;
-    launch_sub(b, t, N, w, s);
+    // r0 = b - A x0 = b for the initial guess x0 = 0 (the reference applies the operator to the
+    // zero guess, which gives exactly 0)
+    CK(cudaMemcpyAsync(w, b, sizeof(double2) * N, cudaMemcpyDeviceToDevice, s));
     double beta; if ((rc = dnorm(w, beta))) return rc;
     const double r0n = beta;
     est = 1.0;
@@ -636,7 +648,7 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         bool stop = false;
         while (j < m && !stop) {
             const int nb = std::min(4, m - j);
-            for (int q = 0; q < nb; ++q) CK(cudaGraphLaunch(G.exec[mode], s));
+            for (int q = 0; q < nb; ++q) CK(cudaGraphLaunch(G.exec[gi], s));
             // columns j .. j+nb-1, rows 0 .. j+nb
             CK(cudaMemcpy2DAsync(G.H_host + (size_t)j * ldh, ldh * sizeof(double2), G.H.p + (size_t)j * ldh, ldh * sizeof(double2),
                                  (size_t)(j + nb + 1) * sizeof(double2), nb, cudaMemcpyDeviceToHost, s));
@@ -669,7 +681,7 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
             yv[i] = make_double2(yi.real(), yi.imag());
         }
         CK(cudaMemcpyAsync(G.y.p, yv.data(), sizeof(double2) * jcols, cudaMemcpyHostToDevice, s));
-        launch_multi_axpy(V, N, jcols, G.y.p, 1.0, N, x, s);
+        launch_multi_axpy(net ? G.Z.p : V, N, jcols, G.y.p, 1.0, N, x, s);   // x += V y, or Z y (flexible)
         if (stop) break;
         // restart: r = b - A x (the residual estimate keeps the first ||r0||, opGMRES.hpp:207)
         if ((rc = apply_dev(ctx, x, t, mode))) return rc;
@@ -742,6 +754,77 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
         }
     }
     CK(cudaMemcpyAsync(xout, x.p, sizeof(double2) * N, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (iters_out) *iters_out = iters;
+    if (err_out) *err_out = est;
+    return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}
+
+// ------------------------------------------------------------------ learned right preconditioner
+// Flexible GMRES with z_j = M(v_j) from the network, inside FP64 iterative refinement: the
+// residual b - A x with the FP64 operator (the stop test), corrections from flexible GMRES on
+// the operator of `mode`.  A preconditioned correction that misses its tolerance (a stall)
+// switches the rest of the solve to plain GMRES.
+extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* xout, int mode, double tol,
+                                    int restart, int max_iters, int* iters_out, double* err_out) {
+    if (!ctx || !net || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
+        return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");
+    if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
+    const Discretisation& D = ctx->D;
+    const long long N = D.N;
+    cudaStream_t s = ctx->stream;
+    {
+        std::vector<double> geom((size_t)N * 4);
+        for (long long i = 0; i < N; ++i) {
+            geom[4 * i] = D.kappa[i]; geom[4 * i + 1] = -D.ny[i]; geom[4 * i + 2] = D.nx[i]; geom[4 * i + 3] = D.wq[i];
+        }
+        CK(cudaStreamSynchronize(s));
+        std::string msg;
+        int rc = net_prepare_single(net, N, geom.data(), ctx->k, msg);
+        if (rc != IFGF2D_OK) return fail(ctx, rc, msg);
+    }
+    if (!ctx->gw) ctx->gw.reset(new GmresWork);
+    GmresWork& GW = *ctx->gw;
+    // the network's buffers may have moved since the last capture: recapture the flexible iterations
+    for (int q = 3; q < 6; ++q) if (GW.exec[q]) { cudaGraphExecDestroy(GW.exec[q]); GW.exec[q] = nullptr; }
+    if (GW.sn != N) {
+        CK(GW.sb.alloc(N)); CK(GW.sx.alloc(N)); CK(GW.sr.alloc(N)); CK(GW.sd.alloc(N)); CK(GW.st.alloc(N)); CK(GW.shb.alloc(1));
+        GW.sn = N;
+    }
+    double2 *b = GW.sb.p, *x = GW.sx.p, *r = GW.sr.p, *d = GW.sd.p, *t = GW.st.p, *hb = GW.shb.p;
+    CK(cudaMemcpyAsync(b, rhs, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, s));
+    auto nrm = [&](const double2* v, double& out) -> int {
+        launch_multidot(v, N, 1, v, N, hb, s);
+        double2 q; CK(cudaMemcpyAsync(&q, hb, sizeof(double2), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        out = std::sqrt(std::max(q.x, 0.0));
+        return IFGF2D_OK;
+    };
+    const int outer_mode = mode == IFGF2D_APPLY_DIRECT ? IFGF2D_APPLY_DIRECT : IFGF2D_APPLY_IFGF;
+    int rc, iters = 0;
+    double bn; if ((rc = nrm(b, bn))) return rc;
+    CK(cudaMemcpyAsync(r, b, sizeof(double2) * N, cudaMemcpyDeviceToDevice, s));
+    double rn = bn, est = bn > 0 ? 1.0 : 0.0;
+    bool use_net = true;
+    for (int outer = 0; outer < 30 && est >= tol && iters < max_iters; ++outer) {
+        const double want = tol * bn / rn;
+        const double inner_tol = mode == IFGF2D_APPLY_IFGF_MIXED ? std::max(2e-7, 0.3 * want) : 0.5 * want;
+        int it = 0; double e = 0.0;
+        if ((rc = gmres_core(ctx, r, d, mode, inner_tol, restart, max_iters - iters, it, e, use_net ? net : nullptr))) return rc;
+        iters += it;
+        if (use_net && e >= inner_tol) use_net = false;   // stalled: plain GMRES from here on
+        double2 one = make_double2(1.0, 0.0);
+        CK(cudaMemcpyAsync(hb, &one, sizeof(double2), cudaMemcpyHostToDevice, s));
+        launch_multi_axpy(d, N, 1, hb, 1.0, N, x, s);   // x += d
+        if ((rc = apply_dev(ctx, x, t, outer_mode))) return rc;
+        launch_sub(b, t, N, r, s);
+        if ((rc = nrm(r, rn))) return rc;
+        est = rn / bn;
+    }
+    CK(cudaMemcpyAsync(xout, x, sizeof(double2) * N, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (iters_out) *iters_out = iters;
     if (err_out) *err_out = est;

@@ -244,6 +244,47 @@ __global__ void k_copy_col(const double2* __restrict__ V, long long n, const int
     if (i < n) out[i] = V[(long long)(*jp) * n + i];
     if (i == 0 && nrm2) *nrm2 = 0.0;
 }
+// h[c] = V[:, c]^H w for c <= *jp in two deterministic stages: blocks (row chunk, column)
+// write partial sums, then one thread per column adds its chunks in order.  The grid spans
+// every column and row chunk, so even the first iterations keep all SMs busy.
+constexpr int kDotChunk = 2048;
+__global__ void __launch_bounds__(256) k_multidot_part(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                                                       const double2* __restrict__ w, long long n, double2* __restrict__ part) {
+    const int col = blockIdx.y;
+    if (col > *jp) return;
+    const int chunk = blockIdx.x;
+    const long long i0 = (long long)chunk * kDotChunk;
+    const long long i1 = i0 + kDotChunk < n ? i0 + kDotChunk : n;
+    const double2* v = V + (long long)col * ldv;
+    double re = 0.0, im = 0.0;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const double2 a = v[i], b = w[i];
+        re = fma(a.x, b.x, fma(a.y, b.y, re));
+        im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+    __shared__ double sr[8], si[8];
+    re = warp_sum(re); im = warp_sum(im);
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = re; si[threadIdx.x >> 5] = im; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += sr[q]; b += si[q]; }
+        part[(long long)col * gridDim.x + chunk] = make_double2(a, b);
+    }
+}
+__global__ void k_multidot_fin(const double2* __restrict__ part, int nchunk, const int* __restrict__ jp, int ncol,
+                               double2* __restrict__ h) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ncol || col > *jp) return;
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < nchunk; ++q) { const double2 v = part[(long long)col * nchunk + q]; a += v.x; b += v.y; }
+    h[col] = make_double2(a, b);
+}
+// Z[:, *jp] = z (flexible GMRES keeps the preconditioned vectors)
+__global__ void k_store_col(const double2* __restrict__ z, long long n, const int* __restrict__ jp, double2* __restrict__ Z) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) Z[(long long)(*jp) * n + i] = z[i];
+}
 __global__ void k_multidot_dyn(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
                                const double2* __restrict__ w, long long n, double2* __restrict__ h) {
     const int j = blockIdx.x;
@@ -384,16 +425,22 @@ void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaSt
 void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s) {
     k_sub<<<nblk(n, 256), 256, 0, s>>>(a, b, n, out);
 }
+int arnoldi_part_size(long long n, int m) { return (int)(((n + kDotChunk - 1) / kDotChunk) * (m + 1)); }
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         cudaStream_t s) {
+                         double2* part, cudaStream_t s) {
     // w holds A v_j on entry (the apply ran between k_copy_col and this call)
     const int ldh = m + 1;
     for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice; the second pass sums ||w||^2
-        k_multidot_dyn<<<m + 1, 256, 0, s>>>(V, n, jp, w, n, h);
+        const int nchunk = (int)((n + kDotChunk - 1) / kDotChunk);
+        k_multidot_part<<<dim3(nchunk, m + 1), 256, 0, s>>>(V, n, jp, w, n, part);
+        k_multidot_fin<<<nblk(m + 1, 128), 128, 0, s>>>(part, nchunk, jp, m + 1, h);
         k_cgs_update_dyn<<<nblk(n, 64), 256, 0, s>>>(V, n, jp, h, n, w, H, ldh, pass, pass ? nrm2 : nullptr);
     }
     k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, nrm2, n, V, jp, H, ldh);
     k_advance<<<1, 32, 0, s>>>(jp);
+}
+void launch_store_col(const double2* z, long long n, const int* jp, double2* Z, cudaStream_t s) {
+    k_store_col<<<nblk(n, 256), 256, 0, s>>>(z, n, jp, Z);
 }
 void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, double* nrm2, cudaStream_t s) {
     k_copy_col<<<nblk(n, 256), 256, 0, s>>>(V, n, jp, out, nrm2);

@@ -150,7 +150,11 @@ void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream
 // CGS2 against V[:, 0..j] into the Hessenberg column j, ||w||^2 into *nrm2 (zeroed by
 // launch_copy_col), h_{j+1,j} and V[:, j+1] = w / h_{j+1,j}, then j += 1
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         cudaStream_t s);
+                         double2* part, cudaStream_t s);
+// size (double2 entries) of the partial-sum buffer launch_arnoldi_step needs
+int arnoldi_part_size(long long n, int m);
+// Z[:, *jp] = z
+void launch_store_col(const double2* z, long long n, const int* jp, double2* Z, cudaStream_t s);
 // out = V[:, *jp]; zeroes *nrm2 when given
 void launch_copy_col(const double2* V, long long n, const int* jp, double2* out, double* nrm2, cudaStream_t s);
 // FP64 FMA throughput (TFLOP/s) of the current device; false on a CUDA error

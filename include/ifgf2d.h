@@ -171,6 +171,44 @@ int ifgf2d_eval_offsurface(ifgf2d_ctx* ctx, const double* density, double* out);
  * evaluations */
 int ifgf2d_eval_offsurface_counts(const ifgf2d_ctx* ctx, long long out[4]);
 
+/* The learned right preconditioner (no counterpart in the reference, which runs GMRES
+ * unpreconditioned).  A 1D convolutional network along the boundary parameter: 6 layers of
+ * kernel 7 with circular padding, 64 channels, BF16 weights and activations with FP32
+ * accumulation on the tensor cores.  Per point it reads the residual turned to its canonical
+ * phase and over its RMS (r e^{-i phi} / sigma, sigma = RMS(r), phi = arg(sum r^2) / 2),
+ * curvature / k, the unit tangent and k h (h the quadrature weight), and returns two channels
+ * o; the preconditioner is M(r) = 2 r + sigma e^{i phi} (o_0 + i o_1), and the training target
+ * is o = (e - 2 r) e^{-i phi} / sigma.  A new network's output layer is zero (M = 2 I).  Samples (one residual each, in a curve's patch order) are passed
+ * concatenated: len[s] points each, complex interleaved r / e, geom = 4 doubles per point
+ * (curvature, tangent x, tangent y, h, as ifgf2d_get_geometry_features gives them), k per
+ * sample.  Parameters: per layer the FP32 weights [cout][7][cin] then the bias [cout], with
+ * cin / cout padded to 16, 64, 64, 64, 64, 64 / 64, 64, 64, 64, 64, 16. */
+typedef struct ifgf2d_net ifgf2d_net;
+long long ifgf2d_net_num_params(void);
+int ifgf2d_net_create(unsigned long long seed, ifgf2d_net** out);
+int ifgf2d_net_destroy(ifgf2d_net* net);
+const char* ifgf2d_net_last_error(const ifgf2d_net* net);
+int ifgf2d_net_get_params(ifgf2d_net* net, float* params);
+int ifgf2d_net_set_params(ifgf2d_net* net, const float* params);
+/* mean squared error of o against its target and the gradient w.r.t. the parameters */
+int ifgf2d_net_gradient(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* e, const double* geom,
+                        const double* k, double* loss, float* grad);
+/* one AdamW step (beta 0.9 / 0.999) on that loss */
+int ifgf2d_net_train_step(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* e, const double* geom,
+                          const double* k, float lr, float weight_decay, double* loss);
+/* z = M(r) per sample (complex interleaved), and / or the raw outputs o (2 floats per point) */
+int ifgf2d_net_apply(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* geom, const double* k, double* z,
+                     float* out2);
+/* ifgf2d_solve with the network as right preconditioner: flexible GMRES (z_j = M(v_j)) on the
+ * operator of `mode` inside FP64 iterative refinement (the stop test is the FP64 relative
+ * residual, formed with the FP64 IFGF operator, or the direct one in IFGF2D_APPLY_DIRECT).  A
+ * preconditioned correction that misses its tolerance switches the rest of the solve to plain
+ * GMRES.  *iters counts inner iterations. */
+int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* x, int mode, double tol, int restart,
+                         int max_iters, int* iters, double* est_error);
+/* per point of the context (patch order): curvature, unit tangent x, y, quadrature weight */
+int ifgf2d_get_geometry_features(const ifgf2d_ctx* ctx, double* geom);
+
 /* Device Hankel evaluator (replaces sp_bessel::hankelH1, complex_bessel
  * besselFunctions.h:313-341, for real arguments): out[i] = H_order^(1)(x[i]), order 0 or 1. */
 int ifgf2d_hankel(int order, long long n, const double* x, double* out);

@@ -1,0 +1,106 @@
+"""The learned right preconditioner -- needs a GPU.
+
+Device forward pass and parameter gradients against the CPU torch oracle (oracle/net_oracle.py,
+FP64 autograd with the device's BF16 roundings emulated); training reduces the loss; a fresh
+network is the identity; flexible GMRES with the network reaches the FP64 tolerance, with the
+identity network it takes GMRES's iterations, and a trained network's effect on the
+iteration count is measured against plain GMRES.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _samples(seed, lens=(40, 77, 130), k=60.0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in lens:
+        th = np.linspace(0, 2 * np.pi, n, endpoint=False)
+        r = rng.normal(size=n) + 1j * rng.normal(size=n) + 2 * np.exp(3j * th)
+        # a local complex-linear map plus a little noise: learnable by the network
+        e = 2 * r + 0.4j * (np.roll(r, 1) - np.roll(r, -1)) + 0.02 * (rng.normal(size=n) + 1j * rng.normal(size=n))
+        geom = np.stack([1 + 0.2 * np.cos(2 * th), -np.sin(th), np.cos(th), np.full(n, 2 * np.pi / n)], axis=1)
+        out.append((r, e, geom, k))
+    return out
+
+
+def test_gpu_net_forward_matches_oracle(lib):
+    pytest.importorskip("torch")
+    from oracle import net_oracle as NO
+    from ifgf2d_gb300.learned import PreconditionerNet
+    net = PreconditionerNet(0)
+    assert net.nparam == NO.num_params()
+    p = NO.random_params(3, scale_last=1.0)
+    net.params = p
+    smp = _samples(1)
+    z, o = net.apply(smp)
+    off = 0
+    for (r, e, g, k), zs in zip(smp, z):
+        zr, orf = NO.apply(p, r, g, k, bf16=True)
+        od = o[off:off + len(r)].T
+        off += len(r)
+        assert np.abs(od - orf).max() <= 2e-2 * np.abs(orf).max()
+        assert np.linalg.norm(zs - zr) <= 2e-2 * np.linalg.norm(zr - 2 * r) + 1e-12 * np.linalg.norm(r)
+
+
+def test_gpu_net_gradient_matches_oracle(lib):
+    """device gradients (BF16 operands, FP32 sums) against FP64 autograd of the oracle"""
+    pytest.importorskip("torch")
+    from oracle import net_oracle as NO
+    from ifgf2d_gb300.learned import PreconditionerNet
+    net = PreconditionerNet(0)
+    p = NO.random_params(5, scale_last=1.0)
+    net.params = p
+    smp = _samples(2)
+    loss, g = net.gradient(smp)
+    lo, go = NO.loss_and_grad(p, smp, bf16=True)
+    assert abs(loss - lo) <= 1e-2 * lo
+    assert np.linalg.norm(g - go) <= 5e-2 * np.linalg.norm(go)
+    off = 0   # layer by layer (weights, then bias)
+    for l in range(NO.LAYERS):
+        for n in (NO.cout(l) * NO.TAPS * NO.cin(l), NO.cout(l)):
+            gl, ol = g[off:off + n], go[off:off + n]
+            off += n
+            if np.linalg.norm(ol) > 0:
+                assert np.linalg.norm(gl - ol) <= 1e-1 * np.linalg.norm(ol), l
+
+
+def test_gpu_net_identity_and_training(lib):
+    from ifgf2d_gb300.learned import PreconditionerNet
+    net = PreconditionerNet(0)
+    smp = _samples(4)
+    z, o = net.apply(smp)
+    for (r, *_), zs in zip(smp, z):
+        assert np.array_equal(zs, 2 * r)          # zero output layer: M = 2 I
+    l0 = net.gradient(smp)[0]
+    for _ in range(200):
+        net.train_step(smp, lr=3e-3, weight_decay=0.0)
+    assert net.gradient(smp)[0] < 0.15 * l0
+
+
+def test_gpu_fgmres_identity_is_gmres_and_converges(lib, tmp_path):
+    from ifgf2d_gb300.learned import PreconditionerNet
+    k = 80.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=96, formulation="combined")
+    fm.precomps_and_setup(k, 0)
+    b = -np.exp(1j * k * fm.xs_)
+    net = PreconditionerNet(0)
+    x = fm.solve_precond(net, b, tol=1e-8, restart=300, max_iters=500)
+    it_net = fm.last_solve["iters"]
+    assert fm.last_solve["converged"]
+    assert np.linalg.norm(fm.compute_Ax_acc(x) - b) / np.linalg.norm(b) < 1e-8
+    x0 = fm.gmres(b, tol=1e-8, restart=300, max_iters=500)
+    assert abs(it_net - fm.last_solve["iters"]) <= 2
+    assert np.linalg.norm(x - x0) <= 1e-6 * np.linalg.norm(x0)
+    # mixed inner solves with the network
+    xm = fm.solve_precond(net, b, tol=1e-6, restart=300, max_iters=500, mixed=True)
+    assert fm.last_solve["converged"]
+    assert np.linalg.norm(fm.compute_Ax_acc(xm) - b) / np.linalg.norm(b) < 1e-6
+    # save / load round trip of the weight file
+    path = str(tmp_path / "w.bin")
+    net.params = net.params + 1e-3
+    net.save(path)
+    assert np.array_equal(PreconditionerNet.load(path).params, net.params)

@@ -117,3 +117,29 @@ def test_oracle_combined_field_mie(oracle):
     u = fm.propagate_unacc(r * np.cos(th), r * np.sin(th), x)
     ue = _mie_scattered(k, r, th)
     assert np.abs(u - ue).max() / np.abs(ue).max() < 3e-5
+
+
+def test_net_oracle_gradient_matches_finite_differences():
+    """The CPU oracle of the learned preconditioner: its autograd gradient (FP64) agrees with
+    central differences along random directions (so it can judge the device gradients)."""
+    pytest.importorskip("torch")
+    from oracle import net_oracle as NO
+    rng = np.random.default_rng(0)
+    samples = []
+    for n in (24, 37):
+        r = rng.normal(size=n) + 1j * rng.normal(size=n)
+        e = 2 * r + 0.1 * (rng.normal(size=n) + 1j * rng.normal(size=n))
+        th = np.linspace(0, 2 * np.pi, n, endpoint=False)
+        geom = np.stack([np.ones(n), -np.sin(th), np.cos(th), np.full(n, 2 * np.pi / n)], axis=1)
+        samples.append((r, e, geom, 30.0))
+    p = NO.random_params(1, scale_last=1.0).astype(np.float64)
+    L, g = NO.loss_and_grad(p, samples)
+    assert np.isfinite(L) and g.shape == (NO.num_params(),)
+    for seed in range(3):
+        d = np.random.default_rng(seed).normal(size=p.size)
+        d[g == 0] = 0.0           # padded channels stay zero
+        h = 1e-6
+        Lp, _ = NO.loss_and_grad(p + h * d, samples)
+        Lm, _ = NO.loss_and_grad(p - h * d, samples)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - g @ d) <= 1e-6 * max(1.0, abs(fd)), (fd, g @ d)
