@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-angle batch (kite k=2000, N=32768)")
     ap.add_argument("--no-obstacles", action="store_true", help="skip the 256-obstacle workload")
     ap.add_argument("--no-large", action="store_true", help="skip the kite k=8000, N=131072 solve")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
     ap.add_argument("--batch-k", type=float, default=2000.0, help="wavenumber of the batch workload (profiling)")
     ap.add_argument("--batch-patches", type=int, default=2048, help="patches of the batch workload (profiling)")
     return ap.parse_args()
@@ -310,7 +311,41 @@ def run_ours(args, rank, local_rank, world):
         out["large"] = run_large(G)
     if not args.no_obstacles and not args.no_solve:
         out["obstacles"] = run_obstacles()
+    if not args.no_learned and not args.no_solve:
+        out["learned"] = run_learned(G)
     return out
+
+
+def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
+    """The learned right preconditioner (shipped weights, trained at k in [50, 400]) against the
+    same solves without it: plain FP64 GMRES, FP64 refinement around complex64 GMRES, and
+    the latter with the network inside flexible GMRES.  All to a 1e-6 FP64 true residual."""
+    from ifgf2d_gb300.learned import PreconditionerNet, DEFAULT_WEIGHTS
+    if not os.path.exists(DEFAULT_WEIGHTS):
+        return {"unavailable": "no trained weights shipped"}
+    net = PreconditionerNet.load(DEFAULT_WEIGHTS)
+    res = {"weights": os.path.relpath(DEFAULT_WEIGHTS, ROOT), "training": "k ~ U(50, 400), stars and kites, 10 points per wavelength"}
+    for k, npatch in cases:
+        fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, k, Np=NP, patches_per_curve=npatch, formulation="combined")
+        fm.precomps_and_setup(k, 0)
+        b = -np.exp(1j * k * fm.xs_)
+        row = {"N": fm.total_num_unknowns_}
+        for name, fn in (("plain_fp64", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000)),
+                         ("mixed", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000, mixed=True)),
+                         ("mixed_learned", lambda: fm.solve_precond(net, b, tol=1e-6, restart=300, max_iters=3000, mixed=True))):
+            fn()
+            t0 = time.perf_counter()
+            x = fn()
+            dt = time.perf_counter() - t0
+            tr = float(np.linalg.norm(fm.compute_Ax_acc(x) - b) / np.linalg.norm(b))
+            row[name] = {"seconds": dt, "iters": fm.last_solve["iters"], "converged": fm.last_solve["converged"],
+                         "true_rel_residual_fp64": tr}
+        row["speedup_mixed_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed"]["seconds"]
+        row["speedup_learned_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed_learned"]["seconds"]
+        row["learned_iteration_ratio"] = row["mixed_learned"]["iters"] / max(1, row["mixed"]["iters"])
+        res[f"kite_k{int(k)}"] = row
+        del fm
+    return res
 
 
 def run_large(G, k=8000.0, npatch=8192):

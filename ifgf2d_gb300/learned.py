@@ -218,3 +218,32 @@ def train(net, pairs, steps=2000, batch_points=65536, lr=1e-3, lr_min=1e-5, weig
             if log:
                 log(f"step {step}: train {hist[-1]:.4e} val {vhist[-1][1]:.4e} lr {cur:.2e}")
     return hist, vhist
+
+
+def main(argv=None):
+    """Train the network as shipped: python -m ifgf2d_gb300.learned --out PATH"""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description="harvest (residual, error) pairs from plain GMRES and train the network")
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--problems", type=int, default=160)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+    t0 = time.perf_counter()
+    pairs = harvest_set(training_problems(args.problems, seed=args.seed))
+    rng = np.random.default_rng(args.seed)
+    idx = rng.permutation(len(pairs))
+    nval = max(4, len(pairs) // 10)
+    val, tr = [pairs[i] for i in idx[:nval]], [pairs[i] for i in idx[nval:]]
+    print(f"{len(pairs)} pairs ({sum(len(p[0]) for p in pairs)} points) in {time.perf_counter() - t0:.1f} s", flush=True)
+    net = PreconditionerNet(args.seed)
+    t0 = time.perf_counter()
+    train(net, tr, steps=args.steps, seed=args.seed, val=val, log=lambda m: print(m, flush=True))
+    print(f"trained in {time.perf_counter() - t0:.1f} s", flush=True)
+    net.save(args.out)
+    print("saved", args.out)
+
+
+if __name__ == "__main__":
+    main()
