@@ -119,6 +119,7 @@ def make_ours():
     import ifgf2d_gb300 as G
     fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, K_WAVE, Np=NP, patches_per_curve=NPATCH, formulation="combined")
     fm.precomps_and_setup(K_WAVE, 0)
+    fm.tuning = fm.autotune()   # per-level launch shapes timed on this problem (cached on disk)
     return G, fm
 
 
@@ -288,6 +289,9 @@ def run_ours(args, rank, local_rank, world):
         "dtype": "f64", "data": "synthetic (seeded kite geometry, mt19937(0) density)",
         "config": {"workload": WORKLOAD, "N": N, "k": K_WAVE, "nlevels": nl, "patches": NPATCH, "Np": NP,
                    "Ps": fm.Ps, "Pang": fm.Pang, "parallelism": f"replicas x{world}",
+                   "tuning": {"leaf_chunks_fp64": int(fm.tuning[0]), "leaf_chunks_c64": int(fm.tuning[1]),
+                              "prop_cones_per_block_fp64": [int(v) for v in fm.tuning[2:2 + 24][3:nl]],
+                              "prop_cones_per_block_c64": [int(v) for v in fm.tuning[2 + 24:][3:nl]]},
                    "l2": f"per-step streamed tables {wc['resident_bytes'] / 1e6:.0f} MB > 129 MB L2 (no flush)"},
         "e2e": {"value": world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
                 "ms_per_step": e2e_ms},
@@ -355,6 +359,7 @@ def run_large(G, k=8000.0, npatch=8192):
     t0 = time.perf_counter()
     fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, k, Np=NP, patches_per_curve=npatch, formulation="combined")
     fm.precomps_and_setup(k, 0)
+    fm.autotune()
     torch.cuda.synchronize()
     res = {"workload": f"kite k={k:g}, {npatch} patches x {NP} (N={fm.total_num_unknowns_}), combined field, plane wave",
            "N": fm.total_num_unknowns_, "nlevels": fm.nlevels, "setup_s": time.perf_counter() - t0}

@@ -252,6 +252,51 @@ class ForwardMap:
         a host thread that prepares contexts while the GPU serves others."""
         _check(_lib.load().ifgf2d_prepare(self._h, float(wavenumber), int(nlevels)), self._h)
 
+    def autotune(self, reps=5, cache=True, cache_dir=None):
+        """Pick the launch shapes of the leaf and per-level propagation kernels by timing them on
+        this problem (ifgf2d_autotune).  With cache, the choice is stored on disk, keyed by the GPU
+        and the problem signature, and reused without timing.  Returns the tuning table."""
+        import json
+        import os
+        L = _lib.load()
+        n = int(L.ifgf2d_tuning_size())
+        c = np.zeros(n, dtype=np.int32)
+        cp = c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        key = path = None
+        if cache:
+            try:
+                import torch
+                dev = torch.cuda.get_device_name(torch.cuda.current_device())
+            except Exception:
+                dev = "gpu"
+            wc = self.work_counts()
+            key = f"{dev}|N={self.total_num_unknowns_}|k={self.wavenumber:.17g}|P={self.Ps}x{self.Pang}|" \
+                  f"nl={self.nlevels}|cones={wc['cones']}|prop={wc['prop_evals']}"
+            d = cache_dir or os.environ.get("IFGF2D_TUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "ifgf2d_gb300")
+            path = os.path.join(d, "tuning.json")
+            try:
+                table = json.load(open(path))
+            except Exception:
+                table = {}
+            if key in table and len(table[key]) == n:
+                c[:] = table[key]
+                _check(L.ifgf2d_set_tuning(self._h, cp), self._h)
+                return c.copy()
+        _check(L.ifgf2d_autotune(self._h, int(reps), cp), self._h)
+        if cache:
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                try:
+                    table = json.load(open(path))
+                except Exception:
+                    table = {}
+                table[key] = [int(v) for v in c]
+                with open(path, "w") as f:
+                    json.dump(table, f, indent=0)
+            except OSError:
+                pass
+        return c.copy()
+
     def getSorting(self):
         s = np.empty(self.total_num_unknowns_, dtype=np.int64)
         _check(_lib.load().ifgf2d_get_sorting(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))), self._h)

@@ -32,7 +32,8 @@ EXPORTS = [
     "ifgf2d_apply_direct_noalloc", "ifgf2d_apply_batch", "ifgf2d_apply_batch_device", "ifgf2d_solve_batch",
     "ifgf2d_set_host_threads", "ifgf2d_prepare", "ifgf2d_net_num_params", "ifgf2d_net_create", "ifgf2d_net_destroy",
     "ifgf2d_net_last_error", "ifgf2d_net_get_params", "ifgf2d_net_set_params", "ifgf2d_net_gradient",
-    "ifgf2d_net_train_step", "ifgf2d_net_apply", "ifgf2d_get_geometry_features", "ifgf2d_solve_precond", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
+    "ifgf2d_net_train_step", "ifgf2d_net_apply", "ifgf2d_get_geometry_features", "ifgf2d_solve_precond",
+    "ifgf2d_tuning_size", "ifgf2d_autotune", "ifgf2d_get_tuning", "ifgf2d_set_tuning", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
 ]
 
 
@@ -112,6 +113,9 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_net_train_step.argtypes = [P, ctypes.c_int, IP, D, D, D, D, ctypes.c_float, ctypes.c_float, D]
         L.ifgf2d_net_apply.argtypes = [P, ctypes.c_int, IP, D, D, D, D, F]
         L.ifgf2d_get_geometry_features.argtypes = [P, D]
+        L.ifgf2d_autotune.argtypes = [P, ctypes.c_int, IP]
+        L.ifgf2d_get_tuning.argtypes = [P, IP]
+        L.ifgf2d_set_tuning.argtypes = [P, IP]
         L.ifgf2d_solve_precond.argtypes = [P, P, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int), D]
         L.ifgf2d_eval_offsurface_setup.argtypes = [P, ctypes.c_longlong, D, D]

@@ -365,6 +365,7 @@ extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, i
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     const long long N = ctx->D.N;
+    if (!all_finite(x, 2 * N * nrhs)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the densities");
     const int chunk = std::min(nrhs, kMaxBatch);
     if (!ctx->bw) ctx->bw = new BatchWork;
     BatchWork& W = *ctx->bw;
@@ -386,6 +387,7 @@ extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x,
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     const long long N = ctx->D.N;
+    if (!all_finite(rhs, 2 * N * nrhs)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the right-hand sides");
     bool all_ok = true;
     if (mode == IFGF2D_APPLY_DIRECT) {   // one right-hand side at a time
         for (int r = 0; r < nrhs; ++r) {

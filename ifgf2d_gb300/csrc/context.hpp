@@ -16,6 +16,7 @@
 
 struct BatchWork;
 struct EvalWork;
+constexpr int kTuneLevels = 24;   // levels covered by the launch-shape table
 
 namespace ifgf {
 
@@ -83,6 +84,11 @@ struct ifgf2d_ctx {
     bool device_ready = false, precomputed = false, ifgf_ready = false;
     std::vector<int> h_nsp_ptr, h_nsp, h_srow_ptr, h_srow_col;
     int nlevels = 0;
+    // launch shapes per precision (0 FP64, 1 complex64): leaf-kernel source chunks, and cones
+    // per block of each level's propagation (0 = the most that fit 256 threads); set by
+    // ifgf2d_autotune / ifgf2d_set_tuning
+    int tune_leaf[2] = {5, 5};
+    int tune_prop[2][kTuneLevels] = {};
     // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
     bool prep_ready = false;
     double prep_k = 0.0;
@@ -145,6 +151,14 @@ struct ifgf2d_ctx {
     } while (0)
 
 static inline int fail(ifgf2d_ctx* ctx, int code, const std::string& msg) { ctx->err = msg; return code; }
+
+// true when all n doubles are finite (host buffers at the C ABI: a NaN or Inf density or
+// right-hand side is reported as IFGF2D_ERR_NONFINITE instead of spreading through the solve)
+static inline bool all_finite(const double* v, long long n) {
+    for (long long i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
 
 namespace ifgf {
 // single-vector apply on device vectors in original order: y = A x (ifgf2d_capi.cu)

@@ -412,13 +412,14 @@ static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, con
     const int Dl = ctx->nlevels - 1, P = T.P;
     const TreeLevel& LD = T.L[Dl];
     cudaStream_t s = ctx->stream;
+    const int pr = sizeof(R) == 4 ? 1 : 0;
     launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
-                           ctx->leaf_off.p, leafL, rho, P, coef, s);
+                           ctx->leaf_off.p, leafL, rho, P, coef, s, ctx->tune_leaf[pr]);
     if (ev) cudaEventRecord(ev[0], s);
     for (int l = Dl; l >= 3; --l) {
         const TreeLevel& Lp = T.L[l - 1];
         launch_propagate_t<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pp,
-                              T.Ps, T.Pang, Gsep, coef, s);
+                              T.Ps, T.Pang, Gsep, coef, s, l < kTuneLevels ? ctx->tune_prop[pr][l] : 0);
     }
     if (ev) cudaEventRecord(ev[1], s);
     launch_final_t<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
@@ -505,6 +506,92 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
     return IFGF2D_OK;
 }
 
+// ------------------------------------------------------------------ launch-shape autotuner
+// Times every launch shape of the leaf kernel (source chunks 1, 2, 5, 10) and of each level's
+// propagation (2, 4 or the most cones per block) on this context's own tables, both
+// precisions, and keeps the fastest (median of `reps` CUDA-event timings).  choices (may be
+// NULL) receives the table: leaf FP64, leaf complex64, then kTuneLevels propagation entries
+// per precision.
+static void write_tuning(const ifgf2d_ctx* ctx, int* c) {
+    c[0] = ctx->tune_leaf[0]; c[1] = ctx->tune_leaf[1];
+    for (int p = 0; p < 2; ++p)
+        for (int l = 0; l < kTuneLevels; ++l) c[2 + p * kTuneLevels + l] = ctx->tune_prop[p][l];
+}
+extern "C" int ifgf2d_tuning_size(void) { return 2 + 2 * kTuneLevels; }
+extern "C" int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices) {
+    if (!ctx || !choices) return IFGF2D_ERR_ARG;
+    write_tuning(ctx, choices);
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* c) {
+    if (!ctx || !c) return IFGF2D_ERR_ARG;
+    ctx->tune_leaf[0] = c[0]; ctx->tune_leaf[1] = c[1];
+    for (int p = 0; p < 2; ++p)
+        for (int l = 0; l < kTuneLevels; ++l) ctx->tune_prop[p][l] = c[2 + p * kTuneLevels + l];
+    if (ctx->gw) ctx->gw->drop_graphs();   // the captured iterations hold the old launch shapes
+    return IFGF2D_OK;
+}
+template <typename R>
+static int tune_precision(ifgf2d_ctx* ctx, int reps, const V2<R>* rho, const V2<R>* leafL, const PropE<R>* pp, const R* Gsep,
+                          V2<R>* coef) {
+    const Tree& T = ctx->T;
+    const int Dl = ctx->nlevels - 1, P = T.P, pr = sizeof(R) == 4 ? 1 : 0;
+    const TreeLevel& LD = T.L[Dl];
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    auto time_it = [&](auto&& launch) -> float {
+        std::vector<float> t(reps);
+        launch();   // warm
+        for (int q = 0; q < reps; ++q) {
+            cudaEventRecord(e0, s); launch(); cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&t[q], e0, e1);
+        }
+        std::sort(t.begin(), t.end());
+        return t[reps / 2];
+    };
+    float best = 1e30f; int bestc = 5;
+    for (int ch : {1, 2, 5, 10}) {
+        const float ms = time_it([&] {
+            launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p,
+                                   ctx->leaf_count.p, ctx->leaf_off.p, leafL, rho, P, coef, s, ch);
+        });
+        if (ms < best) { best = ms; bestc = ch; }
+    }
+    ctx->tune_leaf[pr] = bestc;
+    for (int l = Dl; l >= 3 && l < kTuneLevels; --l) {
+        const TreeLevel& Lp = T.L[l - 1];
+        best = 1e30f; int bestp = 0;
+        for (int cpb : {2, 4, 0}) {
+            const float ms = time_it([&] {
+                launch_propagate_t<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pp,
+                                      T.Ps, T.Pang, Gsep, coef, s, cpb);
+            });
+            if (ms < best) { best = ms; bestp = cpb; }
+        }
+        ctx->tune_prop[pr][l] = bestp;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices) {
+    if (!ctx || reps <= 0 || reps > 1000) return IFGF2D_ERR_ARG;
+    if (!ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before autotuning");
+    // realistic intensities in both precisions from one apply of each form on the stored vector
+    CK(cudaMemsetAsync(ctx->vin.p, 0, sizeof(double2) * ctx->D.N, ctx->stream));
+    int rc;
+    if ((rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, IFGF2D_APPLY_IFGF))) return rc;
+    if ((rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, IFGF2D_APPLY_IFGF_MIXED))) return rc;
+    if ((rc = tune_precision<double>(ctx, reps, ctx->rho.p, ctx->leafL.p, ctx->pp.p, ctx->Gsep.p, ctx->coef.p))) return rc;
+    if ((rc = tune_precision<float>(ctx, reps, ctx->rho32.p, ctx->leafL32.p, ctx->pp32.p, ctx->Gsep32.p, ctx->coef32.p))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->gw) ctx->gw->drop_graphs();
+    if (choices) write_tuning(ctx, choices);
+    return IFGF2D_OK;
+}
+
 extern "C" int ifgf2d_measure_fp64_peak(double* tflops) {
     if (!tflops) return IFGF2D_ERR_ARG;
     return launch_fp64_peak(tflops) ? IFGF2D_OK : IFGF2D_ERR_CUDA;
@@ -522,12 +609,14 @@ extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mod
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF apply");
+    if (!all_finite(x, 2 * ctx->D.N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the density");
     const size_t bytes = sizeof(double2) * ctx->D.N;
     CK(cudaMemcpyAsync(ctx->vin.p, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
     int rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, mode);
     if (rc != IFGF2D_OK) return rc;
     CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (!all_finite(y, 2 * ctx->D.N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the result");
     return IFGF2D_OK;
 }
 
@@ -702,6 +791,7 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
         return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
     const long long N = ctx->D.N;
+    if (!all_finite(rhs, 2 * N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the right-hand side");
     cudaStream_t s = ctx->stream;
     if (!ctx->gw) ctx->gw.reset(new GmresWork);
     GmresWork& GW = *ctx->gw;
@@ -774,6 +864,7 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
     if (mode != IFGF2D_APPLY_DIRECT && !ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an IFGF solve");
     const Discretisation& D = ctx->D;
     const long long N = D.N;
+    if (!all_finite(rhs, 2 * N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the right-hand side");
     cudaStream_t s = ctx->stream;
     {
         std::vector<double> geom((size_t)N * 4);

@@ -88,10 +88,11 @@ template <typename R>
 void launch_intensities_t(const double2* x, const double* wq, const long long* perm, int N, V2<R>* rho, cudaStream_t s);
 template <typename R>
 void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
-                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s);
+                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s,
+                         int chunks = 5);
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
-                        int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s);
+                        int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block = 0);
 template <typename R>
 void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
                     const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,

@@ -11,6 +11,7 @@
 //   k_final        near field + every level's cousin interpolants, one warp per target,
 //                  result added to y at the target's original index               BoxTree.h:614-683, 876-937, 1063-1069
 #include "ifgf_device.cuh"
+#include <type_traits>
 
 namespace ifgf {
 
@@ -69,11 +70,11 @@ __global__ void __launch_bounds__(256) k_leaf_apply_t(const int* __restrict__ co
 
 // thread = (parent cone, interpolation node); CPB cones per block.  Gsep = [PS x PS radial
 // map | PA x PA angular map] of the values->coefficients transform, normalisation included.
-template <typename R, int PS, int PA>
+template <typename R, int PS, int PA, int CPB>
 __global__ void __launch_bounds__(256) k_propagate_t(int pbegin, int pend, const long long* __restrict__ pp_ptr,
                                                      const int* __restrict__ pp_nchild, const PropE<R>* __restrict__ pp,
                                                      const R* __restrict__ Gsep, V2<R>* __restrict__ coef) {
-    constexpr int P = PS * PA, CPB = 256 / P;
+    constexpr int P = PS * PA;
     __shared__ V2<R> sv[CPB][P];
     __shared__ V2<R> su[CPB][P];
     __shared__ R sGs[PS * PS], sGa[PA * PA];
@@ -198,25 +199,35 @@ void launch_intensities_t(const double2* x, const double* wq, const long long* p
 }
 template <typename R>
 void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
-                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s) {
+                         const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s,
+                         int chunks) {
     if (ncones <= 0) return;
-    constexpr int CH = 5;
-    const int cpb = 256 / (P * CH);
-    if (cpb >= 1) {
+    // chunks per coefficient (the tuning variant): 1, 2, 5 or 10; a block holds 256 / (P * CH) cones
+    auto go = [&](auto ch_tag) {
+        constexpr int CH = decltype(ch_tag)::value;
+        const int cpb = 256 / (P * CH);
         k_leaf_apply_t<R, CH><<<nblk_a(ncones, cpb), cpb * P * CH, 0, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count,
                                                                           leaf_off, L, rho, P, coef);
-    } else {   // P > 51: one chunk per coefficient
-        k_leaf_apply_t<R, 1><<<nblk_a(ncones, 256 / P), (256 / P) * P, 0, s>>>(cone_box, ncones, cone_base, leaf_start,
-                                                                              leaf_count, leaf_off, L, rho, P, coef);
-    }
+    };
+    if (chunks == 10 && 256 / (P * 10) >= 1) go(std::integral_constant<int, 10>{});
+    else if (chunks == 2 && 256 / (P * 2) >= 1) go(std::integral_constant<int, 2>{});
+    else if (chunks == 1 || 256 / (P * 5) < 1) go(std::integral_constant<int, 1>{});
+    else go(std::integral_constant<int, 5>{});
 }
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps, int Pang,
-                        const R* Gsep, V2<R>* coef, cudaStream_t s) {
+                        const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block) {
     if (pend <= pbegin) return;
+    // cones per block (the tuning variant): 2, 4 or the most that fit 256 threads
     IFGF_DISPATCH_P(Ps, Pang, {
-        constexpr int CPB = 256 / (PS * PA);
-        k_propagate_t<R, PS, PA><<<nblk_a(pend - pbegin, CPB), CPB * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);
+        constexpr int CPBMAX = 256 / (PS * PA);
+        if (cones_per_block == 2 && CPBMAX >= 2)
+            k_propagate_t<R, PS, PA, 2><<<nblk_a(pend - pbegin, 2), 2 * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);
+        else if (cones_per_block == 4 && CPBMAX >= 4)
+            k_propagate_t<R, PS, PA, 4><<<nblk_a(pend - pbegin, 4), 4 * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);
+        else
+            k_propagate_t<R, PS, PA, CPBMAX><<<nblk_a(pend - pbegin, CPBMAX), CPBMAX * PS * PA, 0, s>>>(pbegin, pend, pp_ptr,
+                                                                                                     pp_nchild, pp, Gsep, coef);
     });
 }
 template <typename R>
@@ -235,9 +246,9 @@ void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
 #define IFGF_INSTANTIATE(R)                                                                                          \
     template void launch_intensities_t<R>(const double2*, const double*, const long long*, int, V2<R>*, cudaStream_t); \
     template void launch_leaf_apply_t<R>(const int*, int, int, const int*, const int*, const long long*, const V2<R>*,  \
-                                         const V2<R>*, int, V2<R>*, cudaStream_t);                                    \
+                                         const V2<R>*, int, V2<R>*, cudaStream_t, int);                               \
     template void launch_propagate_t<R>(int, int, const long long*, const int*, const PropE<R>*, int, int, const R*,   \
-                                        V2<R>*, cudaStream_t);                                                         \
+                                        V2<R>*, cudaStream_t, int);                                                    \
     template void launch_final_t<R>(int, const int*, const int*, const int*, const int*, const int*, const int*,       \
                                     const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,       \
                                     const V2<R>*, int, int, const long long*, double2*, cudaStream_t);

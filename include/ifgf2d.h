@@ -226,6 +226,17 @@ int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]);
  * in ms[4]. */
 int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]);
 
+/* Launch-shape autotuner (no counterpart in the reference): times every launch shape of the
+ * leaf-cone kernel (source chunks per coefficient 1, 2, 5, 10) and of each level's propagation
+ * (2, 4 or the most cones per block) on this context's own tables, in both precisions, and
+ * keeps the fastest.  The table has ifgf2d_tuning_size() ints: leaf FP64, leaf complex64, then
+ * per precision one propagation entry per level (0 = the most cones per block).  get / set
+ * read and restore it (e.g. from an on-disk cache); applies use the context's current table. */
+int ifgf2d_tuning_size(void);
+int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices);
+int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices);
+int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* choices);
+
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a dependent-FMA microbenchmark); the
  * roofline denominator of the FP64 kernels (no counterpart in the reference). */
 int ifgf2d_measure_fp64_peak(double* tflops);

@@ -268,3 +268,54 @@ def test_gpu_combined_kite_k500_solve_converges(lib):
     xm = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=1000, mixed=True)
     assert fm.last_solve["converged"]
     assert rel(fm.compute_Ax_acc(xm), b) < 1e-6
+
+
+def test_gpu_nonfinite_inputs_are_reported(lib, oracle):
+    """A NaN or Inf density or right-hand side at the host entry points is reported as
+    IFGF2D_ERR_NONFINITE before any device work, not spread through the operator or GMRES."""
+    k = 40.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
+    fm.precomps_and_setup(k, 0)
+    n = fm.total_num_unknowns_
+    d = oracle.seeded_density(n)
+    bad = d.copy()
+    bad[7] = np.nan
+    with pytest.raises(lib.IFGF2DError, match="NONFINITE"):
+        fm.compute_Ax_acc(bad)
+    bad[7] = np.inf * 1j
+    with pytest.raises(lib.IFGF2DError, match="NONFINITE"):
+        fm.gmres(bad, tol=1e-6)
+    with pytest.raises(lib.IFGF2DError, match="NONFINITE"):
+        fm.gmres_batch(np.stack([d, bad], axis=1), tol=1e-6, mixed=True)
+    with pytest.raises(lib.IFGF2DError, match="NONFINITE"):
+        fm.apply_batch(np.stack([bad, d], axis=1))
+    # the context stays usable
+    assert np.isfinite(fm.compute_Ax_acc(d)).all()
+
+
+def test_gpu_autotune_keeps_results_and_caches(lib, oracle, tmp_path):
+    """Every launch shape the autotuner may pick computes the same apply; the chosen table is
+    stored on disk and restored without timing."""
+    k = 100.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=128, formulation="combined")
+    fm.precomps_and_setup(k, 0)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    y64, y32 = fm.compute_Ax_acc(d), fm.compute_Ax_acc(d, mixed=True)
+    L = lib._lib.load()
+    n = int(L.ifgf2d_tuning_size())
+    import ctypes
+    for leaf, prop in ((1, 2), (2, 4), (10, 0), (5, 2)):
+        c = np.zeros(n, dtype=np.int32)
+        c[:2] = leaf
+        c[2:] = prop
+        assert L.ifgf2d_set_tuning(fm.handle, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
+        assert rel(fm.compute_Ax_acc(d), y64) < 1e-14
+        assert rel(fm.compute_Ax_acc(d, mixed=True), y32) < 1e-6
+    t1 = fm.autotune(cache_dir=str(tmp_path))
+    assert (tmp_path / "tuning.json").exists()
+    assert set(t1[:2]) <= {1, 2, 5, 10}
+    assert rel(fm.compute_Ax_acc(d), y64) < 1e-14
+    t2 = fm.autotune(cache_dir=str(tmp_path))        # from the cache
+    assert np.array_equal(t1, t2)
+    x = fm.gmres(-np.exp(1j * k * fm.xs_), tol=1e-8, restart=300, max_iters=500)   # recaptured iterations
+    assert fm.last_solve["converged"]
