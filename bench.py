@@ -438,7 +438,13 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
     ext = torch.cuda.ExternalStream(fm.stream())
     res = {"workload": f"kite k={k:g}, {npatch} patches x {NP} (N={N}), combined field, {nrhs} plane waves at 2 pi j/{nrhs}",
            "N": N, "nrhs": nrhs, "nlevels": fm.nlevels, "setup_s": setup_s}
-    for mixed in (True, False):
+    # complex64 as configured, complex64 with every kernel on FP32 FMA, with the leaf-cone sums and
+    # with leaf and propagation on the tcgen05 tensor cores (3xTF32); FP64
+    default_tc = fm.batch_tensor_cores
+    for name, mixed, tc in (("mixed", True, default_tc), ("mixed_fma", True, 0), ("mixed_tcgen05_leaf", True, fm.BATCH_TC_LEAF),
+                            ("mixed_tcgen05_leaf_propagation", True, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION),
+                            ("fp64", False, default_tc)):
+        fm.batch_tensor_cores = tc
         reps = 10 if mixed else 2
         for _ in range(2):
             fm.apply_batch_device(xt, yt, nrhs, mixed=mixed)
@@ -449,7 +455,9 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
             fm.apply_batch_device(xt, yt, nrhs, mixed=mixed)
         e1.record(ext)
         torch.cuda.synchronize()
-        res["apply_" + ("mixed" if mixed else "fp64") + "_us_per_rhs"] = e0.elapsed_time(e1) / reps / nrhs * 1e3
+        res["apply_" + name + "_us_per_rhs"] = e0.elapsed_time(e1) / reps / nrhs * 1e3
+    fm.batch_tensor_cores = default_tc
+    res["tcgen05_kernels"] = default_tc
     # one right-hand side through the single-vector path, for the per-RHS comparison
     y1 = torch.empty(N, dtype=torch.complex128, device="cuda")
     for mixed in (True, False):

@@ -252,6 +252,35 @@ class ForwardMap:
         a host thread that prepares contexts while the GPU serves others."""
         _check(_lib.load().ifgf2d_prepare(self._h, float(wavenumber), int(nlevels)), self._h)
 
+    def get_tuning(self):
+        """the context's launch-shape table (ifgf2d_get_tuning)"""
+        L = _lib.load()
+        c = np.zeros(int(L.ifgf2d_tuning_size()), dtype=np.int32)
+        _check(L.ifgf2d_get_tuning(self._h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), self._h)
+        return c
+
+    def set_tuning(self, table):
+        L = _lib.load()
+        c = np.ascontiguousarray(table, dtype=np.int32)
+        if c.size != int(L.ifgf2d_tuning_size()):
+            raise ValueError(f"a tuning table has {int(L.ifgf2d_tuning_size())} entries, got {c.size}")
+        _check(L.ifgf2d_set_tuning(self._h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), self._h)
+
+    BATCH_TC_LEAF = 1
+    BATCH_TC_PROPAGATION = 2
+
+    @property
+    def batch_tensor_cores(self):
+        """bit mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor
+        cores (BATCH_TC_LEAF, BATCH_TC_PROPAGATION; the last entry of the tuning table)"""
+        return int(self.get_tuning()[-1])
+
+    @batch_tensor_cores.setter
+    def batch_tensor_cores(self, mask):
+        c = self.get_tuning()
+        c[-1] = int(mask)
+        self.set_tuning(c)
+
     def autotune(self, reps=5, cache=True, cache_dir=None):
         """Pick the launch shapes of the leaf and per-level propagation kernels by timing them on
         this problem (ifgf2d_autotune).  With cache, the choice is stored on disk, keyed by the GPU

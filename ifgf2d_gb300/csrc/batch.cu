@@ -24,6 +24,10 @@ struct BatchWork {
     DBuf<float2> W32;                          // complex64 copy of the singular-correction weights
     DBuf<float2> xt32;                         // complex64 copy of the interleaved input (mixed form)
     DBuf<double2> xcm, ycm;                    // column-major staging of the host entry points
+    // the tensor-core propagation: its error flag (an mbarrier wait that ran out) and the SM count
+    DBuf<int> t5err;
+    int nsm = 0;
+    DBuf<int4> leaf_items;                     // (leaf box, first cone, end cone, 0) of the tensor-core leaf kernel
     // GMRES
     int m = 0, scap = 0;
     DBuf<double2> V, w, t, h, H, part, Y, hn, b, x, r, d, ones;
@@ -75,6 +79,20 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
             CK(W.rho32.alloc((size_t)N * W.cap)); CK(W.coef32.alloc(ncoef * W.cap)); CK(W.xt32.alloc((size_t)N * W.cap));
         }
         if (!W.pb32.p) CK(W.pb32.upload(sorted_plan<float>(ctx->T)));
+        if (!W.t5err.p) {
+            CK(prop_t5_init_attributes());
+            CK(W.t5err.alloc(1));
+            CK(cudaMemsetAsync(W.t5err.p, 0, sizeof(int), ctx->stream));
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&W.nsm, cudaDevAttrMultiProcessorCount, dev));
+            const TreeLevel& LD = ctx->T.L[ctx->nlevels - 1];
+            std::vector<int4> items;
+            for (size_t b = 0; b + 1 < LD.cone_ptr.size(); ++b)   // at most kLeafT5Cones cones per item
+                for (int c = LD.cone_ptr[b]; c < LD.cone_ptr[b + 1]; c += kLeafT5Cones)
+                    items.push_back(make_int4((int)b, c, std::min(c + kLeafT5Cones, LD.cone_ptr[b + 1]), 0));
+            CK(W.leaf_items.upload(items));
+        }
         if (!W.W32.p) {
             CK(W.W32.alloc(ctx->W.n));
             launch_d2f(ctx->W.p, (long long)ctx->W.n, W.W32.p, ctx->stream);
@@ -93,12 +111,26 @@ void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* le
     const int Dl = ctx->nlevels - 1;
     const TreeLevel& LD = T.L[Dl];
     cudaStream_t s = ctx->stream;
-    launch_leaf_b<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
-                     ctx->leaf_off.p, leafL, rho, T.Ps, T.Pang, B, coef, s);
+    bool leaf_done = false;
+    if constexpr (sizeof(R) == 4) {
+        BatchWork& W = *ctx->bw;
+        if (ctx->tune_batch_tc & kBatchTcLeaf)
+            leaf_done = launch_leaf_t5(W.leaf_items.p, (int)W.leaf_items.n, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p,
+                                       leafL, rho, T.Ps, T.Pang, B, coef + (long long)LD.cone_base * T.P * B, W.t5err.p, W.nsm, s);
+    }
+    if (!leaf_done)
+        launch_leaf_b<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                         ctx->leaf_off.p, leafL, rho, T.Ps, T.Pang, B, coef, s);
     for (int l = Dl; l >= 3; --l) {
         const TreeLevel& Lp = T.L[l - 1];
-        launch_prop_b<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps,
-                         T.Pang, Gsep, B, coef, s);
+        const int p0 = Lp.cone_base, p1 = Lp.cone_base + (int)Lp.cone_nonrel.size();
+        if constexpr (sizeof(R) == 4) {
+            BatchWork& W = *ctx->bw;
+            if ((ctx->tune_batch_tc & kBatchTcProp) && launch_prop_t5(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef,
+                                                     W.t5err.p, W.nsm, s))
+                continue;
+        }
+        launch_prop_b<R>(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, s);
     }
     launch_final_b<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
                       ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p,
@@ -122,6 +154,16 @@ int apply_il(ifgf2d_ctx* ctx, const double2* xt, double2* yt, int B, int mode) {
         far_b<double>(ctx, W.rho64.p, ctx->near.p, ctx->leafL.p, W.pb64.p, ctx->ip.p, ctx->Gsep.p, W.coef64.p, B, yt);
     CK(cudaGetLastError());
     return IFGF2D_OK;
+}
+
+// after a synchronisation: did a tensor-core propagation give up on a wait?
+int check_t5(ifgf2d_ctx* ctx) {
+    if (!ctx->bw || !ctx->bw->t5err.p) return IFGF2D_OK;
+    int v = 0;
+    CK(cudaMemcpy(&v, ctx->bw->t5err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!v) return IFGF2D_OK;
+    CK(cudaMemset(ctx->bw->t5err.p, 0, sizeof(int)));
+    return fail(ctx, IFGF2D_ERR_CUDA, "tensor-core propagation: a tensor-memory completion wait ran out");
 }
 
 int check_mode(ifgf2d_ctx* ctx, int mode) {
@@ -378,7 +420,7 @@ extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, i
         CK(cudaMemcpyAsync(y + 2 * (size_t)N * r0, W.ycm.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    return IFGF2D_OK;
+    return check_t5(ctx);
 }
 
 extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
@@ -418,6 +460,7 @@ extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x,
         launch_deinterleave(W.x.p, N, B, W.ycm.p, s);
         CK(cudaMemcpyAsync(x + 2 * (size_t)N * r0, W.ycm.p, bytes, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        if ((rc = check_t5(ctx))) return rc;
         for (int r = 0; r < B; ++r) {
             if (iters) iters[r0 + r] = it[r];
             if (est_error) est_error[r0 + r] = e[r];

@@ -17,6 +17,8 @@
 struct BatchWork;
 struct EvalWork;
 constexpr int kTuneLevels = 24;   // levels covered by the launch-shape table
+constexpr int kBatchTcLeaf = 1;   // leaf-cone sums (k_leaf_t5)
+constexpr int kBatchTcProp = 2;   // propagation (k_prop_t5)
 
 namespace ifgf {
 
@@ -89,6 +91,8 @@ struct ifgf2d_ctx {
     // ifgf2d_autotune / ifgf2d_set_tuning
     int tune_leaf[2] = {5, 5};
     int tune_prop[2][kTuneLevels] = {};
+    // batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (bit mask, else FP32 FMA)
+    int tune_batch_tc = 0;
     // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
     bool prep_ready = false;
     double prep_k = 0.0;

@@ -511,13 +511,15 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
 // propagation (2, 4 or the most cones per block) on this context's own tables, both
 // precisions, and keeps the fastest (median of `reps` CUDA-event timings).  choices (may be
 // NULL) receives the table: leaf FP64, leaf complex64, then kTuneLevels propagation entries
-// per precision.
+// per precision, then the batched complex64 kernels on the tcgen05 tensor cores (bit 0 leaf
+// cones, bit 1 propagation; FP32 FMA otherwise).
 static void write_tuning(const ifgf2d_ctx* ctx, int* c) {
     c[0] = ctx->tune_leaf[0]; c[1] = ctx->tune_leaf[1];
     for (int p = 0; p < 2; ++p)
         for (int l = 0; l < kTuneLevels; ++l) c[2 + p * kTuneLevels + l] = ctx->tune_prop[p][l];
+    c[2 + 2 * kTuneLevels] = ctx->tune_batch_tc;
 }
-extern "C" int ifgf2d_tuning_size(void) { return 2 + 2 * kTuneLevels; }
+extern "C" int ifgf2d_tuning_size(void) { return 3 + 2 * kTuneLevels; }
 extern "C" int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices) {
     if (!ctx || !choices) return IFGF2D_ERR_ARG;
     write_tuning(ctx, choices);
@@ -528,6 +530,7 @@ extern "C" int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* c) {
     ctx->tune_leaf[0] = c[0]; ctx->tune_leaf[1] = c[1];
     for (int p = 0; p < 2; ++p)
         for (int l = 0; l < kTuneLevels; ++l) ctx->tune_prop[p][l] = c[2 + p * kTuneLevels + l];
+    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp);
     if (ctx->gw) ctx->gw->drop_graphs();   // the captured iterations hold the old launch shapes
     return IFGF2D_OK;
 }

@@ -123,6 +123,19 @@ void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* le
 template <typename R>
 void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
                    const R* Gsep, int B, V2<R>* coef, cudaStream_t s);
+// the complex64 propagation on the tcgen05 tensor cores in 3xTF32 (batch_tcgen05.cu); false when
+// the shape is not supported (Ps x Pang other than 5 x 5, more than 64 right-hand sides) and
+// nothing was launched.  *err is set when a completion wait runs out.  The kernel's shared-memory
+// attribute must be set once per device (prop_t5_init_attributes), outside stream capture.
+bool launch_prop_t5(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
+                    const float* Gsep, int B, float2* coef, int* err, int nsm, cudaStream_t s);
+// the complex64 leaf-cone sums on the tcgen05 tensor cores in 3xTF32: items[i] = (leaf box, first
+// cone, end cone, 0), at most kLeafT5Cones cones, indices local to the leaf level; coef offset to
+// the level's first cone
+constexpr int kLeafT5Cones = 5;
+bool launch_leaf_t5(const int4* items, int nitems, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
+                    const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, cudaStream_t s);
+cudaError_t prop_t5_init_attributes();
 template <typename R>
 void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
                     const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,

@@ -230,8 +230,12 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
  * leaf-cone kernel (source chunks per coefficient 1, 2, 5, 10) and of each level's propagation
  * (2, 4 or the most cones per block) on this context's own tables, in both precisions, and
  * keeps the fastest.  The table has ifgf2d_tuning_size() ints: leaf FP64, leaf complex64, then
- * per precision one propagation entry per level (0 = the most cones per block).  get / set
- * read and restore it (e.g. from an on-disk cache); applies use the context's current table. */
+ * per precision one propagation entry per level (0 = the most cones per block), then a bit
+ * mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor cores
+ * (IFGF2D_BATCH_TC_LEAF, IFGF2D_BATCH_TC_PROPAGATION; FP32 FMA otherwise).  get / set read and
+ * restore it (e.g. from an on-disk cache); applies use the context's current table. */
+#define IFGF2D_BATCH_TC_LEAF 1
+#define IFGF2D_BATCH_TC_PROPAGATION 2
 int ifgf2d_tuning_size(void);
 int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices);
 int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices);

@@ -53,6 +53,29 @@ def test_gpu_batch_apply_matches_single(lib, oracle, form, nrhs):
     assert rel(Y[:, c], om.compute_Ax_acc(X[:, c])) < tol
 
 
+@pytest.mark.parametrize("k,npatch,nrhs", [(100.0, 128, 64), (300.0, 384, 13), (40.0, 64, 1)])
+def test_gpu_batch_tensor_core_kernels(lib, oracle, k, npatch, nrhs):
+    """The batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (leaf cones,
+    propagation, both) against the FP32 FMA kernels and the FP64 apply: every complex64 form
+    within 2e-6 of FP64 and within 1.5e-6 of the FMA form (FP32-level agreement; a single TF32
+    product would give ~1e-3); repeated applies are bit-identical."""
+    fm = _kite(lib, k, npatch)
+    n = fm.total_num_unknowns_
+    X = _densities(oracle, n, nrhs)
+    Y = fm.apply_batch(X)
+    fm.batch_tensor_cores = 0
+    Yf = fm.apply_batch(X, mixed=True)
+    for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION):
+        fm.batch_tensor_cores = mask
+        assert fm.batch_tensor_cores == mask
+        Yt = fm.apply_batch(X, mixed=True)
+        assert np.array_equal(fm.apply_batch(X, mixed=True), Yt)
+        for r in range(nrhs):
+            assert rel(Yt[:, r], Y[:, r]) < 2e-6, (mask, r)
+            assert rel(Yf[:, r], Y[:, r]) < 2e-6, (mask, r)
+            assert rel(Yt[:, r], Yf[:, r]) < 1.5e-6, (mask, r)
+
+
 def test_gpu_batch_apply_direct_and_device(lib, oracle):
     import torch
     k = 40.0
