@@ -114,9 +114,10 @@ void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* le
     bool leaf_done = false;
     if constexpr (sizeof(R) == 4) {
         BatchWork& W = *ctx->bw;
-        if (ctx->tune_batch_tc & kBatchTcLeaf)
+        if (ctx->tune_batch_tc & (kBatchTcLeaf | kBatchTcLeaf6))
             leaf_done = launch_leaf_t5(W.leaf_items.p, (int)W.leaf_items.n, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p,
-                                       leafL, rho, T.Ps, T.Pang, B, coef + (long long)LD.cone_base * T.P * B, W.t5err.p, W.nsm, s);
+                                       leafL, rho, T.Ps, T.Pang, B, coef + (long long)LD.cone_base * T.P * B, W.t5err.p, W.nsm,
+                                       (ctx->tune_batch_tc & kBatchTcLeaf6) ? 3 : 2, s);
     }
     if (!leaf_done)
         launch_leaf_b<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,

@@ -80,12 +80,6 @@ __device__ __forceinline__ void st4_split(unsigned char* sm, int off_hi, int off
     st4(sm, off_lo + off, sign * al, sign * bl, sign * cl, sign * dl);
 }
 
-// store pre-split values: four hi and four lo, each times sign
-__device__ __forceinline__ void st4_pair(unsigned char* sm, int off_hi, int off_lo, uint32_t off, const float* h, const float* l,
-                                         float sign) {
-    st4(sm, off_hi + off, sign * h[0], sign * h[1], sign * h[2], sign * h[3]);
-    st4(sm, off_lo + off, sign * l[0], sign * l[1], sign * l[2], sign * l[3]);
-}
 // one thread waits for the MMAs (the others wait at the barrier that follows); true when they completed
 __device__ __forceinline__ bool wait_one(int tid, uint32_t bar, uint32_t parity) {
     return tid == 0 ? tc5::mbar_wait(bar, parity, kT5WaitCycles) : true;
@@ -291,10 +285,10 @@ constexpr int kL5Src = 16;                   // sources per chunk: K = 32
 constexpr int kL5K = 2 * kL5Src;
 constexpr int kL5Cones = 5;                  // cones per work item (125 columns of N = 128)
 constexpr int kL5N = 128;
-constexpr int L5_T = 128 * kL5K * 4;         // 16384: one 128-row tile, hi or lo
-constexpr int L5_OFF_AH = 0, L5_OFF_AL = L5_T, L5_OFF_BH = 2 * L5_T, L5_OFF_BL = 3 * L5_T;
-constexpr int L5_OFF_BAR = 4 * L5_T;
-constexpr int L5_SMEM = L5_OFF_BAR + 16;
+constexpr int L5_T = 128 * kL5K * 4;         // 16384: one 128-row tile of one split term
+// NS split terms per operand: A tiles at t L5_T, B tiles at (NS + t) L5_T, the mbarrier after them
+__host__ __device__ constexpr int l5_off_bar(int NS) { return 2 * NS * L5_T; }
+__host__ __device__ constexpr int l5_smem(int NS) { return l5_off_bar(NS) + 16; }
 // per thread and source chunk: one density item (right-hand side, 4 sources) and two table items
 // (row = (cone, m), 4 sources); the 125 x 4 table items of a chunk take 500 of the 512 slots
 constexpr int kL5BItems = 2;
@@ -329,32 +323,66 @@ __device__ __forceinline__ void leaf_load(LeafChunk<P>& t, int tid, int sb, int 
         }
     }
 }
-template <int P>
+// x = sum of NS TF32 terms, each the rounding of what the previous ones left
+template <int NS>
+__device__ __forceinline__ void split_n(float x, float* t) {
+#pragma unroll
+    for (int i = 0; i < NS - 1; ++i) { t[i] = tc5::tf32_hi(x); x -= t[i]; }
+    t[NS - 1] = tc5::tf32_hi(x);
+}
+// four values (each split in NS terms, term i of value j at v[j][i]) to tile `base + i L5_T`
+template <int NS>
+__device__ __forceinline__ void st4_terms(unsigned char* sm, int base, uint32_t off, const float (*v)[NS], float sign) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) st4(sm, base + i * L5_T + off, sign * v[0][i], sign * v[1][i], sign * v[2][i], sign * v[3][i]);
+}
+template <int P, int NS>
 __device__ __forceinline__ void leaf_store(const LeafChunk<P>& t, int tid, unsigned char* sm) {
+    constexpr int offA = 0, offB = NS * L5_T;
     {
         const int rr = tid & 63, k0 = 4 * (tid >> 6);
-        float reh[4], rel[4], imh[4], iml[4];
+        float re[4][NS], im[4][NS];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) { tc5::split3(t.a[j].x, reh[j], rel[j]); tc5::split3(t.a[j].y, imh[j], iml[j]); }
+        for (int j = 0; j < 4; ++j) { split_n<NS>(t.a[j].x, re[j]); split_n<NS>(t.a[j].y, im[j]); }
         // rows 2 r = [Re rho | -Im rho], 2 r + 1 = [Im rho | Re rho]
-        st4_pair(sm, L5_OFF_AH, L5_OFF_AL, tc5::kmajor_off(128, 2 * rr, k0), reh, rel, 1.f);
-        st4_pair(sm, L5_OFF_AH, L5_OFF_AL, tc5::kmajor_off(128, 2 * rr, kL5Src + k0), imh, iml, -1.f);
-        st4_pair(sm, L5_OFF_AH, L5_OFF_AL, tc5::kmajor_off(128, 2 * rr + 1, k0), imh, iml, 1.f);
-        st4_pair(sm, L5_OFF_AH, L5_OFF_AL, tc5::kmajor_off(128, 2 * rr + 1, kL5Src + k0), reh, rel, 1.f);
+        st4_terms<NS>(sm, offA, tc5::kmajor_off(128, 2 * rr, k0), re, 1.f);
+        st4_terms<NS>(sm, offA, tc5::kmajor_off(128, 2 * rr, kL5Src + k0), im, -1.f);
+        st4_terms<NS>(sm, offA, tc5::kmajor_off(128, 2 * rr + 1, k0), im, 1.f);
+        st4_terms<NS>(sm, offA, tc5::kmajor_off(128, 2 * rr + 1, kL5Src + k0), re, 1.f);
     }
 #pragma unroll
     for (int q = 0; q < kL5BItems; ++q) {
         const int i = tid + q * kL5Threads;
         if (i >= kL5Cones * P * 4) continue;
         const int row = i % (kL5Cones * P), k0 = 4 * (i / (kL5Cones * P));
-        const float2* v = t.b[q];
+        float re[4][NS], im[4][NS];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { split_n<NS>(t.b[q][j].x, re[j]); split_n<NS>(t.b[q][j].y, im[j]); }
         // row (cone, m) = [Re L[src][m] | Im L[src][m]]
-        st4_split(sm, L5_OFF_BH, L5_OFF_BL, tc5::kmajor_off(kL5N, row, k0), v[0].x, v[1].x, v[2].x, v[3].x, 1.f);
-        st4_split(sm, L5_OFF_BH, L5_OFF_BL, tc5::kmajor_off(kL5N, row, kL5Src + k0), v[0].y, v[1].y, v[2].y, v[3].y, 1.f);
+        st4_terms<NS>(sm, offB, tc5::kmajor_off(kL5N, row, k0), re, 1.f);
+        st4_terms<NS>(sm, offB, tc5::kmajor_off(kL5N, row, kL5Src + k0), im, 1.f);
     }
 }
+// D (+)= sum over term pairs (i, j) with i + j < NS + 1 (0-based i + j <= NS - 1) of A_i B_j, the
+// smallest products first: 3 MMAs per K step for two terms (3xTF32), 6 for three
+template <int NS>
+__device__ __forceinline__ void issue_split(uint32_t d, uint32_t a0, uint32_t b0, uint32_t tile, uint32_t lbo, int ksteps,
+                                            uint32_t idesc, bool accumulate) {
+    uint32_t acc = accumulate ? 1u : 0u;
+#pragma unroll
+    for (int sum = NS - 1; sum >= 0; --sum)
+#pragma unroll
+        for (int i = 0; i <= sum; ++i) {
+            const int j = sum - i;
+            for (int ks = 0; ks < ksteps; ++ks) {
+                const uint32_t o = ks * 2 * lbo;
+                tc5::mma_tf32(d, tc5::smem_desc(a0 + i * tile + o, lbo, 128), tc5::smem_desc(b0 + j * tile + o, lbo, 128), idesc, acc);
+                acc = 1u;
+            }
+        }
+}
 
-template <int P>
+template <int P, int NS>
 __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restrict__ items, int nitems, const int* __restrict__ leaf_start,
                                                         const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
                                                         const float2* __restrict__ L, const float2* __restrict__ rho, int B,
@@ -362,15 +390,15 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
     static_assert(kL5Cones * P <= kL5N && kL5Cones * P * 4 <= kL5BItems * kL5Threads, "a work item's table must fit");
     extern __shared__ __align__(1024) unsigned char sm[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t bar = tc5::smem_u32(sm + L5_OFF_BAR), tslot = tc5::smem_u32(sm + L5_OFF_BAR + 8);
-    const uint32_t sAH = tc5::smem_u32(sm + L5_OFF_AH), sAL = tc5::smem_u32(sm + L5_OFF_AL);
-    const uint32_t sBH = tc5::smem_u32(sm + L5_OFF_BH), sBL = tc5::smem_u32(sm + L5_OFF_BL);
+    constexpr int OFF_BAR5 = l5_off_bar(NS);
+    const uint32_t bar = tc5::smem_u32(sm + OFF_BAR5), tslot = tc5::smem_u32(sm + OFF_BAR5 + 8);
+    const uint32_t sA = tc5::smem_u32(sm), sB = tc5::smem_u32(sm + NS * L5_T);
     if (tid == 0) tc5::mbar_init(bar, 1);
     if (warp == 0) tc5::tmem_alloc(tslot, kL5N);
     tc5::fence_before_sync();
     __syncthreads();
     tc5::fence_after_sync();
-    const uint32_t tmem = *(volatile uint32_t*)(sm + L5_OFF_BAR + 8);
+    const uint32_t tmem = *(volatile uint32_t*)(sm + OFF_BAR5 + 8);
     // read-back: warp w holds accumulator rows 32 (w % 4) .. + 31, columns 64 (w / 4) .. + 63
     const uint32_t tread = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64 * (warp >> 2);
     const int row = 32 * (warp & 3) + (tid & 31), r = row >> 1, part = row & 1, col0 = 64 * (warp >> 2);
@@ -388,13 +416,13 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
             bool done = true;
             if (ch > 0) { done = wait_one(tid, bar, phase & 1u); ++phase; }
             if (!__syncthreads_and(done)) { ok = false; break; }   // the previous chunk's MMAs have read the tiles
-            leaf_store<P>(t, tid, sm);
+            leaf_store<P, NS>(t, tid, sm);
             tc5::fence_async_smem();
             tc5::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc5::fence_after_sync();
-                issue_3xtf32(tmem, sAH, sAL, kLbo, sBH, sBL, kLbo, kL5K / 8, idesc, ch > 0);
+                issue_split<NS>(tmem, sA, sB, L5_T, kLbo, kL5K / 8, idesc, ch > 0);
                 tc5::commit(bar);
             }
             if (ch + 1 < nch) leaf_load<P>(t, tid, (ch + 1) * kL5Src, n, s0, item.y, item.z, leaf_off, L, rho, B);
@@ -436,16 +464,21 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
 
 cudaError_t prop_t5_init_attributes() {
     cudaError_t e = cudaFuncSetAttribute(k_prop_t5<5, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, T5_SMEM);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_leaf_t5<25>, cudaFuncAttributeMaxDynamicSharedMemorySize, L5_SMEM);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_leaf_t5<25, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, l5_smem(2));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_leaf_t5<25, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, l5_smem(3));
     return e;
 }
 
 bool launch_leaf_t5(const int4* items, int nitems, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
-                    const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, cudaStream_t s) {
-    if (Ps != 5 || Pang != 5 || B > kT5MaxB || B <= 0) return false;
+                    const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, int terms,
+                    cudaStream_t s) {
+    if (Ps != 5 || Pang != 5 || B > kT5MaxB || B <= 0 || (terms != 2 && terms != 3)) return false;
     if (nitems <= 0) return true;
     const int grid = std::min(nitems, 2 * std::max(nsm, 1));
-    k_leaf_t5<25><<<grid, kL5Threads, L5_SMEM, s>>>(items, nitems, leaf_start, leaf_count, leaf_off, L, rho, B, coef, err);
+    if (terms == 3)
+        k_leaf_t5<25, 3><<<grid, kL5Threads, l5_smem(3), s>>>(items, nitems, leaf_start, leaf_count, leaf_off, L, rho, B, coef, err);
+    else
+        k_leaf_t5<25, 2><<<grid, kL5Threads, l5_smem(2), s>>>(items, nitems, leaf_start, leaf_count, leaf_off, L, rho, B, coef, err);
     return true;
 }
 

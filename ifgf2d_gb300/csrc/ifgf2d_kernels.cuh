@@ -133,8 +133,11 @@ bool launch_prop_t5(int pbegin, int pend, const long long* pp_ptr, const int* pp
 // cone, end cone, 0), at most kLeafT5Cones cones, indices local to the leaf level; coef offset to
 // the level's first cone
 constexpr int kLeafT5Cones = 5;
+// terms = 2: 3xTF32 (each operand hi + lo, 3 products); terms = 3: three TF32 terms per operand
+// and 6 products, FP32-level operands
 bool launch_leaf_t5(const int4* items, int nitems, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
-                    const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, cudaStream_t s);
+                    const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, int terms,
+                    cudaStream_t s);
 cudaError_t prop_t5_init_attributes();
 template <typename R>
 void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,

@@ -234,8 +234,9 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
  * mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor cores
  * (IFGF2D_BATCH_TC_LEAF, IFGF2D_BATCH_TC_PROPAGATION; FP32 FMA otherwise).  get / set read and
  * restore it (e.g. from an on-disk cache); applies use the context's current table. */
-#define IFGF2D_BATCH_TC_LEAF 1
-#define IFGF2D_BATCH_TC_PROPAGATION 2
+#define IFGF2D_BATCH_TC_LEAF 1          /* leaf-cone sums, 3xTF32 (two TF32 terms per operand) */
+#define IFGF2D_BATCH_TC_PROPAGATION 2   /* propagation, 3xTF32 */
+#define IFGF2D_BATCH_TC_LEAF_FP32 4     /* leaf-cone sums, three TF32 terms per operand (6 products) */
 int ifgf2d_tuning_size(void);
 int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices);
 int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices);

@@ -55,17 +55,18 @@ def test_gpu_batch_apply_matches_single(lib, oracle, form, nrhs):
 
 @pytest.mark.parametrize("k,npatch,nrhs", [(100.0, 128, 64), (300.0, 384, 13), (40.0, 64, 1)])
 def test_gpu_batch_tensor_core_kernels(lib, oracle, k, npatch, nrhs):
-    """The batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (leaf cones,
-    propagation, both) against the FP32 FMA kernels and the FP64 apply: every complex64 form
-    within 2e-6 of FP64 and within 1.5e-6 of the FMA form (FP32-level agreement; a single TF32
-    product would give ~1e-3); repeated applies are bit-identical."""
+    """The batched complex64 kernels on the tcgen05 tensor cores (leaf cones in 3xTF32 and with
+    three TF32 terms per operand, propagation in 3xTF32, leaf and propagation) against the FP32
+    FMA kernels and the FP64 apply: every complex64 form within 2e-6 of FP64 and within 1.5e-6 of
+    the FMA form (FP32-level agreement; a single TF32 product would give ~1e-3); repeated
+    applies are bit-identical."""
     fm = _kite(lib, k, npatch)
     n = fm.total_num_unknowns_
     X = _densities(oracle, n, nrhs)
     Y = fm.apply_batch(X)
     fm.batch_tensor_cores = 0
     Yf = fm.apply_batch(X, mixed=True)
-    for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION):
+    for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_LEAF_FP32, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION):
         fm.batch_tensor_cores = mask
         assert fm.batch_tensor_cores == mask
         Yt = fm.apply_batch(X, mixed=True)
