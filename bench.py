@@ -438,10 +438,14 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
     ext = torch.cuda.ExternalStream(fm.stream())
     res = {"workload": f"kite k={k:g}, {npatch} patches x {NP} (N={N}), combined field, {nrhs} plane waves at 2 pi j/{nrhs}",
            "N": N, "nrhs": nrhs, "nlevels": fm.nlevels, "setup_s": setup_s}
-    # complex64 as configured, complex64 with every kernel on FP32 FMA, with the leaf-cone sums and
-    # with leaf and propagation on the tcgen05 tensor cores (3xTF32); FP64
+    # complex64 as configured; with every kernel on FP32 FMA; with the FMA propagation fed by TMA
+    # bulk copies; with the leaf-cone sums, and leaf and propagation, on the tcgen05 tensor cores
+    # (3xTF32); FP64
     default_tc = fm.batch_tensor_cores
-    for name, mixed, tc in (("mixed", True, default_tc), ("mixed_fma", True, 0), ("mixed_tcgen05_leaf", True, fm.BATCH_TC_LEAF),
+    for name, mixed, tc in (("mixed", True, default_tc), ("mixed_fma", True, 0),
+                            ("mixed_tma_propagation", True, fm.BATCH_BULK_PROPAGATION),
+                            ("mixed_tcgen05_leaf_tma_propagation", True, fm.BATCH_TC_LEAF | fm.BATCH_BULK_PROPAGATION),
+                            ("mixed_tcgen05_leaf", True, fm.BATCH_TC_LEAF),
                             ("mixed_tcgen05_leaf_propagation", True, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION),
                             ("fp64", False, default_tc)):
         fm.batch_tensor_cores = tc

@@ -269,6 +269,7 @@ class ForwardMap:
     BATCH_TC_LEAF = 1
     BATCH_TC_PROPAGATION = 2
     BATCH_TC_LEAF_FP32 = 4
+    BATCH_BULK_PROPAGATION = 8
 
     @property
     def batch_tensor_cores(self):

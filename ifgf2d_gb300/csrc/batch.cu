@@ -130,6 +130,9 @@ void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* le
             if ((ctx->tune_batch_tc & kBatchTcProp) && launch_prop_t5(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef,
                                                      W.t5err.p, W.nsm, s))
                 continue;
+            if ((ctx->tune_batch_tc & kBatchBulkProp) &&
+                launch_prop_bk(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, W.t5err.p, s))
+                continue;
         }
         launch_prop_b<R>(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, s);
     }

@@ -20,6 +20,7 @@ constexpr int kTuneLevels = 24;   // levels covered by the launch-shape table
 constexpr int kBatchTcLeaf = 1;   // leaf-cone sums (k_leaf_t5)
 constexpr int kBatchTcProp = 2;   // propagation (k_prop_t5)
 constexpr int kBatchTcLeaf6 = 4;  // leaf-cone sums with three TF32 terms per operand (6 products)
+constexpr int kBatchBulkProp = 8; // FP32 FMA propagation with TMA-staged child coefficients (k_prop_bk)
 
 namespace ifgf {
 

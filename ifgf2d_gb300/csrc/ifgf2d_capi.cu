@@ -513,7 +513,7 @@ extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, i
 // NULL) receives the table: leaf FP64, leaf complex64, then kTuneLevels propagation entries
 // per precision, then the batched complex64 kernels on the tcgen05 tensor cores (bit 0 leaf
 // cones in 3xTF32, bit 1 propagation, bit 2 leaf cones with three TF32 terms per operand; FP32
-// FMA otherwise).
+// FMA otherwise) and bit 3, the FMA propagation with TMA-staged child coefficients.
 static void write_tuning(const ifgf2d_ctx* ctx, int* c) {
     c[0] = ctx->tune_leaf[0]; c[1] = ctx->tune_leaf[1];
     for (int p = 0; p < 2; ++p)
@@ -531,7 +531,7 @@ extern "C" int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* c) {
     ctx->tune_leaf[0] = c[0]; ctx->tune_leaf[1] = c[1];
     for (int p = 0; p < 2; ++p)
         for (int l = 0; l < kTuneLevels; ++l) ctx->tune_prop[p][l] = c[2 + p * kTuneLevels + l];
-    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6);
+    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6 | kBatchBulkProp);
     if (ctx->gw) ctx->gw->drop_graphs();   // the captured iterations hold the old launch shapes
     return IFGF2D_OK;
 }

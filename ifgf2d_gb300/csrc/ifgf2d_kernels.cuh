@@ -139,6 +139,11 @@ bool launch_leaf_t5(const int4* items, int nitems, const int* leaf_start, const 
                     const float2* L, const float2* rho, int Ps, int Pang, int B, float2* coef, int* err, int nsm, int terms,
                     cudaStream_t s);
 cudaError_t prop_t5_init_attributes();
+// the complex64 FMA propagation with each child cone's coefficient block staged in shared memory
+// by a TMA bulk copy one group ahead; false when the shape is not supported (Ps x Pang other
+// than 5 x 5, B odd or above 64) and nothing was launched
+bool launch_prop_bk(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
+                    const float* Gsep, int B, float2* coef, int* err, cudaStream_t s);
 template <typename R>
 void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
                     const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,

@@ -18,6 +18,7 @@
 //
 // plus the batched GMRES vector kernels (per-RHS dot products, CGS updates, scaling).
 #include "ifgf_device.cuh"
+#include "tcgen05.cuh"
 
 namespace ifgf {
 
@@ -299,6 +300,114 @@ __global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const
     }
 }
 
+// ------------------------------------------------------------------ propagation, TMA-staged
+// k_prop_b (complex64) with its loads taken off the FMA loop: the parent's terms are staged in
+// shared memory at the start, and the child cones' coefficient blocks by the tensor memory
+// accelerator.  When the block starts a group of terms, thread 0 issues a bulk copy
+// (cp.async.bulk, completion counted on an mbarrier) of the NEXT group's 25 x B block into
+// shared memory, so it has landed by the time the FMA loop needs it.  Two warps share one parent
+// cone and one staging buffer, 32 right-hand sides each (half the shared memory per warp of a
+// warp per cone, twice the resident warps).  B must be even (the block is a multiple of 16
+// bytes).  Waits are bounded; one that runs out sets *err and the block stops.
+constexpr int kPropBkWarps = 2;
+template <int PS, int PA>
+__global__ void __launch_bounds__(32 * kPropBkWarps) k_prop_bk(int pbegin, int pend, const long long* __restrict__ pp_ptr,
+                                                               const int* __restrict__ pp_nchild, const PropB<float>* __restrict__ pb,
+                                                               const float* __restrict__ Gsep, int B, float2* __restrict__ coef,
+                                                               int* __restrict__ err) {
+    constexpr int P = PS * PA;
+    __shared__ __align__(128) float2 buf[P * 32 * kPropBkWarps];
+    __shared__ float2 sv[P][32 * kPropBkWarps];
+    __shared__ float sG[PS * PS + PA * PA];
+    __shared__ PropB<float> st[4 * P];
+    __shared__ __align__(8) unsigned long long mbar;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int pc = pbegin + blockIdx.x;
+    if (pc >= pend) return;
+    for (int i = tid; i < PS * PS + PA * PA; i += blockDim.x) sG[i] = Gsep[i];
+    const uint32_t bar = tc5::smem_u32(&mbar), sbuf = tc5::smem_u32(buf);
+    const int r = tid;                        // this thread's right-hand side
+    const bool act = r < B;
+    const int rr = act ? r : 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) sv[q][tid] = make_float2(0.f, 0.f);
+    const long long e0 = pp_ptr[pc];
+    const int ne = pp_nchild[pc] * P;   // at most four children
+    const uint32_t bytes = (uint32_t)(P * B * sizeof(float2));
+    if (tid == 0) {
+        tc5::mbar_init(bar, 1);
+        if (ne > 0) tc5::bulk_g2s(sbuf, coef + (long long)pb[e0].child_cone * P * B, bytes, bar);
+    }
+    for (int i = tid; i < ne; i += blockDim.x) st[i] = pb[e0 + i];   // the parent's terms
+    __syncthreads();
+    uint32_t phase = 0;
+    bool ok = true;
+    float2 cc[P];
+    int cur = -1;
+    for (int e = 0; e < ne; ++e) {
+        const PropB<float> E = st[e];
+        if (E.child_cone != cur) {             // block-uniform
+            cur = E.child_cone;
+            ok = __syncthreads_and(tc5::mbar_wait(bar, phase & 1u, 2000000000ll));
+            ++phase;
+            if (!ok) break;
+#pragma unroll
+            for (int q = 0; q < P; ++q) cc[q] = buf[q * B + rr];
+            __syncthreads();                   // every thread has read the block before it is overwritten
+            if (tid < 32) {                    // the next group: the first later term with another child cone
+                int nxt = -1;
+                for (int base = e + 1; base < ne && nxt < 0; base += 32) {
+                    const int idx = base + lane;
+                    const int cn = idx < ne ? st[idx].child_cone : cur;
+                    const unsigned m = __ballot_sync(0xffffffffu, cn != cur);
+                    if (m) nxt = __shfl_sync(0xffffffffu, cn, __ffs(m) - 1);
+                }
+                if (nxt >= 0 && tid == 0) tc5::bulk_g2s(sbuf, coef + (long long)nxt * P * B, bytes, bar);
+            }
+        }
+        float Ts[PS], Tt[PA];
+        cheb_row<float, PS>(E.s, Ts);
+        cheb_row<float, PA>(E.th, Tt);
+        const float2 it = interp_eval_tt<float, PS, PA>(cc, Ts, Tt);
+        float2 a = sv[E.pt][tid];
+        cmac<float>(a, it, make_float2(E.wr, E.wi));
+        sv[E.pt][tid] = a;
+    }
+    if (!ok) {   // the copy of the group that timed out may still land: one more bounded wait
+        if (tid == 0) { atomicExch(err, 1); tc5::mbar_wait(bar, (phase - 1u) & 1u, 2000000000ll); }
+        return;
+    }
+    // u[l][m] = sum_k Gs[m][k] v[l][k];  c[n][m] = sum_l Ga[n][l] u[l][m], stored at n*PS + m
+    float2 u[P];
+#pragma unroll
+    for (int l = 0; l < PA; ++l) {
+        float2 v[PS];
+#pragma unroll
+        for (int q = 0; q < PS; ++q) v[q] = sv[l * PS + q][tid];
+#pragma unroll
+        for (int m = 0; m < PS; ++m) {
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < PS; ++q) { const float g = sG[m * PS + q]; a.x = fmaf(g, v[q].x, a.x); a.y = fmaf(g, v[q].y, a.y); }
+            u[l * PS + m] = a;
+        }
+    }
+    if (!act) return;
+    float2* out = coef + (long long)pc * P * B + r;
+#pragma unroll
+    for (int n = 0; n < PA; ++n)
+#pragma unroll
+        for (int m = 0; m < PS; ++m) {
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int l = 0; l < PA; ++l) {
+                const float g = sG[PS * PS + n * PA + l];
+                a.x = fmaf(g, u[l * PS + m].x, a.x); a.y = fmaf(g, u[l * PS + m].y, a.y);
+            }
+            out[(long long)(n * PS + m) * B] = a;
+        }
+}
+
 // ------------------------------------------------------------------ near field + interpolation
 // warp = one Morton-sorted target x 32*RPL right-hand sides; y accumulated at the original index
 template <typename R, int PS, int PA, int RPL>
@@ -492,6 +601,13 @@ void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_
         k_prop_b<R, PS, PA, WPB, RPL><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32 * RPL)), WPB * 32, 0, s>>>(
             pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
     });
+}
+bool launch_prop_bk(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
+                    const float* Gsep, int B, float2* coef, int* err, cudaStream_t s) {
+    if (Ps != 5 || Pang != 5 || B > 64 || B <= 0 || (B & 1)) return false;
+    if (pend <= pbegin) return true;
+    k_prop_bk<5, 5><<<pend - pbegin, 32 * kPropBkWarps, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef, err);
+    return true;
 }
 template <typename R>
 void launch_final_b(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,

@@ -1,6 +1,8 @@
 // tcgen05.cuh -- the fifth-generation tensor core interface (sm_100a / sm_103a) used by the
 // 3xTF32 kernels: shared-memory operand descriptors, the instruction descriptor of a TF32 MMA,
-// tensor-memory (TMEM) allocation and loads, and the mbarrier completion wait.  Inline PTX only.
+// tensor-memory (TMEM) allocation and loads, and the mbarrier completion wait; plus the bulk
+// global -> shared copy of the tensor memory accelerator (cp.async.bulk) that stages blocks for
+// the FMA kernels.  Inline PTX only.
 //
 // Operand layout ("K-major, no swizzle"): a tile of R rows x K TF32 values is stored as core
 // matrices of 8 rows x 16 bytes (4 values), each 128 contiguous bytes, ordered
@@ -118,6 +120,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to shared
+// memory by one thread; the mbarrier's current phase completes when the bytes have landed
+// (its arrival count must be 1: this arrival sets the expected transaction bytes)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst_smem, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // earlier reads of dst come first
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_smem),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 
 // x = hi + lo with hi, lo TF32 (round to nearest, ties away; the low 13 bits of each are zero)

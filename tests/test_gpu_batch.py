@@ -59,13 +59,18 @@ def test_gpu_batch_tensor_core_kernels(lib, oracle, k, npatch, nrhs):
     three TF32 terms per operand, propagation in 3xTF32, leaf and propagation) against the FP32
     FMA kernels and the FP64 apply: every complex64 form within 2e-6 of FP64 and within 1.5e-6 of
     the FMA form (FP32-level agreement; a single TF32 product would give ~1e-3); repeated
-    applies are bit-identical."""
+    applies are bit-identical.  The FMA propagation with TMA-staged child coefficients is
+    bit-identical to the one with global loads."""
     fm = _kite(lib, k, npatch)
     n = fm.total_num_unknowns_
     X = _densities(oracle, n, nrhs)
     Y = fm.apply_batch(X)
     fm.batch_tensor_cores = 0
     Yf = fm.apply_batch(X, mixed=True)
+    # the FMA propagation with TMA-staged child coefficients does the same arithmetic in the same
+    # order (B even; an odd batch falls back to the global-load kernel)
+    fm.batch_tensor_cores = fm.BATCH_BULK_PROPAGATION
+    assert np.array_equal(fm.apply_batch(X, mixed=True), Yf)
     for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_LEAF_FP32, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION):
         fm.batch_tensor_cores = mask
         assert fm.batch_tensor_cores == mask
