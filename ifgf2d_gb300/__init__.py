@@ -428,7 +428,8 @@ class ForwardMap:
         rc = _lib.load().ifgf2d_solve_batch(self._h, _dp(Bf), _dp(X), nrhs, mode,
                                             float(tol), int(restart), int(max_iters),
                                             it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
-        self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0))
+        self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0),
+                               refinements=int(_lib.load().ifgf2d_last_refinements(self._h)) if mixed else 0)
         if rc == 8:
             if raise_on_noconv:
                 raise NoConvergence(f"GMRES: iterations {it.tolist()}, estimated errors {err.tolist()}")
@@ -464,7 +465,8 @@ class ForwardMap:
                                       (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT,
                                       float(tol), int(restart),
                                       int(max_iters), ctypes.byref(it), ctypes.byref(err))
-        self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0))
+        self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0),
+                               refinements=int(_lib.load().ifgf2d_last_refinements(self._h)) if (mixed and accelerated) else 0)
         if rc == 8:
             if raise_on_noconv:
                 raise NoConvergence(f"GMRES: {it.value} iterations, estimated error {err.value:.3e}")

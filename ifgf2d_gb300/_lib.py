@@ -28,7 +28,7 @@ EXPORTS = [
     "ifgf2d_get_points", "ifgf2d_get_patches", "ifgf2d_get_near_singular", "ifgf2d_precompute",
     "ifgf2d_get_precomputations", "ifgf2d_setup", "ifgf2d_get_nlevels", "ifgf2d_get_sorting", "ifgf2d_apply",
     "ifgf2d_apply_device", "ifgf2d_ifgf_far", "ifgf2d_solve", "ifgf2d_propagate", "ifgf2d_hankel",
-    "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
+    "ifgf2d_stream", "ifgf2d_work_counts", "ifgf2d_last_refinements", "ifgf2d_apply_timed", "ifgf2d_measure_fp64_peak",
     "ifgf2d_apply_direct_noalloc", "ifgf2d_apply_batch", "ifgf2d_apply_batch_device", "ifgf2d_solve_batch",
     "ifgf2d_set_host_threads", "ifgf2d_prepare", "ifgf2d_net_num_params", "ifgf2d_net_create", "ifgf2d_net_destroy",
     "ifgf2d_net_last_error", "ifgf2d_net_get_params", "ifgf2d_net_set_params", "ifgf2d_net_gradient",
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_hankel.argtypes = [ctypes.c_int, ctypes.c_longlong, D, D]
         L.ifgf2d_stream.argtypes = [P]; L.ifgf2d_stream.restype = ctypes.c_void_p
         L.ifgf2d_work_counts.argtypes = [P, I64]
+        L.ifgf2d_last_refinements.argtypes = [P]
         L.ifgf2d_apply_timed.argtypes = [P, P, P, ctypes.c_int, D]
         L.ifgf2d_measure_fp64_peak.argtypes = [D]
         L.ifgf2d_apply_direct_noalloc.argtypes = [P, P, P]

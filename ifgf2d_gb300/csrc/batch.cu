@@ -31,6 +31,10 @@ struct BatchWork {
     // GMRES
     int m = 0, scap = 0;
     DBuf<double2> V, w, t, h, H, part, Y, hn, b, x, r, d, ones;
+    // refinement passes after the first work on the columns still short of the tolerance,
+    // gathered into compact [N][Bc] arrays (right-hand side, solution, residual, correction, A x)
+    DBuf<double2> cb, cx, cr, cd, ct;
+    DBuf<int> act;
 };
 
 void ifgf::free_batch(ifgf2d_ctx* ctx) {
@@ -369,30 +373,60 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
     std::vector<double> itol(B);
     std::vector<int> it;
     std::vector<double> e;
+    int passes = 0;
     for (int outer = 0; outer < 30; ++outer) {
-        bool left = false;
+        std::vector<int> act;
         int most = 0;
         for (int r = 0; r < B; ++r) {
-            if (!done[r] && iters[r] < max_iters) left = true;
+            if (!done[r] && iters[r] < max_iters) act.push_back(r);
             most = std::max(most, iters[r]);
             itol[r] = std::max(2e-7, 0.3 * tol * bn[r] / std::max(rn[r], 1e-300));
         }
-        if (!left) break;
-        std::vector<char> skip(B);
-        for (int r = 0; r < B; ++r) skip[r] = done[r] || iters[r] >= max_iters;
-        if ((rc = gmres_batch(ctx, W.r.p, W.d.p, B, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most), skip,
-                              it, e)))
-            return rc;
-        for (int r = 0; r < B; ++r) iters[r] += it[r];
-        launch_bupdate(W.d.p, 0, 1, W.ones.p, 1.0, N, B, W.x.p, s);   // x += d (d is 0 where skipped)
-        if ((rc = apply_il(ctx, W.x.p, W.t.p, B, IFGF2D_APPLY_IFGF))) return rc;
-        launch_sub(W.b.p, W.t.p, nb, W.r.p, s);
-        if ((rc = bnorms(ctx, W.r.p, B, rn))) return rc;
-        for (int r = 0; r < B; ++r) {
+        if (act.empty()) break;
+        ++passes;
+        const int Bc = (int)act.size();
+        if (Bc == B) {
+            std::vector<char> skip(B, 0);
+            if ((rc = gmres_batch(ctx, W.r.p, W.d.p, B, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most),
+                                  skip, it, e)))
+                return rc;
+            for (int r = 0; r < B; ++r) iters[r] += it[r];
+            launch_bupdate(W.d.p, 0, 1, W.ones.p, 1.0, N, B, W.x.p, s);   // x += d
+            if ((rc = apply_il(ctx, W.x.p, W.t.p, B, IFGF2D_APPLY_IFGF))) return rc;
+            launch_sub(W.b.p, W.t.p, nb, W.r.p, s);
+            if ((rc = bnorms(ctx, W.r.p, B, rn))) return rc;
+        } else {
+            // only the columns still short of the tolerance: the batched applies cost in
+            // proportion to their columns, frozen ones included
+            const size_t nc = (size_t)N * Bc;
+            if (W.cb.n < nc) {
+                CK(W.cb.alloc((size_t)N * B)); CK(W.cx.alloc((size_t)N * B)); CK(W.cr.alloc((size_t)N * B));
+                CK(W.cd.alloc((size_t)N * B)); CK(W.ct.alloc((size_t)N * B));
+            }
+            CK(W.act.upload(act));
+            std::vector<double> itc(Bc), rnc;
+            for (int j = 0; j < Bc; ++j) itc[j] = itol[act[j]];
+            std::vector<char> skip(Bc, 0);
+            launch_gather_cols(W.r.p, B, W.act.p, Bc, N, W.cr.p, s);
+            if ((rc = gmres_batch(ctx, W.cr.p, W.cd.p, Bc, IFGF2D_APPLY_IFGF_MIXED, itc, restart, std::max(1, max_iters - most),
+                                  skip, it, e)))
+                return rc;
+            for (int j = 0; j < Bc; ++j) iters[act[j]] += it[j];
+            launch_scatter_cols(W.cd.p, Bc, W.act.p, B, N, true, W.x.p, s);   // x += d on the active columns
+            launch_gather_cols(W.x.p, B, W.act.p, Bc, N, W.cx.p, s);
+            launch_gather_cols(W.b.p, B, W.act.p, Bc, N, W.cb.p, s);
+            if ((rc = apply_il(ctx, W.cx.p, W.ct.p, Bc, IFGF2D_APPLY_IFGF))) return rc;
+            launch_sub(W.cb.p, W.ct.p, (long long)nc, W.cr.p, s);
+            launch_scatter_cols(W.cr.p, Bc, W.act.p, B, N, false, W.r.p, s);
+            if ((rc = bnorms(ctx, W.cr.p, Bc, rnc))) return rc;
+            for (int j = 0; j < Bc; ++j) rn[act[j]] = rnc[j];
+        }
+        for (int r : act) {
             est[r] = bn[r] > 0 ? rn[r] / bn[r] : 0.0;
             if (est[r] < tol) done[r] = 1;
         }
     }
+    ctx->last_passes = passes;
     return IFGF2D_OK;
 }
 

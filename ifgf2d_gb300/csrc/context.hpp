@@ -145,6 +145,7 @@ struct ifgf2d_ctx {
     BatchWork* bw = nullptr;        // batched apply / solve workspace (batch.cu), freed by destroy
     EvalWork* ew = nullptr;         // off-surface evaluation plan (offsurface.cu), freed by destroy
     long long counts[8] = {0};
+    int last_passes = 0;            // FP64 refinement passes of the last mixed solve (batched: of the batch)
 };
 
 #define CK(call)                                                                          \

@@ -397,6 +397,7 @@ extern "C" int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* s) {
     std::copy(ctx->T.sorting.begin(), ctx->T.sorting.end(), s);
     return IFGF2D_OK;
 }
+extern "C" int ifgf2d_last_refinements(const ifgf2d_ctx* ctx) { return ctx ? ctx->last_passes : -1; }
 extern "C" int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]) {
     if (!ctx || !out) return IFGF2D_ERR_ARG;
     for (int i = 0; i < 8; ++i) out[i] = ctx->counts[i];
@@ -829,7 +830,9 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
         CK(cudaMemcpyAsync(r.p, b.p, sizeof(double2) * N, cudaMemcpyDeviceToDevice, s));
         double rn = bn;
         est = bn > 0 ? 1.0 : 0.0;
+        ctx->last_passes = 0;
         for (int outer = 0; outer < 30 && est >= tol && iters < max_iters; ++outer) {
+            ++ctx->last_passes;
             // inner solves run to 0.3 of what is left of the tolerance, but not below the
             // complex64 operator's own accuracy (~6e-8 relative on the kite at k = 500)
             const double inner_tol = std::max(2e-7, 0.3 * tol * bn / rn);

@@ -167,6 +167,10 @@ void launch_multidot(const double2* V, long long ldv, int ncols, const double2* 
 void launch_multi_axpy(const double2* V, long long ldv, int ncols, const double2* h, double sign, long long n, double2* w, cudaStream_t s);
 void launch_scale(const double2* w, double2 a, long long n, double2* out, cudaStream_t s);
 void launch_sub(const double2* a, const double2* b, long long n, double2* out, cudaStream_t s);
+// out[i][j] = in[i][act[j]] for an interleaved in [N][B] and a compact out [N][Bc], and back
+// (out[i][act[j]] (+)= in[i][j])
+void launch_gather_cols(const double2* in, int B, const int* act, int Bc, long long N, double2* out, cudaStream_t s);
+void launch_scatter_cols(const double2* in, int Bc, const int* act, int B, long long N, bool add, double2* out, cudaStream_t s);
 void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream_t s);
 // one Arnoldi step after w = A v_j, with j read from *jp (for a captured iteration graph):
 // CGS2 against V[:, 0..j] into the Hessenberg column j, ||w||^2 into *nrm2 (zeroed by

@@ -563,7 +563,31 @@ __global__ void k_bscale(const double2* __restrict__ w, const double2* __restric
     out[e] = make_double2(v.x * s, v.y * s);
 }
 
+// columns act[0..Bc) of an interleaved [N][B] array <-> a compact [N][Bc] one
+__global__ void k_gather_cols(const double2* __restrict__ in, int B, const int* __restrict__ act, int Bc, long long N,
+                              double2* __restrict__ out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= N * Bc) return;
+    const long long i = e / Bc;
+    out[e] = in[i * B + act[e - i * Bc]];
+}
+__global__ void k_scatter_cols(const double2* __restrict__ in, int Bc, const int* __restrict__ act, int B, long long N, int add,
+                               double2* __restrict__ out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= N * Bc) return;
+    const long long i = e / Bc;
+    double2& o = out[i * B + act[e - i * Bc]];
+    const double2 v = in[e];
+    if (add) { o.x += v.x; o.y += v.y; } else o = v;
+}
+
 // ------------------------------------------------------------------ launchers
+void launch_gather_cols(const double2* in, int B, const int* act, int Bc, long long N, double2* out, cudaStream_t s) {
+    if (N * Bc > 0) k_gather_cols<<<nblk_b(N * Bc, 256), 256, 0, s>>>(in, B, act, Bc, N, out);
+}
+void launch_scatter_cols(const double2* in, int Bc, const int* act, int B, long long N, bool add, double2* out, cudaStream_t s) {
+    if (N * Bc > 0) k_scatter_cols<<<nblk_b(N * Bc, 256), 256, 0, s>>>(in, Bc, act, B, N, add ? 1 : 0, out);
+}
 void launch_interleave(const double2* x, long long N, int B, double2* xt, cudaStream_t s) {
     if (N <= 0 || B <= 0) return;
     k_interleave<<<dim3(nblk_b(N, 32), nblk_b(B, 32)), dim3(32, 8), 0, s>>>(x, N, B, xt);

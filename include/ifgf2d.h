@@ -218,6 +218,10 @@ void* ifgf2d_stream(ifgf2d_ctx* ctx);
 /* Algorithmic work of one IFGF apply: near pairs, leaf evaluations, propagation evaluations,
  * interpolation evaluations, cones, levels, singular-correction entries, bytes resident. */
 int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]);
+/* FP64 refinement passes of the context's last mixed solve (ifgf2d_solve or
+ * ifgf2d_solve_batch in IFGF2D_APPLY_IFGF_MIXED): each pass is one inner complex64 GMRES and one
+ * FP64 residual.  -1 for a NULL context. */
+int ifgf2d_last_refinements(const ifgf2d_ctx* ctx);
 
 /* Timed apply on device vectors: CUDA events on the context's stream between the phases
  * (no counterpart in the reference, whose timers are std::chrono prints, ForwardMap.tpp:545-563).

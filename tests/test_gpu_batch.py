@@ -151,6 +151,27 @@ def test_gpu_batch_solve_restart_and_zero_column(lib):
         assert rel(X[:, r], x) < 1e-6, r
 
 
+def test_gpu_batch_mixed_solve_compacted_passes(lib):
+    """Refinement passes that run on a subset of the columns (gathered into a compact batch):
+    a zero column is converged from the start, and a tolerance below the complex64 operator's
+    accuracy needs several FP64 passes.  Each other column reaches the FP64 tolerance and
+    agrees with its own single-vector refinement solve."""
+    k = 40.0
+    fm = _kite(lib, k, 64)
+    B = _plane_waves(fm, k, 5)
+    B[:, 2] = 0
+    X = fm.gmres_batch(B, tol=1e-9, restart=300, max_iters=2000, mixed=True)
+    st = fm.last_solve
+    assert st["converged"] and st["refinements"] >= 2
+    assert np.all(X[:, 2] == 0) and st["iters"][2] == 0
+    R = fm.apply_batch(X) - B
+    for r in (0, 1, 3, 4):
+        assert np.linalg.norm(R[:, r]) / np.linalg.norm(B[:, r]) < 1e-9, r
+        x = fm.gmres(B[:, r], tol=1e-9, restart=300, max_iters=2000, mixed=True)
+        assert fm.last_solve["refinements"] >= 2
+        assert rel(X[:, r], x) < 1e-7, r
+
+
 def test_gpu_batch_mixed_solve_reaches_fp64_tolerance(lib):
     """FP64 refinement around batched complex64 inner solves: every column's FP64 residual
     below 1e-6 (plane waves at 8 angles, kite k = 500, N = 8192)."""
