@@ -397,12 +397,13 @@ def run_large(G, k=8000.0, npatch=8192):
 def run_obstacles(n=256, plain_sample=256):
     """256 seeded star obstacles (k ~ U(10, 400), 10 points per wavelength, plane waves),
     each solved to a 1e-6 FP64 residual.  Chosen: host set-up of the next obstacles on 15
-    host threads while one thread runs each obstacle's device work, complex64 inner solves.
-    Plain: one obstacle after another, FP64 GMRES, on the first `plain_sample` obstacles."""
+    host threads while 3 device threads run the obstacles' device work, each on its own
+    context stream, complex64 inner solves.  Plain: one obstacle after another, FP64 GMRES, on
+    the first `plain_sample` obstacles."""
     from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles
     obs = star_obstacles(n)
     t0 = time.perf_counter()
-    solve_obstacles(obs, tol=1e-6, workers=15, mixed=True)
+    solve_obstacles(obs, tol=1e-6, workers=15, mixed=True, device_threads=3)
     dt = time.perf_counter() - t0
     r = [o.result for o in obs]
     sub = star_obstacles(n)[:plain_sample]
@@ -413,7 +414,8 @@ def run_obstacles(n=256, plain_sample=256):
     return {"workload": f"{n} star obstacles r = 1 + sum_m a_m cos mt + b_m sin mt (m <= 5, |a|,|b| < 0.05), "
                         "k ~ U(10, 400), N_i = 16 ceil(10 k L / 2 pi / 16), plane wave at a random angle; numpy default_rng(0)",
             "n": n, "unknowns_total": int(sum(o.npoints for o in obs)),
-            "chosen": {"seconds": dt, "ms_per_obstacle": dt / n * 1e3, "all_converged": all(x["converged"] for x in r),
+            "chosen": {"seconds": dt, "ms_per_obstacle": dt / n * 1e3, "device_threads": 3,
+                       "all_converged": all(x["converged"] for x in r),
                        "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in r),
                        "ifgf": int(sum(x["accelerated"] for x in r)), "direct": int(sum(not x["accelerated"] for x in r))},
             "plain": {"ms_per_obstacle": dtp / plain_sample * 1e3, "sample": f"the first {plain_sample} obstacles, one at a time",

@@ -170,7 +170,7 @@ int check_t5(ifgf2d_ctx* ctx) {
     int v = 0;
     CK(cudaMemcpy(&v, ctx->bw->t5err.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (!v) return IFGF2D_OK;
-    CK(cudaMemset(ctx->bw->t5err.p, 0, sizeof(int)));
+    CK(cudaMemsetAsync(ctx->bw->t5err.p, 0, sizeof(int), ctx->stream));
     return fail(ctx, IFGF2D_ERR_CUDA, "tensor-core propagation: a tensor-memory completion wait ran out");
 }
 
@@ -435,6 +435,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
 // ------------------------------------------------------------------ C ABI
 extern "C" int ifgf2d_apply_batch_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int nrhs, int mode) {
     if (!ctx || nrhs < 0 || (nrhs > 0 && (!d_x || !d_y))) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     return apply_cm(ctx, (const double2*)d_x, (double2*)d_y, nrhs, mode);
@@ -442,6 +443,7 @@ extern "C" int ifgf2d_apply_batch_device(ifgf2d_ctx* ctx, const void* d_x, void*
 
 extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, int nrhs, int mode) {
     if (!ctx || nrhs < 0 || (nrhs > 0 && (!x || !y))) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     const long long N = ctx->D.N;
@@ -464,6 +466,7 @@ extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, i
 extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
                                   int max_iters, int* iters, double* est_error) {
     if (!ctx || nrhs < 0 || (nrhs > 0 && (!rhs || !x)) || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     const long long N = ctx->D.N;

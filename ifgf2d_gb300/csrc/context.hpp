@@ -24,24 +24,63 @@ constexpr int kBatchBulkProp = 8; // FP32 FMA propagation with TMA-staged child 
 
 namespace ifgf {
 
+// The allocation stream of the calling thread.  While an AllocStream guard names a stream,
+// DBuf allocates and frees stream-ordered on it (cudaMallocAsync / cudaFreeAsync from the
+// device's memory pool, no device-wide synchronisation) and uploads with cudaMemcpyAsync, so
+// threads that set up or tear down contexts do not stall one another's streams; otherwise it uses
+// cudaMalloc / cudaFree / cudaMemcpy.  A buffer remembers how and on which stream it was
+// allocated and is freed the same way, on that stream (which must outlive it).
+inline cudaStream_t& alloc_stream() {
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+struct AllocStream {
+    cudaStream_t prev;
+    explicit AllocStream(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+    ~AllocStream() { alloc_stream() = prev; }
+    AllocStream(const AllocStream&) = delete;
+    AllocStream& operator=(const AllocStream&) = delete;
+};
+// keep freed stream-ordered memory in the device's pool for reuse (once per process and device)
+void keep_pool_memory(int device);
+// pinned host scratch of the calling thread (at least n elements; grown, never shrunk, kept for
+// the thread's life): the Hessenberg columns a solve reads back.  A thread runs one solve at a
+// time, so its contexts share it, and no context pays for pinning and unpinning memory (which
+// synchronises the device) at set-up and tear-down.
+double2* pinned_scratch(size_t n);
+
 template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t owner = nullptr;   // non-null: allocated stream-ordered on this stream
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { release(); }
-    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+    void release() {
+        if (p) {
+            if (owner) cudaFreeAsync(p, owner);
+            else cudaFree(p);
+        }
+        p = nullptr;
+        n = 0;
+        owner = nullptr;
+    }
     cudaError_t alloc(size_t cnt) {
         release();
         n = cnt;
         if (cnt == 0) return cudaSuccess;
+        if (cudaStream_t s = alloc_stream()) {
+            owner = s;
+            return cudaMallocAsync((void**)&p, cnt * sizeof(T), s);
+        }
         return cudaMalloc((void**)&p, cnt * sizeof(T));
     }
     cudaError_t upload(const T* src, size_t cnt) {
         cudaError_t e = alloc(cnt);
         if (e != cudaSuccess || cnt == 0) return e;
+        if (owner) return cudaMemcpyAsync(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice, owner);
         return cudaMemcpy(p, src, cnt * sizeof(T), cudaMemcpyHostToDevice);
     }
     cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
@@ -65,18 +104,15 @@ struct GmresWork {
     DBuf<double2> Z, zt;
     DBuf<double> nrm2;
     DBuf<int> jdev;
-    double2* H_host = nullptr;       // pinned copy of the Hessenberg columns read back per batch
     long long n = 0;
     int m = 0;
     cudaGraphExec_t exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // mode x (plain, preconditioned)
     void drop_graphs() {
         for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
     }
-    ~GmresWork() {
-        drop_graphs();
-        if (H_host) cudaFreeHost(H_host);
-    }
+    ~GmresWork() { drop_graphs(); }
 };
+
 
 struct ifgf2d_ctx {
     Discretisation D;

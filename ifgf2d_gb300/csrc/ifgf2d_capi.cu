@@ -1,3 +1,4 @@
+#include <mutex>
 // ifgf2d_capi.cu -- the C ABI (include/ifgf2d.h): context, set-up, apply, GMRES, propagation.
 //
 // Host orchestration of the GB300 forward map.  The context owns every device buffer; set-up
@@ -91,6 +92,8 @@ static int ensure_device(ifgf2d_ctx* ctx) {
     if (ctx->device_ready) return IFGF2D_OK;
     CK(cudaGetDevice(&ctx->device));
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    keep_pool_memory(ctx->device);
+    AllocStream guard(ctx->stream);
     const Discretisation& D = ctx->D;
     CK(ctx->x.upload(D.x)); CK(ctx->y.upload(D.y)); CK(ctx->wq.upload(D.wq)); CK(ctx->edge.upload(D.edge_jac));
     CK(ctx->nx.upload(D.nx)); CK(ctx->ny.upload(D.ny));
@@ -110,13 +113,47 @@ static int ensure_device(ifgf2d_ctx* ctx) {
     return IFGF2D_OK;
 }
 
+double2* ifgf::pinned_scratch(size_t n) {
+    struct Scratch {
+        double2* p = nullptr;
+        size_t n = 0;
+        ~Scratch() { if (p) cudaFreeHost(p); }
+    };
+    static thread_local Scratch sc;
+    if (sc.n < n) {
+        if (sc.p) cudaFreeHost(sc.p);
+        sc.p = nullptr;
+        sc.n = 0;
+        if (cudaMallocHost((void**)&sc.p, n * sizeof(double2)) != cudaSuccess) { sc.p = nullptr; return nullptr; }
+        sc.n = n;
+    }
+    return sc.p;
+}
+
+void ifgf::keep_pool_memory(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = ~0ull;   // freed blocks stay in the pool for the next context's set-up
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done.push_back(device);
+}
+
 extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
     if (!ctx) return IFGF2D_ERR_ARG;
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    free_batch(ctx);
-    free_eval(ctx);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    cudaStream_t s = ctx->stream;
+    if (s) cudaStreamSynchronize(s);
+    {
+        AllocStream guard(s);
+        free_batch(ctx);
+        free_eval(ctx);
+        delete ctx;   // buffers allocated on s are freed on s, before s goes
+    }
+    if (s) cudaStreamDestroy(s);
     return IFGF2D_OK;
 }
 extern "C" int ifgf2d_set_host_threads(int n) {
@@ -159,6 +196,7 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     if (!ctx) return IFGF2D_ERR_ARG;
     if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
     if (int rc = ensure_device(ctx)) return rc;
+    AllocStream guard(ctx->stream);
     const Discretisation& D = ctx->D;
     const int ncols = (int)ctx->hcols.size();
     CK(ctx->M.alloc((size_t)ncols * D.Np));
@@ -184,6 +222,7 @@ extern "C" int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, doub
     if (!ctx || !out || patch < 0 || patch >= ctx->D.num_patches) return IFGF2D_ERR_ARG;
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute first");
     const int c0 = ctx->col_ptr[patch], c1 = ctx->col_ptr[patch + 1];
+    CK(cudaStreamSynchronize(ctx->stream));   // the table was written (and allocated) on the context's stream
     CK(cudaMemcpy(out, ctx->M.p + (size_t)c0 * ctx->D.Np, sizeof(double2) * (size_t)(c1 - c0) * ctx->D.Np, cudaMemcpyDeviceToHost));
     return IFGF2D_OK;
 }
@@ -248,6 +287,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         int rc = ifgf2d_precompute(ctx, k);
         if (rc != IFGF2D_OK) return rc;
     }
+    AllocStream guard(ctx->stream);
     const Discretisation& D = ctx->D;
     if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) {
         int rc = ifgf2d_prepare(ctx, k, nlevels);
@@ -473,6 +513,7 @@ int ifgf::apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) 
 
 extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]) {
     if (!ctx || !d_x || !d_y || !ms) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown apply mode");
@@ -583,6 +624,7 @@ static int tune_precision(ifgf2d_ctx* ctx, int reps, const V2<R>* rho, const V2<
 }
 extern "C" int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices) {
     if (!ctx || reps <= 0 || reps > 1000) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before autotuning");
     // realistic intensities in both precisions from one apply of each form on the stored vector
     CK(cudaMemsetAsync(ctx->vin.p, 0, sizeof(double2) * ctx->D.N, ctx->stream));
@@ -604,11 +646,13 @@ extern "C" int ifgf2d_measure_fp64_peak(double* tflops) {
 
 extern "C" int ifgf2d_apply_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode) {
     if (!ctx || !d_x || !d_y) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     return apply_dev(ctx, (const double2*)d_x, (double2*)d_y, mode);
 }
 
 extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mode) {
     if (!ctx || !x || !y) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     // state and mode before any copy (apply_dev repeats the checks for the device entry point)
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before apply");
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
@@ -627,6 +671,7 @@ extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mod
 
 extern "C" int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intens, double* y) {
     if (!ctx || !intens || !y) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup first");
     const size_t bytes = sizeof(double2) * ctx->D.N;
     CK(cudaMemcpyAsync(ctx->vin.p, intens, bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -644,6 +689,7 @@ extern "C" int ifgf2d_ifgf_far(ifgf2d_ctx* ctx, const double* intens, double* y)
 // ------------------------------------------------------------------ propagation (off-surface)
 extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp, const double* dens, double* out) {
     if (!ctx || m < 0 || (m > 0 && (!xp || !yp || !out)) || !dens) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) first: the wavenumber is set there");
     if (m == 0) return IFGF2D_OK;
     const int N = (int)ctx->D.N;
@@ -682,8 +728,6 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N)); CK(G.vin.alloc(N));
         CK(G.H.alloc((size_t)ldh * m)); CK(G.y.alloc(m)); CK(G.nrm2.alloc(1)); CK(G.jdev.alloc(1));
         CK(G.part.alloc((size_t)arnoldi_part_size(N, m)));
-        if (G.H_host) { cudaFreeHost(G.H_host); G.H_host = nullptr; }
-        CK(cudaMallocHost((void**)&G.H_host, (size_t)ldh * m * sizeof(double2)));
         G.Z.release(); G.zt.release();
         G.n = N; G.m = m;
     }
@@ -710,6 +754,8 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         cudaGraphDestroy(graph);
     }
     double2 *V = G.V.p, *w = G.w.p, *h = G.h.p, *t = G.t.p;
+    double2* H_host = pinned_scratch((size_t)ldh * m);
+    if (!H_host) return fail(ctx, IFGF2D_ERR_CUDA, "cudaMallocHost of the Hessenberg read-back buffer failed");
     CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, s));
     auto dnorm = [&](const double2* v, double& out) -> int {
         launch_multidot(v, N, 1, v, N, h + m + 1, s);
@@ -744,14 +790,14 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
             const int nb = std::min(4, m - j);
             for (int q = 0; q < nb; ++q) CK(cudaGraphLaunch(G.exec[gi], s));
             // columns j .. j+nb-1, rows 0 .. j+nb
-            CK(cudaMemcpy2DAsync(G.H_host + (size_t)j * ldh, ldh * sizeof(double2), G.H.p + (size_t)j * ldh, ldh * sizeof(double2),
+            CK(cudaMemcpy2DAsync(H_host + (size_t)j * ldh, ldh * sizeof(double2), G.H.p + (size_t)j * ldh, ldh * sizeof(double2),
                                  (size_t)(j + nb + 1) * sizeof(double2), nb, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             CK(cudaGetLastError());
             for (int q = 0; q < nb; ++q) {
                 const int c = j + q;
                 std::complex<double>* col = &R[(size_t)c * ldh];
-                for (int i = 0; i <= c + 1; ++i) col[i] = std::complex<double>(G.H_host[(size_t)c * ldh + i].x, G.H_host[(size_t)c * ldh + i].y);
+                for (int i = 0; i <= c + 1; ++i) col[i] = std::complex<double>(H_host[(size_t)c * ldh + i].x, H_host[(size_t)c * ldh + i].y);
                 const double hn = std::abs(col[c + 1]);
                 for (int i = 0; i < c; ++i) rot(Gr[i], col[i], col[i + 1]);
                 if (col[c + 1] != 0.0) {
@@ -791,6 +837,7 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
 extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, int mode, double tol, int restart, int max_iters,
                             int* iters_out, double* err_out) {
     if (!ctx || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");
@@ -865,6 +912,7 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
 extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* xout, int mode, double tol,
                                     int restart, int max_iters, int* iters_out, double* err_out) {
     if (!ctx || !net || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");

@@ -85,6 +85,7 @@ void launch_eval_targets(long long M, const double* tx, const double* ty, const 
 
 extern "C" int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const double* xp, const double* yp) {
     if (!ctx || m < 0 || (m > 0 && (!xp || !yp))) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->ifgf_ready) return fail(ctx, IFGF2D_ERR_STATE, "setup before an off-surface evaluation plan");
     free_eval(ctx);
     ctx->ew = new EvalWork;
@@ -131,6 +132,7 @@ extern "C" int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const 
 
 extern "C" int ifgf2d_eval_offsurface(ifgf2d_ctx* ctx, const double* density, double* out) {
     if (!ctx || !density) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
     if (!ctx->ew) return fail(ctx, IFGF2D_ERR_STATE, "ifgf2d_eval_offsurface_setup first");
     EvalWork& W = *ctx->ew;
     if (W.M == 0) return IFGF2D_OK;

@@ -180,6 +180,7 @@ int net_stage(ifgf2d_net* net, int nseg, const int* len, const double* r, const 
 }  // namespace
 
 int ifgf::net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, double k, std::string& err) {
+    AllocStream guard(nullptr);   // the network's buffers belong to its own stream: plain allocations
     if (!net || N <= 0 || N > (1LL << 30)) { err = "learned preconditioner: bad network or size"; return IFGF2D_ERR_ARG; }
     const int len = (int)N;
     int rc = net_layout(net, 1, &len);

@@ -86,36 +86,68 @@ def _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters):
 
 
 def solve_obstacles(obstacles, tol=1e-6, workers=15, mixed=True, direct_below=0, restart=300, max_iters=1000,
-                    keep_solutions=False, lookahead=None):
+                    keep_solutions=False, lookahead=None, device_threads=3):
     """Solve every obstacle (plane-wave scattering, combined field) to `tol`.  Returns the
     densities when keep_solutions, else None; each obstacle's `result` holds iterations,
     convergence, the true FP64 relative residual and the operator used.  workers = 0 runs
-    everything on the calling thread."""
+    everything on the calling thread.  device_threads > 1 runs the device part of that many
+    obstacles at once (obstacle i on thread i mod device_threads), each on its own context
+    stream; contexts allocate stream-ordered, so their set-up and tear-down do not stall one
+    another."""
+    import threading
     from . import _lib
     import ifgf2d_gb300 as G
     L = _lib.load()
-    xs = []
+    n = len(obstacles)
+    xs = [None] * n
     if workers <= 0:
-        for ob in obstacles:
+        for i, ob in enumerate(obstacles):
             fm, accel = _prepare_one(G, ob, direct_below)
             x = _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters)
             del fm
-            xs.append(x if keep_solutions else None)
+            xs[i] = x if keep_solutions else None
         return xs if keep_solutions else None
-    ahead = lookahead or 2 * workers
+    T = max(1, int(device_threads))
+    ahead = max(lookahead or 2 * workers, T)
+    slots = threading.Semaphore(ahead)          # host preparations submitted but not yet taken
+    futs = [None] * n
+    ready = [threading.Event() for _ in range(n)]
+    stop = threading.Event()
     L.ifgf2d_set_host_threads(1)
     try:
-        with ThreadPoolExecutor(workers) as ex:
-            futs = {}
-            nxt = 0
-            for i, ob in enumerate(obstacles):
-                while nxt < len(obstacles) and nxt < i + ahead:
-                    futs[nxt] = ex.submit(_prepare_one, G, obstacles[nxt], direct_below)
-                    nxt += 1
-                fm, accel = futs.pop(i).result()
-                x = _device_one(G, ob, fm, accel, tol, mixed, restart, max_iters)
-                del fm
-                xs.append(x if keep_solutions else None)
+        with ThreadPoolExecutor(workers) as ex, ThreadPoolExecutor(T) as dev:
+            def submit_all():
+                for i, ob in enumerate(obstacles):
+                    while not slots.acquire(timeout=0.1):
+                        if stop.is_set():
+                            return
+                    futs[i] = ex.submit(_prepare_one, G, ob, direct_below)
+                    ready[i].set()
+
+            def device_loop(t):
+                try:
+                    for i in range(t, n, T):
+                        while not ready[i].wait(timeout=0.1):
+                            if stop.is_set():
+                                return
+                        fm, accel = futs[i].result()
+                        futs[i] = None
+                        slots.release()
+                        x = _device_one(G, obstacles[i], fm, accel, tol, mixed, restart, max_iters)
+                        del fm
+                        xs[i] = x if keep_solutions else None
+                except BaseException:
+                    stop.set()
+                    raise
+
+            sub = threading.Thread(target=submit_all, daemon=True)
+            sub.start()
+            try:
+                for f in [dev.submit(device_loop, t) for t in range(T)]:
+                    f.result()
+            finally:
+                stop.set()
+                sub.join()
     finally:
         L.ifgf2d_set_host_threads(0)
     return xs if keep_solutions else None

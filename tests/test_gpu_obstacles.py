@@ -1,8 +1,8 @@
 """Many independent obstacles (ifgf2d_gb300.scatterers) -- needs a GPU.
 
 Every obstacle of the seeded star configuration reaches the FP64 tolerance through the
-pipelined driver (host set-up on worker threads, device work on the calling thread), and the
-pipelined solutions equal those of a plain one-at-a-time run of the same code path.
+pipelined driver (host set-up on worker threads, device work on one or more device threads),
+and the pipelined solutions equal those of a plain one-at-a-time run of the same code path.
 """
 import numpy as np
 import pytest
@@ -10,10 +10,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_gpu_obstacles_pipelined_match_sequential(lib):
+@pytest.mark.parametrize("device_threads", [1, 3])
+def test_gpu_obstacles_pipelined_match_sequential(lib, device_threads):
+    """Pipelined (and, with device_threads > 1, several obstacles at once on their own streams)
+    equals one at a time, bit for bit."""
     from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles
     obs = star_obstacles(12, seed=1, kmax=150.0)
-    xs = solve_obstacles(obs, tol=1e-8, workers=4, mixed=False, keep_solutions=True)
+    xs = solve_obstacles(obs, tol=1e-8, workers=4, mixed=False, keep_solutions=True, device_threads=device_threads)
     assert all(o.result["converged"] for o in obs)
     assert max(o.result["true_rel_residual"] for o in obs) < 1e-7
     ref = star_obstacles(12, seed=1, kmax=150.0)
@@ -26,7 +29,7 @@ def test_gpu_obstacles_pipelined_match_sequential(lib):
 def test_gpu_obstacles_mixed_reach_tolerance(lib):
     from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles
     obs = star_obstacles(16, seed=2)
-    solve_obstacles(obs, tol=1e-6, workers=4, mixed=True)
+    solve_obstacles(obs, tol=1e-6, workers=4, mixed=True, device_threads=2)
     assert all(o.result["converged"] for o in obs)
     assert max(o.result["true_rel_residual"] for o in obs) < 1e-6
     # the seeded configuration: N_i = 16 ceil(10 k L / 2 pi / 16)
