@@ -240,7 +240,8 @@ int bnorms(ifgf2d_ctx* ctx, const double2* v, int B, std::vector<double>& out) {
 // Right-hand side r stops when |g_{j+1}| / ||r0|| < tol[r] (opGMRES.hpp:207), after max_iters
 // iterations, or at the start when skip[r]; a stopped right-hand side keeps its x.
 int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, const std::vector<double>& tol, int restart,
-                int max_iters, const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est) {
+                int max_iters, const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est,
+                int gs_passes = 2) {
     const long long N = ctx->D.N;
     const int m = (int)std::min<long long>(restart, N);
     int rc = ensure_solve(ctx, B, m);
@@ -285,7 +286,7 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
             double2* vj = W.V.p + (long long)j * nb;
             double2* Hcol = W.H.p + (long long)j * ldh * B;
             if ((rc = apply_il(ctx, vj, W.w.p, B, mode))) return rc;
-            for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice
+            for (int pass = 0; pass < gs_passes; ++pass) {   // classical Gram-Schmidt, once or twice
                 launch_bdot(W.V.p, nb, j + 1, W.w.p, N, B, W.part.p, W.h.p, Hcol, pass, -1, s);
                 launch_bupdate(W.V.p, nb, j + 1, W.h.p, -1.0, N, B, W.w.p, s);
             }
@@ -346,6 +347,13 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
     return IFGF2D_OK;
 }
 
+// Gram-Schmidt passes of the complex64 inner solves.  They stop at a relative residual of 2e-7
+// or more, and every correction is checked by the FP64 residual of the refinement; one
+// classical pass (half the basis traffic of two) keeps them at their iteration counts, and a
+// correction that came out short costs one more refinement pass, not a wrong answer.  The FP64
+// solves keep the second pass.
+constexpr int kInnerGsPasses = 1;
+
 // solve B <= kMaxBatch interleaved right-hand sides W.b into W.x
 int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_iters, std::vector<int>& iters,
              std::vector<double>& est) {
@@ -388,7 +396,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
         if (Bc == B) {
             std::vector<char> skip(B, 0);
             if ((rc = gmres_batch(ctx, W.r.p, W.d.p, B, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most),
-                                  skip, it, e)))
+                                  skip, it, e, kInnerGsPasses)))
                 return rc;
             for (int r = 0; r < B; ++r) iters[r] += it[r];
             launch_bupdate(W.d.p, 0, 1, W.ones.p, 1.0, N, B, W.x.p, s);   // x += d
@@ -409,7 +417,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
             std::vector<char> skip(Bc, 0);
             launch_gather_cols(W.r.p, B, W.act.p, Bc, N, W.cr.p, s);
             if ((rc = gmres_batch(ctx, W.cr.p, W.cd.p, Bc, IFGF2D_APPLY_IFGF_MIXED, itc, restart, std::max(1, max_iters - most),
-                                  skip, it, e)))
+                                  skip, it, e, kInnerGsPasses)))
                 return rc;
             for (int j = 0; j < Bc; ++j) iters[act[j]] += it[j];
             launch_scatter_cols(W.cd.p, Bc, W.act.p, B, N, true, W.x.p, s);   // x += d on the active columns
