@@ -363,23 +363,34 @@ __device__ __forceinline__ void leaf_store(const LeafChunk<P>& t, int tid, unsig
         st4_terms<NS>(sm, offB, tc5::kmajor_off(kL5N, row, kL5Src + k0), im, 1.f);
     }
 }
-// D (+)= sum over term pairs (i, j) with i + j < NS + 1 (0-based i + j <= NS - 1) of A_i B_j, the
-// smallest products first: 3 MMAs per K step for two terms (3xTF32), 6 for three
+// D_big (+)= A_0 B_0 and D_small (+)= the other term pairs (i, j) with i + j <= NS - 1, the
+// smallest first: 2 + 1 MMAs per K step for two terms (3xTF32), 5 + 1 for three.  The tensor
+// core's FP32 accumulator rounds each addition toward zero, so its error grows with the number
+// of additions into a large value; keeping the large products in their own tile (one addition
+// per K step) and the small ones apart, and adding the two tiles in FP32 at read-back, holds the
+// result to FP32 accuracy (one tile for all products over 65 sources: about 4x the FP32 error).
 template <int NS>
-__device__ __forceinline__ void issue_split(uint32_t d, uint32_t a0, uint32_t b0, uint32_t tile, uint32_t lbo, int ksteps,
-                                            uint32_t idesc, bool accumulate) {
+__device__ __forceinline__ void issue_split(uint32_t d_big, uint32_t d_small, uint32_t a0, uint32_t b0, uint32_t tile, uint32_t lbo,
+                                            int ksteps, uint32_t idesc, bool accumulate) {
     uint32_t acc = accumulate ? 1u : 0u;
 #pragma unroll
-    for (int sum = NS - 1; sum >= 0; --sum)
+    for (int sum = NS - 1; sum >= 1; --sum)
 #pragma unroll
         for (int i = 0; i <= sum; ++i) {
             const int j = sum - i;
             for (int ks = 0; ks < ksteps; ++ks) {
                 const uint32_t o = ks * 2 * lbo;
-                tc5::mma_tf32(d, tc5::smem_desc(a0 + i * tile + o, lbo, 128), tc5::smem_desc(b0 + j * tile + o, lbo, 128), idesc, acc);
+                tc5::mma_tf32(d_small, tc5::smem_desc(a0 + i * tile + o, lbo, 128), tc5::smem_desc(b0 + j * tile + o, lbo, 128), idesc,
+                              acc);
                 acc = 1u;
             }
         }
+    acc = accumulate ? 1u : 0u;
+    for (int ks = 0; ks < ksteps; ++ks) {
+        const uint32_t o = ks * 2 * lbo;
+        tc5::mma_tf32(d_big, tc5::smem_desc(a0 + o, lbo, 128), tc5::smem_desc(b0 + o, lbo, 128), idesc, acc);
+        acc = 1u;
+    }
 }
 
 template <int P, int NS>
@@ -394,7 +405,7 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
     const uint32_t bar = tc5::smem_u32(sm + OFF_BAR5), tslot = tc5::smem_u32(sm + OFF_BAR5 + 8);
     const uint32_t sA = tc5::smem_u32(sm), sB = tc5::smem_u32(sm + NS * L5_T);
     if (tid == 0) tc5::mbar_init(bar, 1);
-    if (warp == 0) tc5::tmem_alloc(tslot, kL5N);
+    if (warp == 0) tc5::tmem_alloc(tslot, 2 * kL5N);   // large-product tile, then small-product tile
     tc5::fence_before_sync();
     __syncthreads();
     tc5::fence_after_sync();
@@ -422,7 +433,7 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
             __syncthreads();
             if (tid == 0) {
                 tc5::fence_after_sync();
-                issue_split<NS>(tmem, sA, sB, L5_T, kLbo, kL5K / 8, idesc, ch > 0);
+                issue_split<NS>(tmem, tmem + kL5N, sA, sB, L5_T, kLbo, kL5K / 8, idesc, ch > 0);
                 tc5::commit(bar);
             }
             if (ch + 1 < nch) leaf_load<P>(t, tid, (ch + 1) * kL5Src, n, s0, item.y, item.z, leaf_off, L, rho, B);
@@ -438,8 +449,11 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
         const long long cstride = 2ll * B;
 #pragma unroll 1
         for (int q = 0; q < 4; ++q) {
-            float v[16];
+            float v[16], v2[16];
             tc5::tmem_ld16(tread + 16 * q, v);
+            tc5::tmem_ld16(tread + kL5N + 16 * q, v2);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] += v2[j];
             const int cb = col0 + 16 * q;
             if (r < B) {
                 float* o = out + cb * cstride;
@@ -457,7 +471,7 @@ __global__ void __launch_bounds__(kL5Threads, 2) k_leaf_t5(const int4* __restric
     }
     tc5::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc5::tmem_dealloc(tmem, kL5N);
+    if (warp == 0) tc5::tmem_dealloc(tmem, 2 * kL5N);
 }
 
 }  // namespace

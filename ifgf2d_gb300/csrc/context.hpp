@@ -130,7 +130,7 @@ struct ifgf2d_ctx {
     int tune_leaf[2] = {5, 5};
     int tune_prop[2][kTuneLevels] = {};
     // batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (bit mask, else FP32 FMA)
-    int tune_batch_tc = 0;
+    int tune_batch_tc = kBatchTcLeaf;
     // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
     bool prep_ready = false;
     double prep_k = 0.0;

@@ -236,8 +236,9 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
  * keeps the fastest.  The table has ifgf2d_tuning_size() ints: leaf FP64, leaf complex64, then
  * per precision one propagation entry per level (0 = the most cones per block), then a bit
  * mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor cores
- * (IFGF2D_BATCH_TC_LEAF, IFGF2D_BATCH_TC_PROPAGATION; FP32 FMA otherwise).  get / set read and
- * restore it (e.g. from an on-disk cache); applies use the context's current table. */
+ * (IFGF2D_BATCH_TC_LEAF, the default, IFGF2D_BATCH_TC_PROPAGATION; FP32 FMA otherwise).  get /
+ * set read and restore it (e.g. from an on-disk cache); applies use the context's current
+ * table. */
 #define IFGF2D_BATCH_TC_LEAF 1          /* leaf-cone sums, 3xTF32 (two TF32 terms per operand) */
 #define IFGF2D_BATCH_TC_PROPAGATION 2   /* propagation, 3xTF32 */
 #define IFGF2D_BATCH_TC_LEAF_FP32 4     /* leaf-cone sums, three TF32 terms per operand (6 products) */
