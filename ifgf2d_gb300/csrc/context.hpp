@@ -127,7 +127,7 @@ struct ifgf2d_ctx {
     // launch shapes per precision (0 FP64, 1 complex64): leaf-kernel source chunks, and cones
     // per block of each level's propagation (0 = the most that fit 256 threads); set by
     // ifgf2d_autotune / ifgf2d_set_tuning
-    int tune_leaf[2] = {5, 5};
+    int tune_leaf[2] = {5, 5};      // complex64 also 0: the table streamed by TMA bulk copies (k_leaf_tma)
     int tune_prop[2][kTuneLevels] = {};
     // batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (bit mask, else FP32 FMA)
     int tune_batch_tc = kBatchTcLeaf;
@@ -182,6 +182,8 @@ struct ifgf2d_ctx {
     EvalWork* ew = nullptr;         // off-surface evaluation plan (offsurface.cu), freed by destroy
     long long counts[8] = {0};
     int last_passes = 0;            // FP64 refinement passes of the last mixed solve (batched: of the batch)
+    int nsm = 0;                    // SMs of the context's device
+    DBuf<int> kerr;                 // set by a kernel whose bounded wait ran out (checked after synchronisations)
 };
 
 #define CK(call)                                                                          \

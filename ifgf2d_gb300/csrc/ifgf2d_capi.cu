@@ -415,9 +415,12 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     }
     CK(ctx->coef.alloc((size_t)T.total_cones * P));
     CK(ctx->coef32.alloc((size_t)T.total_cones * P));
-    CK(ctx->rho32.alloc(N));
+    CK(ctx->rho32.alloc(N + 2));   // + padding: the TMA leaf kernel copies from 16-byte boundaries
     CK(ctx->near32.alloc(ctx->near.n));
-    CK(ctx->leafL32.alloc(ctx->leafL.n));
+    CK(ctx->leafL32.alloc(ctx->leafL.n + 2));   // + padding: the TMA leaf kernel copies from 16-byte boundaries
+    CK(leaf_tma_init());
+    CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    if (!ctx->kerr.p) { CK(ctx->kerr.alloc(1)); CK(cudaMemsetAsync(ctx->kerr.p, 0, sizeof(int), ctx->stream)); }
     launch_d2f(ctx->near.p, (long long)ctx->near.n, ctx->near32.p, ctx->stream);
     launch_d2f(ctx->leafL.p, (long long)ctx->leafL.n, ctx->leafL32.p, ctx->stream);
     CK(cudaGetLastError());
@@ -444,6 +447,17 @@ extern "C" int ifgf2d_work_counts(const ifgf2d_ctx* ctx, long long out[8]) {
     return IFGF2D_OK;
 }
 
+// after a synchronisation: did a kernel give up on a bounded wait?
+static int check_kerr(ifgf2d_ctx* ctx) {
+    if (!ctx->kerr.p) return IFGF2D_OK;
+    int v = 0;
+    CK(cudaMemcpyAsync(&v, ctx->kerr.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (!v) return IFGF2D_OK;
+    CK(cudaMemsetAsync(ctx->kerr.p, 0, sizeof(int), ctx->stream));
+    return fail(ctx, IFGF2D_ERR_CUDA, "a kernel's bounded wait for a bulk copy ran out");
+}
+
 // ------------------------------------------------------------------ apply
 // y += far field of the Morton-ordered intensities (rho / rho32), BoxTree.h:1037-1061
 template <typename R>
@@ -454,8 +468,15 @@ static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, con
     const TreeLevel& LD = T.L[Dl];
     cudaStream_t s = ctx->stream;
     const int pr = sizeof(R) == 4 ? 1 : 0;
-    launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
-                           ctx->leaf_off.p, leafL, rho, P, coef, s, ctx->tune_leaf[pr]);
+    bool leaf_done = false;
+    if constexpr (sizeof(R) == 4) {
+        if (ctx->tune_leaf[1] == 0)
+            leaf_done = launch_leaf_tma(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p,
+                                        ctx->leaf_count.p, ctx->leaf_off.p, leafL, rho, P, coef, ctx->kerr.p, ctx->nsm, s);
+    }
+    if (!leaf_done)
+        launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p, ctx->leaf_count.p,
+                               ctx->leaf_off.p, leafL, rho, P, coef, s, ctx->tune_leaf[pr]);
     if (ev) cudaEventRecord(ev[0], s);
     for (int l = Dl; l >= 3; --l) {
         const TreeLevel& Lp = T.L[l - 1];
@@ -598,10 +619,18 @@ static int tune_precision(ifgf2d_ctx* ctx, int reps, const V2<R>* rho, const V2<
         return t[reps / 2];
     };
     float best = 1e30f; int bestc = 5;
-    for (int ch : {1, 2, 5, 10}) {
+    for (int ch : {1, 2, 5, 10, 0}) {   // 0: complex64 only, the table streamed by TMA bulk copies
+        if (ch == 0 && sizeof(R) != 4) continue;
         const float ms = time_it([&] {
-            launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p,
-                                   ctx->leaf_count.p, ctx->leaf_off.p, leafL, rho, P, coef, s, ch);
+            bool done = false;
+            if constexpr (sizeof(R) == 4) {
+                if (ch == 0)
+                    done = launch_leaf_tma(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p,
+                                           ctx->leaf_count.p, ctx->leaf_off.p, leafL, rho, P, coef, ctx->kerr.p, ctx->nsm, s);
+            }
+            if (!done)
+                launch_leaf_apply_t<R>(ctx->leaf_cone_box.p, (int)LD.cone_nonrel.size(), LD.cone_base, ctx->leaf_start.p,
+                                       ctx->leaf_count.p, ctx->leaf_off.p, leafL, rho, P, coef, s, ch);
         });
         if (ms < best) { best = ms; bestc = ch; }
     }
@@ -665,6 +694,7 @@ extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mod
     if (rc != IFGF2D_OK) return rc;
     CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (int rk = check_kerr(ctx)) return rk;
     if (!all_finite(y, 2 * ctx->D.N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the result");
     return IFGF2D_OK;
 }
@@ -901,6 +931,7 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
     CK(cudaStreamSynchronize(s));
     if (iters_out) *iters_out = iters;
     if (err_out) *err_out = est;
+    if (int rk = check_kerr(ctx)) return rk;
     return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
 }
 
@@ -974,6 +1005,7 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
     CK(cudaStreamSynchronize(s));
     if (iters_out) *iters_out = iters;
     if (err_out) *err_out = est;
+    if (int rk = check_kerr(ctx)) return rk;
     return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
 }
 

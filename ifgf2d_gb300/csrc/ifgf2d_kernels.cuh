@@ -90,6 +90,14 @@ template <typename R>
 void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
                          const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s,
                          int chunks = 5);
+// complex64 leaf cones with the table streamed through shared memory by TMA bulk copies
+// (P = 25); false when not launched (other P, or leaf_tma_init not run).  *err is set when a
+// completion wait runs out.  leaf_tma_init sets the kernel's shared-memory attribute (outside
+// stream capture).  The table array must carry 16 bytes of padding after its end.
+bool launch_leaf_tma(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                     const long long* leaf_off, const float2* L, const float2* rho, int P, float2* coef, int* err, int nsm,
+                     cudaStream_t s);
+cudaError_t leaf_tma_init();
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
                         int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block = 0);

@@ -11,7 +11,10 @@
 //   k_final        near field + every level's cousin interpolants, one warp per target,
 //                  result added to y at the target's original index               BoxTree.h:614-683, 876-937, 1063-1069
 #include "ifgf_device.cuh"
+#include "tcgen05.cuh"
 #include <type_traits>
+#include <algorithm>
+#include <atomic>
 
 namespace ifgf {
 
@@ -65,6 +68,104 @@ __global__ void __launch_bounds__(256) k_leaf_apply_t(const int* __restrict__ co
         V2<R> acc = a0;
         for (int q = 1; q < CH; ++q) { const V2<R> v = part[local * per_cone + q * P + m]; acc.x += v.x; acc.y += v.y; }
         coef[(long long)(cone_base + c) * P + m] = acc;
+    }
+}
+
+// complex64 leaf cones with the table streamed by the tensor memory accelerator.  A persistent
+// CTA walks its cones (blockIdx.x, + gridDim.x, ...) in pieces of at most kLtSrc sources; thread 0
+// keeps kLtStages pieces in flight, each two cp.async.bulk copies (the piece's table rows and its
+// densities) into a shared-memory ring, counted on the stage's mbarrier.  Each copy starts at the
+// 16-byte boundary at or below its data (the table and density arrays carry 16 bytes of padding
+// at their ends).  Threads (chunk, m) sum L[s][m] rho[s] over the piece's sources s = chunk mod kLtChunks,
+// and a cone's chunk partials are reduced in shared memory.  Waits are bounded: one that runs
+// out sets *err, waits once more for the copies in flight and stops the CTA.
+constexpr int kLtSrc = 64, kLtStages = 4, kLtChunks = 5, kLtThreads = 128;
+template <int P>
+struct LeafTma {
+    static constexpr int table = (kLtSrc * P * 8 + 16 + 127) / 128 * 128;   // table rows, then the densities
+    static constexpr int stage = table + (kLtSrc * 8 + 16 + 127) / 128 * 128;
+    static constexpr int part_off = kLtStages * stage;
+    static constexpr int bar_off = part_off + kLtChunks * P * 8;
+    static constexpr int smem = bar_off + 8 * kLtStages;
+};
+template <int P>
+__global__ void __launch_bounds__(kLtThreads) k_leaf_tma(const int* __restrict__ cone_box, int ncones, int cone_base,
+                                                         const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
+                                                         const long long* __restrict__ leaf_off, const float2* __restrict__ L,
+                                                         const float2* __restrict__ rho, float2* __restrict__ coef,
+                                                         int* __restrict__ err) {
+    static_assert(kLtChunks * P <= kLtThreads, "a thread per (chunk, coefficient)");
+    using LT = LeafTma<P>;
+    extern __shared__ __align__(128) unsigned char sm[];
+    const int tid = threadIdx.x;
+    const bool comp = tid < kLtChunks * P;
+    const int ch = tid / P, m = tid - (tid / P) * P;
+    float2* part = reinterpret_cast<float2*>(sm + LT::part_off);
+    auto bar = [&](int st) { return tc5::smem_u32(sm + LT::bar_off + 8 * st); };
+    // producer cursor (thread 0): the next piece to fetch
+    int fc = blockIdx.x, fq = 0;
+    auto piece_src = [&](int c, int q, int& n, int& len) {
+        n = leaf_count[cone_box[c]];
+        len = min(kLtSrc, n - q * kLtSrc);
+        return reinterpret_cast<unsigned long long>(L + leaf_off[c] + (long long)q * kLtSrc * P);
+    };
+    auto fetch = [&](int st) {
+        if (fc >= ncones) return;
+        int n, len;
+        const unsigned long long a = piece_src(fc, fq, n, len);
+        const unsigned long long a0 = a & ~15ull;
+        const uint32_t bytes = (uint32_t)(((a - a0) + (unsigned long long)len * P * 8 + 15) & ~15ull);
+        const unsigned long long r = reinterpret_cast<unsigned long long>(rho + leaf_start[cone_box[fc]] + fq * kLtSrc);
+        const unsigned long long r0 = r & ~15ull;
+        const uint32_t rbytes = (uint32_t)(((r - r0) + (unsigned long long)len * 8 + 15) & ~15ull);
+        tc5::mbar_expect_tx(bar(st), bytes + rbytes);
+        tc5::bulk_g2s_counted(tc5::smem_u32(sm + st * LT::stage), reinterpret_cast<const void*>(a0), bytes, bar(st));
+        tc5::bulk_g2s_counted(tc5::smem_u32(sm + st * LT::stage + LT::table), reinterpret_cast<const void*>(r0), rbytes, bar(st));
+        if (++fq * kLtSrc >= n) { fq = 0; fc += gridDim.x; }
+    };
+    if (tid == 0) {
+        for (int st = 0; st < kLtStages; ++st) tc5::mbar_init(bar(st), 1);
+        for (int st = 0; st < kLtStages; ++st) fetch(st);
+    }
+    __syncthreads();
+    long long piece = 0;
+    int c = blockIdx.x, q = 0;
+    float2 acc = make_float2(0.f, 0.f);
+    bool ok = true;
+    while (c < ncones) {
+        const int st = (int)(piece % kLtStages);
+        ok = __syncthreads_and(tc5::mbar_wait(bar(st), (uint32_t)((piece / kLtStages) & 1), 2000000000ll));
+        if (!ok) break;
+        int n, len;
+        const unsigned long long a = piece_src(c, q, n, len);
+        const float2* data = reinterpret_cast<const float2*>(sm + st * LT::stage + (a & 15ull));
+        if (comp) {
+            const unsigned long long r = reinterpret_cast<unsigned long long>(rho + leaf_start[cone_box[c]] + q * kLtSrc);
+            const float2* rh = reinterpret_cast<const float2*>(sm + st * LT::stage + LT::table + (r & 15ull));
+            for (int s2 = ch; s2 < len; s2 += kLtChunks) cmac<float>(acc, data[s2 * P + m], rh[s2]);
+        }
+        __syncthreads();                        // the stage has been read
+        if (tid == 0) fetch(st);                // refill it with the piece kLtStages ahead
+        ++piece;
+        if (++q * kLtSrc >= n) {                // the cone is complete
+            if (comp) part[ch * P + m] = acc;
+            __syncthreads();
+            if (comp && ch == 0) {
+                float2 t = part[m];
+                for (int k2 = 1; k2 < kLtChunks; ++k2) { t.x += part[k2 * P + m].x; t.y += part[k2 * P + m].y; }
+                coef[(long long)(cone_base + c) * P + m] = t;
+            }
+            acc = make_float2(0.f, 0.f);
+            q = 0;
+            c += gridDim.x;
+        }
+    }
+    if (!ok && tid == 0) {   // the pieces fetched ahead may still land: one more bounded wait each
+        atomicExch(err, 1);
+        for (int i = 0; i < kLtStages; ++i) {
+            const long long p2 = piece + i;
+            tc5::mbar_wait(bar((int)(p2 % kLtStages)), (uint32_t)((p2 / kLtStages) & 1), 2000000000ll);
+        }
     }
 }
 
@@ -213,6 +314,24 @@ void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const i
     else if (chunks == 2 && 256 / (P * 2) >= 1) go(std::integral_constant<int, 2>{});
     else if (chunks == 1 || 256 / (P * 5) < 1) go(std::integral_constant<int, 1>{});
     else go(std::integral_constant<int, 5>{});
+}
+static std::atomic<int> g_leaf_tma_ready{0};
+cudaError_t leaf_tma_init() {
+    if (g_leaf_tma_ready.load()) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(k_leaf_tma<25>, cudaFuncAttributeMaxDynamicSharedMemorySize, LeafTma<25>::smem);
+    if (e == cudaSuccess) g_leaf_tma_ready.store(1);
+    return e;
+}
+bool launch_leaf_tma(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
+                     const long long* leaf_off, const float2* L, const float2* rho, int P, float2* coef, int* err, int nsm,
+                     cudaStream_t s) {
+    if (P != 25) return false;
+    if (ncones <= 0) return true;
+    if (!g_leaf_tma_ready.load()) return false;   // leaf_tma_init not run on this device
+    const int grid = std::min(ncones, 4 * std::max(nsm, 1));
+    k_leaf_tma<25><<<grid, kLtThreads, LeafTma<25>::smem, s>>>(cone_box, ncones, cone_base, leaf_start, leaf_count, leaf_off, L,
+                                                              rho, coef, err);
+    return true;
 }
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps, int Pang,
