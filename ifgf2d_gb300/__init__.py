@@ -270,6 +270,7 @@ class ForwardMap:
     BATCH_TC_PROPAGATION = 2
     BATCH_TC_LEAF_FP32 = 4
     BATCH_BULK_PROPAGATION = 8
+    BATCH_GROUPED_INTERP = 16
 
     @property
     def batch_tensor_cores(self):

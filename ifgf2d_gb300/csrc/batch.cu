@@ -28,6 +28,9 @@ struct BatchWork {
     DBuf<int> t5err;
     int nsm = 0;
     DBuf<int4> leaf_items;                     // (leaf box, first cone, end cone, 0) of the tensor-core leaf kernel
+    // the complex64 interpolation grouped by cone: work items (terms, targets) and their terms
+    DBuf<int4> ig_items;
+    DBuf<InterpG> ig_terms;
     // GMRES
     int m = 0, scap = 0;
     DBuf<double2> V, w, t, h, H, part, Y, hn, b, x, r, d, ones;
@@ -43,6 +46,42 @@ void ifgf::free_batch(ifgf2d_ctx* ctx) {
 }
 
 namespace {
+
+// The interpolation terms of each leaf box's targets, kInterpGrpTargets targets per work item,
+// sorted by cone (stable) within an item: items (first term, end term, first target, targets).
+void grouped_interp_plan(const Tree& T, std::vector<int4>& items, std::vector<InterpG>& terms) {
+    const int nleaf = (int)T.leaf_start.size();
+    std::vector<long long> item_ptr(nleaf + 1, 0), term_ptr(nleaf + 1, 0);
+    for (int b = 0; b < nleaf; ++b) {
+        const int t0 = T.leaf_start[b], n = T.leaf_count[b];
+        item_ptr[b + 1] = item_ptr[b] + (n + kInterpGrpTargets - 1) / kInterpGrpTargets;
+        term_ptr[b + 1] = term_ptr[b] + (n > 0 ? T.ip_ptr[t0 + n] - T.ip_ptr[t0] : 0);
+    }
+    items.resize(item_ptr[nleaf]);
+    terms.resize(term_ptr[nleaf]);
+    parallel_for(nleaf, [&](long long b0, long long b1) {
+        std::vector<int> idx;
+        for (long long b = b0; b < b1; ++b) {
+            const int t0 = T.leaf_start[b], n = T.leaf_count[b];
+            long long it = item_ptr[b], e = term_ptr[b];
+            for (int c0 = 0; c0 < n; c0 += kInterpGrpTargets, ++it) {
+                const int nt = std::min(kInterpGrpTargets, n - c0);
+                const int e0 = T.ip_ptr[t0 + c0], e1 = T.ip_ptr[t0 + c0 + nt];
+                idx.resize(e1 - e0);
+                for (int i = 0; i < e1 - e0; ++i) idx[i] = e0 + i;
+                std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return T.ip[a].cone < T.ip[c].cone; });
+                const long long first = e;
+                for (int i : idx) {
+                    int t = t0 + c0;
+                    while (T.ip_ptr[t + 1] <= i) ++t;   // the target owning term i
+                    const InterpEntry& q = T.ip[i];
+                    terms[e++] = InterpG{q.cone, t, (float)q.s, (float)q.th, (float)q.fr, (float)q.fi};
+                }
+                items[it] = make_int4((int)first, (int)e, t0 + c0, nt);
+            }
+        }
+    }, 64);
+}
 
 // a parent's propagation terms sorted by child cone (stable), with the parent node recorded
 template <typename R>
@@ -96,6 +135,11 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
                 for (int c = LD.cone_ptr[b]; c < LD.cone_ptr[b + 1]; c += kLeafT5Cones)
                     items.push_back(make_int4((int)b, c, std::min(c + kLeafT5Cones, LD.cone_ptr[b + 1]), 0));
             CK(W.leaf_items.upload(items));
+            std::vector<int4> gi;
+            std::vector<InterpG> gt;
+            grouped_interp_plan(ctx->T, gi, gt);
+            CK(W.ig_items.upload(gi));
+            CK(W.ig_terms.upload(gt));
         }
         if (!W.W32.p) {
             CK(W.W32.alloc(ctx->W.n));
@@ -140,9 +184,17 @@ void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* le
         }
         launch_prop_b<R>(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, s);
     }
+    bool grouped = false;
+    if constexpr (sizeof(R) == 4) grouped = (ctx->tune_batch_tc & kBatchGroupedInterp) && B <= 64 && T.Ps == 5 && T.Pang == 5;
     launch_final_b<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
-                      ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p,
-                      B, yt, s);
+                      ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, grouped ? nullptr : ip, coef, T.Ps, T.Pang,
+                      ctx->sorting.p, B, yt, s);
+    if constexpr (sizeof(R) == 4) {
+        if (grouped) {
+            BatchWork& W = *ctx->bw;
+            launch_interp_grp(W.ig_items.p, (int)W.ig_items.n, W.ig_terms.p, coef, T.Ps, T.Pang, ctx->sorting.p, B, yt, s);
+        }
+    }
 }
 
 // yt = A xt for B <= kMaxBatch interleaved right-hand sides (IFGF modes)

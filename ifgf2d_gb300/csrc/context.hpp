@@ -21,6 +21,7 @@ constexpr int kBatchTcLeaf = 1;   // leaf-cone sums (k_leaf_t5)
 constexpr int kBatchTcProp = 2;   // propagation (k_prop_t5)
 constexpr int kBatchTcLeaf6 = 4;  // leaf-cone sums with three TF32 terms per operand (6 products)
 constexpr int kBatchBulkProp = 8; // FP32 FMA propagation with TMA-staged child coefficients (k_prop_bk)
+constexpr int kBatchGroupedInterp = 16;   // interpolation grouped by cone per leaf box (k_interp_grp)
 
 namespace ifgf {
 
@@ -130,7 +131,7 @@ struct ifgf2d_ctx {
     int tune_leaf[2] = {5, 5};      // complex64 also 0: the table streamed by TMA bulk copies (k_leaf_tma)
     int tune_prop[2][kTuneLevels] = {};
     // batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (bit mask, else FP32 FMA)
-    int tune_batch_tc = kBatchTcLeaf;
+    int tune_batch_tc = kBatchTcLeaf | kBatchGroupedInterp;
     // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
     bool prep_ready = false;
     double prep_k = 0.0;

@@ -594,7 +594,7 @@ extern "C" int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* c) {
     ctx->tune_leaf[0] = c[0]; ctx->tune_leaf[1] = c[1];
     for (int p = 0; p < 2; ++p)
         for (int l = 0; l < kTuneLevels; ++l) ctx->tune_prop[p][l] = c[2 + p * kTuneLevels + l];
-    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6 | kBatchBulkProp);
+    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6 | kBatchBulkProp | kBatchGroupedInterp);
     if (ctx->gw) ctx->gw->drop_graphs();   // the captured iterations hold the old launch shapes
     return IFGF2D_OK;
 }

@@ -40,6 +40,9 @@ template <typename R> using V2 = typename Cx<R>::V;
 template <typename R> struct InterpE;
 template <> struct InterpE<double> { int cone; int pad; double s, th, fr, fi; };
 template <> struct InterpE<float> { int cone; float s, th, fr, fi; };
+// batched complex64 interpolation term, grouped by leaf box and cone: cone id, Morton target,
+// (s, theta), factor
+struct InterpG { int cone; int t; float s, th, fr, fi; };
 // one (parent cone, child, node) propagation term: child cone id, (s, theta), factor ratio
 template <typename R> struct PropE;
 template <> struct PropE<double> { int child_cone; int pad; double s, th, wr, wi; };
@@ -150,6 +153,12 @@ cudaError_t prop_t5_init_attributes();
 // the complex64 FMA propagation with each child cone's coefficient block staged in shared memory
 // by a TMA bulk copy one group ahead; false when the shape is not supported (Ps x Pang other
 // than 5 x 5, B odd or above 64) and nothing was launched
+// yt[sorting[t]] += the cousin-cone interpolation of the targets of each work item
+// items[i] = (first term, end term, first Morton target, targets <= kInterpGrpTargets), terms
+// sorted by cone within an item; complex64 coefficients [cone][P][B], B <= 64
+constexpr int kInterpGrpTargets = 8;
+bool launch_interp_grp(const int4* items, int nitems, const InterpG* terms, const float2* coef, int Ps, int Pang,
+                       const long long* sorting, int B, double2* yt, cudaStream_t s);
 bool launch_prop_bk(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
                     const float* Gsep, int B, float2* coef, int* err, cudaStream_t s);
 template <typename R>

@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ 
         }
         sg += c;
     }
-    for (int e = ip_ptr[i]; e < ip_ptr[i + 1]; ++e) {
+    for (int e = ip ? ip_ptr[i] : 0; ip && e < ip_ptr[i + 1]; ++e) {   // ip null: near field only
         const InterpE<R> E = ip[e];
         R Ts[PS], Tt[PA];
         cheb_row<R, PS>(E.s, Ts);
@@ -485,6 +485,75 @@ __global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ 
         double2 v = *yo;
         v.x += (double)acc[k].x; v.y += (double)acc[k].y;
         *yo = v;
+    }
+}
+
+// ------------------------------------------------------------------ interpolation grouped by cone
+// warp = one work item (up to kInterpGrpTargets targets of one leaf box) x 64 right-hand sides.
+// The item's terms are sorted by cone, so each cone's 25 x 64 coefficient block is loaded once
+// for every target of the item that reads it (k_final_b loads it once per target); per-target
+// sums accumulate in shared memory, then are added into yt.
+template <int PS, int PA>
+__global__ void __launch_bounds__(32) k_interp_grp(const int4* __restrict__ items, int nitems, const InterpG* __restrict__ terms,
+                                                   const float2* __restrict__ coef, const long long* __restrict__ sorting, int B,
+                                                   double2* __restrict__ yt) {
+    constexpr int P = PS * PA, RPL = 2;
+    __shared__ float2 acc[kInterpGrpTargets][32 * RPL];
+    const int it = blockIdx.x;
+    if (it >= nitems) return;
+    const int4 I = items[it];   // terms [x, y), targets [z, z + w)
+    const int lane = threadIdx.x;
+    int rr[RPL];
+    bool act[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+        const int r = 32 * k + lane;
+        act[k] = r < B;
+        rr[k] = act[k] ? r : 0;
+    }
+    for (int t = 0; t < I.w; ++t)
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) acc[t][32 * k + lane] = make_float2(0.f, 0.f);
+    __syncwarp();
+    float2 cc[RPL][P];
+    int cur = -1;
+    InterpG En{};
+    if (I.x < I.y) En = terms[I.x];
+    for (int e = I.x; e < I.y; ++e) {
+        const InterpG E = En;
+        if (e + 1 < I.y) En = terms[e + 1];     // next term in flight during this one
+        if (E.cone != cur) {                    // warp-uniform
+            cur = E.cone;
+            const float2* src = coef + (long long)cur * P * B;
+#pragma unroll
+            for (int k = 0; k < RPL; ++k)
+#pragma unroll
+                for (int q = 0; q < P; ++q) cc[k][q] = src[(long long)q * B + rr[k]];
+        }
+        float Ts[PS], Tt[PA];
+        cheb_row<float, PS>(E.s, Ts);
+        cheb_row<float, PA>(E.th, Tt);
+        const float2 f = make_float2(E.fr, E.fi);
+        const int tl = E.t - I.z;
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) {
+            float2 a = acc[tl][32 * k + lane];
+            cmac<float>(a, interp_eval_tt<float, PS, PA>(cc[k], Ts, Tt), f);
+            acc[tl][32 * k + lane] = a;
+        }
+    }
+    __syncwarp();
+    for (int t = 0; t < I.w; ++t) {
+        const long long o = sorting[I.z + t];
+#pragma unroll
+        for (int k = 0; k < RPL; ++k) {
+            if (!act[k]) continue;
+            double2* yo = yt + o * B + rr[k];
+            const float2 a = acc[t][32 * k + lane];
+            double2 v = *yo;
+            v.x += (double)a.x; v.y += (double)a.y;
+            *yo = v;
+        }
     }
 }
 
@@ -625,6 +694,13 @@ void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_
         k_prop_b<R, PS, PA, WPB, RPL><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32 * RPL)), WPB * 32, 0, s>>>(
             pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
     });
+}
+bool launch_interp_grp(const int4* items, int nitems, const InterpG* terms, const float2* coef, int Ps, int Pang,
+                       const long long* sorting, int B, double2* yt, cudaStream_t s) {
+    if (Ps != 5 || Pang != 5 || B > 64 || B <= 0) return false;
+    if (nitems <= 0) return true;
+    k_interp_grp<5, 5><<<nitems, 32, 0, s>>>(items, nitems, terms, coef, sorting, B, yt);
+    return true;
 }
 bool launch_prop_bk(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
                     const float* Gsep, int B, float2* coef, int* err, cudaStream_t s) {

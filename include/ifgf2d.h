@@ -243,6 +243,7 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
 #define IFGF2D_BATCH_TC_PROPAGATION 2   /* propagation, 3xTF32 */
 #define IFGF2D_BATCH_TC_LEAF_FP32 4     /* leaf-cone sums, three TF32 terms per operand (6 products) */
 #define IFGF2D_BATCH_BULK_PROPAGATION 8 /* FP32 FMA propagation, child coefficients staged by TMA bulk copies */
+#define IFGF2D_BATCH_GROUPED_INTERP 16  /* complex64 interpolation grouped by cone per leaf box */
 int ifgf2d_tuning_size(void);
 int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices);
 int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices);

@@ -71,7 +71,8 @@ def test_gpu_batch_tensor_core_kernels(lib, oracle, k, npatch, nrhs):
     # order (B even; an odd batch falls back to the global-load kernel)
     fm.batch_tensor_cores = fm.BATCH_BULK_PROPAGATION
     assert np.array_equal(fm.apply_batch(X, mixed=True), Yf)
-    for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_LEAF_FP32, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION):
+    for mask in (fm.BATCH_TC_LEAF, fm.BATCH_TC_LEAF_FP32, fm.BATCH_TC_PROPAGATION, fm.BATCH_TC_LEAF | fm.BATCH_TC_PROPAGATION,
+                 fm.BATCH_GROUPED_INTERP, fm.BATCH_GROUPED_INTERP | fm.BATCH_TC_LEAF):
         fm.batch_tensor_cores = mask
         assert fm.batch_tensor_cores == mask
         Yt = fm.apply_batch(X, mixed=True)
