@@ -489,71 +489,50 @@ __global__ void __launch_bounds__(256) k_final_b(int N, const int* __restrict__ 
 }
 
 // ------------------------------------------------------------------ interpolation grouped by cone
-// warp = one work item (up to kInterpGrpTargets targets of one leaf box) x 64 right-hand sides.
-// The item's terms are sorted by cone, so each cone's 25 x 64 coefficient block is loaded once
-// for every target of the item that reads it (k_final_b loads it once per target); per-target
-// sums accumulate in shared memory, then are added into yt.
+// Two warps = one work item (up to kInterpGrpTargets targets of one leaf box), 32 right-hand
+// sides each.  The item's terms are sorted by cone, so each cone's 25 x B coefficient block is
+// loaded once for every target of the item that reads it (k_final_b loads it once per target);
+// per-target sums accumulate in shared memory, then are added into yt.
 template <int PS, int PA>
-__global__ void __launch_bounds__(32) k_interp_grp(const int4* __restrict__ items, int nitems, const InterpG* __restrict__ terms,
+__global__ void __launch_bounds__(64) k_interp_grp(const int4* __restrict__ items, int nitems, const InterpG* __restrict__ terms,
                                                    const float2* __restrict__ coef, const long long* __restrict__ sorting, int B,
                                                    double2* __restrict__ yt) {
-    constexpr int P = PS * PA, RPL = 2;
-    __shared__ float2 acc[kInterpGrpTargets][32 * RPL];
+    constexpr int P = PS * PA;
+    __shared__ float2 acc[kInterpGrpTargets][64];
     const int it = blockIdx.x;
     if (it >= nitems) return;
     const int4 I = items[it];   // terms [x, y), targets [z, z + w)
-    const int lane = threadIdx.x;
-    int rr[RPL];
-    bool act[RPL];
-#pragma unroll
-    for (int k = 0; k < RPL; ++k) {
-        const int r = 32 * k + lane;
-        act[k] = r < B;
-        rr[k] = act[k] ? r : 0;
-    }
-    for (int t = 0; t < I.w; ++t)
-#pragma unroll
-        for (int k = 0; k < RPL; ++k) acc[t][32 * k + lane] = make_float2(0.f, 0.f);
-    __syncwarp();
-    float2 cc[RPL][P];
+    const int r = threadIdx.x;  // this thread's right-hand side
+    const bool act = r < B;
+    const int rr = act ? r : 0;
+    for (int t = 0; t < I.w; ++t) acc[t][r] = make_float2(0.f, 0.f);   // each thread its own column
+    float2 cc[P];
     int cur = -1;
     InterpG En{};
     if (I.x < I.y) En = terms[I.x];
     for (int e = I.x; e < I.y; ++e) {
         const InterpG E = En;
         if (e + 1 < I.y) En = terms[e + 1];     // next term in flight during this one
-        if (E.cone != cur) {                    // warp-uniform
+        if (E.cone != cur) {                    // uniform over the block
             cur = E.cone;
             const float2* src = coef + (long long)cur * P * B;
 #pragma unroll
-            for (int k = 0; k < RPL; ++k)
-#pragma unroll
-                for (int q = 0; q < P; ++q) cc[k][q] = src[(long long)q * B + rr[k]];
+            for (int q = 0; q < P; ++q) cc[q] = src[(long long)q * B + rr];
         }
         float Ts[PS], Tt[PA];
         cheb_row<float, PS>(E.s, Ts);
         cheb_row<float, PA>(E.th, Tt);
-        const float2 f = make_float2(E.fr, E.fi);
-        const int tl = E.t - I.z;
-#pragma unroll
-        for (int k = 0; k < RPL; ++k) {
-            float2 a = acc[tl][32 * k + lane];
-            cmac<float>(a, interp_eval_tt<float, PS, PA>(cc[k], Ts, Tt), f);
-            acc[tl][32 * k + lane] = a;
-        }
+        float2 a = acc[E.t - I.z][r];
+        cmac<float>(a, interp_eval_tt<float, PS, PA>(cc, Ts, Tt), make_float2(E.fr, E.fi));
+        acc[E.t - I.z][r] = a;
     }
-    __syncwarp();
+    if (!act) return;
     for (int t = 0; t < I.w; ++t) {
-        const long long o = sorting[I.z + t];
-#pragma unroll
-        for (int k = 0; k < RPL; ++k) {
-            if (!act[k]) continue;
-            double2* yo = yt + o * B + rr[k];
-            const float2 a = acc[t][32 * k + lane];
-            double2 v = *yo;
-            v.x += (double)a.x; v.y += (double)a.y;
-            *yo = v;
-        }
+        double2* yo = yt + sorting[I.z + t] * B + r;
+        const float2 a = acc[t][r];
+        double2 v = *yo;
+        v.x += (double)a.x; v.y += (double)a.y;
+        *yo = v;
     }
 }
 
@@ -699,7 +678,7 @@ bool launch_interp_grp(const int4* items, int nitems, const InterpG* terms, cons
                        const long long* sorting, int B, double2* yt, cudaStream_t s) {
     if (Ps != 5 || Pang != 5 || B > 64 || B <= 0) return false;
     if (nitems <= 0) return true;
-    k_interp_grp<5, 5><<<nitems, 32, 0, s>>>(items, nitems, terms, coef, sorting, B, yt);
+    k_interp_grp<5, 5><<<nitems, 64, 0, s>>>(items, nitems, terms, coef, sorting, B, yt);
     return true;
 }
 bool launch_prop_bk(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<float>* pb, int Ps, int Pang,
