@@ -231,14 +231,15 @@ int ifgf2d_last_refinements(const ifgf2d_ctx* ctx);
 int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]);
 
 /* Launch-shape autotuner (no counterpart in the reference): times every launch shape of the
- * leaf-cone kernel (source chunks per coefficient 1, 2, 5, 10) and of each level's propagation
+ * leaf-cone kernel (source chunks per coefficient 1, 2, 5, 10; complex64 also 0, the table
+ * streamed through shared memory by TMA bulk copies) and of each level's propagation
  * (2, 4 or the most cones per block) on this context's own tables, in both precisions, and
  * keeps the fastest.  The table has ifgf2d_tuning_size() ints: leaf FP64, leaf complex64, then
  * per precision one propagation entry per level (0 = the most cones per block), then a bit
  * mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor cores
- * (IFGF2D_BATCH_TC_LEAF, the default, IFGF2D_BATCH_TC_PROPAGATION; FP32 FMA otherwise).  get /
- * set read and restore it (e.g. from an on-disk cache); applies use the context's current
- * table. */
+ * (IFGF2D_BATCH_TC_*; FP32 FMA otherwise) and of the other batched kernel choices below;
+ * the default is IFGF2D_BATCH_TC_LEAF | IFGF2D_BATCH_GROUPED_INTERP.  get / set read and restore
+ * it (e.g. from an on-disk cache); applies use the context's current table. */
 #define IFGF2D_BATCH_TC_LEAF 1          /* leaf-cone sums, 3xTF32 (two TF32 terms per operand) */
 #define IFGF2D_BATCH_TC_PROPAGATION 2   /* propagation, 3xTF32 */
 #define IFGF2D_BATCH_TC_LEAF_FP32 4     /* leaf-cone sums, three TF32 terms per operand (6 products) */
