@@ -383,7 +383,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     CK(ctx->leaf_cone_box.upload(LD.cone_box)); CK(ctx->leaf_off.upload(loff));
     CK(ctx->leafL.alloc(loff[ncl]));
     launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,
-                      ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, P, k, ctx->form, ctx->eta, ctx->Gm.p,
+                      ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, T.Ps, T.Pang, k, ctx->form, ctx->eta, ctx->Gsep.p,
                       ctx->leafL.p, ctx->stream);
     CK(cudaGetLastError());
     // propagation and interpolation plans

@@ -65,31 +65,78 @@ __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __re
 // One warp per (leaf cone, source): lanes are the P interpolation nodes; each lane evaluates
 // G(source, node) / (e^{ikr}/sqrt r), then the values-to-coefficients map (Interpolator.h:81-120)
 // is applied across lanes.  L layout: [cone][source][coefficient].
-__global__ void k_leaf_setup(const int* __restrict__ cone_box, int ncones, const int* __restrict__ leaf_start,
-                             const int* __restrict__ leaf_count, const long long* __restrict__ leaf_off,
-                             const LeafNode* __restrict__ nodes, const double* __restrict__ xs,
-                             const double* __restrict__ ys, const double* __restrict__ nxs, const double* __restrict__ nys,
-                             int P, double k, int form, double eta, const double* __restrict__ Gm,
-                             double2* __restrict__ L) {
-    extern __shared__ double sG[];
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) sG[i] = Gm[i];
+// block = one leaf cone, warp = one source at a time: the Green values at the cone's P nodes
+// (node l * Ps + q: angular l, radial q) times 1/factorization, then the values -> coefficients
+// map in separable form through the warp's shared memory, u[l][m] = sum_q Gs[m][q] h[l][q] and
+// c[n * Ps + m] = sum_l Ga[n][l] u[l][m].  Up to 64 nodes (two per lane).
+constexpr int kLeafSetupWarps = 8;
+__global__ void __launch_bounds__(kLeafSetupWarps * 32) k_leaf_setup(const int* __restrict__ cone_box, int ncones,
+                                                                     const int* __restrict__ leaf_start,
+                                                                     const int* __restrict__ leaf_count,
+                                                                     const long long* __restrict__ leaf_off,
+                                                                     const LeafNode* __restrict__ nodes, const double* __restrict__ xs,
+                                                                     const double* __restrict__ ys, const double* __restrict__ nxs,
+                                                                     const double* __restrict__ nys, int Ps, int Pa, double k, int form,
+                                                                     double eta, const double* __restrict__ Gsep,
+                                                                     double2* __restrict__ L) {
+    __shared__ double sG[2 * 64];
+    __shared__ double2 hv[kLeafSetupWarps][64], uv[kLeafSetupWarps][64];
+    for (int i = threadIdx.x; i < Ps * Ps + Pa * Pa; i += blockDim.x) sG[i] = Gsep[i];
     __syncthreads();
+    const double* Gs = sG;
+    const double* Ga = sG + Ps * Ps;
+    const int P = Ps * Pa;
     const int c = blockIdx.x;
     if (c >= ncones) return;
     const int b = cone_box[c];
     const int n = leaf_count[b], s0 = leaf_start[b];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    LeafNode nd = lane < P ? nodes[(long long)c * P + lane] : LeafNode{0, 0, 0, 0};
-    for (int s = warp; s < n; s += nw) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    LeafNode nd[2];
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+        const int q = lane + 32 * h2;
+        nd[h2] = q < P ? nodes[(long long)c * P + q] : LeafNode{0, 0, 0, 0};
+    }
+    for (int s = warp; s < n; s += kLeafSetupWarps) {
         const int j = s0 + s;
-        double2 h = make_double2(0.0, 0.0);
-        if (lane < P) h = cmul(green_form(form, nd.x - xs[j], nd.y - ys[j], nxs[j], nys[j], k, eta), make_double2(nd.ir, nd.ii));
-        double2 acc = make_double2(0.0, 0.0);
-        for (int q = 0; q < P; ++q) {
-            const double hx = __shfl_sync(0xffffffffu, h.x, q), hy = __shfl_sync(0xffffffffu, h.y, q);
-            if (lane < P) { const double g = sG[lane * P + q]; acc.x = fma(g, hx, acc.x); acc.y = fma(g, hy, acc.y); }
+        const double xj = xs[j], yj = ys[j], nxj = nxs[j], nyj = nys[j];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int q = lane + 32 * h2;
+            if (q < P)
+                hv[warp][q] = cmul(green_form(form, nd[h2].x - xj, nd[h2].y - yj, nxj, nyj, k, eta), make_double2(nd[h2].ir, nd[h2].ii));
         }
-        if (lane < P) L[leaf_off[c] + (long long)s * P + lane] = acc;
+        __syncwarp();
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int o = lane + 32 * h2;
+            if (o < P) {
+                const int l = o / Ps, m = o - (o / Ps) * Ps;
+                double2 u = make_double2(0.0, 0.0);
+                for (int q = 0; q < Ps; ++q) {
+                    const double g = Gs[m * Ps + q];
+                    const double2 v = hv[warp][l * Ps + q];
+                    u.x = fma(g, v.x, u.x); u.y = fma(g, v.y, u.y);
+                }
+                uv[warp][o] = u;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int o = lane + 32 * h2;
+            if (o < P) {
+                const int nn = o / Ps, m = o - (o / Ps) * Ps;
+                double2 a = make_double2(0.0, 0.0);
+                for (int l = 0; l < Pa; ++l) {
+                    const double g = Ga[nn * Pa + l];
+                    const double2 v = uv[warp][l * Ps + m];
+                    a.x = fma(g, v.x, a.x); a.y = fma(g, v.y, a.y);
+                }
+                L[leaf_off[c] + (long long)s * P + o] = a;
+            }
+        }
+        __syncwarp();   // hv and uv are rewritten for the next source
     }
 }
 
@@ -382,11 +429,11 @@ void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* 
                                        nsp, k, form, eta, near);
 }
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
-                       const LeafNode* nodes, const double* xs, const double* ys, const double* nxs, const double* nys, int P,
-                       double k, int form, double eta, const double* Gm, double2* L, cudaStream_t s) {
-    if (ncones <= 0) return;
-    k_leaf_setup<<<ncones, 256, P * P * sizeof(double), s>>>(cone_box, ncones, leaf_start, leaf_count, leaf_off, nodes, xs, ys,
-                                                             nxs, nys, P, k, form, eta, Gm, L);
+                       const LeafNode* nodes, const double* xs, const double* ys, const double* nxs, const double* nys, int Ps,
+                       int Pang, double k, int form, double eta, const double* Gsep, double2* L, cudaStream_t s) {
+    if (ncones <= 0 || Ps * Pang > 64 || Ps * Ps + Pang * Pang > 128) return;
+    k_leaf_setup<<<ncones, kLeafSetupWarps * 32, 0, s>>>(cone_box, ncones, leaf_start, leaf_count, leaf_off, nodes, xs, ys, nxs, nys, Ps, Pang, k,
+                                        form, eta, Gsep, L);
 }
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols,
                        int N, int Np, double half, double2* y, cudaStream_t s) {

@@ -67,10 +67,13 @@ void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* 
                        const long long* near_off, int nleaf, const double* xs, const double* ys,
                        const double* nxs, const double* nys, const int* patch_s, const int* nsp_ptr,
                        const int* nsp, double k, int form, double eta, double2* near, cudaStream_t s);
+// leaf-cone tables: Green values at the cone nodes times 1/factorization, mapped to Chebyshev
+// coefficients with the separable map Gsep (Ps x Ps radial, then Pang x Pang angular);
+// Ps * Pang <= 64
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count,
                        const long long* leaf_off, const LeafNode* nodes, const double* xs, const double* ys,
-                       const double* nxs, const double* nys, int P, double k, int form, double eta,
-                       const double* Gm, double2* L, cudaStream_t s);
+                       const double* nxs, const double* nys, int Ps, int Pang, double k, int form, double eta,
+                       const double* Gsep, double2* L, cudaStream_t s);
 
 // ---------------- per-apply kernels ----------------
 // y = singular correction (+ half * x: the jump term of the combined formulation)

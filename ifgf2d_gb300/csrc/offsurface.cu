@@ -114,7 +114,8 @@ extern "C" int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const 
         CK(W.leaf_cone_box.upload(LD.cone_box)); CK(W.leaf_off.upload(loff));
         CK(W.leafL.alloc(loff[ncl]));
         launch_leaf_setup(W.leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, W.leaf_off.p, W.nodes.p, ctx->xs_s.p,
-                          ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, P, ctx->k, ctx->form, ctx->eta, ctx->Gm.p, W.leafL.p, s);
+                          ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, ctx->T.Ps, ctx->T.Pang, ctx->k, ctx->form, ctx->eta, ctx->Gsep.p,
+                          W.leafL.p, s);
         CK(cudaGetLastError());
     }
     static_assert(sizeof(PropEntry) == sizeof(PropEntryD) && sizeof(InterpEntry) == sizeof(InterpEntryD),

@@ -93,6 +93,28 @@ def test_gpu_ifgf_matches_oracle_ifgf(lib, oracle, k, npatch, nlevels):
     assert rel(far, om.direct_excluded(d * w)) < 5e-4
 
 
+@pytest.mark.parametrize("Ps,Pang", [(3, 3), (3, 5), (4, 4), (5, 7), (6, 6), (7, 7)])
+def test_gpu_ifgf_interpolation_orders_match_oracle(lib, oracle, Ps, Pang):
+    """Every compiled cone interpolation order besides 5 x 5 (up to 49 nodes per cone) against
+    the oracle's IFGF on the same tree; the complex64 single and batched applies against FP64."""
+    k = 100.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, 4.0, Np=16, Ps=Ps, Pang=Pang, patches_per_curve=128)
+    om = oracle.OracleForwardMap([oracle.curve_kite()], 16, 0.01, 1.0, k, 4.0, patches_per_curve=128)
+    fm.precomps_and_setup(k, 0)
+    om.precompute(k)
+    om.setup_ifgf(k, fm.nlevels, Ps, Pang)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    y = fm.compute_Ax_acc(d)
+    assert rel(y, om.compute_Ax_acc(d)) < 1e-11
+    assert rel(fm.compute_Ax_acc(d, mixed=True), y) < 2e-6
+    X = np.stack([d, (0.5 - 1j) * d[::-1]], axis=1)
+    Y = fm.apply_batch(X)
+    Ym = fm.apply_batch(X, mixed=True)
+    assert rel(Y[:, 0], y) < 1e-13
+    for r in range(2):
+        assert rel(Ym[:, r], Y[:, r]) < 2e-6, r
+
+
 def test_gpu_ifgf_against_direct_config2_size(lib, oracle):
     """Config 2 geometry (kite, k=500, 512 patches x 16 = 8192): IFGF vs the direct map."""
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 500.0, Np=16, patches_per_curve=512)
