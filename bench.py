@@ -264,6 +264,26 @@ def run_ours(args, rank, local_rank, world):
                          "frac": (flops_d / (acc[dom] * 1e-3) / 1e12) / max(fp64_peak.value, 1e-9),
                          "peak_source": "measured (ifgf2d_measure_fp64_peak)"},
                 "phase_ms": dict(zip(phases, [float(v) for v in acc]))}
+    # every phase against its own roof (FP64 pipe or HBM), weighted by its time
+    per_phase = {}
+    for i, ph in enumerate(phases):
+        b_i, f_i = model[ph]
+        t_i = acc[i] * 1e-3
+        per_phase[ph] = max(b_i / t_i / 1e9 / hbm, f_i / t_i / 1e12 / max(fp64_peak.value, 1e-9))
+    roofline["time_weighted"] = {"frac": float(sum(acc[i] * per_phase[ph] for i, ph in enumerate(phases)) / acc.sum()),
+                                 "per_phase_frac": per_phase,
+                                 "roofs": "each phase: max(HBM bytes / measured copy GB/s, FP64 flops / measured FP64 peak)"}
+    # the fixed nominal weights of the work model: 60 flops per Hankel value, 20 per e^{ikr}/sqrt(r),
+    # 8 per complex multiply-add; compulsory HBM bytes with complex128 = 16 B
+    F_H, F_E = 60, 20
+    sing_mv = wc["sing_entries"] + fm.num_patches_ * NP * NP
+    nom_flops = (wc["near_pairs"] * (8 + F_H) + wc["leaf_evals"] * (8 + F_H) + wc["prop_evals"] * (8 * P + F_E)
+                 + wc["interp_evals"] * (8 * P + F_E) + wc["cones"] * P * 2 * (fm.Ps + fm.Pang) * 4 + 8 * sing_mv)
+    nom_bytes = N * (32 + 16 + 16) + 16 * wc["sing_entries"] + 2 * 16 * P * wc["cones"]
+    t_mv = ms / args.steps * 1e-3
+    roofline["nominal_model"] = {"flops_per_matvec": int(nom_flops), "bytes_per_matvec": int(nom_bytes),
+                                 "tflops": nom_flops / t_mv / 1e12, "gbs": nom_bytes / t_mv / 1e9,
+                                 "weights": {"hankel": F_H, "exp_over_sqrt": F_E, "complex_mac": 8}}
     # GMRES solve to 1e-6 (plane wave at angle 0), plain FP64 IFGF
     solve = None
     if not args.no_solve:
@@ -308,6 +328,8 @@ def run_ours(args, rank, local_rank, world):
     }
     if world > 1:   # the extra workloads are single-GPU measurements, reported at N = 1
         return out
+    if not args.no_solve:
+        out["config1"] = run_config1(G)
     if not args.no_batch:
         del fm
         torch.cuda.synchronize()
@@ -351,6 +373,43 @@ def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
         res[f"kite_k{int(k)}"] = row
         del fm
     return res
+
+
+def run_config1(G, repeats=5):
+    """Unit circle, k = 10, 20 equal patches x 10 Fejer nodes (N = 200), combined field with
+    eta = k, direct operator with the rectangular-polar singular weights, plane wave at angle 0,
+    GMRES to 1e-10.  Device: precomputation + GMRES through the public API with host vectors
+    (median of the repeats after the first).  CPU: the oracle's precomputation + Householder
+    GMRES on one thread, as the reference runs (median of the second and third of three runs)."""
+    from oracle import oracle as O
+    O.build()
+    k = 10.0
+    fm = G.ForwardMap(DELTA, [G.Circle()], (), 1.0, k, Np=10, patches_per_curve=20, formulation="combined")
+    b = -np.exp(1j * k * fm.xs_)
+    dev = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        x = fm.solve(b, k, accelerated=False, tol=1e-10)
+        dev.append(time.perf_counter() - t0)
+    it_dev = fm.last_solve["iters"]
+    res_dev = float(np.linalg.norm(fm.compute_Ax_unacc(x) - b) / np.linalg.norm(b))
+    om = O.OracleForwardMap([O.curve_circle()], 10, DELTA, 1.0, k, patches_per_curve=20, formulation="combined")
+    cpu = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        om.precompute(k)
+        xo, info = om.solve(b, False, tol=1e-10)
+        cpu.append(time.perf_counter() - t0)
+    res_cpu = float(np.linalg.norm(om.compute_Ax_unacc(xo) - b) / np.linalg.norm(b))
+    return {"workload": "unit circle k=10, 20 equal patches x 10 (N=200), combined field eta=k, direct operator, "
+                        "plane wave at angle 0, GMRES to 1e-10",
+            "N": fm.total_num_unknowns_,
+            "device": {"seconds": float(np.median(dev[1:])), "seconds_first_call": dev[0], "iters": it_dev,
+                       "true_rel_residual": res_dev, "path": "ifgf2d_precompute + ifgf2d_solve, host vectors"},
+            "cpu_oracle_1_thread": {"seconds": float(np.median(cpu[1:])), "iters": int(info["iters"]),
+                                    "true_rel_residual": res_cpu,
+                                    "path": "oracle precompute + Householder GMRES (opGMRES.hpp:68-269)"},
+            "rel_diff_solutions": float(np.linalg.norm(x - xo) / np.linalg.norm(xo))}
 
 
 def run_large(G, k=8000.0, npatch=8192):
@@ -594,6 +653,8 @@ def main():
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = time_oracle(budget_s=12.0)
+            one = time_oracle(budget_s=6.0, threads=1)
+            out["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": one["unit"], "sample": one["sample"]}
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -230,6 +230,47 @@ __global__ void __launch_bounds__(kTile) k_direct_far(const double* __restrict__
     }
 }
 
+// The same sum with one 128-thread block per target, for target counts that would leave most
+// SMs idle with one thread per target (N = 200: 2 blocks).  Thread t takes sources t, t + 128, ...;
+// the partial sums combine in a fixed order (warp butterfly, then warps 0..3), so the result
+// does not depend on scheduling.
+constexpr int kDirectSplitBelow = 2 * 152 * kTile;
+__global__ void __launch_bounds__(kTile) k_direct_far_split(const double* __restrict__ tx, const double* __restrict__ ty,
+                             const int* __restrict__ t_patch, const int* __restrict__ t_nsp_ptr, const int* __restrict__ t_nsp,
+                             const double* __restrict__ sx, const double* __restrict__ sy, const double* __restrict__ snx,
+                             const double* __restrict__ sny, const int* __restrict__ s_patch,
+                             const double2* __restrict__ rho, int ns, double k, int form, double eta,
+                             double2* __restrict__ y, int accumulate) {
+    __shared__ double2 part[kTile / 32];
+    const int i = blockIdx.x;
+    const double xi = tx[i], yi = ty[i];
+    const int pi = t_patch ? t_patch[i] : -1;
+    int ex[8], nex = 0;
+    if (t_nsp_ptr) for (int q = t_nsp_ptr[i]; q < t_nsp_ptr[i + 1] && nex < 8; ++q) ex[nex++] = t_nsp[q];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = threadIdx.x; j < ns; j += kTile) {
+        bool skip = false;
+        if (s_patch) {
+            const int pj = s_patch[j];
+            skip = (pj == pi);
+            for (int q = 0; q < nex; ++q) skip |= (ex[q] == pj);
+        }
+        if (!skip) cfma(acc, green_form(form, xi - sx[j], yi - sy[j], snx ? snx[j] : 0.0, sny ? sny[j] : 0.0, k, eta), rho[j]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = part[0];
+        for (int w = 1; w < kTile / 32; ++w) t = cadd(t, part[w]);
+        if (accumulate) { const double2 v = y[i]; y[i] = cadd(v, t); } else y[i] = t;
+    }
+}
+
 // ------------------------------------------------------------------ tests and GMRES helpers
 __global__ void k_hankel(int order, const double* __restrict__ x, int n, double2* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,8 +493,12 @@ void launch_direct_far(const double* tx, const double* ty, int nt, const int* t_
                        const double* sx, const double* sy, const double* snx, const double* sny, const int* s_patch,
                        const double2* rho, int ns, double k, int form, double eta, double2* y, int accumulate, cudaStream_t s) {
     if (nt <= 0) return;
-    k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, snx, sny, s_patch, rho, ns, k,
-                                                   form, eta, y, accumulate);
+    if (nt < kDirectSplitBelow)
+        k_direct_far_split<<<nt, kTile, 0, s>>>(tx, ty, t_patch, t_nsp_ptr, t_nsp, sx, sy, snx, sny, s_patch, rho, ns, k, form, eta,
+                                                y, accumulate);
+    else
+        k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, snx, sny, s_patch, rho, ns, k,
+                                                       form, eta, y, accumulate);
 }
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s) {
     if (n <= 0) return;
