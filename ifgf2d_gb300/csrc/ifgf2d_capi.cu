@@ -1011,7 +1011,7 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
 
 // ------------------------------------------------------------------ Hankel test entry
 extern "C" int ifgf2d_hankel(int order, long long n, const double* x, double* out) {
-    if (order < 0 || order > 1 || n < 0 || (n > 0 && (!x || !out))) return IFGF2D_ERR_ARG;
+    if (order < 0 || order > 3 || n < 0 || (n > 0 && (!x || !out))) return IFGF2D_ERR_ARG;
     if (n == 0) return IFGF2D_OK;
     if (n > (1LL << 30)) return IFGF2D_ERR_ARG;
     DBuf<double> dx; DBuf<double2> dout;

@@ -275,6 +275,12 @@ __global__ void __launch_bounds__(kTile) k_direct_far_split(const double* __rest
 __global__ void k_hankel(int order, const double* __restrict__ x, int n, double2* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order >= 2) {   // the fused evaluator of the combined-field kernel: 2 -> its H0, 3 -> its H1
+        double2 h0, h1;
+        hankel01(x[i], h0, h1);
+        out[i] = order == 2 ? h0 : h1;
+        return;
+    }
     out[i] = order == 0 ? hankel1<0>(x[i]) : hankel1<1>(x[i]);
 }
 

@@ -210,7 +210,9 @@ int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, do
 int ifgf2d_get_geometry_features(const ifgf2d_ctx* ctx, double* geom);
 
 /* Device Hankel evaluator (replaces sp_bessel::hankelH1, complex_bessel
- * besselFunctions.h:313-341, for real arguments): out[i] = H_order^(1)(x[i]), order 0 or 1. */
+ * besselFunctions.h:313-341, for real arguments): out[i] = H_order^(1)(x[i]), order 0 or 1.
+ * Orders 2 and 3 give H0 and H1 from the fused evaluator of the combined-field kernel (both
+ * orders of one argument at once); they equal orders 0 and 1 bit for bit. */
 int ifgf2d_hankel(int order, long long n, const double* x, double* out);
 
 /* The context's CUDA stream (cudaStream_t) for callers that time or order work on it. */

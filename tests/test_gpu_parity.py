@@ -34,6 +34,14 @@ def test_gpu_hankel_dense_sweep(lib, oracle):
         assert r.max() < 5e-15, (order, r.max(), x[r.argmax()])
 
 
+def test_gpu_hankel_fused_orders_equal_separate(lib):
+    """The combined-field kernel evaluates H0 and H1 of one argument together; each equals the
+    separate evaluation bit for bit in all three regions (series, Chebyshev pieces, asymptotic)."""
+    x = np.concatenate([np.logspace(-6, 5, 200_000), [2.999999, 3.0, 24.999999, 25.0]])
+    for order in (0, 1):
+        assert np.array_equal(lib.hankel1(order + 2, x), lib.hankel1(order, x)), order
+
+
 def _pair(lib, oracle, kind, Np, delta, wl, k, p=4.0, ppc=0, form="single_layer"):
     gc = {"circle": lib.Circle(), "kite": lib.Kite(), "line": lib.Line(-1, -0.2, 1, -0.2)}[kind]
     oc = {"circle": oracle.curve_circle(), "kite": oracle.curve_kite(), "line": oracle.curve_line(-1, -0.2, 1, -0.2)}[kind]
