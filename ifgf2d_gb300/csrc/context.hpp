@@ -171,6 +171,7 @@ struct ifgf2d_ctx {
     DBuf<double2> coef;
     DBuf<double> Gm, Gsep;          // full and separable values->coefficients maps
     DBuf<int> near_rowlen;          // per leaf box: sources in its 3x3 neighbourhood
+    DBuf<int> near_src_off, near_src;   // per leaf box: the Morton indices of those sources, in row order
     // complex64 copies of the IFGF tables (mixed form)
     DBuf<float2> near32, leafL32, coef32, rho32;
     DBuf<PropE<float>> pp32;

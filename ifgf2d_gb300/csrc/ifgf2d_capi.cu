@@ -333,9 +333,16 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     }
     CK(ctx->near_off.upload(noff));
     {
-        std::vector<int> rl(nleaf);
-        for (int b = 0; b < nleaf; ++b) rl[b] = (int)((noff[b + 1] - noff[b]) / std::max(1, T.leaf_count[b]));
+        std::vector<int> rl(nleaf), soff(nleaf + 1, 0), src;
+        for (int b = 0; b < nleaf; ++b) {
+            rl[b] = (int)((noff[b + 1] - noff[b]) / std::max(1, T.leaf_count[b]));
+            for (int q = T.nbr_ptr[b]; q < T.nbr_ptr[b + 1]; ++q)   // the row order of the near table
+                for (int j = 0; j < T.leaf_count[T.nbr_box[q]]; ++j) src.push_back(T.leaf_start[T.nbr_box[q]] + j);
+            soff[b + 1] = (int)src.size();
+        }
         CK(ctx->near_rowlen.upload(rl));
+        CK(ctx->near_src_off.upload(soff));
+        CK(ctx->near_src.upload(src));
     }
     CK(ctx->near.alloc(noff[nleaf]));
     launch_near_setup(ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p, ctx->near_off.p, nleaf,
@@ -484,7 +491,7 @@ static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, con
                               T.Ps, T.Pang, Gsep, coef, s, l < kTuneLevels ? ctx->tune_prop[pr][l] : 0);
     }
     if (ev) cudaEventRecord(ev[1], s);
-    launch_final_t<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p,
+    launch_final_t<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->near_src_off.p, ctx->near_src.p,
                       ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p, y, s);
 }
 

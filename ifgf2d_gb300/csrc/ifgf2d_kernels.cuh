@@ -108,8 +108,8 @@ template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
                         int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block = 0);
 template <typename R>
-void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
-                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near,
+void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* near_src_off, const int* near_src,
+                    const int* near_rowlen, const long long* near_off, const V2<R>* near,
                     const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
                     const long long* sorting, double2* y, cudaStream_t s);
 void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s);

@@ -246,11 +246,13 @@ __global__ void __launch_bounds__(256) k_propagate_t(int pbegin, int pend, const
     }
 }
 
-// one warp per Morton-sorted target; near row layout [target][neighbour sources]
+// one warp per Morton-sorted target; near row layout [target][neighbour sources], and
+// near_src[near_src_off[b] + e] the Morton index of entry e's source in leaf box b's rows, so the
+// lanes stride over one flat row with independent loads
 template <typename R, int PS, int PA>
 __global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
-                                                 const int* __restrict__ leaf_count, const int* __restrict__ nbr_ptr,
-                                                 const int* __restrict__ nbr_box, const int* __restrict__ near_rowlen,
+                                                 const int* __restrict__ near_src_off, const int* __restrict__ near_src,
+                                                 const int* __restrict__ near_rowlen,
                                                  const long long* __restrict__ near_off, const V2<R>* __restrict__ near,
                                                  const V2<R>* __restrict__ rho, const int* __restrict__ ip_ptr,
                                                  const InterpE<R>* __restrict__ ip, const V2<R>* __restrict__ coef,
@@ -261,15 +263,12 @@ __global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ 
     if (i >= N) return;
     const int b = point_leaf[i];
     const int t = i - leaf_start[b];
-    const V2<R>* row = near + near_off[b] + (long long)t * near_rowlen[b];
+    const int rl = near_rowlen[b];
+    const V2<R>* row = near + near_off[b] + (long long)t * rl;
+    const int* src = near_src + near_src_off[b];
     V2<R> acc; acc.x = R(0); acc.y = R(0);
-    int sg = 0;
-    for (int q = nbr_ptr[b]; q < nbr_ptr[b + 1]; ++q) {
-        const int bb = nbr_box[q];
-        const int c = leaf_count[bb], s0 = leaf_start[bb];
-        for (int s = lane; s < c; s += 32) cmac<R>(acc, row[sg + s], rho[s0 + s]);
-        sg += c;
-    }
+#pragma unroll 4
+    for (int e = lane; e < rl; e += 32) cmac<R>(acc, row[e], rho[src[e]]);
     for (int e = ip_ptr[i] + lane; e < ip_ptr[i + 1]; e += 32) {
         const InterpE<R> E = ip[e];
         const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.cone * P, E.s, E.th);
@@ -350,12 +349,12 @@ void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int
     });
 }
 template <typename R>
-void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* nbr_ptr,
-                    const int* nbr_box, const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
+void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* near_src_off, const int* near_src,
+                    const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
                     const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang, const long long* sorting,
                     double2* y, cudaStream_t s) {
     IFGF_DISPATCH_P(Ps, Pang, (k_final_t<R, PS, PA><<<nblk_a((long long)N * 32, 256), 256, 0, s>>>(
-                                   N, point_leaf, leaf_start, leaf_count, nbr_ptr, nbr_box, near_rowlen, near_off, near, rho,
+                                   N, point_leaf, leaf_start, near_src_off, near_src, near_rowlen, near_off, near, rho,
                                    ip_ptr, ip, coef, sorting, y)));
 }
 void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
@@ -368,7 +367,7 @@ void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
                                          const V2<R>*, int, V2<R>*, cudaStream_t, int);                               \
     template void launch_propagate_t<R>(int, int, const long long*, const int*, const PropE<R>*, int, int, const R*,   \
                                         V2<R>*, cudaStream_t, int);                                                    \
-    template void launch_final_t<R>(int, const int*, const int*, const int*, const int*, const int*, const int*,       \
+    template void launch_final_t<R>(int, const int*, const int*, const int*, const int*, const int*,                   \
                                     const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,       \
                                     const V2<R>*, int, int, const long long*, double2*, cudaStream_t);
 IFGF_INSTANTIATE(double)
