@@ -786,7 +786,11 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         } else {
             rc = apply_dev(ctx, G.vin.p, G.w.p, mode);
         }
-        launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.w.p, G.h.p, G.H.p, G.nrm2.p, G.part.p, s);
+        // the complex64 inner solves of the refinement take one Gram-Schmidt pass, as the batched
+        // ones do: each correction is checked by the FP64 residual, and a short one costs one more
+        // refinement pass, not a wrong answer
+        launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.w.p, G.h.p, G.H.p, G.nrm2.p, G.part.p, s,
+                            mode == IFGF2D_APPLY_IFGF_MIXED ? 1 : 2);
         cudaError_t ec = cudaStreamEndCapture(s, &graph);
         if (rc != IFGF2D_OK) return rc;
         CK(ec);

@@ -525,14 +525,14 @@ void launch_sub(const double2* a, const double2* b, long long n, double2* out, c
 }
 int arnoldi_part_size(long long n, int m) { return (int)(((n + kDotChunk - 1) / kDotChunk) * (m + 1)); }
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         double2* part, cudaStream_t s) {
+                         double2* part, cudaStream_t s, int passes) {
     // w holds A v_j on entry (the apply ran between k_copy_col and this call)
     const int ldh = m + 1;
-    for (int pass = 0; pass < 2; ++pass) {   // classical Gram-Schmidt, twice; the second pass sums ||w||^2
+    for (int pass = 0; pass < passes; ++pass) {   // classical Gram-Schmidt; the last pass sums ||w||^2
         const int nchunk = (int)((n + kDotChunk - 1) / kDotChunk);
         k_multidot_part<<<dim3(nchunk, m + 1), 256, 0, s>>>(V, n, jp, w, n, part);
         k_multidot_fin<<<nblk(m + 1, 128), 128, 0, s>>>(part, nchunk, jp, m + 1, h);
-        k_cgs_update_dyn<<<nblk(n, 64), 256, 0, s>>>(V, n, jp, h, n, w, H, ldh, pass, pass ? nrm2 : nullptr);
+        k_cgs_update_dyn<<<nblk(n, 64), 256, 0, s>>>(V, n, jp, h, n, w, H, ldh, pass, pass == passes - 1 ? nrm2 : nullptr);
     }
     k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, nrm2, n, V, jp, H, ldh);
     k_advance<<<1, 32, 0, s>>>(jp);

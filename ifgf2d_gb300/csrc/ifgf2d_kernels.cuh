@@ -193,10 +193,11 @@ void launch_gather_cols(const double2* in, int B, const int* act, int Bc, long l
 void launch_scatter_cols(const double2* in, int Bc, const int* act, int B, long long N, bool add, double2* out, cudaStream_t s);
 void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream_t s);
 // one Arnoldi step after w = A v_j, with j read from *jp (for a captured iteration graph):
-// CGS2 against V[:, 0..j] into the Hessenberg column j, ||w||^2 into *nrm2 (zeroed by
-// launch_copy_col), h_{j+1,j} and V[:, j+1] = w / h_{j+1,j}, then j += 1
+// classical Gram-Schmidt against V[:, 0..j], `passes` times (2: CGS2), into the Hessenberg
+// column j, ||w||^2 into *nrm2 (zeroed by launch_copy_col), h_{j+1,j} and
+// V[:, j+1] = w / h_{j+1,j}, then j += 1
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         double2* part, cudaStream_t s);
+                         double2* part, cudaStream_t s, int passes = 2);
 // size (double2 entries) of the partial-sum buffer launch_arnoldi_step needs
 int arnoldi_part_size(long long n, int m);
 // Z[:, *jp] = z
