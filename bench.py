@@ -542,10 +542,12 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
         return res
     # chosen: batched mixed solve (second call timed: the first allocates the Krylov basis)
     times = []
-    for _ in range(2):
+    for i in range(2):
+        torch.cuda.nvtx.range_push(f"batch_solve_{i}")   # profiler ranges (ncu --nvtx-include)
         t0 = time.perf_counter()
         X = fm.gmres_batch(B, tol=1e-6, restart=300, max_iters=3000, mixed=True)
         times.append(time.perf_counter() - t0)
+        torch.cuda.nvtx.range_pop()
     st = fm.last_solve
     R = fm.apply_batch(X) - B
     rr = np.linalg.norm(R, axis=0) / np.linalg.norm(B, axis=0)
