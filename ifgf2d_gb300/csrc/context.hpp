@@ -110,8 +110,10 @@ struct GmresWork {
     long long n = 0;
     int m = 0;
     cudaGraphExec_t exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // mode x (plain, preconditioned)
+    cudaGraphExec_t apply_exec[3] = {nullptr, nullptr, nullptr};   // per mode: one apply, vin -> vout
     void drop_graphs() {
         for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        for (auto& e : apply_exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
     }
     ~GmresWork() { drop_graphs(); }
 };

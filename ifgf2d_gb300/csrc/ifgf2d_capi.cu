@@ -697,8 +697,22 @@ extern "C" int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mod
     if (!all_finite(x, 2 * ctx->D.N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the density");
     const size_t bytes = sizeof(double2) * ctx->D.N;
     CK(cudaMemcpyAsync(ctx->vin.p, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    int rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, mode);
-    if (rc != IFGF2D_OK) return rc;
+    // the device part on the context's own vectors, captured once per mode as a CUDA graph (one
+    // launch instead of one per kernel); set-up, precomputation and tuning changes drop it
+    if (!ctx->gw) ctx->gw.reset(new GmresWork);
+    cudaGraphExec_t& ex = ctx->gw->apply_exec[mode];
+    if (!ex) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = apply_dev(ctx, ctx->vin.p, ctx->vout.p, mode);
+        const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc != IFGF2D_OK) { if (ec == cudaSuccess) cudaGraphDestroy(graph); return rc; }
+        CK(ec);
+        const cudaError_t ei = cudaGraphInstantiate(&ex, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ei);
+    }
+    CK(cudaGraphLaunch(ex, ctx->stream));
     CK(cudaMemcpyAsync(y, ctx->vout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     // of the single-vector kernels only the TMA-streamed complex64 leaf kernel can set the
