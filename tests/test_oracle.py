@@ -121,7 +121,7 @@ def test_oracle_combined_field_mie(oracle):
 
 def test_net_oracle_gradient_matches_finite_differences():
     """The CPU oracle of the learned preconditioner: its autograd gradient (FP64) agrees with
-    central differences along random directions (so it can judge the device gradients)."""
+    central differences along random directions (so it can check the device gradients)."""
     pytest.importorskip("torch")
     from oracle import net_oracle as NO
     rng = np.random.default_rng(0)
