@@ -205,6 +205,12 @@ def run_ours(args, rank, local_rank, world):
     fm.apply_device(x, y)
     torch.cuda.synchronize()
     mixed_err = float(np.linalg.norm(y_mixed - y.cpu().numpy()) / np.linalg.norm(y.cpu().numpy()))
+    # both forms against the FP64 O(N^2) direct sum with the same singular corrections
+    y_direct = fm.compute_Ax_unacc(x_h)
+    accuracy = {"ifgf_fp64_rel_err_vs_direct": float(np.linalg.norm(y.cpu().numpy() - y_direct) / np.linalg.norm(y_direct)),
+                "ifgf_mixed_rel_err_vs_direct": float(np.linalg.norm(y_mixed - y_direct) / np.linalg.norm(y_direct)),
+                "mixed_rel_err_vs_fp64_ifgf": mixed_err,
+                "direct": "O(N^2) FP64 sum excluding same-patch and near-singular pairs, plus the singular corrections"}
     # end to end: host buffers through the C ABI (copies in the timed region)
     xp = torch.from_numpy(x_h).pin_memory()
     yp = torch.empty_like(xp).pin_memory()
@@ -327,6 +333,7 @@ def run_ours(args, rank, local_rank, world):
                    "rel_err_vs_fp64": mixed_err,
                    "phase_ms": dict(zip(phases, [float(v) for v in acc_mixed]))},
         "work": wc,
+        "accuracy": accuracy,
     }
     if world > 1:   # the extra workloads are single-GPU measurements, reported at N = 1
         return out
@@ -527,6 +534,19 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
         res["apply_" + name + "_us_per_rhs"] = e0.elapsed_time(e1) / reps / nrhs * 1e3
     fm.batch_tensor_cores = default_tc
     res["tcgen05_kernels"] = default_tc
+    # per right-hand side: the complex64 batched apply against the FP64 one; the FP64 IFGF
+    # against the FP64 O(N^2) direct sum for the first incidence angle
+    fm.apply_batch_device(xt, yt, nrhs, mixed=False)
+    torch.cuda.synchronize()   # the apply runs on the context's stream
+    y64 = yt.cpu().numpy()
+    fm.apply_batch_device(xt, yt, nrhs, mixed=True)
+    torch.cuda.synchronize()
+    y32 = yt.cpu().numpy()
+    errs = np.linalg.norm(y32 - y64, axis=1) / np.linalg.norm(y64, axis=1)
+    yd = fm.compute_Ax_unacc(B[:, 0])
+    res["accuracy"] = {"mixed_rel_err_vs_fp64_per_rhs_max": float(errs.max()),
+                       "mixed_rel_err_vs_fp64_per_rhs_median": float(np.median(errs)),
+                       "ifgf_fp64_rel_err_vs_direct_rhs0": float(np.linalg.norm(y64[0] - yd) / np.linalg.norm(yd))}
     # one right-hand side through the single-vector path, for the per-RHS comparison
     y1 = torch.empty(N, dtype=torch.complex128, device="cuda")
     for mixed in (True, False):
