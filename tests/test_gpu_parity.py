@@ -123,6 +123,35 @@ def test_gpu_ifgf_interpolation_orders_match_oracle(lib, oracle, Ps, Pang):
         assert rel(Ym[:, r], Y[:, r]) < 2e-6, r
 
 
+def test_gpu_host_apply_graph_follows_setup(lib, oracle):
+    """The host-buffer apply runs a CUDA graph captured on first use; a new set-up (another
+    tree depth, new tables) and a new precomputation must replace it.  Checked against the
+    device-pointer apply, which launches kernel by kernel, in all three modes."""
+    torch = pytest.importorskip("torch")
+    k = 100.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=128, formulation="combined")
+    fm.precomps_and_setup(k, 0)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    x = torch.from_numpy(d).cuda()
+    y = torch.empty_like(x)
+
+    def device_apply(**kw):
+        fm.apply_device(x, y, **kw)
+        torch.cuda.synchronize()
+        return y.cpu().numpy()
+
+    for mixed in (False, True):
+        fm.compute_Ax_acc(d, mixed=mixed)                      # captures the graph
+    nl = fm.nlevels
+    fm.precomps_and_setup(k, nl - 1)                           # another tree: new tables
+    assert fm.nlevels == nl - 1
+    for mixed in (False, True):
+        assert rel(fm.compute_Ax_acc(d, mixed=mixed), device_apply(mixed=mixed)) < 1e-14
+    fm.compute_Ax_unacc(d)
+    fm.compute_precomputations(1.5 * k)                        # new wavenumber: new RP weights
+    assert rel(fm.compute_Ax_unacc(d), device_apply(accelerated=False)) < 1e-14
+
+
 def test_gpu_ifgf_against_direct_config2_size(lib, oracle):
     """Config 2 geometry (kite, k=500, 512 patches x 16 = 8192): IFGF vs the direct map."""
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 500.0, Np=16, patches_per_curve=512)
