@@ -118,7 +118,9 @@ int ifgf2d_get_nlevels(const ifgf2d_ctx* ctx);
 int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* sorting);
 
 /* y = A x, host vectors of N complex values (LinearOperator::operator*,
- * ForwardMap/LinearOperator.cpp:14-22 -> compute_Ax_unacc / compute_Ax_acc). */
+ * ForwardMap/LinearOperator.cpp:14-22 -> compute_Ax_unacc / compute_Ax_acc).  The first call
+ * per mode after a set-up, precomputation or tuning change captures the device part as a CUDA
+ * graph; later calls launch that graph between the two copies. */
 int ifgf2d_apply(ifgf2d_ctx* ctx, const double* x, double* y, int mode);
 /* the same on device-resident vectors (cudaMalloc'ed, N complex each) */
 int ifgf2d_apply_device(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode);
