@@ -99,6 +99,10 @@ void orc_fm_apply_sing(void* h, const double* in, double* out) {
 // 1 when a singular or near-singular point is outside the leaf neighbourhood, 2 on other errors.
 int orc_fm_setup_ifgf(void* hh, double k, int nlevels, int Ps, int Pang) {
     OracleFM* h = (OracleFM*)hh; ForwardMap& F = *h->fm;
+    // the far-field kernel's wavenumber and coupling, also when no precomputation ran (far-field
+    // and exclusion-matched direct sums need no rectangular-polar weights)
+    F.wavenumber = k;
+    F.eta = F.coupling > 0 ? F.coupling : k;
     try {
         h->tree.reset(new BoxTree(Ps, Pang));
         h->tree->Reinitialize(F.xs, F.ys, F.nxs, F.nys, nlevels, k, F.form, F.coupling > 0 ? F.coupling : k);

@@ -121,6 +121,29 @@ def test_prepare_builds_the_oracle_tree_without_a_gpu(lib, oracle):
             fm.compute_Ax_acc(np.ones(fm.total_num_unknowns_, dtype=complex))
     assert seen[0] == seen[1]
     assert L.ifgf2d_set_host_threads(-1) == 1
+
+
+@pytest.mark.parametrize("k,patches", [(500.0, 512), (2000.0, 2048), (8000.0, 8192)],
+                         ids=["kite_k500_N8192", "kite_k2000_N32768", "kite_k8000_N131072"])
+def test_prepare_tree_equals_oracle_at_full_size(lib, oracle, k, patches):
+    """The benchmark kites at their full sizes (N = 8192, 32768, 131072; trees of depth 7, 8
+    and 10): the host tree's depth choice, Morton sorting and per-apply work counts (near pairs,
+    leaf-cone, propagation and interpolation evaluations, relevant cones) equal the oracle's
+    BoxTree (BoxTree.h:61-600; cone counts per level from Level.h:88-142).  A cone or
+    relevant-box rule that differs only at high k * box size shows here, without a GPU."""
+    L = lib._lib.load()
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=patches)
+    fm.prepare(k, 0)
+    nl = int(L.ifgf2d_get_nlevels(fm.handle))
+    om = oracle.OracleForwardMap([oracle.curve_kite()], 16, 0.01, 1.0, k, patches_per_curve=patches)
+    om.setup_ifgf(k, nl)
+    with pytest.raises(RuntimeError, match="neighborhood"):
+        om.setup_ifgf(k, nl + 1)      # the depth is the deepest one the oracle accepts
+    om.setup_ifgf(k, nl)
+    assert np.array_equal(fm.getSorting(), om.sorting())
+    wc, ow = fm.work_counts(), om.work()
+    for key in ("near_pairs", "leaf_evals", "prop_evals", "interp_evals", "cones"):
+        assert wc[key] == ow[key], key
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
     assert L.ifgf2d_prepare(fm.handle, k, 2) == 4          # IFGF2D_ERR_NLEVELS, BoxTree.h:1117
     assert L.ifgf2d_prepare(fm.handle, -1.0, 0) == 1
