@@ -161,6 +161,10 @@ def replica_value(world, steps, ms):
     return world * steps / (ms * 1e-3)
 
 
+# the device results the CPU-baseline leg compares with the oracle (filled by run_ours)
+CHECK = {}
+
+
 def run_ours(args, rank, local_rank, world):
     import torch
     torch.cuda.set_device(local_rank)
@@ -205,7 +209,11 @@ def run_ours(args, rank, local_rank, world):
     fm.apply_device(x, y)
     torch.cuda.synchronize()
     mixed_err = float(np.linalg.norm(y_mixed - y.cpu().numpy()) / np.linalg.norm(y.cpu().numpy()))
-    # both forms against the FP64 O(N^2) direct sum with the same singular corrections
+    # both forms against the FP64 O(N^2) direct sum with the same singular corrections (the
+    # device's own direct map here; the oracle's is compared in the CPU-baseline leg)
+    CHECK["density"] = x_h
+    CHECK["y_fp64"] = y.cpu().numpy()
+    CHECK["y_mixed"] = y_mixed
     y_direct = fm.compute_Ax_unacc(x_h)
     accuracy = {"ifgf_fp64_rel_err_vs_direct": float(np.linalg.norm(y.cpu().numpy() - y_direct) / np.linalg.norm(y_direct)),
                 "ifgf_mixed_rel_err_vs_direct": float(np.linalg.norm(y_mixed - y_direct) / np.linalg.norm(y_direct)),
@@ -267,7 +275,10 @@ def run_ours(args, rank, local_rank, world):
         except Exception:
             traffic = None
     roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "frac": achieved / hbm, "traffic": traffic,
+                "traffic_source": "profiles/traffic.json: ncu dram__bytes_read.sum + dram__bytes_write.sum of this phase's "
+                                  "kernels in one FP64 apply of this workload (not measured in this run)",
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "fp64": {"achieved_tflops": flops_d / (acc[dom] * 1e-3) / 1e12, "peak_tflops": fp64_peak.value,
                          "frac": (flops_d / (acc[dom] * 1e-3) / 1e12) / max(fp64_peak.value, 1e-9),
                          "peak_source": "measured (ifgf2d_measure_fp64_peak)"},
@@ -362,10 +373,14 @@ def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
     net = PreconditionerNet.load(DEFAULT_WEIGHTS)
     res = {"weights": os.path.relpath(DEFAULT_WEIGHTS, ROOT), "training": "k ~ U(50, 400), stars and kites, 10 points per wavelength"}
     for k, npatch in cases:
+        import torch
+        t0 = time.perf_counter()
         fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, k, Np=NP, patches_per_curve=npatch, formulation="combined")
         fm.precomps_and_setup(k, 0)
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
         b = -np.exp(1j * k * fm.xs_)
-        row = {"N": fm.total_num_unknowns_}
+        row = {"N": fm.total_num_unknowns_, "setup_s": setup_s}
         for name, fn in (("plain_fp64", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000)),
                          ("mixed", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000, mixed=True)),
                          ("mixed_learned", lambda: fm.solve_precond(net, b, tol=1e-6, restart=300, max_iters=3000, mixed=True))):
@@ -379,6 +394,8 @@ def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
         row["speedup_mixed_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed"]["seconds"]
         row["speedup_learned_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed_learned"]["seconds"]
         row["learned_iteration_ratio"] = row["mixed_learned"]["iters"] / max(1, row["mixed"]["iters"])
+        row["with_setup"] = {n: setup_s + row[n]["seconds"] for n in ("plain_fp64", "mixed", "mixed_learned")}
+        row["with_setup"]["speedup_mixed_vs_plain"] = row["with_setup"]["plain_fp64"] / row["with_setup"]["mixed"]
         res[f"kite_k{int(k)}"] = row
         del fm
     return res
@@ -428,10 +445,15 @@ def run_large(G, k=8000.0, npatch=8192):
     t0 = time.perf_counter()
     fm = G.ForwardMap(DELTA, [G.Kite()], (), 1.0, k, Np=NP, patches_per_curve=npatch, formulation="combined")
     fm.precomps_and_setup(k, 0)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
     fm.autotune()
     torch.cuda.synchronize()
     res = {"workload": f"kite k={k:g}, {npatch} patches x {NP} (N={fm.total_num_unknowns_}), combined field, plane wave",
-           "N": fm.total_num_unknowns_, "nlevels": fm.nlevels, "setup_s": time.perf_counter() - t0}
+           "N": fm.total_num_unknowns_, "nlevels": fm.nlevels, "setup_s": setup_s,
+           "setup": "ForwardMap constructor (discretisation) + precomps_and_setup (RP weights, tree, plans, device tables)",
+           "autotune_s": time.perf_counter() - t0}
     N = fm.total_num_unknowns_
     x = torch.from_numpy(G.seeded_density(N)).cuda()
     y = torch.empty_like(x)
@@ -459,6 +481,10 @@ def run_large(G, k=8000.0, npatch=8192):
                      "fp64_refinement_passes": fm.last_solve.get("refinements", 0),
                      "converged": fm.last_solve["converged"], "true_rel_residual_fp64": tr}
     res["speedup_chosen_vs_plain"] = res["plain_fp64"]["seconds"] / res["chosen_mixed"]["seconds"]
+    res["with_setup"] = {"plain_fp64_s": setup_s + res["plain_fp64"]["seconds"],
+                         "chosen_mixed_s": setup_s + res["chosen_mixed"]["seconds"],
+                         "speedup_chosen_vs_plain": (setup_s + res["plain_fp64"]["seconds"]) /
+                                                    (setup_s + res["chosen_mixed"]["seconds"])}
     return res
 
 
@@ -593,10 +619,15 @@ def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):
     return res
 
 
-def time_oracle(budget_s=12.0, max_steps=None, threads=None):
+def time_oracle(budget_s=12.0, max_steps=None, threads=None, check=None):
     """The CPU oracle (restatement of the reference path, which is single-threaded) on the same
     workload, on every host thread: one oracle context per thread, each running whole IFGF
-    matvecs until the common deadline; the value is all threads' matvecs over the wall time."""
+    matvecs until the common deadline; the value is all threads' matvecs over the wall time.
+
+    With `check` (the device's FP64 and complex64 applies of the seeded density), the oracle's
+    FP64 direct forward map of the same density -- singular corrections plus the O(N^2) sum
+    with the same exclusions plus the jump term, rows split over the threads' contexts -- and
+    its IFGF apply are compared with them."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle as O
@@ -640,9 +671,32 @@ def time_oracle(budget_s=12.0, max_steps=None, threads=None):
         t.join()
     wall = max(ends) - t_start
     steps = sum(counts)
-    return {"value": steps / wall, "unit": UNIT, "cores": nt, "kind": "port",
-            "sample": f"{steps} full IFGF matvecs of the same workload (nlevels {ctxs[0][1]}) on {nt} threads, "
-                      f"one oracle context each, {wall:.1f} s wall"}
+    out = {"value": steps / wall, "unit": UNIT, "cores": nt, "kind": "port",
+           "sample": f"{steps} full IFGF matvecs of the same workload (nlevels {ctxs[0][1]}) on {nt} threads, "
+                     f"one oracle context each, {wall:.1f} s wall"}
+    if check:
+        dens = check["density"]
+        om0 = ctxs[0][0]
+        w = om0.point_weights()[0]
+        n = om0.N
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(nt) as ex:
+            bounds = [(n * i // nt, n * (i + 1) // nt) for i in range(nt)]
+            parts = list(ex.map(lambda i: ctxs[i][0].direct_excluded(dens * w, bounds[i]), range(nt)))
+        y_dir = om0.sing_near_sing(dens) + np.concatenate(parts) + 0.5 * dens   # combined field: + 1/2 I
+        y_ifgf = om0.compute_Ax_acc(dens)
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+        out["check"] = {"ifgf_fp64_rel_err_vs_oracle_direct": rel(check["y_fp64"], y_dir),
+                        "ifgf_mixed_rel_err_vs_oracle_direct": rel(check["y_mixed"], y_dir),
+                        "ifgf_fp64_rel_err_vs_oracle_ifgf": rel(check["y_fp64"], y_ifgf),
+                        "oracle_ifgf_rel_err_vs_oracle_direct": rel(y_ifgf, y_dir),
+                        "oracle_s": time.perf_counter() - t0,
+                        "direct": "the oracle's FP64 O(N^2) direct map: singular corrections, the sum excluding "
+                                  "same-patch and near-singular pairs, the jump term"}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -676,7 +730,7 @@ def main():
     out = run_ours(args, rank, local_rank, world)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = time_oracle(budget_s=12.0)
+            out["cpu_baseline"] = time_oracle(budget_s=12.0, check=CHECK or None)
             one = time_oracle(budget_s=6.0, threads=1)
             out["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": one["unit"], "sample": one["sample"]}
         print(json.dumps(out), flush=True)

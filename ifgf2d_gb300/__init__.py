@@ -151,11 +151,13 @@ class ForwardMap:
     ``patches_per_curve > 0`` selects an equal-parameter split instead of the arc-length rule.
     ``formulation="combined"`` selects the sound-soft combined field operator (1/2 I + K - i eta S)
     with eta = ``coupling`` (eta = k when coupling <= 0); the default is the reference's single layer.
+    ``device_geometry=True`` computes the points, patch bounding boxes and near-singular points on
+    the GPU (the patch limits stay on the host).
     """
 
     def __init__(self, delta, curves, curve_touch_tracker=(), wavelengths_per_patch=1.0,
                  patch_split_wavenumber=1.0, p=4.0, *, Np=10, Ps=5, Pang=5, patches_per_curve=0,
-                 formulation="single_layer", coupling=0.0):
+                 formulation="single_layer", coupling=0.0, device_geometry=False):
         L = _lib.load()
         curves = list(curves)
         if not curves:
@@ -167,7 +169,7 @@ class ForwardMap:
         if formulation not in forms:
             raise ValueError(f"formulation must be one of {sorted(forms)}")
         opt = _lib.Options(Np, delta, wavelengths_per_patch, patch_split_wavenumber, p, patches_per_curve, Ps, Pang,
-                           forms[formulation], float(coupling))
+                           forms[formulation], float(coupling), 1 if device_geometry else 0)
         self.formulation = formulation
         h = ctypes.c_void_p()
         rc = L.ifgf2d_create(carr, len(curves), jarr, len(jl), ctypes.byref(opt), ctypes.byref(h))
@@ -348,8 +350,13 @@ class ForwardMap:
         _check(_lib.load().ifgf2d_apply(self._h, _dp(xin.view(np.float64)), _dp(out.view(np.float64)), mode), self._h)
         return out
 
-    def compute_Ax_unacc(self, density, out=None):
-        """ForwardMap.tpp:517-540: singular correction + direct O(N^2) far sum."""
+    def compute_Ax_unacc(self, density, out=None, wavenumber=None):
+        """ForwardMap.tpp:517-540: singular correction + direct O(N^2) far sum.
+
+        The operator belongs to the wavenumber of the last precomputation; a ``wavenumber``
+        other than that one raises ValueError (the reference would mix the two)."""
+        if wavenumber is not None and float(wavenumber) != self.wavenumber:
+            raise ValueError(f"compute_Ax_unacc: wavenumber {wavenumber} differs from the precomputed {self.wavenumber}")
         y = self._apply(density, APPLY_DIRECT)
         if out is not None:
             out[...] = y

@@ -50,7 +50,7 @@ class Options(ctypes.Structure):
     _fields_ = [("Np", ctypes.c_int), ("delta", ctypes.c_double), ("wavelengths_per_patch", ctypes.c_double),
                 ("patch_split_wavenumber", ctypes.c_double), ("p", ctypes.c_double),
                 ("patches_per_curve", ctypes.c_int), ("Ps", ctypes.c_int), ("Pang", ctypes.c_int),
-                ("formulation", ctypes.c_int), ("coupling", ctypes.c_double)]
+                ("formulation", ctypes.c_int), ("coupling", ctypes.c_double), ("device_geometry", ctypes.c_int)]
 SINGLE_LAYER, COMBINED = 0, 2
 
 

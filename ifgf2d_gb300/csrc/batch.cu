@@ -5,7 +5,7 @@
 // every call re-reads the same operator.  Here up to kMaxBatch right-hand sides share one pass
 // over the tables (ifgf_batch.cu), and GMRES runs for all of them in lock step: one batched
 // apply per iteration, per-RHS Gram-Schmidt coefficients from batched reductions, and each
-// right-hand side's own Givens rotations, residual estimate and stop test on the host.
+// right-hand side's own Givens rotations, residual estimate and stop test on the device.
 #include "context.hpp"
 #include "host_threads.hpp"
 
@@ -38,6 +38,11 @@ struct BatchWork {
     // gathered into compact [N][Bc] arrays (right-hand side, solution, residual, correction, A x)
     DBuf<double2> cb, cx, cr, cd, ct;
     DBuf<int> act;
+    // least squares on the device (LsqBatchDev), per-RHS cycle parameters and the per-iteration
+    // count of the right-hand sides still running
+    DBuf<double2> lsR, lsg, lsgs;
+    DBuf<double> lsgc, lssc, lspar;
+    DBuf<int> lsst, lsact;
 };
 
 void ifgf::free_batch(ifgf2d_ctx* ctx) {
@@ -83,29 +88,6 @@ void grouped_interp_plan(const Tree& T, std::vector<int4>& items, std::vector<In
     }, 64);
 }
 
-// a parent's propagation terms sorted by child cone (stable), with the parent node recorded
-template <typename R>
-std::vector<PropB<R>> sorted_plan(const Tree& T) {
-    std::vector<PropB<R>> out(T.pp.size());
-    const int P = T.P;
-    parallel_for(T.total_cones, [&](long long p0, long long p1) {
-        std::vector<int> idx;
-        for (long long pc = p0; pc < p1; ++pc) {
-            const long long e0 = T.pp_ptr[pc];
-            const int ne = (int)(T.pp_ptr[pc + 1] - e0);
-            idx.resize(ne);
-            for (int i = 0; i < ne; ++i) idx[i] = i;
-            std::stable_sort(idx.begin(), idx.end(),
-                             [&](int a, int b) { return T.pp[e0 + a].child_cone < T.pp[e0 + b].child_cone; });
-            for (int q = 0; q < ne; ++q) {
-                const PropEntry& e = T.pp[e0 + idx[q]];
-                out[e0 + q] = PropB<R>{e.child_cone, idx[q] % P, (R)e.s, (R)e.th, (R)e.wr, (R)e.wi};
-            }
-        }
-    }, 256);
-    return out;
-}
-
 int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
     if (!ctx->bw) ctx->bw = new BatchWork;
     BatchWork& W = *ctx->bw;
@@ -121,7 +103,11 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
         if (!W.rho32.p) {
             CK(W.rho32.alloc((size_t)N * W.cap)); CK(W.coef32.alloc(ncoef * W.cap)); CK(W.xt32.alloc((size_t)N * W.cap));
         }
-        if (!W.pb32.p) CK(W.pb32.upload(sorted_plan<float>(ctx->T)));
+        if (!W.pb32.p) {
+            CK(W.pb32.alloc(ctx->pp.n));
+            launch_sort_plan<float>(ctx->pp_ptr.p, ctx->T.total_cones, ctx->pp.p, ctx->T.P, W.pb32.p, ctx->stream);
+            CK(cudaGetLastError());
+        }
         if (!W.t5err.p) {
             CK(prop_t5_init_attributes());
             CK(W.t5err.alloc(1));
@@ -147,7 +133,11 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
         }
     } else {
         if (!W.rho64.p) { CK(W.rho64.alloc((size_t)N * W.cap)); CK(W.coef64.alloc(ncoef * W.cap)); }
-        if (!W.pb64.p) CK(W.pb64.upload(sorted_plan<double>(ctx->T)));
+        if (!W.pb64.p) {
+            CK(W.pb64.alloc(ctx->pp.n));
+            launch_sort_plan<double>(ctx->pp_ptr.p, ctx->T.total_cones, ctx->pp.p, ctx->T.P, W.pb64.p, ctx->stream);
+            CK(cudaGetLastError());
+        }
     }
     return IFGF2D_OK;
 }
@@ -268,6 +258,9 @@ int ensure_solve(ifgf2d_ctx* ctx, int B, int m) {
         CK(W.b.alloc(nb)); CK(W.x.alloc(nb)); CK(W.r.alloc(nb)); CK(W.d.alloc(nb));
         CK(W.h.alloc((size_t)(m + 1) * B)); CK(W.H.alloc((size_t)m * (m + 1) * B));
         CK(W.part.alloc((size_t)bdot_chunks(N) * (m + 1) * B)); CK(W.Y.alloc((size_t)m * B)); CK(W.hn.alloc(B));
+        CK(W.lsR.alloc((size_t)B * (m + 1) * m)); CK(W.lsg.alloc((size_t)B * (m + 1))); CK(W.lsgc.alloc((size_t)B * m));
+        CK(W.lsgs.alloc((size_t)B * m)); CK(W.lssc.alloc((size_t)3 * B)); CK(W.lspar.alloc((size_t)3 * B));
+        CK(W.lsst.alloc((size_t)4 * B)); CK(W.lsact.alloc(m));
         std::vector<double2> one(B, make_double2(1.0, 0.0));
         CK(W.ones.upload(one));
         W.scap = B; W.m = m;
@@ -290,7 +283,11 @@ int bnorms(ifgf2d_ctx* ctx, const double2* v, int B, std::vector<double>& out) {
 
 // x = A^{-1} b for B interleaved right-hand sides, initial guess 0 (opGMRES.hpp:383-392).
 // Right-hand side r stops when |g_{j+1}| / ||r0|| < tol[r] (opGMRES.hpp:207), after max_iters
-// iterations, or at the start when skip[r]; a stopped right-hand side keeps its x.
+// iterations, or at the start when skip[r]; a stopped right-hand side keeps its x.  Each
+// right-hand side's Givens rotations, estimate and stop test run on the device
+// (launch_lsq_givens_batch).  The host reads back only how many still run, 4 bytes per
+// iteration; a batched iteration is long (milliseconds at k = 2000), so that wait costs less
+// than running one iteration past the last stop would.
 int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, const std::vector<double>& tol, int restart,
                 int max_iters, const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est,
                 int gs_passes = 2) {
@@ -314,25 +311,29 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
         est[r] = done[r] ? 0.0 : 1.0;
     }
     CK(cudaMemcpyAsync(W.w.p, b, sizeof(double2) * nb, cudaMemcpyDeviceToDevice, s));
-    using C = std::complex<double>;
-    std::vector<std::vector<C>> R(B), g(B);
-    std::vector<std::vector<Giv>> G(B);
-    std::vector<int> jcols(B);
-    std::vector<char> active(B);
-    std::vector<double2> Hh((size_t)(m + 1) * B), Yh((size_t)m * B);
+    const LsqBatchDev L{W.lsR.p, W.lsg.p, W.lsgc.p, W.lsgs.p, W.lsst.p, W.lssc.p, m, B};
+    // pinned host mirror: per-RHS parameters (3 B doubles), estimates (3 B doubles), states
+    // (4 B ints), running counts (m ints)
+    const size_t pin_bytes = sizeof(double) * 6 * B + sizeof(int) * (4 * B + m);
+    char* pin = reinterpret_cast<char*>(pinned_scratch((pin_bytes + 15) / 16));
+    if (!pin) return fail(ctx, IFGF2D_ERR_CUDA, "cudaMallocHost of the GMRES read-back buffer failed");
+    double* h_par = reinterpret_cast<double*>(pin);
+    double* h_sc = h_par + 3 * B;
+    int* h_st = reinterpret_cast<int*>(h_sc + 3 * B);
+    int* h_act = h_st + 4 * B;
     auto all_done = [&]() { for (int r = 0; r < B; ++r) if (!done[r]) return false; return true; };
+    const long long cap = std::min<long long>(max_iters, N);
     while (!all_done()) {
         // v_0 = r / ||r|| (W.hn holds ||r|| per RHS; 0 gives a zero vector)
         launch_bscale(W.w.p, W.hn.p, N, B, W.V.p, s);
         CK(cudaMemsetAsync(W.H.p, 0, sizeof(double2) * (size_t)m * ldh * B, s));
         for (int r = 0; r < B; ++r) {
-            R[r].clear();
-            g[r].assign(m + 1, C(0.0));
-            g[r][0] = beta[r];
-            G[r].assign(m, Giv{1.0, 0.0});
-            jcols[r] = 0;
-            active[r] = !done[r];
+            h_par[3 * r] = r0n[r];
+            h_par[3 * r + 1] = tol[r];
+            h_par[3 * r + 2] = done[r] ? 0.0 : (double)std::max<long long>(0, cap - iters[r]);
         }
+        CK(cudaMemcpyAsync(W.lspar.p, h_par, sizeof(double) * 3 * B, cudaMemcpyHostToDevice, s));
+        launch_lsq_init_batch(L, W.hn.p, W.lspar.p, s);
         int ncols = 0;
         for (int j = 0; j < m; ++j) {
             double2* vj = W.V.p + (long long)j * nb;
@@ -344,49 +345,25 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
             }
             launch_bdot(W.w.p, 0, 1, W.w.p, N, B, W.part.p, nullptr, Hcol, 0, j + 1, s);
             launch_bscale(W.w.p, Hcol + (long long)(j + 1) * B, N, B, W.V.p + (long long)(j + 1) * nb, s);
-            CK(cudaMemcpyAsync(Hh.data(), Hcol, sizeof(double2) * (size_t)(j + 2) * B, cudaMemcpyDeviceToHost, s));
+            launch_lsq_givens_batch(Hcol, j, L, W.lsact.p, s);
+            CK(cudaMemcpyAsync(h_act + j, W.lsact.p + j, sizeof(int), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            CK(cudaGetLastError());
             ncols = j + 1;
-            bool any = false;
-            for (int r = 0; r < B; ++r) {
-                if (!active[r]) continue;
-                R[r].resize((size_t)(j + 1) * ldh);
-                C* col = &R[r][(size_t)j * ldh];
-                for (int i = 0; i <= j + 1; ++i) col[i] = C(Hh[(size_t)i * B + r].x, Hh[(size_t)i * B + r].y);
-                const double hnv = std::abs(col[j + 1]);
-                for (int i = 0; i < j; ++i) rot(G[r][i], col[i], col[i + 1]);
-                if (col[j + 1] != 0.0) {
-                    G[r][j] = make_giv(col[j], col[j + 1]);
-                    rot(G[r][j], col[j], col[j + 1]);
-                    rot(G[r][j], g[r][j], g[r][j + 1]);
-                }
-                ++iters[r];
-                jcols[r] = j + 1;
-                est[r] = std::abs(g[r][j + 1]) / r0n[r];
-                if (est[r] < tol[r] || iters[r] >= max_iters || iters[r] >= N || hnv == 0.0) {
-                    active[r] = 0;
-                    done[r] = 1;
-                } else {
-                    any = true;
-                }
-            }
-            if (!any) break;
+            if (h_act[j] == 0) break;
         }
         // y_r = R_r^{-1} g_r over its own column count, x += V Y
-        std::fill(Yh.begin(), Yh.end(), make_double2(0.0, 0.0));
-        for (int r = 0; r < B; ++r) {
-            const int jc = jcols[r];
-            std::vector<C> yv(jc);
-            for (int i = jc - 1; i >= 0; --i) {
-                C acc = g[r][i];
-                for (int q = i + 1; q < jc; ++q) acc -= R[r][(size_t)q * ldh + i] * yv[q];
-                yv[i] = acc / R[r][(size_t)i * ldh + i];
-                Yh[(size_t)i * B + r] = make_double2(yv[i].real(), yv[i].imag());
-            }
-        }
-        CK(cudaMemcpyAsync(W.Y.p, Yh.data(), sizeof(double2) * (size_t)ncols * B, cudaMemcpyHostToDevice, s));
+        launch_lsq_solve_batch(L, ncols, W.Y.p, s);
         launch_bupdate(W.V.p, nb, ncols, W.Y.p, 1.0, N, B, x, s);
+        CK(cudaMemcpyAsync(h_sc, W.lssc.p, sizeof(double) * 3 * B, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h_st, W.lsst.p, sizeof(int) * 4 * B, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        for (int r = 0; r < B; ++r) {
+            if (done[r]) continue;
+            iters[r] += h_st[4 * r + 3];
+            est[r] = h_sc[3 * r];
+            if (h_st[4 * r] || h_st[4 * r + 3] <= 0) done[r] = 1;
+        }
         if (all_done()) break;
         // restart: r = b - A x; the estimate keeps the first ||r0|| (opGMRES.hpp:207)
         if ((rc = apply_il(ctx, x, W.t.p, B, mode))) return rc;

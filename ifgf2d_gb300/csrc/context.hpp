@@ -107,6 +107,11 @@ struct GmresWork {
     DBuf<double2> Z, zt;
     DBuf<double> nrm2;
     DBuf<int> jdev;
+    // least squares on the device (LsqDev): rotated columns, rotated right-hand side, rotations,
+    // cycle state
+    DBuf<double2> lsR, lsg, lsgs;
+    DBuf<double> lsgc, lssc;
+    DBuf<int> lsst;
     long long n = 0;
     int m = 0;
     cudaGraphExec_t exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // mode x (plain, preconditioned)
@@ -234,34 +239,15 @@ void free_eval(ifgf2d_ctx* ctx);
 // network out for N points with the curve's geometry (host call, synchronous, not capturable);
 // launch queues z = M(r) on stream s (capturable; the buffers stay fixed until the next prepare)
 int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, double k, std::string& err);
+// the propagation plan's entries from the tree's slot form, on the device (plan_device.cu):
+// FP64 into pp64 and, when pp32 is not null, the complex64 copy; *err is set when a node's child
+// cone does not exist (an inconsistent tree).  Synchronises the stream before returning.
+cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s);
+// a parent's propagation terms sorted by child cone (stable), with the parent node recorded, for
+// the batched propagation
+template <typename R>
+void launch_sort_plan(const long long* pp_ptr, int ncones, const PropE<double>* pp, int P, PropB<R>* out, cudaStream_t s);
+// the complex64 copy of the interpolation plan
+void launch_interp_to_c64(const InterpE<double>* in, long long n, InterpE<float>* out, cudaStream_t s);
 void net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cudaStream_t s);
-}  // namespace ifgf
-
-// Givens rotation G with G^* [p; q] = [r; 0] (Eigen's JacobiRotation::makeGivens, complex case)
-namespace ifgf {
-struct Giv { std::complex<double> c, s; };
-inline Giv make_giv(std::complex<double> p, std::complex<double> q) {
-    Giv g;
-    if (q == 0.0) { g.c = p.real() < 0 ? -1.0 : 1.0; g.s = 0.0; return g; }
-    if (p == 0.0) { g.c = 0.0; g.s = -q / std::abs(q); return g; }
-    const double p1 = std::fabs(p.real()) + std::fabs(p.imag()), q1 = std::fabs(q.real()) + std::fabs(q.imag());
-    if (p1 >= q1) {
-        std::complex<double> ps = p / p1, qs = q / p1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = std::sqrt(1.0 + q2 / p2); if (p.real() < 0) u = -u;
-        g.c = 1.0 / u; g.s = -qs * std::conj(ps) * (g.c.real() / p2);
-    } else {
-        std::complex<double> ps = p / q1, qs = q / q1;
-        const double p2 = std::norm(ps), q2 = std::norm(qs);
-        double u = q1 * std::sqrt(p2 + q2); if (p.real() < 0) u = -u;
-        const double pa = std::abs(p); ps = p / pa;
-        g.c = pa / u; g.s = -std::conj(ps) * (q / u);
-    }
-    return g;
-}
-// (x, y) <- G^* (x, y) with G = [c, conj(s); -s, conj(c)]
-inline void rot(const Giv& g, std::complex<double>& x, std::complex<double>& y) {
-    const std::complex<double> nx = std::conj(g.c) * x - std::conj(g.s) * y, ny = g.s * x + g.c * y;
-    x = nx; y = ny;
-}
 }  // namespace ifgf

@@ -33,5 +33,8 @@ struct DirectView {
 int direct_view(ifgf2d_ctx* ctx, DirectView* v);
 // Sets the context's error message (ifgf2d_last_error).
 void set_error(ifgf2d_ctx* ctx, const char* msg);
+// Set-up work of ifgf2d_apply_direct_noalloc on `device` (the current device): resolves its
+// scratch array's address and loads its kernels, so that the call allocates nothing.
+int noalloc_prepare(int device);
 
 }  // namespace ifgf

@@ -273,6 +273,7 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
             touch[J.curve].push_back(J);
         }
     }
+    const bool on_device = opt.device_geometry != 0;
     std::vector<int> per(ncurves), first(ncurves), past(ncurves);
     for (int c = 0; c < ncurves; ++c) {
         const HostCurve& cv = D.curves[c];
@@ -287,7 +288,7 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
             const bool open = !cv.closed;
             const int s1 = open && (np == 1 || pi == 0), s2 = open && (np == 1 || pi == np - 1);
             D.ist1sing.push_back(s1); D.ist2sing.push_back(s2);
-            for (int j = 0; j < Np; ++j) {
+            for (int j = 0; j < Np && !on_device; ++j) {
                 const double z = D.fej_n[j];
                 double tm = z, ej = 0.0;
                 if (s1 && s2) { tm = edge_both(z, p); ej = dedge_both(z, p); }
@@ -309,11 +310,6 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
         }
     }
     D.N = D.num_patches * Np;
-    // patch bounding boxes (Patch.tpp:36-64), one per patch, independent of each other
-    std::vector<Box4> boxes(D.num_patches);
-    parallel_for(D.num_patches, [&](long long p0, long long p1) {
-        for (long long pi = p0; pi < p1; ++pi) boxes[pi] = patch_box(D.curves[D.curve_of[pi]], D.t1[pi], D.t2[pi], D.delta);
-    }, 16);
     // candidate patches (ForwardMap.tpp:164-219); junction entries keep the reference's
     // `curve_patches_end` index, which names the patch after the touching curve
     std::vector<std::vector<long long>> cand(D.num_patches);
@@ -333,6 +329,13 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
             } else { e.push_back(s + pi - 1); e.push_back(s + pi + 1); }
         }
     }
+    // points, bounding boxes and near-singular points on the GPU (geometry_device.cu)
+    if (on_device) return discretise_on_device(D, cand);
+    // patch bounding boxes (Patch.tpp:36-64), one per patch, independent of each other
+    std::vector<Box4> boxes(D.num_patches);
+    parallel_for(D.num_patches, [&](long long p0, long long p1) {
+        for (long long pi = p0; pi < p1; ++pi) boxes[pi] = patch_box(D.curves[D.curve_of[pi]], D.t1[pi], D.t2[pi], D.delta);
+    }, 16);
     // near-singular points (ForwardMap.tpp:224-285), per patch in parallel, then concatenated
     std::vector<std::vector<std::pair<long long, double>>> found(D.num_patches);
     parallel_for(D.num_patches, [&](long long p0, long long p1) {

@@ -60,4 +60,9 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
 
 void fejer_rule(int n, std::vector<double>& nodes, std::vector<double>& weights);
 
+// The per-point discretisation, the patch bounding boxes and the near-singular detection of
+// `D` (whose patches are set) on the current GPU (geometry_device.cu); cand holds each patch's
+// candidate patches.  Returns an empty string on success, else an error message.
+std::string discretise_on_device(Discretisation& D, const std::vector<std::vector<long long>>& cand);
+
 }  // namespace ifgf

@@ -12,6 +12,7 @@
 #include <memory>
 
 #include "context.hpp"
+#include "direct_view.hpp"
 #include "host_threads.hpp"
 
 using namespace ifgf;
@@ -208,6 +209,8 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     launch_rp_fold(ctx->M.p, ctx->cols.p, ncols, ctx->edge.p, ctx->patches.p, D.Np, ctx->W.p, ctx->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ifgf::noalloc_prepare(ctx->device) != IFGF2D_OK)
+        return fail(ctx, IFGF2D_ERR_CUDA, "loading the scratch array of ifgf2d_apply_direct_noalloc failed");
     ctx->k = k;
     ctx->precomputed = true;
     ctx->ifgf_ready = false;
@@ -393,32 +396,25 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
                       ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, T.Ps, T.Pang, k, ctx->form, ctx->eta, ctx->Gsep.p,
                       ctx->leafL.p, ctx->stream);
     CK(cudaGetLastError());
-    // propagation and interpolation plans
+    // propagation and interpolation plans: the propagation entries are computed on the device
+    // from the tree's slot form, the interpolation entries come from the host tree
     {
-        // the host plan entries have the device layout of the FP64 form
-        static_assert(sizeof(PropEntry) == sizeof(PropEntryD) && sizeof(InterpEntry) == sizeof(InterpEntryD),
-                      "host and device plan layouts differ");
-        CK(ctx->pp.upload(reinterpret_cast<const PropEntryD*>(T.pp.data()), T.pp.size()));
+        CK(ctx->pp.alloc((size_t)T.pp_total)); CK(ctx->pp32.alloc((size_t)T.pp_total));
         CK(ctx->pp_ptr.upload(T.pp_ptr)); CK(ctx->pp_nchild.upload(T.pp_nchild));
+        DBuf<int> perr;
+        CK(perr.alloc(1));
+        CK(cudaMemsetAsync(perr.p, 0, sizeof(int), ctx->stream));
+        CK(build_prop_plan(T, ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+        int bad = 0;
+        CK(cudaMemcpyAsync(&bad, perr.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (bad) return fail(ctx, IFGF2D_ERR_GEOMETRY, "internal: a propagation node's child cone is missing");
+        static_assert(sizeof(InterpEntry) == sizeof(InterpEntryD), "host and device plan layouts differ");
         CK(ctx->ip.upload(reinterpret_cast<const InterpEntryD*>(T.ip.data()), T.ip.size()));
         CK(ctx->ip_ptr.upload(T.ip_ptr));
-        // complex64 copies for the mixed form (values computed in FP64, rounded once)
-        std::vector<PropE<float>> pf(T.pp.size());
-        parallel_for((long long)T.pp.size(), [&](long long i0, long long i1) {
-            for (long long i = i0; i < i1; ++i) {
-                const PropEntry& e = T.pp[i];
-                pf[i] = PropE<float>{e.child_cone, (float)e.s, (float)e.th, (float)e.wr, (float)e.wi};
-            }
-        }, 1 << 16);
-        CK(ctx->pp32.upload(pf));
-        std::vector<InterpE<float>> jf(T.ip.size());
-        parallel_for((long long)T.ip.size(), [&](long long i0, long long i1) {
-            for (long long i = i0; i < i1; ++i) {
-                const InterpEntry& e = T.ip[i];
-                jf[i] = InterpE<float>{e.cone, (float)e.s, (float)e.th, (float)e.fr, (float)e.fi};
-            }
-        }, 1 << 16);
-        CK(ctx->ip32.upload(jf));
+        CK(ctx->ip32.alloc(T.ip.size()));
+        launch_interp_to_c64(ctx->ip.p, (long long)T.ip.size(), ctx->ip32.p, ctx->stream);
+        CK(cudaGetLastError());
     }
     CK(ctx->coef.alloc((size_t)T.total_cones * P));
     CK(ctx->coef32.alloc((size_t)T.total_cones * P));
@@ -762,14 +758,15 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
 // ------------------------------------------------------------------ GMRES on the device
 
 // GMRES core on device vectors: x = A^{-1} b from the initial guess 0 (the reference's guess,
-// opGMRES.hpp:383-392).  Arnoldi with classical Gram-Schmidt twice (CGS2).  One iteration --
-// copy of v_j, the whole apply, CGS2 into the Hessenberg column, ||w||, v_{j+1} = w / ||w|| --
-// is a captured CUDA graph whose kernels read j from device memory, so the same graph serves
-// every iteration.  The host launches it in batches of four, reads the new Hessenberg columns
-// back once per batch and does the small sequential work (Givens rotations, residual estimate,
-// back-substitution) itself: on GB300 one CPU core runs scalar FP64 far faster than one GPU
-// thread.  Stops when |g_{j+1}| / ||r0|| < tol (the first ||r0||, opGMRES.hpp:207) or after
-// max_iters iterations; iterations run past the stop inside a batch are discarded.
+// opGMRES.hpp:383-392).  Arnoldi with classical Gram-Schmidt twice (CGS2), Givens rotations and
+// the residual estimate on the device (gmres_device.cu).  One restart cycle is one launch of a
+// captured CUDA graph: a while-loop whose body is one iteration -- copy of v_j, the whole apply,
+// CGS2 into the Hessenberg column, ||w||, v_{j+1} = w / ||w||, the Givens step -- and whose
+// condition the Givens step clears when the cycle ends.  The kernels read j from device memory,
+// so the same graph serves every iteration and every cycle.  After the loop one warp solves the
+// triangular system, x += V y, and the host reads the cycle's state (a few bytes) once.  Stops
+// when |g_{j+1}| / ||r0|| < tol (the first ||r0||, opGMRES.hpp:207) or after max_iters
+// iterations.
 static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, double tol, int restart,
                       int max_iters, int& iters, double& est, ifgf2d_net* net = nullptr) {
     const long long N = ctx->D.N;
@@ -782,14 +779,32 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         CK(G.V.alloc((size_t)N * (m + 1))); CK(G.w.alloc(N)); CK(G.h.alloc(m + 2)); CK(G.t.alloc(N)); CK(G.vin.alloc(N));
         CK(G.H.alloc((size_t)ldh * m)); CK(G.y.alloc(m)); CK(G.nrm2.alloc(1)); CK(G.jdev.alloc(1));
         CK(G.part.alloc((size_t)arnoldi_part_size(N, m)));
+        CK(G.lsR.alloc((size_t)ldh * m)); CK(G.lsg.alloc(m + 1)); CK(G.lsgc.alloc(m)); CK(G.lsgs.alloc(m));
+        CK(G.lsst.alloc(4)); CK(G.lssc.alloc(3));
         G.Z.release(); G.zt.release();
         G.n = N; G.m = m;
     }
     if (net && !G.Z.p) { CK(G.Z.alloc((size_t)N * m)); CK(G.zt.alloc(N)); }
+    const LsqDev L{G.lsR.p, G.lsg.p, G.lsgc.p, G.lsgs.p, G.lsst.p, G.lssc.p, m};
     const int gi = mode + (net ? 3 : 0);
     if (!G.exec[gi]) {
         cudaGraph_t graph;
-        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        CK(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle cond;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(s, np.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return fail(ctx, IFGF2D_ERR_CUDA, std::string("building the GMRES cycle graph: ") + cudaGetErrorString(e));
+        }
         launch_copy_col(G.V.p, N, G.jdev.p, G.vin.p, G.nrm2.p, s);
         int rc;
         if (net) {
@@ -804,16 +819,25 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         // ones do: each correction is checked by the FP64 residual, and a short one costs one more
         // refinement pass, not a wrong answer
         launch_arnoldi_step(G.V.p, N, m, G.jdev.p, G.w.p, G.h.p, G.H.p, G.nrm2.p, G.part.p, s,
-                            mode == IFGF2D_APPLY_IFGF_MIXED ? 1 : 2);
-        cudaError_t ec = cudaStreamEndCapture(s, &graph);
-        if (rc != IFGF2D_OK) return rc;
-        CK(ec);
-        CK(cudaGraphInstantiate(&G.exec[gi], graph, 0));
+                            mode == IFGF2D_APPLY_IFGF_MIXED ? 1 : 2, &L, cond, true);
+        cudaGraph_t body = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s, &body);
+        if (rc != IFGF2D_OK || ec != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            if (rc != IFGF2D_OK) return rc;
+            CK(ec);
+        }
+        e = cudaGraphInstantiate(&G.exec[gi], graph, 0);
         cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { G.exec[gi] = nullptr; CK(e); }
     }
     double2 *V = G.V.p, *w = G.w.p, *h = G.h.p, *t = G.t.p;
-    double2* H_host = pinned_scratch((size_t)ldh * m);
-    if (!H_host) return fail(ctx, IFGF2D_ERR_CUDA, "cudaMallocHost of the Hessenberg read-back buffer failed");
+    // the cycle state read back after each cycle: estimate (double), then [stopped, columns,
+    // limit, iterations] (ints)
+    double2* rb = pinned_scratch(4);
+    if (!rb) return fail(ctx, IFGF2D_ERR_CUDA, "cudaMallocHost of the GMRES read-back buffer failed");
+    double* rb_est = reinterpret_cast<double*>(rb);
+    int* rb_st = reinterpret_cast<int*>(rb + 2);
     CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, s));
     auto dnorm = [&](const double2* v, double& out) -> int {
         launch_multidot(v, N, 1, v, N, h + m + 1, s);
@@ -833,54 +857,22 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
     const double r0n = beta;
     est = 1.0;
     if (beta == 0.0) { est = 0.0; return IFGF2D_OK; }
-    std::vector<std::complex<double>> R((size_t)ldh * m), g(m + 1);
-    std::vector<Giv> Gr(m);
-    std::vector<double2> yv(m);
     for (;;) {
+        const long long limit = std::min<long long>(max_iters, N) - iters;
+        if (limit <= 0) break;
         launch_scale(w, make_double2(1.0 / beta, 0.0), N, V, s);
         CK(cudaMemsetAsync(G.H.p, 0, sizeof(double2) * ldh * m, s));
-        CK(cudaMemsetAsync(G.jdev.p, 0, sizeof(int), s));
-        std::fill(g.begin(), g.end(), 0.0);
-        g[0] = beta;
-        int j = 0, jcols = 0;
-        bool stop = false;
-        while (j < m && !stop) {
-            const int nb = std::min(4, m - j);
-            for (int q = 0; q < nb; ++q) CK(cudaGraphLaunch(G.exec[gi], s));
-            // columns j .. j+nb-1, rows 0 .. j+nb
-            CK(cudaMemcpy2DAsync(H_host + (size_t)j * ldh, ldh * sizeof(double2), G.H.p + (size_t)j * ldh, ldh * sizeof(double2),
-                                 (size_t)(j + nb + 1) * sizeof(double2), nb, cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            CK(cudaGetLastError());
-            for (int q = 0; q < nb; ++q) {
-                const int c = j + q;
-                std::complex<double>* col = &R[(size_t)c * ldh];
-                for (int i = 0; i <= c + 1; ++i) col[i] = std::complex<double>(H_host[(size_t)c * ldh + i].x, H_host[(size_t)c * ldh + i].y);
-                const double hn = std::abs(col[c + 1]);
-                for (int i = 0; i < c; ++i) rot(Gr[i], col[i], col[i + 1]);
-                if (col[c + 1] != 0.0) {
-                    Gr[c] = make_giv(col[c], col[c + 1]);
-                    rot(Gr[c], col[c], col[c + 1]);
-                    rot(Gr[c], g[c], g[c + 1]);
-                } else {
-                    Gr[c] = Giv{1.0, 0.0};
-                }
-                ++iters;
-                est = std::abs(g[c + 1]) / r0n;
-                if (iters >= N || est < tol || iters >= max_iters || hn == 0.0) { stop = true; jcols = c + 1; break; }
-            }
-            if (!stop) { j += nb; jcols = j; }
-        }
-        // y = R^{-1} g (host back-substitution), x += V y
-        for (int i = jcols - 1; i >= 0; --i) {
-            std::complex<double> acc = g[i];
-            for (int q = i + 1; q < jcols; ++q) acc -= R[(size_t)q * ldh + i] * std::complex<double>(yv[q].x, yv[q].y);
-            const std::complex<double> yi = acc / R[(size_t)i * ldh + i];
-            yv[i] = make_double2(yi.real(), yi.imag());
-        }
-        CK(cudaMemcpyAsync(G.y.p, yv.data(), sizeof(double2) * jcols, cudaMemcpyHostToDevice, s));
-        launch_multi_axpy(net ? G.Z.p : V, N, jcols, G.y.p, 1.0, N, x, s);   // x += V y, or Z y (flexible)
-        if (stop) break;
+        launch_lsq_init(L, G.jdev.p, beta, r0n, tol, (int)std::min<long long>(limit, 1 << 30), s);
+        CK(cudaGraphLaunch(G.exec[gi], s));
+        launch_lsq_solve(L, ldh, G.y.p, s);
+        launch_multi_axpy_dyn(net ? G.Z.p : V, N, G.lsst.p + 1, G.y.p, N, x, s);   // x += V y, or Z y (flexible)
+        CK(cudaMemcpyAsync(rb_est, G.lssc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rb_st, G.lsst.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        iters += rb_st[3];
+        est = *rb_est;
+        if (rb_st[0] || rb_st[3] <= 0) break;   // converged, out of iterations or broken down
         // restart: r = b - A x (the residual estimate keeps the first ||r0||, opGMRES.hpp:207)
         if ((rc = apply_dev(ctx, x, t, mode))) return rc;
         launch_sub(b, t, N, w, s);
@@ -1051,7 +1043,6 @@ extern "C" int ifgf2d_hankel(int order, long long n, const double* x, double* ou
 }
 
 // ------------------------------------------------------------------ views for other translation units
-#include "direct_view.hpp"
 
 int ifgf::direct_view(ifgf2d_ctx* ctx, ifgf::DirectView* v) {
     if (!ctx || !v) return IFGF2D_ERR_ARG;

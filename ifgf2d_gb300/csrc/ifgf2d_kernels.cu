@@ -506,6 +506,13 @@ void launch_direct_far(const double* tx, const double* ty, int nt, const int* t_
         k_direct_far<<<nblk(nt, kTile), kTile, 0, s>>>(tx, ty, nt, t_patch, t_nsp_ptr, t_nsp, sx, sy, snx, sny, s_patch, rho, ns, k,
                                                        form, eta, y, accumulate);
 }
+cudaError_t preload_direct_kernels() {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, k_sing_apply<double2>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_direct_far_split);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_direct_far);
+    return e;
+}
 void launch_hankel(int order, const double* x, int n, double2* out, cudaStream_t s) {
     if (n <= 0) return;
     k_hankel<<<nblk(n, 256), 256, 0, s>>>(order, x, n, out);
@@ -525,7 +532,8 @@ void launch_sub(const double2* a, const double2* b, long long n, double2* out, c
 }
 int arnoldi_part_size(long long n, int m) { return (int)(((n + kDotChunk - 1) / kDotChunk) * (m + 1)); }
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         double2* part, cudaStream_t s, int passes) {
+                         double2* part, cudaStream_t s, int passes, const LsqDev* lsq, cudaGraphConditionalHandle cond,
+                         bool use_cond) {
     // w holds A v_j on entry (the apply ran between k_copy_col and this call)
     const int ldh = m + 1;
     for (int pass = 0; pass < passes; ++pass) {   // classical Gram-Schmidt; the last pass sums ||w||^2
@@ -535,7 +543,8 @@ void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, do
         k_cgs_update_dyn<<<nblk(n, 64), 256, 0, s>>>(V, n, jp, h, n, w, H, ldh, pass, pass == passes - 1 ? nrm2 : nullptr);
     }
     k_scale_next<<<nblk(n, 256), 256, 0, s>>>(w, nrm2, n, V, jp, H, ldh);
-    k_advance<<<1, 32, 0, s>>>(jp);
+    if (lsq) launch_lsq_givens(H, ldh, jp, *lsq, cond, use_cond, s);
+    else k_advance<<<1, 32, 0, s>>>(jp);
 }
 void launch_store_col(const double2* z, long long n, const int* jp, double2* Z, cudaStream_t s) {
     k_store_col<<<nblk(n, 256), 256, 0, s>>>(z, n, jp, Z);

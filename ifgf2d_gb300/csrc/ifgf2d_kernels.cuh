@@ -113,6 +113,11 @@ void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const i
                     const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
                     const long long* sorting, double2* y, cudaStream_t s);
 void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s);
+// Load the direct map's kernels (singular correction, FP64 intensities, both far-sum shapes) into
+// the current device's context now.  Under lazy module loading a kernel is otherwise loaded,
+// with a device allocation for its code, on its first launch.
+cudaError_t preload_direct_kernels();
+cudaError_t preload_intensities_kernel();
 // direct path intensities (patch order), as in ForwardMap::compute_intensities
 inline void launch_intensities(const double2* x, const double* wq, const long long* perm, int N, double2* rho, cudaStream_t s) {
     launch_intensities_t<double>(x, wq, perm, N, rho, s);
@@ -192,12 +197,45 @@ void launch_sub(const double2* a, const double2* b, long long n, double2* out, c
 void launch_gather_cols(const double2* in, int B, const int* act, int Bc, long long N, double2* out, cudaStream_t s);
 void launch_scatter_cols(const double2* in, int Bc, const int* act, int B, long long N, bool add, double2* out, cudaStream_t s);
 void launch_nonfinite_check(const double2* v, long long n, int* flag, cudaStream_t s);
+// ---------------- GMRES least squares on the device (gmres_device.cu) ----------------
+// One right-hand side: R (ldh x m, column-major) the Hessenberg columns rotated to upper
+// triangular form, g (m + 1) the rotated right-hand side, gc / gs (m) the rotations, st the
+// cycle state [stopped, columns, iteration limit, iterations], sc [estimate, ||r0||, tol].
+struct LsqDev {
+    double2* R; double2* g; double* gc; double2* gs; int* st; double* sc; int m;
+};
+// B right-hand sides, each with the arrays of LsqDev at offsets r * ldh * m (R), r * (m + 1) (g),
+// r * m (gc, gs), 4 r (st), 3 r (sc)
+struct LsqBatchDev {
+    double2* R; double2* g; double* gc; double2* gs; int* st; double* sc; int m; int B;
+};
+// a restart cycle starts: g = beta e_1, j = 0, limit iterations allowed
+void launch_lsq_init(LsqDev L, int* jp, double beta, double r0n, double tol, int limit, cudaStream_t s);
+// after the Arnoldi step of column j = *jp: rotate it into R, update g and the estimate
+// |g_{j+1}| / ||r0||, stop on convergence, the limit or a breakdown, j += 1; with use_cond, set
+// the condition of the graph while-loop around the iteration (0 ends the cycle)
+void launch_lsq_givens(const double2* H, int ldh, int* jp, LsqDev L, cudaGraphConditionalHandle cond, bool use_cond,
+                       cudaStream_t s);
+// y = R^{-1} g over the cycle's columns (st[1])
+void launch_lsq_solve(LsqDev L, int ldh, double2* y, cudaStream_t s);
+// w += sum_{c < *ncols} V[:, c] y[c]
+void launch_multi_axpy_dyn(const double2* V, long long ldv, const int* ncols, const double2* y, long long n, double2* w,
+                           cudaStream_t s);
+// batched: init from per-RHS norms beta[r].x and par[3 r ..] = (||r0||, tol, iteration limit; <= 0 frozen)
+void launch_lsq_init_batch(LsqBatchDev L, const double2* beta, const double* par, cudaStream_t s);
+// column j (host index) of every running right-hand side, Hcol[i * B + r]; active[j] = how many still run
+void launch_lsq_givens_batch(const double2* Hcol, int j, LsqBatchDev L, int* active, cudaStream_t s);
+// Y[i * B + r] = (R_r^{-1} g_r)_i, zero from the right-hand side's own column count up to ncols
+void launch_lsq_solve_batch(LsqBatchDev L, int ncols, double2* Y, cudaStream_t s);
+
 // one Arnoldi step after w = A v_j, with j read from *jp (for a captured iteration graph):
 // classical Gram-Schmidt against V[:, 0..j], `passes` times (2: CGS2), into the Hessenberg
 // column j, ||w||^2 into *nrm2 (zeroed by launch_copy_col), h_{j+1,j} and
-// V[:, j+1] = w / h_{j+1,j}, then j += 1
+// V[:, j+1] = w / h_{j+1,j}; then, with lsq, the Givens step of launch_lsq_givens (which
+// advances j), else j += 1
 void launch_arnoldi_step(double2* V, long long n, int m, int* jp, double2* w, double2* h, double2* H, double* nrm2,
-                         double2* part, cudaStream_t s, int passes = 2);
+                         double2* part, cudaStream_t s, int passes = 2, const LsqDev* lsq = nullptr,
+                         cudaGraphConditionalHandle cond = 0, bool use_cond = false);
 // size (double2 entries) of the partial-sum buffer launch_arnoldi_step needs
 int arnoldi_part_size(long long n, int m);
 // Z[:, *jp] = z

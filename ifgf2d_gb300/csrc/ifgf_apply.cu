@@ -297,6 +297,10 @@ template <typename R>
 void launch_intensities_t(const double2* x, const double* wq, const long long* perm, int N, V2<R>* rho, cudaStream_t s) {
     k_intensities_t<R><<<nblk_a(N, 256), 256, 0, s>>>(x, wq, perm, N, rho);
 }
+cudaError_t preload_intensities_kernel() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, k_intensities_t<double>);
+}
 template <typename R>
 void launch_leaf_apply_t(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
                          const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int P, V2<R>* coef, cudaStream_t s,

@@ -8,6 +8,11 @@
 // at the point of the call: a host application or plugin framework that owns the device
 // memory budget and forbids driver allocations, or a latency-critical loop that cannot
 // afford the implicit synchronisation of cudaMalloc / cudaFree.
+//
+// Under CUDA's lazy module loading, the module holding the array is loaded (and the array
+// allocated) by the first lookup of its address, and each kernel by its first launch or
+// attribute query.  Both happen in the context's set-up (noalloc_prepare, called by
+// ifgf2d_precompute and so by ifgf2d_setup), never in the call itself.
 #include "../../include/ifgf2d.h"
 #include "direct_view.hpp"
 
@@ -15,30 +20,35 @@
 
 namespace {
 
-// Scratch of ifgf2d_apply_direct_noalloc: IFGF2D_NOALLOC_MAX_N complex values (1 MiB).  Every
-// GPU that loads the library holds it until the process exits.  All calls share it.
+// Scratch of ifgf2d_apply_direct_noalloc: IFGF2D_NOALLOC_MAX_N complex values (1 MiB).  Each
+// GPU holds it from the set-up of the first context on it until the process exits.  All calls
+// share it.
 static __device__ __align__(256) double2 g_noalloc_scratch[IFGF2D_NOALLOC_MAX_N];
 
 constexpr int kMaxDevices = 64;
 double2* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_lock;
 
-// Device address of the scratch array on `device`, which must be the current device.  The
-// host-side symbol is only a stand-in, so the address is looked up with cudaGetSymbolAddress
-// once per device and cached.
-int scratch_address(int device, double2** out) {
+}  // namespace
+
+namespace ifgf {
+
+// Resolves the scratch array's device address on `device` (the current device) with
+// cudaGetSymbolAddress, and loads the kernels the entry point launches.  The host-side symbol
+// is only a stand-in for the array, so the address is looked up here and cached per device.
+// It is looked up again at every set-up, so a set-up after cudaDeviceReset (which frees the
+// array and invalidates the cached address) refreshes it.
+int noalloc_prepare(int device) {
+    if (device < 0 || device >= kMaxDevices) return IFGF2D_OK;   // such a device cannot use the entry point
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IFGF2D_ERR_CUDA;
+    if (preload_direct_kernels() != cudaSuccess || preload_intensities_kernel() != cudaSuccess) return IFGF2D_ERR_CUDA;
     std::lock_guard<std::mutex> guard(g_scratch_lock);
-    if (device < 0 || device >= kMaxDevices) return IFGF2D_ERR_ARG;
-    if (!g_scratch_addr[device]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IFGF2D_ERR_CUDA;
-        g_scratch_addr[device] = static_cast<double2*>(p);
-    }
-    *out = g_scratch_addr[device];
+    g_scratch_addr[device] = static_cast<double2*>(p);
     return IFGF2D_OK;
 }
 
-}  // namespace
+}  // namespace ifgf
 
 extern "C" int ifgf2d_apply_direct_noalloc(ifgf2d_ctx* ctx, const void* d_x, void* d_y) {
     if (!ctx || !d_x || !d_y) return IFGF2D_ERR_ARG;
@@ -55,9 +65,19 @@ extern "C" int ifgf2d_apply_direct_noalloc(ifgf2d_ctx* ctx, const void* d_x, voi
         ifgf::set_error(ctx, "ifgf2d_apply_direct_noalloc: make the context's device current before the call");
         return IFGF2D_ERR_ARG;
     }
+    if (v.device < 0 || v.device >= kMaxDevices) {
+        ifgf::set_error(ctx, "ifgf2d_apply_direct_noalloc: supports device ordinals 0 to 63");
+        return IFGF2D_ERR_ARG;
+    }
     double2* rho = nullptr;
-    rc = scratch_address(v.device, &rho);
-    if (rc != IFGF2D_OK) { ifgf::set_error(ctx, "cudaGetSymbolAddress of the scratch array failed"); return rc; }
+    {
+        std::lock_guard<std::mutex> guard(g_scratch_lock);
+        rho = g_scratch_addr[v.device];
+    }
+    if (!rho) {
+        ifgf::set_error(ctx, "ifgf2d_apply_direct_noalloc: no set-up on this device resolved the scratch array");
+        return IFGF2D_ERR_STATE;
+    }
     const double2* x = static_cast<const double2*>(d_x);
     double2* y = static_cast<double2*>(d_y);
     // every entry of the scratch is rewritten by the intensities kernel before it is read

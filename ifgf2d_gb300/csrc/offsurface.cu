@@ -118,10 +118,19 @@ extern "C" int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const 
                           W.leafL.p, s);
         CK(cudaGetLastError());
     }
-    static_assert(sizeof(PropEntry) == sizeof(PropEntryD) && sizeof(InterpEntry) == sizeof(InterpEntryD),
-                  "host and device plan layouts differ");
-    CK(W.pp.upload(reinterpret_cast<const PropEntryD*>(E.pp.data()), E.pp.size()));
+    static_assert(sizeof(InterpEntry) == sizeof(InterpEntryD), "host and device plan layouts differ");
+    CK(W.pp.alloc((size_t)E.pp_total));
     CK(W.pp_ptr.upload(E.pp_ptr)); CK(W.pp_nchild.upload(E.pp_nchild));
+    {
+        DBuf<int> perr;
+        CK(perr.alloc(1));
+        CK(cudaMemsetAsync(perr.p, 0, sizeof(int), s));
+        CK(build_prop_plan(E, W.pp.p, nullptr, perr.p, s));
+        int bad = 0;
+        CK(cudaMemcpyAsync(&bad, perr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (bad) { free_eval(ctx); return fail(ctx, IFGF2D_ERR_GEOMETRY, "internal: a propagation node's child cone is missing"); }
+    }
     CK(W.ip.upload(reinterpret_cast<const InterpEntryD*>(E.ip.data()), E.ip.size()));
     CK(W.ip_ptr.upload(E.ip_ptr));
     CK(W.nb_ptr.upload(E.nbr_ptr)); CK(W.nb_box.upload(E.nbr_box));

@@ -197,49 +197,66 @@ void cousins_of(const TreeLevel& L, long long m, std::vector<int>& out) {
 // Cones of level l and the propagation plan of its parents.  `part` holds the wanted cones
 // (box index << 32 | nonrel cone, each list sorted and unique) that the targets see; the cones
 // needed by the parents' interpolation nodes are added here through the protobox routing table
-// (BoxTree.h:299-428).  Fills T.L[l]'s cone lists and appends, for every parent cone of level
-// l-1 in global-id order, its plan entries to `lp` and its CSR row to T.pp_ptr / pp_nchild.
+// (BoxTree.h:299-428).  Fills T.L[l]'s cone lists and, for l > 2, appends the level's slot form
+// of the propagation plan (PropSlots, entries in global parent-id order) and its CSR rows to
+// T.pp_ptr / pp_nchild.
 std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long long>>& part, const std::vector<double>& ns,
-                     const std::vector<double>& na, std::vector<PropEntry>& lp) {
+                         const std::vector<double>& na) {
     TreeLevel& L = T.L[l];
     LevelGeo G{&L, T.min_x, T.min_y};
     const int P = T.P, Ps = T.Ps;
-    const double k = T.k;
     auto key = [](long long b, long long nonrel) { return ((unsigned long long)b << 32) | (unsigned long long)nonrel; };
     // cones needed by the parents' interpolation nodes, through the protobox routing
     // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
     // routing is computed once, from the first parent box (in cone order) that has it.
-    struct Route { long long pnc; int pos; int first_pc; std::vector<std::pair<long long, int>> e; };
+    struct Route { long long pnc; int pos; int first_pc; std::vector<long long> nr, uniq; };
     std::vector<Route> routes;
     std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
+    std::vector<int> child_box;         // per (parent box * 4 + pos): child box index or -1
     const TreeLevel* Lpp = l > 2 ? &T.L[l - 1] : nullptr;
     if (Lpp) {
         const TreeLevel& Lp = *Lpp;
         LevelGeo Gp{&Lp, T.min_x, T.min_y};
         const size_t npar = Lp.cone_nonrel.size();
+        // the children of each parent box: the child level's boxes are sorted, so a parent's
+        // children follow one another
+        child_box.assign(Lp.boxes.size() * 4, -1);
+        parallel_for((long long)L.boxes.size(), [&](long long c0, long long c1) {
+            for (long long c = c0; c < c1; ++c) {
+                const int pb = Lp.find_box(L.boxes[c] / 4);
+                if (pb >= 0) child_box[(size_t)pb * 4 + (size_t)(L.boxes[c] % 4)] = (int)c;
+            }
+        });
         route_of.assign(npar * 4, -1);
-        std::unordered_map<long long, int> seen;   // pnc * 4 + pos -> route
+        // pnc * 4 + pos -> route, over the parent level's cone segment numbers
+        long long maxnc = 0;
+        for (long long nc : Lp.cone_nonrel) maxnc = std::max(maxnc, nc);
+        std::vector<int> seen((size_t)(maxnc + 1) * 4, -1);
         for (size_t pc = 0; pc < npar; ++pc) {
-            const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
+            const long long pnc = Lp.cone_nonrel[pc];
             for (int pos = 0; pos < 4; ++pos) {
-                if (L.find_box(pm * 4 + pos) < 0) continue;
-                auto it = seen.find(pnc * 4 + pos);
-                if (it == seen.end()) {
-                    it = seen.emplace(pnc * 4 + pos, (int)routes.size()).first;
-                    routes.push_back(Route{pnc, pos, (int)pc, {}});
+                if (child_box[(size_t)Lp.cone_box[pc] * 4 + pos] < 0) continue;
+                int& r = seen[(size_t)(pnc * 4 + pos)];
+                if (r < 0) {
+                    r = (int)routes.size();
+                    routes.push_back(Route{pnc, pos, (int)pc, {}, {}});
                 }
-                route_of[pc * 4 + pos] = it->second;
+                route_of[pc * 4 + pos] = r;
             }
         }
         parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
             for (long long r = r0; r < r1; ++r) {
                 Route& R = routes[r];
                 const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
+                R.nr.resize(P);
                 for (int it = 0; it < P; ++it) {
                     double px = ns[it % Ps], py = na[it / Ps];
                     Gp.cheb_to_cart(pm, R.pnc, px, py);
-                    R.e.push_back({G.nonrel_of(pm * 4 + R.pos, px, py), it});
+                    R.nr[it] = G.nonrel_of(pm * 4 + R.pos, px, py);
                 }
+                R.uniq = R.nr;
+                std::sort(R.uniq.begin(), R.uniq.end());
+                R.uniq.erase(std::unique(R.uniq.begin(), R.uniq.end()), R.uniq.end());
             }
         });
         const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, (long long)npar / 256));
@@ -250,12 +267,11 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
                 const size_t p0 = npar * c / nchunk, p1 = npar * (c + 1) / nchunk;
                 auto& w = part[base + c];
                 for (size_t pc = p0; pc < p1; ++pc) {
-                    const long long pm = Lp.boxes[Lp.cone_box[pc]];
                     for (int pos = 0; pos < 4; ++pos) {
                         const int r = route_of[pc * 4 + pos];
                         if (r < 0) continue;
-                        const int cb = L.find_box(pm * 4 + pos);
-                        for (auto& e : routes[r].e) w.push_back(key(cb, e.first));
+                        const int cb = child_box[(size_t)Lp.cone_box[pc] * 4 + pos];
+                        for (long long nr : routes[r].uniq) w.push_back(key(cb, nr));
                     }
                 }
                 sort_unique(w);
@@ -275,57 +291,45 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
     L.cone_base = T.total_cones;
     T.total_cones += (int)L.cone_nonrel.size();
     if (!Lpp) return "";
-    // propagation plan of this level: parents are the cones of level l-1, entries in
+    // propagation plan of this level in slot form: parents are the cones of level l-1, slots in
     // global parent-id order (levels are built upwards, so level l-1's id range is final)
     const TreeLevel& Lp = *Lpp;
-    LevelGeo Gp{&Lp, T.min_x, T.min_y};
     if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
     if ((long long)T.pp_ptr.size() - 1 != Lp.cone_base) return "internal: propagation plan out of order";
     const size_t npar = Lp.cone_nonrel.size();
-    std::vector<int> nchv(npar, 0);
-    for (size_t pc = 0; pc < npar; ++pc)
-        for (int pos = 0; pos < 4; ++pos) nchv[pc] += route_of[pc * 4 + pos] >= 0;
-    std::vector<size_t> off(npar + 1, 0);
-    for (size_t pc = 0; pc < npar; ++pc) off[pc + 1] = off[pc] + (size_t)nchv[pc] * P;
-    lp.resize(off[npar]);
-    std::vector<char> bad(npar, 0);
+    PropSlots S;
+    S.level = l;
+    S.entry_base = T.pp_total;
+    for (const Route& R : routes) S.route_nonrel.insert(S.route_nonrel.end(), R.nr.begin(), R.nr.end());
+    long long done = T.pp_ptr.back();
+    std::vector<long long> first(npar + 1, 0);   // per parent cone: its first slot
+    for (size_t pc = 0; pc < npar; ++pc) {
+        int nch = 0;
+        for (int pos = 0; pos < 4; ++pos) nch += route_of[pc * 4 + pos] >= 0;
+        first[pc + 1] = first[pc] + nch;
+        done += (long long)nch * P;
+        T.pp_nchild.push_back(nch);
+        T.pp_ptr.push_back(done);
+        T.prop_evals += (long long)nch * P;
+    }
+    const size_t nslot = (size_t)first[npar];
+    S.slot_parent.resize(nslot); S.slot_child_box.resize(nslot); S.slot_pos.resize(nslot); S.slot_route.resize(nslot);
     parallel_for((long long)npar, [&](long long p0, long long p1) {
         for (long long pc = p0; pc < p1; ++pc) {
-            const long long pm = Lp.boxes[Lp.cone_box[pc]], pnc = Lp.cone_nonrel[pc];
-            size_t o = off[pc];
+            long long q = first[pc];
             for (int pos = 0; pos < 4; ++pos) {
                 const int r = route_of[pc * 4 + pos];
                 if (r < 0) continue;
-                const long long cm = pm * 4 + pos;
-                const int cb = L.find_box(cm);
-                PropEntry* slot = &lp[o];
-                for (int it = 0; it < P; ++it) slot[it] = PropEntry{0, 0, 0.0, 0.0, 0.0, 0.0};
-                for (auto& e : routes[r].e) {
-                    const int it = e.second;
-                    double px = ns[it % Ps], py = na[it / Ps];
-                    const double rp = Gp.cheb_to_radius(pnc % Lp.nrad, px);
-                    Gp.cheb_to_cart(pm, pnc, px, py);
-                    double lx = px, ly = py;
-                    G.cart_to_cheb(cm, e.first, lx, ly);
-                    const double rc = G.cheb_to_radius(e.first % L.nrad, lx);
-                    const int cc = L.find_cone(cb, e.first);
-                    if (cc < 0) { bad[pc] = 1; continue; }
-                    const std::complex<double> fc = std::complex<double>(std::cos(k * rc), std::sin(k * rc)) / std::sqrt(rc);
-                    const std::complex<double> fp = std::complex<double>(std::cos(k * rp), std::sin(k * rp)) / std::sqrt(rp);
-                    const std::complex<double> w = fc / fp;
-                    slot[it] = PropEntry{L.cone_base + cc, it, lx, ly, w.real(), w.imag()};
-                }
-                o += P;
+                S.slot_parent[q] = (int)pc;
+                S.slot_child_box[q] = child_box[(size_t)Lp.cone_box[pc] * 4 + pos];
+                S.slot_pos[q] = pos;
+                S.slot_route[q] = r;
+                ++q;
             }
         }
-    });
-    long long done = T.pp_ptr.back();
-    for (size_t pc = 0; pc < npar; ++pc) {
-        if (bad[pc]) return "internal: child cone missing";
-        T.pp_nchild.push_back(nchv[pc]);
-        T.pp_ptr.push_back(done + (long long)off[pc + 1]);
-        T.prop_evals += (long long)nchv[pc] * P;
-    }
+    }, 4096);
+    T.pp_total = done;
+    T.prop_slots.push_back(std::move(S));
     return "";
 }
 
@@ -436,7 +440,6 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     // relevant cones, level by level (BoxTree.h:553-583).  A wanted cone is the key
     // (box index << 32 | nonrel cone); each level's keys are collected per thread, then sorted
     // and deduplicated, which gives the cones in (box, nonrel) order.
-    std::vector<std::vector<PropEntry>> level_pp(nlevels);
     for (int l = 2; l < nlevels; ++l) {
         TreeLevel& L = T.L[l];
         LevelGeo G{&L, T.min_x, T.min_y};
@@ -462,27 +465,43 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                 }
             }, 1);
         }
-        std::string msg = finish_level(T, l, part, ns, na, level_pp[l]);
+        std::string msg = finish_level(T, l, part, ns, na);
         if (!msg.empty()) return msg;
-    }
-    {
-        size_t tot = 0;
-        for (auto& v : level_pp) tot += v.size();
-        T.pp.reserve(tot);
-        for (auto& v : level_pp) { T.pp.insert(T.pp.end(), v.begin(), v.end()); std::vector<PropEntry>().swap(v); }
     }
     // leaf-level cones have no children: close the propagation CSR for them
     if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
-    while ((long long)T.pp_ptr.size() - 1 < T.total_cones) { T.pp_ptr.push_back((long long)T.pp.size()); T.pp_nchild.push_back(0); }
+    while ((long long)T.pp_ptr.size() - 1 < T.total_cones) { T.pp_ptr.push_back(T.pp_total); T.pp_nchild.push_back(0); }
     for (size_t c = 0; c < T.L[D].cone_nonrel.size(); ++c) T.leaf_evals += (long long)P * T.leaf_count[T.L[D].cone_box[c]];
 
-    // interpolation plan (BoxTree.h:876-937): per sorted target, all levels, all cousins
+    // interpolation plan (BoxTree.h:876-937): per sorted target, all levels, all cousins.  A
+    // first pass counts each target's terms (its boxes' cousin counts), a second fills them in
+    // place.
     T.ip_ptr.assign(N + 1, 0);
     {
-        std::vector<std::vector<InterpEntry>> per(N);
+        std::vector<std::vector<int>> ncous(nlevels);   // per level and box: cousin count
+        for (int l = 2; l <= D; ++l) {
+            const TreeLevel& L = T.L[l];
+            ncous[l].assign(L.boxes.size(), 0);
+            parallel_for((long long)L.boxes.size(), [&](long long b0, long long b1) {
+                std::vector<int> cs;
+                for (long long b = b0; b < b1; ++b) { cousins_of(L, L.boxes[b], cs); ncous[l][b] = (int)cs.size(); }
+            }, 256);
+        }
+        std::vector<int> cnt(N, 0);
+        parallel_for(N, [&](long long i0, long long i1) {
+            for (int l = D; l >= 2; --l) {
+                const TreeLevel& L = T.L[l];
+                const int shift = 2 * (D - l);
+                for (long long i = i0; i < i1; ++i) cnt[i] += ncous[l][L.find_box(scode[i] >> shift)];
+            }
+        });
+        for (long long i = 0; i < N; ++i) T.ip_ptr[i + 1] = T.ip_ptr[i] + cnt[i];
+        T.ip.resize(T.ip_ptr[N]);
         std::vector<char> bad(N, 0);
         parallel_for(N, [&](long long i0, long long i1) {
             std::vector<int> cs;
+            std::vector<int> o(i1 - i0);
+            for (long long i = i0; i < i1; ++i) o[i - i0] = T.ip_ptr[i];
             for (int l = D; l >= 2; --l) {   // the reference interpolates level D first (BoxTree.h:1049-1061)
                 const TreeLevel& L = T.L[l];
                 LevelGeo G{&L, T.min_x, T.min_y};
@@ -495,18 +514,15 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                         double lx = T.xs[i], ly = T.ys[i];
                         const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
                         const int cc = L.find_cone(c, nonrel);
-                        if (cc < 0) { bad[i] = 1; continue; }
+                        if (cc < 0) { bad[i] = 1; T.ip[o[i - i0]++] = InterpEntry{0, l, 0.0, 0.0, 0.0, 0.0}; continue; }
                         const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
                         const double sr = std::sqrt(r);
-                        per[i].push_back(InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(k * r) / sr, std::sin(k * r) / sr});
+                        T.ip[o[i - i0]++] = InterpEntry{L.cone_base + cc, l, lx, ly, std::cos(k * r) / sr, std::sin(k * r) / sr};
                     }
                 }
             }
         });
         for (long long i = 0; i < N; ++i) if (bad[i]) return "internal: interpolation cone missing";
-        for (long long i = 0; i < N; ++i) T.ip_ptr[i + 1] = T.ip_ptr[i] + (int)per[i].size();
-        T.ip.reserve(T.ip_ptr[N]);
-        for (long long i = 0; i < N; ++i) T.ip.insert(T.ip.end(), per[i].begin(), per[i].end());
         T.interp_evals = T.ip_ptr[N];
     }
     return "";
@@ -521,17 +537,19 @@ void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, s
     for (int i = 0; i < T.Pang; ++i) na[T.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * T.Pang));
     const size_t n = L.cone_nonrel.size() * T.P;
     x.resize(n); y.resize(n); ir.resize(n); ii.resize(n);
-    for (size_t c = 0; c < L.cone_nonrel.size(); ++c) {
-        const long long m = L.boxes[L.cone_box[c]], nonrel = L.cone_nonrel[c];
-        for (int it = 0; it < T.P; ++it) {
-            double px = ns[it % T.Ps], py = na[it / T.Ps];
-            const double r = G.cheb_to_radius(nonrel % L.nrad, px);
-            G.cheb_to_cart(m, nonrel, px, py);
-            const std::complex<double> f = std::complex<double>(std::cos(T.k * r), std::sin(T.k * r)) / std::sqrt(r);
-            const std::complex<double> inv = 1.0 / f;
-            x[c * T.P + it] = px; y[c * T.P + it] = py; ir[c * T.P + it] = inv.real(); ii[c * T.P + it] = inv.imag();
+    parallel_for((long long)L.cone_nonrel.size(), [&](long long c0, long long c1) {
+        for (long long c = c0; c < c1; ++c) {
+            const long long m = L.boxes[L.cone_box[c]], nonrel = L.cone_nonrel[c];
+            for (int it = 0; it < T.P; ++it) {
+                double px = ns[it % T.Ps], py = na[it / T.Ps];
+                const double r = G.cheb_to_radius(nonrel % L.nrad, px);
+                G.cheb_to_cart(m, nonrel, px, py);
+                const std::complex<double> f = std::complex<double>(std::cos(T.k * r), std::sin(T.k * r)) / std::sqrt(r);
+                const std::complex<double> inv = 1.0 / f;
+                x[c * T.P + it] = px; y[c * T.P + it] = py; ir[c * T.P + it] = inv.real(); ii[c * T.P + it] = inv.imag();
+            }
         }
-    }
+    }, 256);
 }
 
 }  // namespace ifgf
@@ -573,7 +591,6 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
     for (int i = 0; i < E.Ps; ++i) ns[E.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Ps));
     for (int i = 0; i < E.Pang; ++i) na[E.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Pang));
     const int P = E.P;
-    std::vector<std::vector<PropEntry>> level_pp(nlevels);
     for (int l = 2; l < nlevels; ++l) {
         TreeLevel& L = E.L[l];
         LevelGeo G{&L, E.min_x, E.min_y};
@@ -596,7 +613,7 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
         bool any = false;
         for (auto& w : part) any = any || !w.empty();
         if (!any && l == 2) part.assign(1, std::vector<unsigned long long>{});
-        std::string msg = finish_level(E, l, part, ns, na, level_pp[l]);
+        std::string msg = finish_level(E, l, part, ns, na);
         if (!msg.empty() && msg != "The number of cone segments on any level cannot be 0") return msg;
         if (!msg.empty()) {   // no cone at this level: empty lists, nothing below needs it either
             TreeLevel& Le = E.L[l];
@@ -610,14 +627,8 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
             }
         }
     }
-    {
-        size_t tot = 0;
-        for (auto& v : level_pp) tot += v.size();
-        E.pp.reserve(tot);
-        for (auto& v : level_pp) { E.pp.insert(E.pp.end(), v.begin(), v.end()); std::vector<PropEntry>().swap(v); }
-    }
     if (E.pp_ptr.empty()) E.pp_ptr.assign(1, 0);
-    while ((long long)E.pp_ptr.size() - 1 < E.total_cones) { E.pp_ptr.push_back((long long)E.pp.size()); E.pp_nchild.push_back(0); }
+    while ((long long)E.pp_ptr.size() - 1 < E.total_cones) { E.pp_ptr.push_back(E.pp_total); E.pp_nchild.push_back(0); }
     for (size_t c = 0; c < E.L[D].cone_nonrel.size(); ++c) E.leaf_evals += (long long)P * E.leaf_count[E.L[D].cone_box[c]];
     // per target: interpolation entries, level D first (BoxTree.h:1049-1061), and the
     // adjacent leaf boxes of the direct near field

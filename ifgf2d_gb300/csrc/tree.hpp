@@ -7,7 +7,8 @@
 //   * an interpolation plan: per target point, its (cone, s, theta, e^{ikr}/sqrt r) entries
 //     over all levels and cousins (BoxTree.h:876-937);
 //   * a propagation plan: per parent cone, per child and interpolation node, the child cone,
-//     its Chebyshev coordinates and the factor ratio (BoxTree.h:767-868);
+//     its Chebyshev coordinates and the factor ratio (BoxTree.h:767-868), kept here in the
+//     compact slot form (PropSlots) whose entries the device computes;
 //   * per leaf box, the neighbour ranges of the near field (BoxTree.h:614-683).
 #pragma once
 
@@ -49,6 +50,22 @@ struct PropEntry {     // one (parent cone, child, node) term of the propagation
     double wr, wi;     // e^{ik r_child}/sqrt(r_child) / (e^{ik r_parent}/sqrt(r_parent))
 };
 
+// The propagation plan of one level pair (parents at level l - 1, children at level l), in
+// the compact form the host builds: the entries themselves (PropEntry, one per slot and node)
+// are computed on the device from it (plan_device.cu).  A slot is one (parent cone, child box)
+// pair; slots are in parent-cone order, then child position, so slot q's entries are
+// pp[entry_base + q * P + node].  route_nonrel holds, per route (a parent cone segment and a
+// child position, BoxTree.h:299-428), the child's cone segment of each of the P parent nodes.
+struct PropSlots {
+    int level = 0;                        // child level l
+    long long entry_base = 0;             // global index of the first entry
+    std::vector<int> slot_parent;         // parent cone, local index at level l - 1
+    std::vector<int> slot_child_box;      // child box index at level l
+    std::vector<int> slot_pos;            // child position 0..3 (child Morton = parent * 4 + pos)
+    std::vector<int> slot_route;          // route index
+    std::vector<long long> route_nonrel;  // per route, P child cone segments in node order
+};
+
 struct Tree {
     int nlevels = 0, Ps = 5, Pang = 5, P = 25;
     long long N = 0;
@@ -65,9 +82,11 @@ struct Tree {
     std::vector<int> ip_ptr;
     std::vector<InterpEntry> ip;
     // propagation plan: for each level l in [3, D] the parent cones are those of level l-1;
-    // CSR over parent global cone ids: pp_ptr[c] .. pp_ptr[c+1], grouped by child then node
+    // CSR over parent global cone ids: pp_ptr[c] .. pp_ptr[c+1], grouped by child then node.
+    // The entries are built on the device from prop_slots (pp_total of them).
     std::vector<long long> pp_ptr;
-    std::vector<PropEntry> pp;
+    std::vector<PropSlots> prop_slots;
+    long long pp_total = 0;
     std::vector<int> pp_nchild;                // per parent cone: number of relevant children
     long long prop_evals = 0, interp_evals = 0, leaf_evals = 0, near_pairs = 0;
 };

@@ -73,6 +73,10 @@ typedef struct ifgf2d_options {
     int Pang;                      /* IFGF angular Chebyshev nodes (template Pang, default 5) */
     int formulation;               /* IFGF2D_SINGLE_LAYER (template Formulation) or IFGF2D_COMBINED */
     double coupling;               /* eta of IFGF2D_COMBINED; <= 0 means eta = wavenumber */
+    int device_geometry;           /* 1: ifgf2d_create computes the points, patch bounding boxes and
+                                    * near-singular points on the current GPU (the patch limits stay on
+                                    * the host); 0: all on the host, bit for bit as the reference's
+                                    * constructor (ForwardMap.tpp:37-285).  Extension. */
 } ifgf2d_options;
 
 typedef struct ifgf2d_ctx ifgf2d_ctx;
@@ -268,11 +272,13 @@ int ifgf2d_measure_fp64_peak(double* tflops);
  * synchronisation of cudaMalloc / cudaFree.  Its scratch (the weighted density) is a fixed
  * 1 MiB device array inside the library, so N must not exceed IFGF2D_NOALLOC_MAX_N
  * (IFGF2D_ERR_ARG otherwise).  The context must have been precomputed (ifgf2d_precompute or
- * ifgf2d_setup) and its device must be current.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Work is queued on the context's stream; synchronise before reading d_y.  All
- * calls share the one array, so calls that overlap on the GPU (several contexts or streams
- * at once) race. */
+ * ifgf2d_setup) and its device must be current.  That set-up looks up the array's device
+ * address (cudaGetSymbolAddress, which under lazy module loading loads the array) and loads
+ * the kernels the call launches, so the call itself loads and allocates nothing.
+ * cudaDeviceReset frees the array: run a set-up again on that device before the next call.
+ * Work is queued on the context's stream; synchronise before reading d_y.  All calls share
+ * the one array, so calls that overlap on the GPU (several contexts or streams at once) race:
+ * order them on one stream or synchronise between them. */
 int ifgf2d_apply_direct_noalloc(ifgf2d_ctx* ctx, const void* d_x, void* d_y);
 
 #ifdef __cplusplus

@@ -1,8 +1,10 @@
 // ifgf2d/ForwardMap.hpp -- header-only C++ drop-in for IFGF2D's ForwardMap, over the C ABI.
 //
 // Keeps the reference's class interface (ForwardMap/ForwardMap.hpp:49-177,
-// ForwardMap/LinearOperator.hpp:27-58, Geometry/Curve.hpp:10-161, IFGF_Source/BoxTree.h) so
-// that code written against the reference compiles against this header:
+// ForwardMap/LinearOperator.hpp:27-58 in ifgf2d/LinearOperator.hpp, the opGMRES solver of
+// ForwardMap/opGMRES.hpp:273-396 in ifgf2d/opGMRES.hpp, Geometry/Curve.hpp:10-161,
+// IFGF_Source/BoxTree.h) so that code written against the reference compiles against this
+// header:
 //
 //   std::vector<std::unique_ptr<Curve>> curves;
 //   curves.emplace_back(std::make_unique<Kite>());
@@ -14,6 +16,9 @@
 // Vectors are Eigen::VectorXcd when Eigen is available (as in the reference), otherwise
 // std::vector<std::complex<double>>.  Errors throw std::logic_error / std::invalid_argument like
 // the reference; BoxTree is an opaque handle (the device tree lives in the ForwardMap's context).
+// The operator is fixed by the wavenumber of the last compute_precomputations /
+// precomps_and_setup: compute_Ax_unacc and propagate_unacc throw std::invalid_argument when
+// called with another one (the reference would mix the two wavenumbers, ForwardMap.tpp:517-540).
 // Link with -lifgf2d.
 #pragma once
 
@@ -26,13 +31,8 @@
 #include <cmath>
 
 #include "../ifgf2d.h"
-
-#if __has_include(<Eigen/Dense>)
-#include <Eigen/Dense>
-namespace ifgf2d_cpp { using Vector = Eigen::VectorXcd; }
-#else
-namespace ifgf2d_cpp { using Vector = std::vector<std::complex<double>>; }
-#endif
+#include "LinearOperator.hpp"
+#include "opGMRES.hpp"
 
 // FormulationType (ForwardMap/GreenFunctions.hpp:15-20).  SingleLayer and Combined are
 // supported; Combined is the sound-soft combined field operator (1/2 I + K - i eta S).
@@ -116,18 +116,15 @@ class BoxTree {
     std::vector<long long> sorting_;
 };
 
-// LinearOperator (ForwardMap/LinearOperator.hpp:43-58)
-class LinearOperator {
-  public:
-    using Vec = ifgf2d_cpp::Vector;
-    LinearOperator(int rows, int cols, const std::function<void(const Vec&, Vec&)>& mapping)
-        : rows_(rows), cols_(cols), mapping_(mapping) {}
-    int rows() const { return rows_; }
-    int cols() const { return cols_; }
-    Vec operator*(const Vec& x) const { Vec y; mapping_(x, y); return y; }
-  protected:
-    int rows_, cols_;
-    std::function<void(const Vec&, Vec&)> mapping_;
+// Patch<Nroot> (Geometry/Patch.hpp:36-110): the parameter limits and near-singular lists of
+// one patch, as the device discretisation computed them.  The rectangular-polar matrix
+// (precomputations_) stays on the device; ForwardMap::precomputations(patch) reads it.
+template <int N>
+struct Patch {
+    double t1 = 0.0, t2 = 0.0;
+    double delta = 0.0;
+    std::vector<long long> near_singular_point_indices_;
+    std::vector<double> near_singular_point_ts_;
 };
 
 template <int Np, FormulationType Formulation, int Ps = 5, int Pang = 5, int Nroot = 10>
@@ -137,19 +134,23 @@ class ForwardMap {
   public:
     using Vec = ifgf2d_cpp::Vector;
 
+    std::vector<Patch<Nroot>> patches_;
     long long num_patches_ = 0;
     long long total_num_unknowns_ = 0;
-    double delta_, p_;
+    double delta_;
+    std::vector<std::unique_ptr<Curve>> curves_;
+    std::vector<std::vector<Junction>> curve_touch_tracker_;
+    double p_;
     double eta_ = 0.0;                   // coupling of Combined (<= 0: eta = wavenumber)
+    std::vector<double> xs_, ys_, nxs_, nys_;
     int GMRES_MAX_ITER_ = 300;
     double GMRES_TOLERANCE_ = 1e-10;
-    std::vector<double> xs_, ys_, nxs_, nys_;
 
     // ForwardMap.tpp:15-35
     ForwardMap(double delta, std::vector<std::unique_ptr<Curve>> curves, const std::vector<std::vector<Junction>>& touch,
                double wavelengths_per_patch, double patch_split_wavenumber, double p = 4, int patches_per_curve = 0,
-               double eta = 0.0)
-        : delta_(delta), p_(p), eta_(eta) {
+               double eta = 0.0, bool device_geometry = false)
+        : delta_(delta), curve_touch_tracker_(touch), p_(p), eta_(eta) {
         std::vector<ifgf2d_curve> cs;
         for (auto& c : curves) cs.push_back(c->descriptor());
         std::vector<ifgf2d_junction> js;
@@ -161,30 +162,64 @@ class ForwardMap {
         o.Ps = Ps; o.Pang = Pang;
         o.formulation = Formulation == FormulationType::Combined ? IFGF2D_COMBINED : IFGF2D_SINGLE_LAYER;
         o.coupling = eta;
+        o.device_geometry = device_geometry ? 1 : 0;
         ifgf2d_ctx* ctx = nullptr;
         const int rc = ifgf2d_create(cs.data(), (int)cs.size(), js.empty() ? nullptr : js.data(), (int)js.size(), &o, &ctx);
         ctx_.reset(ctx);
         check(rc);
+        curves_ = std::move(curves);
         total_num_unknowns_ = ifgf2d_num_unknowns(ctx);
         num_patches_ = ifgf2d_num_patches(ctx);
         const size_t n = (size_t)total_num_unknowns_;
         xs_.resize(n); ys_.resize(n); nxs_.resize(n); nys_.resize(n);
         check(ifgf2d_get_points(ctx, xs_.data(), ys_.data(), nxs_.data(), nys_.data()));
+        // patches_: limits and near-singular lists (ForwardMap.tpp:37-285)
+        std::vector<double> t12(2 * (size_t)num_patches_);
+        std::vector<long long> cnt((size_t)num_patches_);
+        check(ifgf2d_get_patches(ctx, t12.data(), cnt.data()));
+        long long tot = 0;
+        for (long long c : cnt) tot += c;
+        std::vector<long long> idx((size_t)std::max(tot, 1LL));
+        std::vector<double> tv((size_t)std::max(tot, 1LL));
+        check(ifgf2d_get_near_singular(ctx, idx.data(), tv.data()));
+        patches_.resize((size_t)num_patches_);
+        long long o0 = 0;
+        for (long long q = 0; q < num_patches_; ++q) {
+            Patch<Nroot>& P = patches_[(size_t)q];
+            P.t1 = t12[2 * q]; P.t2 = t12[2 * q + 1]; P.delta = delta;
+            P.near_singular_point_indices_.assign(idx.begin() + o0, idx.begin() + o0 + cnt[q]);
+            P.near_singular_point_ts_.assign(tv.begin() + o0, tv.begin() + o0 + cnt[q]);
+            o0 += cnt[q];
+        }
     }
 
     // ForwardMap.tpp:391-423
     void compute_precomputations(std::complex<double> wavenumber) {
-        check(ifgf2d_precompute(ctx_.get(), real_k(wavenumber)));
+        const double k = real_k(wavenumber);
+        check(ifgf2d_precompute(ctx_.get(), k));
+        k_ = k;
+    }
+    // patch p's precomputations_ (Patch.hpp:55): Np x (Np + n_ns), column-major
+    Vec precomputations(long long patch) {
+        if (patch < 0 || patch >= num_patches_) throw std::invalid_argument("patch index out of range");
+        Vec m((size_t)Np * (Np + patches_[(size_t)patch].near_singular_point_indices_.size()));
+        check(ifgf2d_get_precomputations(ctx_.get(), patch, reinterpret_cast<double*>(m.data())));
+        return m;
     }
     // ForwardMap.tpp:542-565 (nlevels <= 0: the deepest tree passing the neighbourhood check)
     void precomps_and_setup(std::complex<double> wavenumber, int nlevels, BoxTree<Ps, Pang>& boxes) {
-        check(ifgf2d_setup(ctx_.get(), real_k(wavenumber), nlevels));
+        const double k = real_k(wavenumber);
+        check(ifgf2d_setup(ctx_.get(), k, nlevels));
+        k_ = k;
         boxes.nlevels_ = ifgf2d_get_nlevels(ctx_.get());
         boxes.sorting_.resize((size_t)total_num_unknowns_);
         check(ifgf2d_get_sorting(ctx_.get(), boxes.sorting_.data()));
     }
     // ForwardMap.tpp:517-540
-    void compute_Ax_unacc(const Vec& density, Vec& out, std::complex<double> /*wavenumber*/) { apply(density, out, IFGF2D_APPLY_DIRECT); }
+    void compute_Ax_unacc(const Vec& density, Vec& out, std::complex<double> wavenumber) {
+        same_k(wavenumber, "compute_Ax_unacc");
+        apply(density, out, IFGF2D_APPLY_DIRECT);
+    }
     Vec compute_Ax_unacc(const Vec& density, std::complex<double> k) { Vec y; compute_Ax_unacc(density, y, k); return y; }
     // ForwardMap.tpp:609-655
     void compute_Ax_acc(const Vec& density, Vec& out, BoxTree<Ps, Pang>& /*boxes*/) { apply(density, out, IFGF2D_APPLY_IFGF); }
@@ -194,32 +229,38 @@ class ForwardMap {
         BoxTree<Ps, Pang> boxes;
         if (accelerated) precomps_and_setup(wavenumber, nlevels, boxes);
         else compute_precomputations(wavenumber);
-        Vec x(rhs.size());
-        int iters = 0;
-        double err = 0.0;
-        const int rc = ifgf2d_solve(ctx_.get(), reinterpret_cast<const double*>(rhs.data()), reinterpret_cast<double*>(x.data()),
-                                    accelerated ? IFGF2D_APPLY_IFGF : IFGF2D_APPLY_DIRECT, GMRES_TOLERANCE_, GMRES_MAX_ITER_,
-                                    GMRES_MAX_ITER_, &iters, &err);
-        last_iters_ = iters; last_error_ = err;
-        if (rc != IFGF2D_OK && rc != IFGF2D_ERR_NOCONV) check(rc);
+        LinearOperator B = linear_operator(boxes, accelerated);
+        Eigen::opGMRES<LinearOperator> func(B);
+        func.setMaxIterations(GMRES_MAX_ITER_);
+        func.set_restart(GMRES_MAX_ITER_);
+        func.setTolerance(GMRES_TOLERANCE_);
+        Vec x = func.solve(rhs);
+        last_iters_ = (int)func.iterations();
+        last_error_ = func.error();
         return x;
     }
     // ForwardMap.tpp:701-727
     Vec propagate_unacc(const std::vector<double> x_prop, const std::vector<double> y_prop, Vec density,
-                        std::complex<double> /*wavenumber*/) {
+                        std::complex<double> wavenumber) {
+        same_k(wavenumber, "propagate_unacc");
         if (x_prop.size() != y_prop.size()) throw std::invalid_argument("x_prop and y_prop differ in length");
+        if ((long long)density.size() != total_num_unknowns_) throw std::invalid_argument("density has the wrong length");
         Vec out(x_prop.size());
         check(ifgf2d_propagate(ctx_.get(), (long long)x_prop.size(), x_prop.data(), y_prop.data(),
                                reinterpret_cast<const double*>(density.data()), reinterpret_cast<double*>(out.data())));
         return out;
     }
+    // The operator ForwardMap::solve hands to GMRES (ForwardMap.tpp:673-682), bound to this map's
+    // context so that Eigen::opGMRES (ifgf2d/opGMRES.hpp) solves it on the GPU.
     LinearOperator linear_operator(BoxTree<Ps, Pang>& boxes, bool accelerated = true) {
         return LinearOperator((int)total_num_unknowns_, (int)total_num_unknowns_,
                               [this, &boxes, accelerated](const Vec& x, Vec& y) {
                                   if (accelerated) compute_Ax_acc(x, y, boxes);
-                                  else compute_Ax_unacc(x, y, 0.0);
-                              });
+                                  else compute_Ax_unacc(x, y, k_);
+                              },
+                              ctx_.get(), accelerated ? IFGF2D_APPLY_IFGF : IFGF2D_APPLY_DIRECT);
     }
+    double wavenumber() const { return k_; }
     int last_iterations() const { return last_iters_; }
     double last_error() const { return last_error_; }
     ifgf2d_ctx* context() { return ctx_.get(); }
@@ -227,12 +268,21 @@ class ForwardMap {
   private:
     struct Deleter { void operator()(ifgf2d_ctx* c) const { if (c) ifgf2d_destroy(c); } };
     std::unique_ptr<ifgf2d_ctx, Deleter> ctx_;
+    double k_ = 0.0;                     // wavenumber of the current operator (0: none yet)
     int last_iters_ = 0;
     double last_error_ = 0.0;
 
     static double real_k(std::complex<double> k) {
         if (k.imag() != 0.0) throw std::invalid_argument("ifgf2d: the wavenumber must be real");
         return k.real();
+    }
+    // the operator's singular corrections were computed for k_; another wavenumber is an error
+    void same_k(std::complex<double> wavenumber, const char* who) const {
+        const double k = real_k(wavenumber);
+        if (k_ == 0.0) throw std::logic_error(std::string("ifgf2d: ") + who + " before compute_precomputations");
+        if (k != k_)
+            throw std::invalid_argument(std::string("ifgf2d: ") + who + " called with wavenumber " + std::to_string(k) +
+                                        ", but the operator was precomputed for " + std::to_string(k_));
     }
     void apply(const Vec& x, Vec& y, int mode) {
         if ((long long)x.size() != total_num_unknowns_) throw std::invalid_argument("density has the wrong length");

@@ -33,11 +33,26 @@ def test_dropin_program_matches_library(lib, tmp_path):
     out = tmp_path / "y.bin"
     r = subprocess.run([exe, str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    y = np.fromfile(out, dtype=np.complex128)
+    raw = np.fromfile(out, dtype=np.uint8)
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 100.0, 4.0, Np=16, patches_per_curve=64)
     fm.precomps_and_setup(100.0, 0)
-    j = np.arange(fm.total_num_unknowns_)
-    x = np.cos(0.1 * j) + 1j * np.sin(0.2 * j)
     n = fm.total_num_unknowns_
+    y = raw[:16 * 5 * n].view(np.complex128)
+    meta = raw[16 * 5 * n:].view(np.float64)
+    j = np.arange(n)
+    x = np.cos(0.1 * j) + 1j * np.sin(0.2 * j)
     assert np.array_equal(y[:n], fm.compute_Ax_acc(x))
-    assert np.array_equal(y[n:], fm.compute_Ax_unacc(x))
+    assert np.array_equal(y[n:2 * n], fm.compute_Ax_unacc(x))
+    # GMRES three ways on the combined-field operator: a user mapping under opGMRES (host
+    # Arnoldi, GPU applies), the bound operator under opGMRES (ifgf2d_solve) and ForwardMap::solve
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 100.0, 4.0, Np=16, patches_per_curve=64, formulation="combined")
+    fm.precomps_and_setup(100.0, 0)
+    b = -np.exp(1j * 100.0 * fm.xs_)
+    x_user, x_dev, x_solve = y[2 * n:3 * n], y[3 * n:4 * n], y[4 * n:5 * n]
+    it_user, err_user, it_dev, err_dev, it_solve, err_solve = meta
+    for xs, err in ((x_user, err_user), (x_dev, err_dev), (x_solve, err_solve)):
+        assert err < 1e-8
+        assert np.linalg.norm(fm.compute_Ax_acc(xs) - b) / np.linalg.norm(b) < 1e-7
+    assert abs(it_user - it_dev) <= 1 and it_dev == it_solve
+    assert np.linalg.norm(x_user - x_dev) / np.linalg.norm(x_dev) < 1e-6
+    assert np.linalg.norm(x_dev - x_solve) / np.linalg.norm(x_solve) < 1e-10   # the same device solve, run twice

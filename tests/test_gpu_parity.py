@@ -13,6 +13,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
+IFGF_SAME_TREE_TOL = 1e-11
 
 
 def rel(a, b):
@@ -229,6 +230,34 @@ def test_gpu_helsing_jiang_known_answer(lib):
     x = fm.solve(f, 3.0, accelerated=False, tol=1e-10)
     u = fm.propagate_unacc([0.17], [0.62], x)[0]
     assert abs(u - ref) < 5e-3
+
+
+RECT_LINES = [(0.5, -0.5, 0.5, 0.5), (0.5, 0.5, -0.5, 0.5), (-0.5, 0.5, -0.5, -0.5), (-0.5, -0.5, 0.5, -0.5)]
+RECT_JUNCTIONS = [(0, 1, 0), (0, 3, 0), (1, 0, 0), (1, 2, 0), (2, 1, 0), (2, 3, 0), (3, 2, 0), (3, 0, 0)]
+
+
+@pytest.mark.parametrize("form", ["single_layer", "combined"])
+def test_gpu_rectangle_junctions_match_oracle(lib, oracle, form):
+    """make_rect (Geometry/Obstacles.cpp:6-23): four open lines joined at corner junctions.  The
+    patches at a corner take the one-sided edge changes of variables (minus1 / plus1,
+    utils/Quadrature.hpp:158-173) in the rectangular-polar weights.  Weights, the direct map and
+    the IFGF apply on the device against the oracle."""
+    k = 40.0      # 28 patches x 10 nodes, a tree of 4 levels
+    fm = lib.ForwardMap(0.01, [lib.Line(*l) for l in RECT_LINES], [lib.Junction(*j) for j in RECT_JUNCTIONS], 1.0, k, 4.0,
+                        Np=10, formulation=form)
+    om = oracle.OracleForwardMap([oracle.curve_line(*l) for l in RECT_LINES], 10, 0.01, 1.0, k, 4.0, junctions=RECT_JUNCTIONS,
+                                 formulation=form)
+    entry_tol, tol = (1e-12, 1e-12) if form == "single_layer" else (CFIE_ENTRY_TOL, CFIE_TOL)
+    fm.precomps_and_setup(k, 0)
+    om.precompute(k)
+    for patch in range(fm.num_patches_):
+        a, b = fm.precomputations(patch), om.precomp_matrix(patch)
+        assert np.abs(a - b).max() <= entry_tol * np.abs(b).max(), patch
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    assert rel(fm.compute_Ax_unacc(d), om.compute_Ax_unacc(d)) < tol
+    om.setup_ifgf(k, fm.nlevels)
+    assert np.array_equal(fm.getSorting(), om.sorting())
+    assert rel(fm.compute_Ax_acc(d), om.compute_Ax_acc(d)) < (IFGF_SAME_TREE_TOL if form == "single_layer" else tol)
 
 
 def test_gpu_propagate_matches_oracle(lib, oracle):

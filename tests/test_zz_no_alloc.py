@@ -3,11 +3,10 @@
 Some callers cannot allocate device memory where they call the forward map (a host
 application that owns the device memory budget, or a latency-critical loop that cannot take
 cudaMalloc's implicit synchronisation).  This entry point keeps its scratch in a fixed array
-inside the library; its output must equal the allocating path's, call after call.  This file
-is collected last so that a stop-at-first-failure run has already run every other test.
+inside the library; its output must equal the allocating path's, call after call, and the
+device's free memory must not move across a call.  This file is collected last so that a
+stop-at-first-failure run has already run every other test.
 """
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -28,7 +27,7 @@ def test_noalloc_direct_map_matches_allocating_path(lib, oracle, geometry):
         k, fm = 10.0, lib.ForwardMap(0.01, [lib.Circle()], (), 1.0, 10.0, Np=10, patches_per_curve=20)
     else:
         k, fm = 100.0, lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 100.0, Np=16, patches_per_curve=128)
-    fm.compute_precomputations(k)
+    fm.compute_precomputations(k)      # set-up resolves the scratch array and loads the kernels
     L = lib._lib.load()
     n = fm.total_num_unknowns_
     outs = []
@@ -37,9 +36,12 @@ def test_noalloc_direct_map_matches_allocating_path(lib, oracle, geometry):
         y_ref = torch.empty_like(x)
         y_new = torch.full_like(x, float("nan"))
         torch.cuda.synchronize()
-        fm.apply_device(x, y_ref, accelerated=False)
+        free_before = torch.cuda.mem_get_info()[0]
         rc = L.ifgf2d_apply_direct_noalloc(fm.handle, x.data_ptr(), y_new.data_ptr())
         assert rc == 0, L.ifgf2d_last_error(fm.handle).decode()
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free_before, "the call changed the device's free memory"
+        fm.apply_device(x, y_ref, accelerated=False)
         torch.cuda.synchronize()
         a, b = y_new.cpu().numpy(), y_ref.cpu().numpy()
         assert np.all(np.isfinite(a))
