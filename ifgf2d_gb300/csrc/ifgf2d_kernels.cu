@@ -37,8 +37,9 @@ __global__ void k_near_setup(const int* __restrict__ leaf_start, const int* __re
                              const long long* __restrict__ near_off, const double* __restrict__ xs,
                              const double* __restrict__ ys, const double* __restrict__ nxs, const double* __restrict__ nys,
                              const int* __restrict__ patch_s, const int* __restrict__ nsp_ptr, const int* __restrict__ nsp,
-                             double k, int form, double eta, double2* __restrict__ near) {
+                             double k0, int form, double eta0, const double2* __restrict__ keta, double2* __restrict__ near) {
     const int b = blockIdx.x;
+    const double k = keta ? keta[b].x : k0, eta = keta ? keta[b].y : eta0;   // per leaf box for a group of obstacles
     const int nB = leaf_count[b], t0 = leaf_start[b];
     const int n0 = nbr_ptr[b], n1 = nbr_ptr[b + 1];
     int nsrc = 0;
@@ -76,9 +77,9 @@ __global__ void __launch_bounds__(kLeafSetupWarps * 32) k_leaf_setup(const int* 
                                                                      const long long* __restrict__ leaf_off,
                                                                      const LeafNode* __restrict__ nodes, const double* __restrict__ xs,
                                                                      const double* __restrict__ ys, const double* __restrict__ nxs,
-                                                                     const double* __restrict__ nys, int Ps, int Pa, double k, int form,
-                                                                     double eta, const double* __restrict__ Gsep,
-                                                                     double2* __restrict__ L) {
+                                                                     const double* __restrict__ nys, int Ps, int Pa, double k0, int form,
+                                                                     double eta0, const double2* __restrict__ keta,
+                                                                     const double* __restrict__ Gsep, double2* __restrict__ L) {
     __shared__ double sG[2 * 64];
     __shared__ double2 hv[kLeafSetupWarps][64], uv[kLeafSetupWarps][64];
     for (int i = threadIdx.x; i < Ps * Ps + Pa * Pa; i += blockDim.x) sG[i] = Gsep[i];
@@ -88,6 +89,7 @@ __global__ void __launch_bounds__(kLeafSetupWarps * 32) k_leaf_setup(const int* 
     const int P = Ps * Pa;
     const int c = blockIdx.x;
     if (c >= ncones) return;
+    const double k = keta ? keta[c].x : k0, eta = keta ? keta[c].y : eta0;   // per cone for a group of obstacles
     const int b = cone_box[c];
     const int n = leaf_count[b], s0 = leaf_start[b];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -470,17 +472,18 @@ static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) 
 void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* nbr_ptr, const int* nbr_box,
                        const long long* near_off, int nleaf, const double* xs, const double* ys, const double* nxs,
                        const double* nys, const int* patch_s, const int* nsp_ptr, const int* nsp, double k, int form,
-                       double eta, double2* near, cudaStream_t s) {
+                       double eta, double2* near, cudaStream_t s, const double2* keta) {
     if (nleaf <= 0) return;
     k_near_setup<<<nleaf, 256, 0, s>>>(leaf_start, leaf_count, nbr_ptr, nbr_box, near_off, xs, ys, nxs, nys, patch_s, nsp_ptr,
-                                       nsp, k, form, eta, near);
+                                       nsp, k, form, eta, keta, near);
 }
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count, const long long* leaf_off,
                        const LeafNode* nodes, const double* xs, const double* ys, const double* nxs, const double* nys, int Ps,
-                       int Pang, double k, int form, double eta, const double* Gsep, double2* L, cudaStream_t s) {
+                       int Pang, double k, int form, double eta, const double* Gsep, double2* L, cudaStream_t s,
+                       const double2* keta) {
     if (ncones <= 0 || Ps * Pang > 64 || Ps * Ps + Pang * Pang > 128) return;
     k_leaf_setup<<<ncones, kLeafSetupWarps * 32, 0, s>>>(cone_box, ncones, leaf_start, leaf_count, leaf_off, nodes, xs, ys, nxs, nys, Ps, Pang, k,
-                                        form, eta, Gsep, L);
+                                        form, eta, keta, Gsep, L);
 }
 void launch_sing_apply(const double2* x, const double2* W, const int* row_ptr, const int* row_col, const RPColumn* cols,
                        int N, int Np, double half, double2* y, cudaStream_t s) {

@@ -58,22 +58,25 @@ using PropEntryD = PropE<double>;
 constexpr int kMaxP = 64;          // Ps * Pang limit of the device interpolator
 
 // ---------------- setup kernels ----------------
+// keta, when given, holds (k, eta) per item (per column, leaf box or leaf cone) and overrides the
+// scalar k and eta: a group of obstacles with their own wavenumbers sets up in one launch.
 void launch_rp_precompute(const RPColumn* cols, int ncols, const DevPatch* patches, const DevCurve* curves,
                           const double* ns_nodes, const double* ns_weights, int Np, double p, double k,
-                          int form, double eta, double2* M, cudaStream_t s);
+                          int form, double eta, double2* M, cudaStream_t s, const double2* keta = nullptr);
 void launch_rp_fold(const double2* M, const RPColumn* cols, int ncols, const double* edge_jac, const DevPatch* patches,
                     int Np, double2* W, cudaStream_t s);
 void launch_near_setup(const int* leaf_start, const int* leaf_count, const int* nbr_ptr, const int* nbr_box,
                        const long long* near_off, int nleaf, const double* xs, const double* ys,
                        const double* nxs, const double* nys, const int* patch_s, const int* nsp_ptr,
-                       const int* nsp, double k, int form, double eta, double2* near, cudaStream_t s);
+                       const int* nsp, double k, int form, double eta, double2* near, cudaStream_t s,
+                       const double2* keta = nullptr);
 // leaf-cone tables: Green values at the cone nodes times 1/factorization, mapped to Chebyshev
 // coefficients with the separable map Gsep (Ps x Ps radial, then Pang x Pang angular);
 // Ps * Pang <= 64
 void launch_leaf_setup(const int* cone_box, int ncones, const int* leaf_start, const int* leaf_count,
                        const long long* leaf_off, const LeafNode* nodes, const double* xs, const double* ys,
                        const double* nxs, const double* nys, int Ps, int Pang, double k, int form, double eta,
-                       const double* Gsep, double2* L, cudaStream_t s);
+                       const double* Gsep, double2* L, cudaStream_t s, const double2* keta = nullptr);
 
 // ---------------- per-apply kernels ----------------
 // y = singular correction (+ half * x: the jump term of the combined formulation)

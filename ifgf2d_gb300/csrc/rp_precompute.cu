@@ -22,11 +22,12 @@ __device__ __forceinline__ double warp_sum_rp(double v) {
 // the Green function at each node, then the Np Chebyshev moments (ForwardMap.tpp:287-389).
 __global__ void k_rp_precompute(const RPColumn* __restrict__ cols, int ncols, const DevPatch* __restrict__ patches,
                                 const DevCurve* __restrict__ curves, const double* __restrict__ nsn,
-                                const double* __restrict__ nsw, int Np, double p, double k, int form, double eta,
-                                double2* __restrict__ M) {
+                                const double* __restrict__ nsw, int Np, double p, double k0, int form, double eta0,
+                                const double2* __restrict__ keta, double2* __restrict__ M) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= ncols) return;
+    const double k = keta ? keta[w].x : k0, eta = keta ? keta[w].y : eta0;   // per column for a group of obstacles
     const RPColumn c = cols[w];
     const DevPatch P = patches[c.patch];
     const DevCurve cv = curves[P.curve];
@@ -111,9 +112,10 @@ static inline unsigned nblk_rp(long long n, int b) { return (unsigned)((n + b - 
 
 void launch_rp_precompute(const RPColumn* cols, int ncols, const DevPatch* patches, const DevCurve* curves,
                           const double* nsn, const double* nsw, int Np, double p, double k, int form, double eta, double2* M,
-                          cudaStream_t s) {
+                          cudaStream_t s, const double2* keta) {
     if (ncols <= 0) return;
-    k_rp_precompute<<<nblk_rp((long long)ncols * 32, 128), 128, 0, s>>>(cols, ncols, patches, curves, nsn, nsw, Np, p, k, form, eta, M);
+    k_rp_precompute<<<nblk_rp((long long)ncols * 32, 128), 128, 0, s>>>(cols, ncols, patches, curves, nsn, nsw, Np, p, k, form, eta,
+                                                                        keta, M);
 }
 void launch_rp_fold(const double2* M, const RPColumn* cols, int ncols, const double* edge, const DevPatch* patches,
                     int Np, double2* W, cudaStream_t s) {
