@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib
 from ._lib import APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED
 
-__all__ = ["ForwardMap", "LinearOperator", "Circle", "Kite", "Line", "Star", "Junction", "hankel1",
+__all__ = ["ForwardMap", "LinearOperator", "Circle", "Kite", "Line", "Star", "Junction", "hankel1", "Group",
            "IFGF2DError", "NeighbourhoodError", "NoConvergence", "load_library"]
 
 
@@ -554,3 +554,75 @@ class ForwardMap:
         _check(_lib.load().ifgf2d_propagate(self._h, xp.size, _dp(xp), _dp(yp), _dp(d.view(np.float64)),
                                             _dp(out.view(np.float64))), self._h)
         return out
+
+
+# ---------------------------------------------------------------- many obstacles
+class Group:
+    """Many obstacles as one block-diagonal operator (ifgf2d_group_*): the prepared ForwardMaps
+    ``members`` (ForwardMap.prepare(k): each its own wavenumber and tree; the same Np, Ps, Pang
+    and formulation) merged so that each phase of the set-up and of an apply is one launch over
+    all of them.  Vectors hold every member's unknowns in member order; ``offsets`` gives each
+    member's first unknown.  The members may be closed afterwards."""
+
+    def __init__(self, members):
+        L = _lib.load()
+        members = list(members)
+        if not members:
+            raise ValueError("a group needs at least one member")
+        arr = (ctypes.c_void_p * len(members))(*[m.handle for m in members])
+        h = ctypes.c_void_p()
+        rc = L.ifgf2d_group_create(arr, len(members), ctypes.byref(h))
+        self._h = h.value
+        if rc != 0:
+            msg = L.ifgf2d_group_last_error(self._h).decode() if self._h else ""
+            self.close()
+            raise (ValueError if rc == 1 else IFGF2DError)(f"ifgf2d_group_create: {_lib.STATUS.get(rc, rc)}: {msg}")
+        self.n = len(members)
+        self.N = int(L.ifgf2d_group_num_unknowns(self._h))
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        L.ifgf2d_group_offsets(self._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+        self.offsets = off
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().ifgf2d_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc == 0:
+            return
+        msg = _lib.load().ifgf2d_group_last_error(self._h).decode()
+        raise (ValueError if rc == 1 else IFGF2DError)(f"ifgf2d group: {_lib.STATUS.get(rc, rc)}: {msg}")
+
+    def split(self, v):
+        """the per-member pieces of a group vector"""
+        return [v[self.offsets[o]:self.offsets[o + 1]] for o in range(self.n)]
+
+    def apply(self, x, mixed=False):
+        xin = _cview(x, self.N)
+        out = np.empty(self.N, dtype=np.complex128)
+        self._check(_lib.load().ifgf2d_group_apply(self._h, _dp(xin.view(np.float64)), _dp(out.view(np.float64)),
+                                                   APPLY_IFGF_MIXED if mixed else APPLY_IFGF))
+        return out
+
+    def solve(self, rhs, tol=1e-6, restart=300, max_iters=1000, mixed=True):
+        """GMRES for every member in lock step; ``self.last_solve`` holds per-member iterations and
+        estimated errors (FP64 relative residuals with mixed=True)."""
+        b = _cview(rhs, self.N)
+        x = np.empty(self.N, dtype=np.complex128)
+        it = np.zeros(self.n, dtype=np.int32)
+        err = np.zeros(self.n)
+        rc = _lib.load().ifgf2d_group_solve(self._h, _dp(b.view(np.float64)), _dp(x.view(np.float64)),
+                                            APPLY_IFGF_MIXED if mixed else APPLY_IFGF, float(tol), int(restart),
+                                            int(max_iters), it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0))
+        if rc != 8:
+            self._check(rc)
+        return x
+

@@ -34,6 +34,8 @@ EXPORTS = [
     "ifgf2d_net_last_error", "ifgf2d_net_get_params", "ifgf2d_net_set_params", "ifgf2d_net_gradient",
     "ifgf2d_net_train_step", "ifgf2d_net_apply", "ifgf2d_get_geometry_features", "ifgf2d_solve_precond",
     "ifgf2d_tuning_size", "ifgf2d_autotune", "ifgf2d_get_tuning", "ifgf2d_set_tuning", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
+    "ifgf2d_group_create", "ifgf2d_group_destroy", "ifgf2d_group_last_error", "ifgf2d_group_num_unknowns",
+    "ifgf2d_group_offsets", "ifgf2d_group_apply", "ifgf2d_group_solve",
 ]
 
 
@@ -125,6 +127,14 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_apply_batch.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int]
         L.ifgf2d_apply_batch_device.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
         L.ifgf2d_solve_batch.argtypes = [P, D, D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int), D]
+        L.ifgf2d_group_create.argtypes = [ctypes.POINTER(P), ctypes.c_int, ctypes.POINTER(P)]
+        L.ifgf2d_group_destroy.argtypes = [P]
+        L.ifgf2d_group_last_error.argtypes = [P]; L.ifgf2d_group_last_error.restype = ctypes.c_char_p
+        L.ifgf2d_group_num_unknowns.argtypes = [P]; L.ifgf2d_group_num_unknowns.restype = ctypes.c_longlong
+        L.ifgf2d_group_offsets.argtypes = [P, I64]
+        L.ifgf2d_group_apply.argtypes = [P, D, D, ctypes.c_int]
+        L.ifgf2d_group_solve.argtypes = [P, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_int), D]
         _lib = L
         return L

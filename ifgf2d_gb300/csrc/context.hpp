@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstring>
 #include <complex>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -229,6 +230,22 @@ static inline bool all_finite(const double* v, long long n) {
 }
 
 namespace ifgf {
+// What a group of obstacles (group.cu) changes in the device part of the IFGF set-up: (k, eta)
+// per leaf box and per leaf cone (device arrays), the leaf-cone nodes (host, per leaf cone and
+// node, from each member's tree) and the propagation plan, built member by member.
+struct SetupExtra {
+    const double2* keta_leafbox = nullptr;
+    const double2* keta_leafcone = nullptr;
+    const std::vector<LeafNode>* leaf_nodes = nullptr;
+    std::function<cudaError_t(PropE<double>*, PropE<float>*, int*, cudaStream_t)> build_plan;
+};
+// the host tables of a context built from ctx->D: near-singular patches per point, the
+// rectangular-polar columns and rows (ifgf2d_capi.cu)
+int init_host_tables(ifgf2d_ctx* ctx);
+// the device copies of the discretisation, made on first use (ifgf2d_capi.cu)
+int ensure_device_ctx(ifgf2d_ctx* ctx);
+// the device tables of an IFGF set-up from ctx->T and ctx->D (ifgf2d_capi.cu); ex for a group
+int setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex);
 // single-vector apply on device vectors in original order: y = A x (ifgf2d_capi.cu)
 int apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode);
 // batched workspace release (batch.cu)
@@ -241,8 +258,12 @@ void free_eval(ifgf2d_ctx* ctx);
 int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, double k, std::string& err);
 // the propagation plan's entries from the tree's slot form, on the device (plan_device.cu):
 // FP64 into pp64 and, when pp32 is not null, the complex64 copy; *err is set when a node's child
-// cone does not exist (an inconsistent tree).  Synchronises the stream before returning.
-cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s);
+// cone does not exist (an inconsistent tree).  Under an AllocStream guard on `s` the work stays
+// queued on `s`; otherwise the stream is synchronised before returning.  For a member of a group
+// of obstacles, level_cone_base[l] replaces level l's first global cone id and
+// level_entry_base[l] the first entry of the slots with children at level l.
+cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
+                            const int* level_cone_base = nullptr, const long long* level_entry_base = nullptr);
 // a parent's propagation terms sorted by child cone (stable), with the parent node recorded, for
 // the batched propagation
 template <typename R>

@@ -233,6 +233,133 @@ __global__ void k_lsq_solve_batch(LsqBatchDev L, int ncols, double2* __restrict_
     }
 }
 
+// column j = *jp of every running right-hand side (Hcol = H + j * (m + 1) * B), for a captured
+// iteration graph: as k_lsq_givens_batch, then j += 1 and the while-loop condition (0 once no
+// right-hand side runs or the cycle is full)
+__global__ void k_lsq_givens_batch_dev(const double2* __restrict__ H, int* __restrict__ jp, LsqBatchDev L,
+                                       int* __restrict__ active, cudaGraphConditionalHandle cond) {
+    const int r = threadIdx.x;
+    const int j = *jp;
+    bool run = false;
+    if (r < L.B && j < L.m) {
+        int* st = L.st + 4 * r;
+        if (!st[0]) {
+            double* sc = L.sc + 3 * r;
+            const int ldh = L.m + 1;
+            double hn = 0.0;
+            const double2* Hcol = H + (long long)j * ldh * L.B;
+            const double est = givens_column(Hcol + r, L.B, j, L.R + (long long)r * ldh * L.m + (long long)j * ldh,
+                                             L.gc + (long long)r * L.m, L.gs + (long long)r * L.m, L.g + (long long)r * (L.m + 1),
+                                             sc[1], hn);
+            const int it = st[3] + 1;
+            st[3] = it;
+            sc[0] = est;
+            st[1] = j + 1;
+            if (!(est >= sc[2]) || it >= st[2] || hn == 0.0) st[0] = 1;
+            else run = true;
+        }
+    }
+    const int n = __syncthreads_count(run);
+    if (threadIdx.x == 0) {
+        if (j < L.m) active[j] = n;
+        *jp = j + 1;
+        cudaGraphSetConditional(cond, (n > 0 && j + 1 < L.m) ? 1u : 0u);
+    }
+}
+
+// ---- segmented vectors: B segments (one per obstacle of a group) side by side in one vector;
+// chunk c covers [chunk_lo[c], chunk_lo[c + 1]) inside one segment, segment s owns chunks
+// [seg_chunk[s], seg_chunk[s + 1])
+constexpr int kSegThreads = 256;
+// part[col * nchunk + c] = V[:, col]^H w over chunk c, for col <= *jp (jp NULL: col 0 only, V = v)
+__global__ void __launch_bounds__(kSegThreads) k_seg_dot_part(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                                                              const double2* __restrict__ w, const long long* __restrict__ chunk_lo,
+                                                              int nchunk, double2* __restrict__ part) {
+    const int c = blockIdx.x, col = blockIdx.y;
+    if (jp ? col > *jp : col > 0) return;
+    const double2* v = V + (long long)col * ldv;
+    double re = 0.0, im = 0.0;
+    for (long long i = chunk_lo[c] + threadIdx.x; i < chunk_lo[c + 1]; i += kSegThreads) {
+        const double2 a = v[i], b = w[i];
+        re = fma(a.x, b.x, fma(a.y, b.y, re));
+        im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { re += __shfl_xor_sync(0xffffffffu, re, o); im += __shfl_xor_sync(0xffffffffu, im, o); }
+    __shared__ double sr[kSegThreads / 32], si[kSegThreads / 32];
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = re; si[threadIdx.x >> 5] = im; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < kSegThreads / 32; ++q) { a += sr[q]; b += si[q]; }
+        part[(long long)col * nchunk + c] = make_double2(a, b);
+    }
+}
+// per (column, segment): the segment's chunks summed in order.  mode 0: hh[col * B + s] and the
+// Hessenberg column j (add: accumulate, for a second Gram-Schmidt pass); mode 1 (norms, col 0):
+// nrm[s] = (sqrt(sum), 0), and with H also the subdiagonal entry H[j][j+1] of segment s
+__global__ void k_seg_dot_fin(const double2* __restrict__ part, int nchunk, const int* __restrict__ seg_chunk, int B,
+                              const int* __restrict__ jp, int ncol, int mode, int add, double2* __restrict__ hh,
+                              double2* __restrict__ H, int ldh) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)ncol * B) return;
+    const int col = (int)(id / B), s = (int)(id - (long long)col * B);
+    const int j = jp ? *jp : 0;
+    if (mode == 0 && col > j) return;
+    double a = 0.0, b = 0.0;
+    for (int c = seg_chunk[s]; c < seg_chunk[s + 1]; ++c) { const double2 v = part[(long long)col * nchunk + c]; a += v.x; b += v.y; }
+    if (mode == 0) {
+        hh[(long long)col * B + s] = make_double2(a, b);
+        double2* e = H + (long long)j * ldh * B + (long long)col * B + s;
+        if (add) { e->x += a; e->y += b; } else *e = make_double2(a, b);
+    } else {
+        const double nv = sqrt(fmax(a, 0.0));
+        hh[s] = make_double2(nv, 0.0);
+        if (H) H[(long long)j * ldh * B + (long long)(j + 1) * B + s] = make_double2(nv, 0.0);
+    }
+}
+// w[i] -= sum_{c <= *jp} V[:, c][i] hh[c * B + seg(i)]
+__global__ void k_seg_update(const double2* __restrict__ V, long long ldv, const int* __restrict__ jp,
+                             const double2* __restrict__ hh, int B, const int* __restrict__ seg_of, long long n,
+                             double2* __restrict__ w) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = *jp, s = seg_of[i];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int c = 0; c <= j; ++c) {
+        const double2 v = V[(long long)c * ldv + i], h = hh[(long long)c * B + s];
+        acc.x = fma(v.x, h.x, fma(-v.y, h.y, acc.x));
+        acc.y = fma(v.x, h.y, fma(v.y, h.x, acc.y));
+    }
+    const double2 o = w[i];
+    w[i] = make_double2(o.x - acc.x, o.y - acc.y);
+}
+// V[:, col][i] = w[i] / nrm[seg(i)] (0 for a zero norm); col = *jp + 1, or 0 without jp
+__global__ void k_seg_scale(const double2* __restrict__ w, const double2* __restrict__ nrm, const int* __restrict__ seg_of,
+                            const int* __restrict__ jp, long long n, double2* __restrict__ V) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int col = jp ? *jp + 1 : 0;
+    const double h = nrm[seg_of[i]].x;
+    const double a = h != 0.0 ? 1.0 / h : 0.0;
+    V[(long long)col * n + i] = make_double2(w[i].x * a, w[i].y * a);
+}
+// x[i] += sum_{c < ncols} V[:, c][i] Y[c * B + seg(i)]
+__global__ void k_seg_axpy(const double2* __restrict__ V, long long ldv, int ncols, const double2* __restrict__ Y, int B,
+                           const int* __restrict__ seg_of, long long n, double2* __restrict__ x) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = seg_of[i];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int c = 0; c < ncols; ++c) {
+        const double2 v = V[(long long)c * ldv + i], y = Y[(long long)c * B + s];
+        acc.x = fma(v.x, y.x, fma(-v.y, y.y, acc.x));
+        acc.y = fma(v.x, y.y, fma(v.y, y.x, acc.y));
+    }
+    const double2 o = x[i];
+    x[i] = make_double2(o.x + acc.x, o.y + acc.y);
+}
+
 inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 }  // namespace
@@ -257,6 +384,34 @@ void launch_lsq_givens_batch(const double2* Hcol, int j, LsqBatchDev L, int* act
 }
 void launch_lsq_solve_batch(LsqBatchDev L, int ncols, double2* Y, cudaStream_t s) {
     k_lsq_solve_batch<<<L.B, 32, 0, s>>>(L, ncols, Y);
+}
+void launch_lsq_givens_batch_dev(const double2* H, int* jp, LsqBatchDev L, int* active, cudaGraphConditionalHandle cond,
+                                 cudaStream_t s) {
+    k_lsq_givens_batch_dev<<<1, ((L.B + 31) / 32) * 32, 0, s>>>(H, jp, L, active, cond);
+}
+void launch_seg_arnoldi(const SegDesc& S, double2* V, int m, int* jp, double2* w, double2* hh, double2* H, double2* nrm,
+                        int passes, cudaStream_t s) {
+    const int ldh = m + 1;
+    for (int pass = 0; pass < passes; ++pass) {
+        k_seg_dot_part<<<dim3(S.nchunk, m + 1), kSegThreads, 0, s>>>(V, S.n, jp, w, S.chunk_lo, S.nchunk, S.part);
+        k_seg_dot_fin<<<nblocks((long long)(m + 1) * S.B, 128), 128, 0, s>>>(S.part, S.nchunk, S.seg_chunk, S.B, jp, m + 1, 0, pass,
+                                                                              hh, H, ldh);
+        k_seg_update<<<nblocks(S.n, 256), 256, 0, s>>>(V, S.n, jp, hh, S.B, S.seg_of, S.n, w);
+    }
+    k_seg_dot_part<<<dim3(S.nchunk, 1), kSegThreads, 0, s>>>(w, 0, nullptr, w, S.chunk_lo, S.nchunk, S.part);
+    k_seg_dot_fin<<<nblocks(S.B, 128), 128, 0, s>>>(S.part, S.nchunk, S.seg_chunk, S.B, jp, 1, 1, 0, nrm, H, ldh);
+    k_seg_scale<<<nblocks(S.n, 256), 256, 0, s>>>(w, nrm, S.seg_of, jp, S.n, V);
+}
+void launch_seg_norms(const SegDesc& S, const double2* v, double2* nrm, cudaStream_t s) {
+    k_seg_dot_part<<<dim3(S.nchunk, 1), kSegThreads, 0, s>>>(v, 0, nullptr, v, S.chunk_lo, S.nchunk, S.part);
+    k_seg_dot_fin<<<nblocks(S.B, 128), 128, 0, s>>>(S.part, S.nchunk, S.seg_chunk, S.B, nullptr, 1, 1, 0, nrm, nullptr, 0);
+}
+void launch_seg_scale0(const SegDesc& S, const double2* w, const double2* nrm, double2* V, cudaStream_t s) {
+    k_seg_scale<<<nblocks(S.n, 256), 256, 0, s>>>(w, nrm, S.seg_of, nullptr, S.n, V);
+}
+void launch_seg_axpy(const SegDesc& S, const double2* V, int ncols, const double2* Y, double2* x, cudaStream_t s) {
+    if (ncols <= 0) return;
+    k_seg_axpy<<<nblocks(S.n, 256), 256, 0, s>>>(V, S.n, ncols, Y, S.B, S.seg_of, S.n, x);
 }
 
 }  // namespace ifgf

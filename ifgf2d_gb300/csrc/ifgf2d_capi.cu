@@ -44,7 +44,16 @@ extern "C" int ifgf2d_create(const ifgf2d_curve* curves, int ncurves, const ifgf
         *out = ctx; ctx->err = msg; return IFGF2D_ERR_GEOMETRY;
     }
     *out = ctx;
+    return ifgf::init_host_tables(ctx);
+}
+
+// The host tables every context derives from its discretisation: per point its near-singular
+// patches, the rectangular-polar columns and, per output row, the columns adding to it.
+int ifgf::init_host_tables(ifgf2d_ctx* ctx) {
     const Discretisation& D = ctx->D;
+    ctx->h_nsp.clear();
+    ctx->hcols.clear();
+    ctx->h_srow_col.clear();
     // per point: the patches it is near-singular to (ForwardMap.tpp:596-604)
     ctx->h_nsp_ptr.assign(D.N + 1, 0);
     {
@@ -291,13 +300,19 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         if (rc != IFGF2D_OK) return rc;
     }
     AllocStream guard(ctx->stream);
-    const Discretisation& D = ctx->D;
     if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) {
         int rc = ifgf2d_prepare(ctx, k, nlevels);
         if (rc != IFGF2D_OK) return rc;
     }
     ctx->prep_ready = false;
-    nlevels = ctx->prep_nlevels;
+    return ifgf::setup_tables(ctx, k, ctx->prep_nlevels, nullptr);
+}
+
+// The device tables of an IFGF set-up from the context's host tree (ctx->T) and discretisation.
+// With `ex` (a group of obstacles, group.cu) the wavenumbers come per leaf box and leaf cone,
+// the leaf-cone nodes from the members' trees, and the propagation plan from ex->build_plan.
+int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex) {
+    const Discretisation& D = ctx->D;
     free_batch(ctx);
     free_eval(ctx);
     Tree& T = ctx->T;
@@ -350,7 +365,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     CK(ctx->near.alloc(noff[nleaf]));
     launch_near_setup(ctx->leaf_start.p, ctx->leaf_count.p, ctx->nbr_ptr.p, ctx->nbr_box.p, ctx->near_off.p, nleaf,
                       ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k,
-                      ctx->form, ctx->eta, ctx->near.p, ctx->stream);
+                      ctx->form, ctx->eta, ctx->near.p, ctx->stream, ex ? ex->keta_leafbox : nullptr);
     CK(cudaGetLastError());
     // values-to-coefficients matrix of the cone interpolant (Interpolator.h:81-120)
     {
@@ -383,7 +398,9 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     const int ncl = (int)LD.cone_nonrel.size();
     std::vector<long long> loff(ncl + 1, 0);
     for (int c = 0; c < ncl; ++c) loff[c + 1] = loff[c] + (long long)P * T.leaf_count[LD.cone_box[c]];
-    {
+    if (ex) {
+        CK(ctx->leaf_nodes_d.upload(*ex->leaf_nodes));
+    } else {
         std::vector<double> nx, ny, nir, nii;
         leaf_nodes(T, nx, ny, nir, nii);
         std::vector<LeafNode> nodes(nx.size());
@@ -394,7 +411,7 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     CK(ctx->leafL.alloc(loff[ncl]));
     launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,
                       ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, T.Ps, T.Pang, k, ctx->form, ctx->eta, ctx->Gsep.p,
-                      ctx->leafL.p, ctx->stream);
+                      ctx->leafL.p, ctx->stream, ex ? ex->keta_leafcone : nullptr);
     CK(cudaGetLastError());
     // propagation and interpolation plans: the propagation entries are computed on the device
     // from the tree's slot form, the interpolation entries come from the host tree
@@ -404,7 +421,8 @@ extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
         DBuf<int> perr;
         CK(perr.alloc(1));
         CK(cudaMemsetAsync(perr.p, 0, sizeof(int), ctx->stream));
-        CK(build_prop_plan(T, ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+        if (ex) CK(ex->build_plan(ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+        else CK(build_prop_plan(T, ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
         int bad = 0;
         CK(cudaMemcpyAsync(&bad, perr.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
@@ -534,6 +552,7 @@ static int apply_dev(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) {
 }
 
 int ifgf::apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode) { return apply_dev(ctx, x, y, mode); }
+int ifgf::ensure_device_ctx(ifgf2d_ctx* ctx) { return ensure_device(ctx); }
 
 extern "C" int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, double ms[5]) {
     if (!ctx || !d_x || !d_y || !ms) return IFGF2D_ERR_ARG;

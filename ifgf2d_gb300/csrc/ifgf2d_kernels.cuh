@@ -230,6 +230,30 @@ void launch_lsq_init_batch(LsqBatchDev L, const double2* beta, const double* par
 void launch_lsq_givens_batch(const double2* Hcol, int j, LsqBatchDev L, int* active, cudaStream_t s);
 // Y[i * B + r] = (R_r^{-1} g_r)_i, zero from the right-hand side's own column count up to ncols
 void launch_lsq_solve_batch(LsqBatchDev L, int ncols, double2* Y, cudaStream_t s);
+// the same Givens step with j = *jp read on the device (H: columns of (m + 1) * B entries), for a
+// captured iteration: active[j] = the right-hand sides still running, j += 1, and the while-loop
+// condition set to 0 once none runs or the cycle is full
+void launch_lsq_givens_batch_dev(const double2* H, int* jp, LsqBatchDev L, int* active, cudaGraphConditionalHandle cond,
+                                 cudaStream_t s);
+// Segmented vectors: B segments side by side in vectors of n entries (one per obstacle of a
+// group).  Chunk c covers [chunk_lo[c], chunk_lo[c + 1]) inside one segment; segment s owns
+// chunks [seg_chunk[s], seg_chunk[s + 1]); seg_of[i] is the segment of entry i; part holds
+// (m + 1) * nchunk partial sums.
+struct SegDesc {
+    long long n; int B; int nchunk;
+    const long long* chunk_lo; const int* seg_chunk; const int* seg_of; double2* part;
+};
+// one Arnoldi step per segment after w = A v_j (j = *jp): classical Gram-Schmidt `passes`
+// times with per-segment coefficients into H column j (layout [row][segment]), the per-segment
+// norms into nrm and H's subdiagonal, V[:, j + 1] = w / norm
+void launch_seg_arnoldi(const SegDesc& S, double2* V, int m, int* jp, double2* w, double2* hh, double2* H, double2* nrm,
+                        int passes, cudaStream_t s);
+// nrm[s] = (||v_s||, 0)
+void launch_seg_norms(const SegDesc& S, const double2* v, double2* nrm, cudaStream_t s);
+// V[:, 0] = w / nrm per segment
+void launch_seg_scale0(const SegDesc& S, const double2* w, const double2* nrm, double2* V, cudaStream_t s);
+// x += V[:, 0..ncols) Y per segment (Y[c * B + s])
+void launch_seg_axpy(const SegDesc& S, const double2* V, int ncols, const double2* Y, double2* x, cudaStream_t s);
 
 // one Arnoldi step after w = A v_j, with j read from *jp (for a captured iteration graph):
 // classical Gram-Schmidt against V[:, 0..j], `passes` times (2: CGS2), into the Hessenberg

@@ -169,7 +169,7 @@ struct LevelBufs {
     DBuf<int> cone_box, cone_ptr;
     DBuf<double> radial;
 };
-cudaError_t upload_level(const TreeLevel& L, LevelBufs& B, LevelDesc& d) {
+cudaError_t upload_level(const TreeLevel& L, int cone_base, LevelBufs& B, LevelDesc& d) {
     cudaError_t e;
     if ((e = B.boxes.upload(L.boxes)) != cudaSuccess) return e;
     if ((e = B.cone_nonrel.upload(L.cone_nonrel)) != cudaSuccess) return e;
@@ -177,13 +177,14 @@ cudaError_t upload_level(const TreeLevel& L, LevelBufs& B, LevelDesc& d) {
     if ((e = B.cone_ptr.upload(L.cone_ptr)) != cudaSuccess) return e;
     if ((e = B.radial.upload(L.radial)) != cudaSuccess) return e;
     d = LevelDesc{B.boxes.p, B.cone_box.p, B.cone_nonrel.p, B.cone_ptr.p, B.radial.p, L.boxsize, L.scaling_r2s, L.nrad,
-                  L.ntheta, L.cone_base};
+                  L.ntheta, cone_base};
     return cudaSuccess;
 }
 
 }  // namespace
 
-cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s) {
+cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
+                            const int* level_cone_base, const long long* level_entry_base) {
     if (T.Ps > 8 || T.Pang > 8) return cudaErrorInvalidValue;
     ChebNodes cn{};
     // Chebyshev nodes of the cone interpolant, ascending (Chebyshev.h:10-24), as the host tree has them
@@ -203,7 +204,7 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
         if (nslots == 0) continue;
         for (int l : {S.level - 1, S.level})
             if (!up[l] && e == cudaSuccess) {
-                e = upload_level(T.L[l], lb[l], ld[l]);
+                e = upload_level(T.L[l], level_cone_base ? level_cone_base[l] : T.L[l].cone_base, lb[l], ld[l]);
                 up[l] = 1;
             }
         if (e == cudaSuccess) e = sp[q].upload(S.slot_parent);
@@ -213,11 +214,15 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
         if (e == cudaSuccess) e = rn[q].upload(S.route_nonrel);
         if (e != cudaSuccess) break;
         const long long n = nslots * T.P;
+        const long long eb = level_entry_base ? level_entry_base[S.level] : S.entry_base;
         k_prop_plan<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ld[S.level - 1], ld[S.level], T.min_x, T.min_y, T.k, T.Ps, cn, T.P,
                                                                  sp[q].p, scb[q].p, spos[q].p, sr[q].p, rn[q].p, nslots,
-                                                                 pp64 + S.entry_base, pp32 ? pp32 + S.entry_base : nullptr, err);
+                                                                 pp64 + eb, pp32 ? pp32 + eb : nullptr, err);
         e = cudaGetLastError();
     }
+    // stream-ordered buffers are freed in stream order after the kernels; plain ones need the
+    // kernels finished first
+    if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;
     const cudaError_t es = cudaStreamSynchronize(s);
     return e != cudaSuccess ? e : es;
 }

@@ -151,3 +151,56 @@ def solve_obstacles(obstacles, tol=1e-6, workers=15, mixed=True, direct_below=0,
     finally:
         L.ifgf2d_set_host_threads(0)
     return xs if keep_solutions else None
+
+
+def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart=300, max_iters=1000,
+                            keep_solutions=False):
+    """Solve every obstacle as one group (ifgf2d_group_*): the host part of each obstacle's
+    set-up (discretisation, tree depth, tree and plans) on `workers` threads, then one merged
+    device set-up and one lock-step GMRES for all obstacles whose points some tree depth keeps in
+    the leaf neighbourhood; each phase of their set-up and of every apply is one launch over all
+    of them.  The others use the direct operator, one at a time.  Each obstacle's `result` holds
+    its iterations, convergence, true FP64 relative residual and operator; returns the densities
+    when keep_solutions."""
+    from . import _lib
+    import ifgf2d_gb300 as G
+    L = _lib.load()
+    n = len(obstacles)
+    L.ifgf2d_set_host_threads(1)
+    try:
+        with ThreadPoolExecutor(max(1, workers)) as ex:
+            prepared = list(ex.map(lambda ob: _prepare_one(G, ob, 0), obstacles))
+    finally:
+        L.ifgf2d_set_host_threads(0)
+    xs = [None] * n
+    acc = [i for i in range(n) if prepared[i][1]]
+    rhs_of = []
+    for i in acc:
+        ob, fm = obstacles[i], prepared[i][0]
+        rhs_of.append(-np.exp(1j * ob.k * (math.cos(ob.angle) * fm.xs_ + math.sin(ob.angle) * fm.ys_)))
+    if acc:
+        grp = G.Group([prepared[i][0] for i in acc])
+        for i in acc:                       # the group holds its own copy of everything
+            prepared[i][0].close()
+        rhs = np.concatenate(rhs_of)
+        x = grp.solve(rhs, tol=tol, restart=restart, max_iters=max_iters, mixed=mixed)
+        st = grp.last_solve
+        res = grp.split(grp.apply(x) - rhs)
+        for q, i in enumerate(acc):
+            b = rhs_of[q]
+            obstacles[i].result = {"iters": st["iters"][q], "error": st["error"][q], "converged": st["error"][q] < tol,
+                                   "true_rel_residual": float(np.linalg.norm(res[q]) / np.linalg.norm(b)),
+                                   "accelerated": True, "N": int(b.size), "grouped": True}
+            if keep_solutions:
+                xs[i] = grp.split(x)[q].copy()
+        grp.close()
+    for i in range(n):
+        if prepared[i][1]:
+            continue
+        fm = prepared[i][0]
+        x = _device_one(G, obstacles[i], fm, False, tol, mixed, restart, max_iters)
+        obstacles[i].result["grouped"] = False
+        xs[i] = x if keep_solutions else None
+        fm.close()
+    return xs if keep_solutions else None
+

@@ -262,6 +262,27 @@ int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* choices);
  * roofline denominator of the FP64 kernels (no counterpart in the reference). */
 int ifgf2d_measure_fp64_peak(double* tflops);
 
+/* Many obstacles as one block-diagonal operator (no counterpart in the reference, which solves one
+ * obstacle per ForwardMap::solve, ForwardMap.tpp:658-697).  group_create merges n <= 1024 contexts, each
+ * created and prepared (ifgf2d_prepare: its wavenumber, tree and plans) with the same Np, Ps,
+ * Pang, p and formulation, into one operator whose tables hold every member side by side, with
+ * the tree levels aligned from the leaves: each phase of its set-up and of an apply is one launch
+ * over all members.  The members may be destroyed afterwards.  Vectors hold every member's
+ * unknowns in member order (member o at ifgf2d_group_offsets()[o]).  group_solve runs GMRES for
+ * all members in lock step, each with its own Krylov basis, Gram-Schmidt sums, rotations and stop
+ * test (IFGF2D_APPLY_IFGF_MIXED: FP64 refinement around complex64 inner solves, each member
+ * stopping on its own FP64 relative residual); iters[o] and est[o] per member. */
+typedef struct ifgf2d_group ifgf2d_group;
+int ifgf2d_group_create(ifgf2d_ctx* const* members, int n, ifgf2d_group** out);
+int ifgf2d_group_destroy(ifgf2d_group* group);
+const char* ifgf2d_group_last_error(const ifgf2d_group* group);
+long long ifgf2d_group_num_unknowns(const ifgf2d_group* group);
+/* n + 1 entries: the first unknown of each member, then the total */
+int ifgf2d_group_offsets(const ifgf2d_group* group, long long* offsets);
+int ifgf2d_group_apply(ifgf2d_group* group, const double* x, double* y, int mode);
+int ifgf2d_group_solve(ifgf2d_group* group, const double* rhs, double* x, int mode, double tol, int restart, int max_iters,
+                       int* iters, double* est);
+
 /* Largest N accepted by ifgf2d_apply_direct_noalloc. */
 #define IFGF2D_NOALLOC_MAX_N 65536
 
