@@ -231,12 +231,12 @@ static inline bool all_finite(const double* v, long long n) {
 
 namespace ifgf {
 // What a group of obstacles (group.cu) changes in the device part of the IFGF set-up: (k, eta)
-// per leaf box and per leaf cone (device arrays), the leaf-cone nodes (host, per leaf cone and
-// node, from each member's tree) and the propagation plan, built member by member.
+// per leaf box and per leaf cone (device arrays), and the leaf-cone nodes and the propagation
+// plan, both built member by member.
 struct SetupExtra {
     const double2* keta_leafbox = nullptr;
     const double2* keta_leafcone = nullptr;
-    const std::vector<LeafNode>* leaf_nodes = nullptr;
+    std::function<cudaError_t(LeafNode*, cudaStream_t)> build_nodes;
     std::function<cudaError_t(PropE<double>*, PropE<float>*, int*, cudaStream_t)> build_plan;
 };
 // the host tables of a context built from ctx->D: near-singular patches per point, the
@@ -264,6 +264,9 @@ int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, do
 // level_entry_base[l] the first entry of the slots with children at level l.
 cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
                             const int* level_cone_base = nullptr, const long long* level_entry_base = nullptr);
+// the leaf-cone interpolation nodes of T (position, 1 / factorization; BoxTree.h:714-745) on the
+// device, P per leaf cone in cone order (plan_device.cu); stream handling as build_prop_plan
+cudaError_t build_leaf_nodes(const Tree& T, LeafNode* out, cudaStream_t s);
 // a parent's propagation terms sorted by child cone (stable), with the parent node recorded, for
 // the batched propagation
 template <typename R>

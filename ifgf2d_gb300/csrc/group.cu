@@ -260,24 +260,28 @@ extern "C" int ifgf2d_group_create(ifgf2d_ctx* const* members, int n, ifgf2d_gro
     CK(cudaGetLastError());
     g->precomputed = true;
     g->counts[6] = (long long)ncols * D.Np;
-    // IFGF tables: (k, eta) per leaf box and leaf cone, the members' leaf nodes and plans
+    // IFGF tables: (k, eta) per leaf box and leaf cone; the members' leaf nodes and plans on the device
     std::vector<double2> kb, kl;
-    std::vector<LeafNode> nodes;
+    std::vector<long long> node_off(n + 1, 0);
     for (int o = 0; o < n; ++o) {
         const Tree& To = members[o]->T;
         const double2 ke = make_double2(G->k[o], G->eta[o]);
         kb.insert(kb.end(), To.leaf_start.size(), ke);
         kl.insert(kl.end(), To.L[To.nlevels - 1].cone_nonrel.size(), ke);
-        std::vector<double> nx, ny, nir, nii;
-        leaf_nodes(To, nx, ny, nir, nii);
-        for (size_t i = 0; i < nx.size(); ++i) nodes.push_back(LeafNode{nx[i], ny[i], nir[i], nii[i]});
+        node_off[o + 1] = node_off[o] + (long long)To.L[To.nlevels - 1].cone_nonrel.size() * To.P;
     }
     CK(keta_box.upload(kb));
     CK(keta_cone.upload(kl));
     SetupExtra ex;
     ex.keta_leafbox = keta_box.p;
     ex.keta_leafcone = keta_cone.p;
-    ex.leaf_nodes = &nodes;
+    ex.build_nodes = [&](LeafNode* out, cudaStream_t s) -> cudaError_t {
+        for (int o = 0; o < n; ++o) {
+            const cudaError_t e = build_leaf_nodes(members[o]->T, out + node_off[o], s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
     ex.build_plan = [&](PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s) -> cudaError_t {
         for (int o = 0; o < n; ++o) {
             const cudaError_t e = build_prop_plan(members[o]->T, pp64, pp32, err, s, cbase[o].data(), ebase[o].data());

@@ -398,15 +398,10 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
     const int ncl = (int)LD.cone_nonrel.size();
     std::vector<long long> loff(ncl + 1, 0);
     for (int c = 0; c < ncl; ++c) loff[c + 1] = loff[c] + (long long)P * T.leaf_count[LD.cone_box[c]];
-    if (ex) {
-        CK(ctx->leaf_nodes_d.upload(*ex->leaf_nodes));
-    } else {
-        std::vector<double> nx, ny, nir, nii;
-        leaf_nodes(T, nx, ny, nir, nii);
-        std::vector<LeafNode> nodes(nx.size());
-        for (size_t i = 0; i < nx.size(); ++i) nodes[i] = LeafNode{nx[i], ny[i], nir[i], nii[i]};
-        CK(ctx->leaf_nodes_d.upload(nodes));
-    }
+    // leaf-cone interpolation nodes, computed on the device
+    CK(ctx->leaf_nodes_d.alloc((size_t)ncl * P));
+    if (ex) CK(ex->build_nodes(ctx->leaf_nodes_d.p, ctx->stream));
+    else CK(build_leaf_nodes(T, ctx->leaf_nodes_d.p, ctx->stream));
     CK(ctx->leaf_cone_box.upload(LD.cone_box)); CK(ctx->leaf_off.upload(loff));
     CK(ctx->leafL.alloc(loff[ncl]));
     launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,

@@ -106,11 +106,8 @@ extern "C" int ifgf2d_eval_offsurface_setup(ifgf2d_ctx* ctx, long long m, const 
     if (ncl > 0) {
         std::vector<long long> loff(ncl + 1, 0);
         for (int c = 0; c < ncl; ++c) loff[c + 1] = loff[c] + (long long)P * E.leaf_count[LD.cone_box[c]];
-        std::vector<double> nx, ny, nir, nii;
-        leaf_nodes(E, nx, ny, nir, nii);
-        std::vector<LeafNode> nodes(nx.size());
-        for (size_t i = 0; i < nx.size(); ++i) nodes[i] = LeafNode{nx[i], ny[i], nir[i], nii[i]};
-        CK(W.nodes.upload(nodes));
+        CK(W.nodes.alloc((size_t)ncl * P));
+        CK(build_leaf_nodes(E, W.nodes.p, s));
         CK(W.leaf_cone_box.upload(LD.cone_box)); CK(W.leaf_off.upload(loff));
         CK(W.leafL.alloc(loff[ncl]));
         launch_leaf_setup(W.leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, W.leaf_off.p, W.nodes.p, ctx->xs_s.p,

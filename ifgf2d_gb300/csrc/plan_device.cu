@@ -128,6 +128,27 @@ __global__ void k_prop_plan(LevelDesc Lp, LevelDesc Lc, double min_x, double min
     if (out32) out32[e] = PropE<float>{child, (float)ls, (float)lt, (float)wr, (float)wi};
 }
 
+// one thread per (leaf cone, node): the node's position and 1 / (e^{ikr}/sqrt(r)) at its radius
+// (BoxTree.h:714-745)
+__global__ void k_leaf_nodes(LevelDesc L, double min_x, double min_y, double k, int Ps, ChebNodes cn, int P, long long ncones,
+                             LeafNode* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncones * P) return;
+    const long long c = idx / P;
+    const int it = (int)(idx - c * P);
+    const long long m = L.boxes[L.cone_box[c]], nonrel = L.cone_nonrel[c];
+    const long long pr = nonrel % L.nrad, pt = nonrel / L.nrad;
+    const double da = kPiD / L.ntheta;
+    const double r = cheb_to_radius(L, pr, cn.s[it % Ps]);
+    const double th = (cn.a[it / Ps] + 1.0) / 2.0 * da + da * pt;
+    double cx, cy;
+    center(L, min_x, min_y, m, cx, cy);
+    double sk, ck;
+    sincos(k * r, &sk, &ck);
+    const double sr = sqrt(r);   // 1 / (e^{ikr} / sqrt(r)) = sqrt(r) e^{-ikr}
+    out[idx] = LeafNode{r * cos(th) + cx, r * sin(th) + cy, ck * sr, -sk * sr};
+}
+
 // a parent's terms sorted by child cone (stable), with the parent node (entry index mod P)
 // recorded: one warp per parent cone, each lane ranking its entries against the parent's
 // child-cone list in shared memory
@@ -223,6 +244,26 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
     // stream-ordered buffers are freed in stream order after the kernels; plain ones need the
     // kernels finished first
     if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;
+    const cudaError_t es = cudaStreamSynchronize(s);
+    return e != cudaSuccess ? e : es;
+}
+
+cudaError_t build_leaf_nodes(const Tree& T, LeafNode* out, cudaStream_t s) {
+    if (T.Ps > 8 || T.Pang > 8) return cudaErrorInvalidValue;
+    const TreeLevel& L = T.L[T.nlevels - 1];
+    const long long nc = (long long)L.cone_nonrel.size();
+    if (nc == 0) return cudaSuccess;
+    ChebNodes cn{};
+    for (int i = 0; i < T.Ps; ++i) cn.s[T.Ps - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Ps));
+    for (int i = 0; i < T.Pang; ++i) cn.a[T.Pang - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Pang));
+    LevelBufs lb;
+    LevelDesc d;
+    cudaError_t e = upload_level(L, L.cone_base, lb, d);
+    if (e != cudaSuccess) return e;
+    const long long n = nc * T.P;
+    k_leaf_nodes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, T.min_x, T.min_y, T.k, T.Ps, cn, T.P, nc, out);
+    e = cudaGetLastError();
+    if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;   // stream-ordered inputs: freed after the kernel
     const cudaError_t es = cudaStreamSynchronize(s);
     return e != cudaSuccess ? e : es;
 }

@@ -528,30 +528,6 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     return "";
 }
 
-void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, std::vector<double>& ir, std::vector<double>& ii) {
-    const int D = T.nlevels - 1;
-    const TreeLevel& L = T.L[D];
-    LevelGeo G{&L, T.min_x, T.min_y};
-    std::vector<double> ns(T.Ps), na(T.Pang);
-    for (int i = 0; i < T.Ps; ++i) ns[T.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * T.Ps));
-    for (int i = 0; i < T.Pang; ++i) na[T.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * T.Pang));
-    const size_t n = L.cone_nonrel.size() * T.P;
-    x.resize(n); y.resize(n); ir.resize(n); ii.resize(n);
-    parallel_for((long long)L.cone_nonrel.size(), [&](long long c0, long long c1) {
-        for (long long c = c0; c < c1; ++c) {
-            const long long m = L.boxes[L.cone_box[c]], nonrel = L.cone_nonrel[c];
-            for (int it = 0; it < T.P; ++it) {
-                double px = ns[it % T.Ps], py = na[it / T.Ps];
-                const double r = G.cheb_to_radius(nonrel % L.nrad, px);
-                G.cheb_to_cart(m, nonrel, px, py);
-                const std::complex<double> f = std::complex<double>(std::cos(T.k * r), std::sin(T.k * r)) / std::sqrt(r);
-                const std::complex<double> inv = 1.0 / f;
-                x[c * T.P + it] = px; y[c * T.P + it] = py; ir[c * T.P + it] = inv.real(); ii[c * T.P + it] = inv.imag();
-            }
-        }
-    }, 256);
-}
-
 }  // namespace ifgf
 
 namespace ifgf {

@@ -107,9 +107,4 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
 long long point_morton(double x, double y, double min_x, double min_y, double boxsize, int level);
 void tree_root_box(const std::vector<double>& x, const std::vector<double>& y, double& min_x, double& min_y, double& size);
 
-// Leaf-cone interpolation nodes (BoxTree.h:714-745): per leaf cone and node, the Cartesian
-// position and 1/(e^{ikr}/sqrt r) at the node radius.  Arrays of size ncones_leaf * P.
-void leaf_nodes(const Tree& T, std::vector<double>& x, std::vector<double>& y, std::vector<double>& ir,
-                std::vector<double>& ii);
-
 }  // namespace ifgf

@@ -3,12 +3,17 @@
 The reference solves one obstacle per ForwardMap (ForwardMap.tpp:658-697).  Here the work of
 an obstacle is split at the host/device line: a pool of host threads runs the host part
 (discretisation, tree depth, tree and plans: ifgf2d_create + ifgf2d_prepare, no CUDA calls)
-a bounded number of obstacles ahead, while one thread runs the device part of each obstacle
-in turn (precomputation, device tables, GMRES, residual).  Host set-up thus overlaps GPU work
-without CUDA calls contending from many threads.  Set-up calls run single-threaded inside
-(ifgf2d_set_host_threads(1)); the pool supplies the host parallelism.  Obstacles below
-`direct_below` unknowns, and those whose points no tree depth keeps in the leaf
-neighbourhood, use the direct operator, which needs no tree.
+ahead of the device part (precomputation, device tables, GMRES, residual).  Set-up calls run
+single-threaded inside (ifgf2d_set_host_threads(1)); the pool supplies the host parallelism.
+
+* solve_obstacles: a few device threads each run one obstacle's device part at a time, on
+  the obstacle's own context stream.
+* solve_obstacles_grouped: the device threads take groups of obstacles, each merged into one
+  block-diagonal operator (ifgf2d_group_*) whose set-up and applies are one launch per phase
+  over the whole group, solved by GMRES per obstacle in lock step.
+
+Obstacles below `direct_below` unknowns, and those whose points no tree depth keeps in the
+leaf neighbourhood, use the direct operator, which needs no tree.
 
 The seeded configuration of `star_obstacles` is the multi-obstacle benchmark: star curves
 r(t) = 1 + sum_{m=1..5} a_m cos mt + b_m sin mt with a_m, b_m ~ U(-0.05, 0.05), k ~ U(10, 400),
@@ -154,31 +159,36 @@ def solve_obstacles(obstacles, tol=1e-6, workers=15, mixed=True, direct_below=0,
 
 
 def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart=300, max_iters=1000,
-                            keep_solutions=False):
-    """Solve every obstacle as one group (ifgf2d_group_*): the host part of each obstacle's
-    set-up (discretisation, tree depth, tree and plans) on `workers` threads, then one merged
-    device set-up and one lock-step GMRES for all obstacles whose points some tree depth keeps in
-    the leaf neighbourhood; each phase of their set-up and of every apply is one launch over all
-    of them.  The others use the direct operator, one at a time.  Each obstacle's `result` holds
-    its iterations, convergence, true FP64 relative residual and operator; returns the densities
-    when keep_solutions."""
+                            keep_solutions=False, chunk=16, device_threads=3):
+    """Solve the obstacles in groups (ifgf2d_group_*) of `chunk` obstacles (None: one group).
+    The host part of each obstacle's set-up (discretisation, tree depth, tree and plans) runs on
+    `workers` threads; `device_threads` threads take the groups in turn as their obstacles are
+    prepared, each merging its group into one context with its own stream and running its device
+    set-up and lock-step GMRES: each phase of a group's set-up and of every apply is one launch
+    over all its obstacles, and several groups overlap on the GPU.  Obstacles whose points no tree
+    depth keeps in the leaf neighbourhood use the direct operator, one at a time.  Each obstacle's
+    `result` holds its iterations, convergence, true FP64 relative residual and operator; returns
+    the densities when keep_solutions."""
     from . import _lib
     import ifgf2d_gb300 as G
     L = _lib.load()
     n = len(obstacles)
-    L.ifgf2d_set_host_threads(1)
-    try:
-        with ThreadPoolExecutor(max(1, workers)) as ex:
-            prepared = list(ex.map(lambda ob: _prepare_one(G, ob, 0), obstacles))
-    finally:
-        L.ifgf2d_set_host_threads(0)
+    size = n if not chunk else max(1, int(chunk))
     xs = [None] * n
-    acc = [i for i in range(n) if prepared[i][1]]
-    rhs_of = []
-    for i in acc:
-        ob, fm = obstacles[i], prepared[i][0]
-        rhs_of.append(-np.exp(1j * ob.k * (math.cos(ob.angle) * fm.xs_ + math.sin(ob.angle) * fm.ys_)))
-    if acc:
+    direct = []
+    futs = [None] * n
+
+    def run_group(c0):
+        idx = list(range(c0, min(n, c0 + size)))
+        prepared = {i: futs[i].result() for i in idx}
+        acc = [i for i in idx if prepared[i][1]]
+        dlist = [(i, prepared[i][0]) for i in idx if not prepared[i][1]]
+        if not acc:
+            return dlist
+        rhs_of = []
+        for i in acc:
+            ob, fm = obstacles[i], prepared[i][0]
+            rhs_of.append(-np.exp(1j * ob.k * (math.cos(ob.angle) * fm.xs_ + math.sin(ob.angle) * fm.ys_)))
         grp = G.Group([prepared[i][0] for i in acc])
         for i in acc:                       # the group holds its own copy of everything
             prepared[i][0].close()
@@ -186,21 +196,29 @@ def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart
         x = grp.solve(rhs, tol=tol, restart=restart, max_iters=max_iters, mixed=mixed)
         st = grp.last_solve
         res = grp.split(grp.apply(x) - rhs)
+        parts = grp.split(x)
         for q, i in enumerate(acc):
             b = rhs_of[q]
             obstacles[i].result = {"iters": st["iters"][q], "error": st["error"][q], "converged": st["error"][q] < tol,
                                    "true_rel_residual": float(np.linalg.norm(res[q]) / np.linalg.norm(b)),
                                    "accelerated": True, "N": int(b.size), "grouped": True}
             if keep_solutions:
-                xs[i] = grp.split(x)[q].copy()
+                xs[i] = parts[q].copy()
         grp.close()
-    for i in range(n):
-        if prepared[i][1]:
-            continue
-        fm = prepared[i][0]
+        return dlist
+
+    L.ifgf2d_set_host_threads(1)                # the pools supply the host parallelism
+    try:
+        with ThreadPoolExecutor(max(1, workers)) as ex, ThreadPoolExecutor(max(1, int(device_threads))) as dev:
+            for i, ob in enumerate(obstacles):
+                futs[i] = ex.submit(_prepare_one, G, ob, 0)
+            for f in [dev.submit(run_group, c0) for c0 in range(0, n, size)]:
+                direct += f.result()
+    finally:
+        L.ifgf2d_set_host_threads(0)
+    for i, fm in direct:
         x = _device_one(G, obstacles[i], fm, False, tol, mixed, restart, max_iters)
         obstacles[i].result["grouped"] = False
         xs[i] = x if keep_solutions else None
         fm.close()
     return xs if keep_solutions else None
-

@@ -6,7 +6,7 @@
 //     besselFunctions.h:313-341).  Method: ascending power series (A&S 9.1.10-9.1.11)
 //     summed in double-double arithmetic for x < 25, Hankel asymptotic expansion
 //     (A&S 9.2.5-9.2.10) for x >= 25.  Pinned against scipy.special.hankel1 by the
-//     tests (tests/test_oracle_hankel.py).
+//     tests (tests/test_oracle.py).
 //   * Fejer quadrature and the rectangular-polar changes of variables
 //     (utils/Quadrature.hpp:12-173).
 //   * 1D Chebyshev transform and root finding (utils/Chebyshev1d.hpp:249-266, 134-163,

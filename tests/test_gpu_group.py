@@ -60,3 +60,18 @@ def test_gpu_group_solve_reaches_every_member(lib, mixed):
         xo = fm.gmres(b, tol=tol, restart=300, max_iters=1000, mixed=mixed)
         assert abs(fm.last_solve["iters"] - g.last_solve["iters"][o]) <= 2, o
         assert rel(xs, xo) < (1e-5 if mixed else 1e-6)
+
+
+def test_gpu_grouped_driver_matches_one_at_a_time(lib):
+    """scatterers.solve_obstacles_grouped: groups of four obstacles on two device threads reach
+    each obstacle's FP64 tolerance, and their solutions equal those of the one-at-a-time path."""
+    from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles, solve_obstacles_grouped
+    obs = star_obstacles(10, seed=5, kmax=150.0)
+    xg = solve_obstacles_grouped(obs, tol=1e-8, workers=4, mixed=False, keep_solutions=True, chunk=4, device_threads=2)
+    assert all(o.result["converged"] for o in obs)
+    assert max(o.result["true_rel_residual"] for o in obs) < 1e-7
+    ref = star_obstacles(10, seed=5, kmax=150.0)
+    xr = solve_obstacles(ref, tol=1e-8, workers=0, mixed=False, keep_solutions=True)
+    for a, b, o, r in zip(xg, xr, obs, ref):
+        assert abs(o.result["iters"] - r.result["iters"]) <= 1
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-6
