@@ -304,7 +304,8 @@ class ForwardMap:
             except Exception:
                 dev = "gpu"
             wc = self.work_counts()
-            key = f"{dev}|N={self.total_num_unknowns_}|k={self.wavenumber:.17g}|P={self.Ps}x{self.Pang}|" \
+            # "v2": the variant set with the shared-memory staged propagation
+            key = f"v2|{dev}|N={self.total_num_unknowns_}|k={self.wavenumber:.17g}|P={self.Ps}x{self.Pang}|" \
                   f"nl={self.nlevels}|cones={wc['cones']}|prop={wc['prop_evals']}"
             d = cache_dir or os.environ.get("IFGF2D_TUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "ifgf2d_gb300")
             path = os.path.join(d, "tuning.json")

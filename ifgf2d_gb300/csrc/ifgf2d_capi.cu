@@ -655,7 +655,7 @@ static int tune_precision(ifgf2d_ctx* ctx, int reps, const V2<R>* rho, const V2<
     for (int l = Dl; l >= 3 && l < kTuneLevels; --l) {
         const TreeLevel& Lp = T.L[l - 1];
         best = 1e30f; int bestp = 0;
-        for (int cpb : {2, 4, 0}) {
+        for (int cpb : {2, 4, 0, kPropStaged}) {
             const float ms = time_it([&] {
                 launch_propagate_t<R>(Lp.cone_base, Lp.cone_base + (int)Lp.cone_nonrel.size(), ctx->pp_ptr.p, ctx->pp_nchild.p, pp,
                                       T.Ps, T.Pang, Gsep, coef, s, cpb);

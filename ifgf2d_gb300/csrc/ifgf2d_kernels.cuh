@@ -107,6 +107,9 @@ bool launch_leaf_tma(const int* cone_box, int ncones, int cone_base, const int* 
                      const long long* leaf_off, const float2* L, const float2* rho, int P, float2* coef, int* err, int nsm,
                      cudaStream_t s);
 cudaError_t leaf_tma_init();
+// the propagation variant that stages child coefficient blocks in shared memory (k_propagate_st);
+// other values of cones_per_block: 2, 4, or 0 for the most that fit 256 threads
+constexpr int kPropStaged = 1;
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
                         int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block = 0);

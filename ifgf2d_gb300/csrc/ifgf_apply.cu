@@ -246,6 +246,136 @@ __global__ void __launch_bounds__(256) k_propagate_t(int pbegin, int pend, const
     }
 }
 
+// k_propagate_t with the child coefficient blocks staged in shared memory.  A parent cone's 25
+// nodes read 1-4 children's blocks each, but the block's ten parent cones touch only about 40
+// distinct child cones (3.4-4.3 per parent cone on the kite trees), so the per-thread gathers
+// of k_propagate_t read each block about twelve times.  Here the block first collects its
+// distinct child cones in a shared hash table (open addressing, at most kStageKeys probes),
+// copies each one's block once with coalesced loads, and evaluates from shared memory.  A child
+// cone that finds no free key or no data slot is read from global memory.  Each thread's
+// arithmetic is that of k_propagate_t in the same order, so the results are bit-identical.
+// FP64 gains a few per cent from it (the autotuner takes it on the finer levels); in complex64
+// the 25 shared-memory reads per term cost as much as the L1 hits they replace.
+constexpr int kStageKeys = 128;
+template <typename R, int P>
+struct PropStage {
+    static constexpr int cap = (size_t)P * sizeof(V2<R>) * 64 <= 26000 ? 64 : (int)(26000 / ((size_t)P * sizeof(V2<R>)));
+};
+template <typename R, int PS, int PA, int CPB>
+__global__ void __launch_bounds__(256) k_propagate_st(int pbegin, int pend, const long long* __restrict__ pp_ptr,
+                                                      const int* __restrict__ pp_nchild, const PropE<R>* __restrict__ pp,
+                                                      const R* __restrict__ Gsep, V2<R>* __restrict__ coef) {
+    constexpr int P = PS * PA;
+    constexpr int CAP = PropStage<R, P>::cap;
+    __shared__ int key[kStageKeys], slot_of[kStageKeys], ulist[CAP];
+    __shared__ int nused;
+    __shared__ V2<R> blk[CAP][P];
+    __shared__ V2<R> sv[CPB][P];
+    __shared__ V2<R> su[CPB][P];
+    __shared__ R sGs[PS * PS], sGa[PA * PA];
+    for (int i = threadIdx.x; i < PS * PS; i += blockDim.x) sGs[i] = Gsep[i];
+    for (int i = threadIdx.x; i < PA * PA; i += blockDim.x) sGa[i] = Gsep[PS * PS + i];
+    for (int i = threadIdx.x; i < kStageKeys; i += blockDim.x) key[i] = -1;
+    if (threadIdx.x == 0) nused = 0;
+    const int local = threadIdx.x / P, pt = threadIdx.x - local * P;
+    const int pc = pbegin + blockIdx.x * CPB + local;
+    const bool active = local < CPB && pc < pend;
+    PropE<R> E[4];
+    int nch = 0, pos[4] = {-1, -1, -1, -1};
+    if (active) {
+        const long long e0 = pp_ptr[pc];
+        nch = min(pp_nchild[pc], 4);
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) if (ch < nch) E[ch] = pp[e0 + (long long)ch * P + pt];
+    }
+    __syncthreads();
+    // the distinct child cones of the block: lanes of a warp that share a cone elect one leader,
+    // which claims (or finds) the cone's key; the thread that claims a key appends the cone
+    const int lane = threadIdx.x & 31;
+    const int wsize = min(32, (int)blockDim.x - (int)(threadIdx.x & ~31u));   // the block's last warp may be partial
+    const unsigned wmask = wsize == 32 ? 0xffffffffu : (1u << wsize) - 1u;
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+        const int c = ch < nch ? E[ch].child_cone : -1;
+        const unsigned peers = __match_any_sync(wmask, c);
+        const int leader = __ffs(peers) - 1;
+        int h = -1;
+        if (c >= 0 && lane == leader) {
+            int q = (int)(((unsigned)c * 2654435761u) >> 25) & (kStageKeys - 1);
+            for (int probe = 0; probe < kStageKeys; ++probe) {
+                const int old = atomicCAS(&key[q], -1, c);
+                if (old == -1) {
+                    const int id = atomicAdd(&nused, 1);
+                    slot_of[q] = id < CAP ? id : -1;
+                    if (id < CAP) ulist[id] = c;
+                    h = q;
+                    break;
+                }
+                if (old == c) { h = q; break; }
+                q = (q + 1) & (kStageKeys - 1);
+            }
+        }
+        h = __shfl_sync(wmask, h, leader);
+        if (c >= 0) pos[ch] = h;
+    }
+    __syncthreads();
+    // one coalesced copy of each distinct child block
+    {
+        const int n = min(nused, CAP) * P;
+        for (int i0 = threadIdx.x; i0 < n; i0 += 4 * blockDim.x) {
+            V2<R> v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * blockDim.x;
+                if (i < n) v[u] = coef[(long long)ulist[i / P] * P + i % P];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * blockDim.x;
+                if (i < n) blk[i / P][i % P] = v[u];
+            }
+        }
+    }
+    __syncthreads();
+    if (active) {
+        V2<R> v; v.x = R(0); v.y = R(0);
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+            if (ch >= nch) break;
+            const int slot = pos[ch] >= 0 ? slot_of[pos[ch]] : -1;
+            const V2<R> it = slot >= 0 ? interp_eval<R, PS, PA>(blk[slot], E[ch].s, E[ch].th)
+                                       : interp_eval<R, PS, PA>(coef + (long long)E[ch].child_cone * P, E[ch].s, E[ch].th);
+            V2<R> w; w.x = E[ch].wr; w.y = E[ch].wi;
+            cmac<R>(v, it, w);
+        }
+        sv[local][pt] = v;
+    }
+    __syncthreads();
+    const int m = pt % PS, l = pt / PS;
+    if (active) {            // u[l][m] = sum_k Gs[m][k] v[l*PS + k]
+        V2<R> u; u.x = R(0); u.y = R(0);
+#pragma unroll
+        for (int k = 0; k < PS; ++k) {
+            const R g = sGs[m * PS + k];
+            const V2<R> vv = sv[local][l * PS + k];
+            u.x = rfma(g, vv.x, u.x); u.y = rfma(g, vv.y, u.y);
+        }
+        su[local][l * PS + m] = u;
+    }
+    __syncthreads();
+    if (active) {            // c[n][m] = sum_l Ga[n][l] u[l][m], stored at n*PS + m
+        const int n = l;
+        V2<R> c; c.x = R(0); c.y = R(0);
+#pragma unroll
+        for (int q = 0; q < PA; ++q) {
+            const R g = sGa[n * PA + q];
+            const V2<R> u = su[local][q * PS + m];
+            c.x = rfma(g, u.x, c.x); c.y = rfma(g, u.y, c.y);
+        }
+        coef[(long long)pc * P + n * PS + m] = c;
+    }
+}
+
 // one warp per Morton-sorted target; near row layout [target][neighbour sources], and
 // near_src[near_src_off[b] + e] the Morton index of entry e's source in leaf box b's rows, so the
 // lanes stride over one flat row with independent loads
@@ -340,10 +470,14 @@ template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps, int Pang,
                         const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block) {
     if (pend <= pbegin) return;
-    // cones per block (the tuning variant): 2, 4 or the most that fit 256 threads
+    // cones per block (the tuning variant): 2, 4 or the most that fit 256 threads; kPropStaged:
+    // the most that fit, child blocks staged in shared memory
     IFGF_DISPATCH_P(Ps, Pang, {
         constexpr int CPBMAX = 256 / (PS * PA);
-        if (cones_per_block == 2 && CPBMAX >= 2)
+        if (cones_per_block == kPropStaged)
+            k_propagate_st<R, PS, PA, CPBMAX><<<nblk_a(pend - pbegin, CPBMAX), CPBMAX * PS * PA, 0, s>>>(pbegin, pend, pp_ptr,
+                                                                                                      pp_nchild, pp, Gsep, coef);
+        else if (cones_per_block == 2 && CPBMAX >= 2)
             k_propagate_t<R, PS, PA, 2><<<nblk_a(pend - pbegin, 2), 2 * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);
         else if (cones_per_block == 4 && CPBMAX >= 4)
             k_propagate_t<R, PS, PA, 4><<<nblk_a(pend - pbegin, 4), 4 * PS * PA, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pp, Gsep, coef);

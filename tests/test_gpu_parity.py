@@ -392,13 +392,23 @@ def test_gpu_autotune_keeps_results_and_caches(lib, oracle, tmp_path):
     L = lib._lib.load()
     n = int(L.ifgf2d_tuning_size())
     import ctypes
-    for leaf, prop in ((1, 2), (2, 4), (10, 0), (5, 2), (0, 4)):   # leaf 0: complex64 table streamed by TMA
+    # leaf 0: complex64 table streamed by TMA; prop 1: child blocks staged in shared memory
+    for leaf, prop in ((1, 2), (2, 4), (10, 0), (5, 2), (0, 4), (5, 1), (0, 1)):
         c = np.zeros(n, dtype=np.int32)
         c[:2] = leaf
         c[2:] = prop
         assert L.ifgf2d_set_tuning(fm.handle, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
         assert rel(fm.compute_Ax_acc(d), y64) < 1e-14
         assert rel(fm.compute_Ax_acc(d, mixed=True), y32) < 1e-6
+    # the staged propagation does the arithmetic of the default one in the same order
+    c = np.asarray(fm.get_tuning()).copy()
+    c[2:-1] = 0
+    fm.set_tuning(c)
+    a64, a32 = fm.compute_Ax_acc(d), fm.compute_Ax_acc(d, mixed=True)
+    c[2:-1] = 1
+    fm.set_tuning(c)
+    assert np.array_equal(fm.compute_Ax_acc(d), a64)
+    assert np.array_equal(fm.compute_Ax_acc(d, mixed=True), a32)
     t1 = fm.autotune(cache_dir=str(tmp_path))
     assert (tmp_path / "tuning.json").exists()
     assert t1[0] in {1, 2, 5, 10} and t1[1] in {0, 1, 2, 5, 10}
