@@ -199,9 +199,10 @@ void cousins_of(const TreeLevel& L, long long m, std::vector<int>& out) {
 // needed by the parents' interpolation nodes are added here through the protobox routing table
 // (BoxTree.h:299-428).  Fills T.L[l]'s cone lists and, for l > 2, appends the level's slot form
 // of the propagation plan (PropSlots, entries in global parent-id order) and its CSR rows to
-// T.pp_ptr / pp_nchild.
+// T.pp_ptr / pp_nchild.  `seen` is the caller's scratch table, all -1 on entry and on return: it
+// grows to the largest level's need once instead of being allocated and filled per level.
 std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long long>>& part, const std::vector<double>& ns,
-                         const std::vector<double>& na) {
+                         const std::vector<double>& na, std::vector<int>& seen) {
     TreeLevel& L = T.L[l];
     LevelGeo G{&L, T.min_x, T.min_y};
     const int P = T.P, Ps = T.Ps;
@@ -209,8 +210,12 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
     // cones needed by the parents' interpolation nodes, through the protobox routing
     // table (BoxTree.h:299-428): for each parent nonrel cone and child position, the
     // routing is computed once, from the first parent box (in cone order) that has it.
-    struct Route { long long pnc; int pos; int first_pc; std::vector<long long> nr, uniq; };
+    // per route: its child cone segment for each of the P parent nodes at rn[r * P ...], and its
+    // nu[r] distinct segments, ascending, at uq[r * P ...]
+    struct Route { long long pnc; int pos; int first_pc; };
     std::vector<Route> routes;
+    std::vector<long long> rn, uq;
+    std::vector<int> nu;
     std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
     std::vector<int> child_box;         // per (parent box * 4 + pos): child box index or -1
     const TreeLevel* Lpp = l > 2 ? &T.L[l - 1] : nullptr;
@@ -231,7 +236,7 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
         // pnc * 4 + pos -> route, over the parent level's cone segment numbers
         long long maxnc = 0;
         for (long long nc : Lp.cone_nonrel) maxnc = std::max(maxnc, nc);
-        std::vector<int> seen((size_t)(maxnc + 1) * 4, -1);
+        if (seen.size() < (size_t)(maxnc + 1) * 4) seen.resize((size_t)(maxnc + 1) * 4, -1);
         for (size_t pc = 0; pc < npar; ++pc) {
             const long long pnc = Lp.cone_nonrel[pc];
             for (int pos = 0; pos < 4; ++pos) {
@@ -239,24 +244,40 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
                 int& r = seen[(size_t)(pnc * 4 + pos)];
                 if (r < 0) {
                     r = (int)routes.size();
-                    routes.push_back(Route{pnc, pos, (int)pc, {}, {}});
+                    routes.push_back(Route{pnc, pos, (int)pc});
                 }
                 route_of[pc * 4 + pos] = r;
             }
         }
+        for (const Route& R : routes) seen[(size_t)(R.pnc * 4 + R.pos)] = -1;
+        rn.resize(routes.size() * P);
+        uq.resize(routes.size() * P);
+        nu.resize(routes.size());
         parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
+            // the parent nodes' radii and angles, once per route (cheb_to_cart's arithmetic)
+            std::vector<double> rr(Ps), cs(T.Pang), sn(T.Pang);
             for (long long r = r0; r < r1; ++r) {
-                Route& R = routes[r];
+                const Route& R = routes[r];
                 const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
-                R.nr.resize(P);
-                for (int it = 0; it < P; ++it) {
-                    double px = ns[it % Ps], py = na[it / Ps];
-                    Gp.cheb_to_cart(pm, R.pnc, px, py);
-                    R.nr[it] = G.nonrel_of(pm * 4 + R.pos, px, py);
+                long long* nr = rn.data() + r * P;
+                long long* u = uq.data() + r * P;
+                const long long pr = R.pnc % Lp.nrad, pt = R.pnc / Lp.nrad;
+                const double da = kPiT / Lp.ntheta;
+                double cx, cy;
+                Gp.center(pm, cx, cy);
+                for (int i = 0; i < Ps; ++i) rr[i] = Gp.cheb_to_radius(pr, ns[i]);
+                for (int j = 0; j < T.Pang; ++j) {
+                    const double th = (na[j] + 1.0) / 2.0 * da + da * pt;
+                    cs[j] = std::cos(th);
+                    sn[j] = std::sin(th);
                 }
-                R.uniq = R.nr;
-                std::sort(R.uniq.begin(), R.uniq.end());
-                R.uniq.erase(std::unique(R.uniq.begin(), R.uniq.end()), R.uniq.end());
+                for (int it = 0; it < P; ++it) {
+                    const double px = rr[it % Ps] * cs[it / Ps] + cx, py = rr[it % Ps] * sn[it / Ps] + cy;
+                    nr[it] = G.nonrel_of(pm * 4 + R.pos, px, py);
+                }
+                std::copy(nr, nr + P, u);
+                std::sort(u, u + P);
+                nu[r] = (int)(std::unique(u, u + P) - u);
             }
         });
         const long long nchunk = std::max<long long>(1, std::min<long long>(4 * kMaxThreads, (long long)npar / 256));
@@ -271,7 +292,7 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
                         const int r = route_of[pc * 4 + pos];
                         if (r < 0) continue;
                         const int cb = child_box[(size_t)Lp.cone_box[pc] * 4 + pos];
-                        for (long long nr : routes[r].uniq) w.push_back(key(cb, nr));
+                        for (int j = 0; j < nu[r]; ++j) w.push_back(key(cb, uq[(size_t)r * P + j]));
                     }
                 }
                 sort_unique(w);
@@ -300,7 +321,7 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
     PropSlots S;
     S.level = l;
     S.entry_base = T.pp_total;
-    for (const Route& R : routes) S.route_nonrel.insert(S.route_nonrel.end(), R.nr.begin(), R.nr.end());
+    S.route_nonrel = std::move(rn);
     long long done = T.pp_ptr.back();
     std::vector<long long> first(npar + 1, 0);   // per parent cone: its first slot
     for (size_t pc = 0; pc < npar; ++pc) {
@@ -437,6 +458,7 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     for (int i = 0; i < Pang; ++i) na[Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Pang));
     const int P = T.P;
 
+    std::vector<int> seen;   // finish_level's route table
     // relevant cones, level by level (BoxTree.h:553-583).  A wanted cone is the key
     // (box index << 32 | nonrel cone); each level's keys are collected per thread, then sorted
     // and deduplicated, which gives the cones in (box, nonrel) order.
@@ -465,7 +487,7 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                 }
             }, 1);
         }
-        std::string msg = finish_level(T, l, part, ns, na);
+        std::string msg = finish_level(T, l, part, ns, na, seen);
         if (!msg.empty()) return msg;
     }
     // leaf-level cones have no children: close the propagation CSR for them
@@ -567,6 +589,7 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
     for (int i = 0; i < E.Ps; ++i) ns[E.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Ps));
     for (int i = 0; i < E.Pang; ++i) na[E.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Pang));
     const int P = E.P;
+    std::vector<int> seen;   // finish_level's route table
     for (int l = 2; l < nlevels; ++l) {
         TreeLevel& L = E.L[l];
         LevelGeo G{&L, E.min_x, E.min_y};
@@ -589,7 +612,7 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
         bool any = false;
         for (auto& w : part) any = any || !w.empty();
         if (!any && l == 2) part.assign(1, std::vector<unsigned long long>{});
-        std::string msg = finish_level(E, l, part, ns, na);
+        std::string msg = finish_level(E, l, part, ns, na, seen);
         if (!msg.empty() && msg != "The number of cone segments on any level cannot be 0") return msg;
         if (!msg.empty()) {   // no cone at this level: empty lists, nothing below needs it either
             TreeLevel& Le = E.L[l];
