@@ -273,17 +273,23 @@ class ForwardMap:
     BATCH_TC_LEAF_FP32 = 4
     BATCH_BULK_PROPAGATION = 8
     BATCH_GROUPED_INTERP = 16
+    SINGLE_INTERP_BY_BOX_FP64 = 32
+    SINGLE_INTERP_BY_BOX_C64 = 64
+
+    _BATCH_BITS = 31
 
     @property
     def batch_tensor_cores(self):
-        """bit mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor
-        cores (BATCH_TC_LEAF, BATCH_TC_PROPAGATION; the last entry of the tuning table)"""
-        return int(self.get_tuning()[-1])
+        """bit mask of the batched complex64 kernel choices (BATCH_*: tcgen05 3xTF32 leaf and
+        propagation, bulk-copy propagation, grouped interpolation).  They share the last entry
+        of the tuning table with the single-vector choices (SINGLE_INTERP_BY_BOX_*), which this
+        property leaves alone."""
+        return int(self.get_tuning()[-1]) & self._BATCH_BITS
 
     @batch_tensor_cores.setter
     def batch_tensor_cores(self, mask):
         c = self.get_tuning()
-        c[-1] = int(mask)
+        c[-1] = (int(c[-1]) & ~self._BATCH_BITS) | (int(mask) & self._BATCH_BITS)
         self.set_tuning(c)
 
     def autotune(self, reps=5, cache=True, cache_dir=None):
@@ -304,8 +310,8 @@ class ForwardMap:
             except Exception:
                 dev = "gpu"
             wc = self.work_counts()
-            # "v2": the variant set with the shared-memory staged propagation
-            key = f"v2|{dev}|N={self.total_num_unknowns_}|k={self.wavenumber:.17g}|P={self.Ps}x{self.Pang}|" \
+            # "v3": the variant set with the staged propagation and the interpolation by leaf box
+            key = f"v3|{dev}|N={self.total_num_unknowns_}|k={self.wavenumber:.17g}|P={self.Ps}x{self.Pang}|" \
                   f"nl={self.nlevels}|cones={wc['cones']}|prop={wc['prop_evals']}"
             d = cache_dir or os.environ.get("IFGF2D_TUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "ifgf2d_gb300")
             path = os.path.join(d, "tuning.json")

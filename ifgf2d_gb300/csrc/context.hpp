@@ -25,6 +25,10 @@ constexpr int kBatchTcProp = 2;   // propagation (k_prop_t5)
 constexpr int kBatchTcLeaf6 = 4;  // leaf-cone sums with three TF32 terms per operand (6 products)
 constexpr int kBatchBulkProp = 8; // FP32 FMA propagation with TMA-staged child coefficients (k_prop_bk)
 constexpr int kBatchGroupedInterp = 16;   // interpolation grouped by cone per leaf box (k_interp_grp)
+constexpr int kSingleInterpBox64 = 32;    // single vector, FP64: interpolation by leaf box (k_interp_box)
+constexpr int kSingleInterpBox32 = 64;    // single vector, complex64: interpolation by leaf box
+constexpr int kKernelBits = kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6 | kBatchBulkProp | kBatchGroupedInterp |
+                            kSingleInterpBox64 | kSingleInterpBox32;
 
 namespace ifgf {
 
@@ -140,8 +144,9 @@ struct ifgf2d_ctx {
     // ifgf2d_autotune / ifgf2d_set_tuning
     int tune_leaf[2] = {5, 5};      // complex64 also 0: the table streamed by TMA bulk copies (k_leaf_tma)
     int tune_prop[2][kTuneLevels] = {};
-    // batched complex64 kernels on the tcgen05 tensor cores in 3xTF32 (bit mask, else FP32 FMA)
-    int tune_batch_tc = kBatchTcLeaf | kBatchGroupedInterp;
+    // kernel choices (bit mask): batched complex64 kernels on the tcgen05 tensor cores in 3xTF32
+    // (else FP32 FMA), the batched grouped interpolation, the single-vector interpolation by box
+    int tune_batch_tc = kBatchTcLeaf | kBatchGroupedInterp | kSingleInterpBox32;
     // a host-side tree from ifgf2d_prepare waiting for ifgf2d_setup (same k and request)
     bool prep_ready = false;
     double prep_k = 0.0;
@@ -187,6 +192,14 @@ struct ifgf2d_ctx {
     DBuf<PropE<float>> pp32;
     DBuf<InterpE<float>> ip32;
     DBuf<float> Gsep32;
+    // interpolation by leaf box (k_interp_box): work items, the plan box-transposed in both
+    // precisions, and the pieces' sums per target
+    DBuf<int4> ib_items;
+    DBuf<int2> nb_items;            // near field by leaf box (k_near_box): (box, first of up to 32 targets)
+    DBuf<InterpE<double>> ipT;
+    DBuf<InterpE<float>> ip32T;
+    DBuf<double2> ib_part;
+    DBuf<float2> ib_part32;
     // work vectors
     DBuf<double2> rho, vin, vout;
     std::unique_ptr<GmresWork> gw;

@@ -429,6 +429,30 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
         launch_interp_to_c64(ctx->ip.p, (long long)T.ip.size(), ctx->ip32.p, ctx->stream);
         CK(cudaGetLastError());
     }
+    {   // interpolation by leaf box: per box, chunks of 32 targets x pieces of kIbPiece terms
+        std::vector<int4> items;
+        std::vector<int2> nitems;
+        int maxpc = 0;
+        for (int b = 0; b < nleaf; ++b) {
+            const int s0 = T.leaf_start[b], n = T.leaf_count[b];
+            if (n <= 0) continue;
+            for (int c0 = 0; c0 < n; c0 += kNearTargets) nitems.push_back(make_int2(b, c0));
+            const int nt = T.ip_ptr[s0 + 1] - T.ip_ptr[s0];   // the same for every target of the box
+            const int npc = (nt + kIbPiece - 1) / kIbPiece;
+            maxpc = std::max(maxpc, npc);
+            for (int c0 = 0; c0 < n; c0 += 32)
+                for (int q = 0; q < npc; ++q) items.push_back(make_int4(b, c0, q * kIbPiece, std::min(nt, (q + 1) * kIbPiece)));
+        }
+        CK(ctx->ib_items.upload(items));
+        CK(ctx->nb_items.upload(nitems));
+        CK(ctx->ipT.alloc(T.ip.size())); CK(ctx->ip32T.alloc(T.ip.size()));
+        launch_interp_transpose<double>((int)N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->ip_ptr.p, ctx->ip.p,
+                                        ctx->ipT.p, ctx->stream);
+        launch_interp_transpose<float>((int)N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->leaf_count.p, ctx->ip_ptr.p, ctx->ip.p,
+                                       ctx->ip32T.p, ctx->stream);
+        CK(cudaGetLastError());
+        CK(ctx->ib_part.alloc((size_t)std::max(maxpc, 1) * N)); CK(ctx->ib_part32.alloc((size_t)std::max(maxpc, 1) * N));
+    }
     CK(ctx->coef.alloc((size_t)T.total_cones * P));
     CK(ctx->coef32.alloc((size_t)T.total_cones * P));
     CK(ctx->rho32.alloc(N + 2));   // + padding: the TMA leaf kernel copies from 16-byte boundaries
@@ -475,6 +499,34 @@ static int check_kerr(ifgf2d_ctx* ctx) {
 }
 
 // ------------------------------------------------------------------ apply
+// y += near field + cousin interpolants of every target (BoxTree.h:1049-1069).  By target:
+// k_final_t, a warp per target.  By leaf box: the interpolation by k_interp_box (pieces per
+// target), then the near field by k_near_box, which adds the pieces in order.
+template <typename R>
+static void launch_interp_final(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const InterpE<R>* ip, const V2<R>* coef,
+                                double2* y, bool by_box) {
+    const Tree& T = ctx->T;
+    const int N = (int)ctx->D.N;
+    if (!by_box || ctx->nb_items.n == 0) {
+        launch_final_t<R>(N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->near_src_off.p, ctx->near_src.p, ctx->near_rowlen.p,
+                          ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p, y, ctx->stream);
+        return;
+    }
+    const V2<R>* part = nullptr;
+    if (ctx->ib_items.n > 0) {
+        V2<R>* pp;
+        const InterpE<R>* ipT;
+        if constexpr (sizeof(R) == 4) { pp = ctx->ib_part32.p; ipT = ctx->ip32T.p; }
+        else { pp = ctx->ib_part.p; ipT = ctx->ipT.p; }
+        launch_interp_box<R>(ctx->ib_items.p, (int)ctx->ib_items.n, N, ctx->leaf_start.p, ctx->leaf_count.p, ctx->ip_ptr.p, ipT,
+                             coef, T.Ps, T.Pang, pp, ctx->stream);
+        part = pp;
+    }
+    launch_near_box<R>(ctx->nb_items.p, (int)ctx->nb_items.n, ctx->leaf_start.p, ctx->leaf_count.p, ctx->near_src_off.p,
+                       ctx->near_src.p, ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, part, N, ctx->sorting.p, y,
+                       ctx->stream);
+}
+
 // y += far field of the Morton-ordered intensities (rho / rho32), BoxTree.h:1037-1061
 template <typename R>
 static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* leafL, const PropE<R>* pp,
@@ -500,8 +552,7 @@ static void far_ifgf_t(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, con
                               T.Ps, T.Pang, Gsep, coef, s, l < kTuneLevels ? ctx->tune_prop[pr][l] : 0);
     }
     if (ev) cudaEventRecord(ev[1], s);
-    launch_final_t<R>((int)ctx->D.N, ctx->point_leaf.p, ctx->leaf_start.p, ctx->near_src_off.p, ctx->near_src.p,
-                      ctx->near_rowlen.p, ctx->near_off.p, near, rho, ctx->ip_ptr.p, ip, coef, T.Ps, T.Pang, ctx->sorting.p, y, s);
+    launch_interp_final<R>(ctx, rho, near, ip, coef, y, (ctx->tune_batch_tc & (pr ? kSingleInterpBox32 : kSingleInterpBox64)) != 0);
 }
 
 // the IFGF far field in the precision of `mode`; x in original order, y += result.  With
@@ -611,7 +662,7 @@ extern "C" int ifgf2d_set_tuning(ifgf2d_ctx* ctx, const int* c) {
     ctx->tune_leaf[0] = c[0]; ctx->tune_leaf[1] = c[1];
     for (int p = 0; p < 2; ++p)
         for (int l = 0; l < kTuneLevels; ++l) ctx->tune_prop[p][l] = c[2 + p * kTuneLevels + l];
-    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & (kBatchTcLeaf | kBatchTcProp | kBatchTcLeaf6 | kBatchBulkProp | kBatchGroupedInterp);
+    ctx->tune_batch_tc = c[2 + 2 * kTuneLevels] & kKernelBits;
     if (ctx->gw) ctx->gw->drop_graphs();   // the captured iterations hold the old launch shapes
     return IFGF2D_OK;
 }
@@ -663,6 +714,17 @@ static int tune_precision(ifgf2d_ctx* ctx, int reps, const V2<R>* rho, const V2<
             if (ms < best) { best = ms; bestp = cpb; }
         }
         ctx->tune_prop[pr][l] = bestp;
+    }
+    {   // the interpolation by leaf box or by target (y: the context's output vector, overwritten later)
+        const int bit = pr ? kSingleInterpBox32 : kSingleInterpBox64;
+        const V2<R>* near;
+        const InterpE<R>* ip;
+        if constexpr (sizeof(R) == 4) { near = ctx->near32.p; ip = ctx->ip32.p; }
+        else { near = ctx->near.p; ip = ctx->ip.p; }
+        const float tb = time_it([&] { launch_interp_final<R>(ctx, rho, near, ip, coef, ctx->vout.p, true); });
+        const float tt = time_it([&] { launch_interp_final<R>(ctx, rho, near, ip, coef, ctx->vout.p, false); });
+        if (tb < tt) ctx->tune_batch_tc |= bit;
+        else ctx->tune_batch_tc &= ~bit;
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     CK(cudaGetLastError());

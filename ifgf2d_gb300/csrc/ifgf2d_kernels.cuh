@@ -113,11 +113,30 @@ constexpr int kPropStaged = 1;
 template <typename R>
 void launch_propagate_t(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropE<R>* pp, int Ps,
                         int Pang, const R* Gsep, V2<R>* coef, cudaStream_t s, int cones_per_block = 0);
+// with `part`, the interpolation terms were summed by launch_interp_box: the near field plus each
+// target's pieces in order
 template <typename R>
 void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* near_src_off, const int* near_src,
                     const int* near_rowlen, const long long* near_off, const V2<R>* near,
                     const V2<R>* rho, const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang,
-                    const long long* sorting, double2* y, cudaStream_t s);
+                    const long long* sorting, double2* y, cudaStream_t s, const V2<R>* part = nullptr);
+// interpolation by leaf box (k_interp_box): items[w] = (leaf box, first target, first term, end
+// term), pieces of kIbPiece terms; part[piece * N + target] receives each piece's sum
+constexpr int kIbPiece = 8;
+template <typename R>
+void launch_interp_box(const int4* items, int nitems, int N, const int* leaf_start, const int* leaf_count, const int* ip_ptr,
+                       const InterpE<R>* ipT, const V2<R>* coef, int Ps, int Pang, V2<R>* part, cudaStream_t s);
+// near field by leaf box (k_near_box): items[w] = (leaf box, first of up to 32 targets); adds the
+// near field, then the target's interpolation pieces (when part is not null), into y
+constexpr int kNearChunk = 1024, kNearTargets = 32;
+template <typename R>
+void launch_near_box(const int2* items, int nitems, const int* leaf_start, const int* leaf_count, const int* near_src_off,
+                     const int* near_src, const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
+                     const int* ip_ptr, const V2<R>* part, int N, const long long* sorting, double2* y, cudaStream_t s);
+// the interpolation plan box-transposed (term j of box target t at the box's first entry + j n + t)
+template <typename R>
+void launch_interp_transpose(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* ip_ptr,
+                             const InterpE<double>* in, InterpE<R>* out, cudaStream_t s);
 void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s);
 // Load the direct map's kernels (singular correction, FP64 intensities, both far-sum shapes) into
 // the current device's context now.  Under lazy module loading a kernel is otherwise loaded,

@@ -376,9 +376,141 @@ __global__ void __launch_bounds__(256) k_propagate_st(int pbegin, int pend, cons
     }
 }
 
+// one warp per (leaf box, up to 32 of its targets, kIbPiece of their interpolation terms), one
+// lane per target.  The targets of a leaf box share their ancestors, hence the same cousin lists
+// in the same order: their j-th terms read the same cousin box, mostly the same cone (2.5-3
+// distinct cones per warp step on the kite trees, against up to 32 when a warp walks one target's
+// terms), so the coefficient gathers are broadcasts.  The plan is stored box-transposed (term j of
+// the box's target t at box base + j n + t) for coalesced entry loads.  Each lane writes its
+// piece's sum to part[piece][target]; k_final_t adds the pieces in order.
+template <typename R, int PS, int PA>
+__global__ void __launch_bounds__(256) k_interp_box(const int4* __restrict__ items, int nitems, int N,
+                                                    const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
+                                                    const int* __restrict__ ip_ptr, const InterpE<R>* __restrict__ ipT,
+                                                    const V2<R>* __restrict__ coef, V2<R>* __restrict__ part) {
+    constexpr int P = PS * PA;
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (w >= nitems) return;
+    const int lane = threadIdx.x & 31;
+    const int4 I = items[w];   // leaf box, first target, terms [z, w)
+    const int s = leaf_start[I.x], n = leaf_count[I.x];
+    const int t = I.y + lane;
+    if (t >= n) return;
+    const InterpE<R>* e = ipT + ip_ptr[s] + t;
+    V2<R> acc; acc.x = R(0); acc.y = R(0);
+    int j = I.z;
+    if constexpr (sizeof(R) == 4) {   // two terms' loads in flight before either is evaluated
+        for (; j + 1 < I.w; j += 2) {
+            const InterpE<R> E0 = e[(long long)j * n], E1 = e[(long long)(j + 1) * n];
+            V2<R> c0[P], c1[P];
+            const V2<R>* b0 = coef + (long long)E0.cone * P;
+            const V2<R>* b1 = coef + (long long)E1.cone * P;
+#pragma unroll
+            for (int q = 0; q < P; ++q) { c0[q] = b0[q]; c1[q] = b1[q]; }
+            V2<R> f; f.x = E0.fr; f.y = E0.fi;
+            cmac<R>(acc, interp_eval<R, PS, PA>(c0, E0.s, E0.th), f);
+            f.x = E1.fr; f.y = E1.fi;
+            cmac<R>(acc, interp_eval<R, PS, PA>(c1, E1.s, E1.th), f);
+        }
+    }
+    for (; j < I.w; ++j) {
+        const InterpE<R> E = e[(long long)j * n];
+        V2<R> c[P];
+        const V2<R>* cb = coef + (long long)E.cone * P;
+#pragma unroll
+        for (int q = 0; q < P; ++q) c[q] = cb[q];
+        V2<R> f; f.x = E.fr; f.y = E.fi;
+        cmac<R>(acc, interp_eval<R, PS, PA>(c, E.s, E.th), f);
+    }
+    part[(long long)(I.z / kIbPiece) * N + s + t] = acc;
+}
+
+// near field by leaf box: one block per (leaf box, up to 32 of its targets).  The box's
+// neighbour densities rho[src[e]] are staged in shared memory kNearChunk at a time, once for all
+// its targets, and each warp streams its targets' table rows (coalesced) against them; a target's
+// chunk sums meet in shared memory in chunk order.  Then the target's interpolation pieces
+// (k_interp_box) are added in order and the sum goes to y at the target's original index.
+template <typename R>
+__global__ void __launch_bounds__(256) k_near_box(const int2* __restrict__ items, const int* __restrict__ leaf_start,
+                                                  const int* __restrict__ leaf_count, const int* __restrict__ near_src_off,
+                                                  const int* __restrict__ near_src, const int* __restrict__ near_rowlen,
+                                                  const long long* __restrict__ near_off, const V2<R>* __restrict__ near,
+                                                  const V2<R>* __restrict__ rho, const int* __restrict__ ip_ptr,
+                                                  const V2<R>* __restrict__ part, int N, const long long* __restrict__ sorting,
+                                                  double2* __restrict__ y) {
+    static_assert(kNearTargets == 4 * 8, "eight warps of four targets");
+    __shared__ V2<R> srho[kNearChunk];
+    __shared__ V2<R> sacc[kNearTargets];
+    const int2 I = items[blockIdx.x];   // leaf box, first target
+    const int b = I.x, s = leaf_start[b], n = min(kNearTargets, leaf_count[b] - I.y);
+    const int rl = near_rowlen[b];
+    const int* src = near_src + near_src_off[b];
+    const V2<R>* rows = near + near_off[b] + (long long)I.y * rl;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < kNearTargets) { sacc[threadIdx.x].x = R(0); sacc[threadIdx.x].y = R(0); }
+    for (int c0 = 0; c0 < rl; c0 += kNearChunk) {
+        const int cn = min(kNearChunk, rl - c0);
+        __syncthreads();   // the previous chunk has been read
+        for (int e = threadIdx.x; e < cn; e += blockDim.x) srho[e] = rho[src[c0 + e]];
+        __syncthreads();
+        // warp w: targets 4 w .. 4 w + 3 together (four independent row loads per density read)
+        const int t0 = 4 * warp;
+        if (t0 < n) {
+            V2<R> acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { acc[u].x = R(0); acc[u].y = R(0); }
+            const V2<R>* row = rows + (long long)t0 * rl + c0;
+#pragma unroll 2
+            for (int e = lane; e < cn; e += 32) {
+                const V2<R> r = srho[e];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (t0 + u < n) cmac<R>(acc[u], row[(long long)u * rl + e], r);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const R ax = warp_sum_r<R>(acc[u].x), ay = warp_sum_r<R>(acc[u].y);
+                if (lane == 0 && t0 + u < n) { sacc[t0 + u].x += ax; sacc[t0 + u].y += ay; }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        const int i = s + I.y + threadIdx.x;
+        V2<R> acc = sacc[threadIdx.x];
+        if (part) {
+            const int npc = (ip_ptr[i + 1] - ip_ptr[i] + kIbPiece - 1) / kIbPiece;
+            for (int q = 0; q < npc; ++q) { const V2<R> a = part[(long long)q * N + i]; acc.x += a.x; acc.y += a.y; }
+        }
+        const long long o = sorting[i];
+        double2 v = y[o];
+        v.x += (double)acc.x; v.y += (double)acc.y;
+        y[o] = v;
+    }
+}
+
+// the interpolation plan of each leaf box transposed: term j of the box's target t moves from
+// ip_ptr[i] + j to ip_ptr[box's first target] + j n + t (every target of a box has as many terms)
+template <typename R>
+__global__ void k_interp_transpose(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
+                                   const int* __restrict__ leaf_count, const int* __restrict__ ip_ptr,
+                                   const InterpE<double>* __restrict__ in, InterpE<R>* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int b = point_leaf[i], s = leaf_start[b], n = leaf_count[b], t = i - s;
+    const int base = ip_ptr[s], nt = ip_ptr[i + 1] - ip_ptr[i];
+    for (int j = 0; j < nt; ++j) {
+        const InterpE<double> E = in[ip_ptr[i] + j];
+        InterpE<R> o{};
+        o.cone = E.cone; o.s = (R)E.s; o.th = (R)E.th; o.fr = (R)E.fr; o.fi = (R)E.fi;
+        out[base + (long long)j * n + t] = o;
+    }
+}
+
 // one warp per Morton-sorted target; near row layout [target][neighbour sources], and
 // near_src[near_src_off[b] + e] the Morton index of entry e's source in leaf box b's rows, so the
-// lanes stride over one flat row with independent loads
+// lanes stride over one flat row with independent loads.  With `part`, the interpolation terms were
+// summed by k_interp_box: the target's pieces are added in order instead.
 template <typename R, int PS, int PA>
 __global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ point_leaf, const int* __restrict__ leaf_start,
                                                  const int* __restrict__ near_src_off, const int* __restrict__ near_src,
@@ -386,7 +518,8 @@ __global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ 
                                                  const long long* __restrict__ near_off, const V2<R>* __restrict__ near,
                                                  const V2<R>* __restrict__ rho, const int* __restrict__ ip_ptr,
                                                  const InterpE<R>* __restrict__ ip, const V2<R>* __restrict__ coef,
-                                                 const long long* __restrict__ sorting, double2* __restrict__ y) {
+                                                 const long long* __restrict__ sorting, double2* __restrict__ y,
+                                                 const V2<R>* __restrict__ part) {
     constexpr int P = PS * PA;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -399,15 +532,21 @@ __global__ void __launch_bounds__(256) k_final_t(int N, const int* __restrict__ 
     V2<R> acc; acc.x = R(0); acc.y = R(0);
 #pragma unroll 4
     for (int e = lane; e < rl; e += 32) cmac<R>(acc, row[e], rho[src[e]]);
-    for (int e = ip_ptr[i] + lane; e < ip_ptr[i + 1]; e += 32) {
-        const InterpE<R> E = ip[e];
-        const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.cone * P, E.s, E.th);
-        V2<R> f; f.x = E.fr; f.y = E.fi;
-        cmac<R>(acc, it, f);
+    if (!part) {
+        for (int e = ip_ptr[i] + lane; e < ip_ptr[i + 1]; e += 32) {
+            const InterpE<R> E = ip[e];
+            const V2<R> it = interp_eval<R, PS, PA>(coef + (long long)E.cone * P, E.s, E.th);
+            V2<R> f; f.x = E.fr; f.y = E.fi;
+            cmac<R>(acc, it, f);
+        }
     }
     acc.x = warp_sum_r<R>(acc.x);
     acc.y = warp_sum_r<R>(acc.y);
     if (lane == 0) {
+        if (part) {
+            const int npc = (ip_ptr[i + 1] - ip_ptr[i] + kIbPiece - 1) / kIbPiece;
+            for (int q = 0; q < npc; ++q) { const V2<R> a = part[(long long)q * N + i]; acc.x += a.x; acc.y += a.y; }
+        }
         const long long o = sorting[i];
         double2 v = y[o];
         v.x += (double)acc.x; v.y += (double)acc.y;
@@ -490,10 +629,30 @@ template <typename R>
 void launch_final_t(int N, const int* point_leaf, const int* leaf_start, const int* near_src_off, const int* near_src,
                     const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
                     const int* ip_ptr, const InterpE<R>* ip, const V2<R>* coef, int Ps, int Pang, const long long* sorting,
-                    double2* y, cudaStream_t s) {
+                    double2* y, cudaStream_t s, const V2<R>* part) {
     IFGF_DISPATCH_P(Ps, Pang, (k_final_t<R, PS, PA><<<nblk_a((long long)N * 32, 256), 256, 0, s>>>(
                                    N, point_leaf, leaf_start, near_src_off, near_src, near_rowlen, near_off, near, rho,
-                                   ip_ptr, ip, coef, sorting, y)));
+                                   ip_ptr, ip, coef, sorting, y, part)));
+}
+template <typename R>
+void launch_interp_box(const int4* items, int nitems, int N, const int* leaf_start, const int* leaf_count, const int* ip_ptr,
+                       const InterpE<R>* ipT, const V2<R>* coef, int Ps, int Pang, V2<R>* part, cudaStream_t s) {
+    if (nitems <= 0) return;
+    IFGF_DISPATCH_P(Ps, Pang, (k_interp_box<R, PS, PA><<<nblk_a((long long)nitems * 32, 256), 256, 0, s>>>(
+                                   items, nitems, N, leaf_start, leaf_count, ip_ptr, ipT, coef, part)));
+}
+template <typename R>
+void launch_near_box(const int2* items, int nitems, const int* leaf_start, const int* leaf_count, const int* near_src_off,
+                     const int* near_src, const int* near_rowlen, const long long* near_off, const V2<R>* near, const V2<R>* rho,
+                     const int* ip_ptr, const V2<R>* part, int N, const long long* sorting, double2* y, cudaStream_t s) {
+    if (nitems > 0)
+        k_near_box<R><<<nitems, 256, 0, s>>>(items, leaf_start, leaf_count, near_src_off, near_src, near_rowlen, near_off, near,
+                                              rho, ip_ptr, part, N, sorting, y);
+}
+template <typename R>
+void launch_interp_transpose(int N, const int* point_leaf, const int* leaf_start, const int* leaf_count, const int* ip_ptr,
+                             const InterpE<double>* in, InterpE<R>* out, cudaStream_t s) {
+    if (N > 0) k_interp_transpose<R><<<nblk_a(N, 256), 256, 0, s>>>(N, point_leaf, leaf_start, leaf_count, ip_ptr, in, out);
 }
 void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
     if (n > 0) k_d2f<<<nblk_a(n, 256), 256, 0, s>>>(a, n, b);
@@ -507,7 +666,14 @@ void launch_d2f(const double2* a, long long n, float2* b, cudaStream_t s) {
                                         V2<R>*, cudaStream_t, int);                                                    \
     template void launch_final_t<R>(int, const int*, const int*, const int*, const int*, const int*,                   \
                                     const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,       \
-                                    const V2<R>*, int, int, const long long*, double2*, cudaStream_t);
+                                    const V2<R>*, int, int, const long long*, double2*, cudaStream_t, const V2<R>*);      \
+    template void launch_interp_box<R>(const int4*, int, int, const int*, const int*, const int*, const InterpE<R>*,     \
+                                       const V2<R>*, int, int, V2<R>*, cudaStream_t);                                    \
+    template void launch_interp_transpose<R>(int, const int*, const int*, const int*, const int*,                        \
+                                             const InterpE<double>*, InterpE<R>*, cudaStream_t);                          \
+    template void launch_near_box<R>(const int2*, int, const int*, const int*, const int*, const int*, const int*,       \
+                                     const long long*, const V2<R>*, const V2<R>*, const int*, const V2<R>*, int,        \
+                                     const long long*, double2*, cudaStream_t);
 IFGF_INSTANTIATE(double)
 IFGF_INSTANTIATE(float)
 

@@ -240,19 +240,24 @@ int ifgf2d_apply_timed(ifgf2d_ctx* ctx, const void* d_x, void* d_y, int mode, do
 
 /* Launch-shape autotuner (no counterpart in the reference): times every launch shape of the
  * leaf-cone kernel (source chunks per coefficient 1, 2, 5, 10; complex64 also 0, the table
- * streamed through shared memory by TMA bulk copies) and of each level's propagation
- * (2, 4 or the most cones per block) on this context's own tables, in both precisions, and
+ * streamed through shared memory by TMA bulk copies), of each level's propagation (2, 4 or the
+ * most cones per block, or 1: child blocks staged in shared memory) and of the single-vector
+ * interpolation (by target or by leaf box) on this context's own tables, in both precisions, and
  * keeps the fastest.  The table has ifgf2d_tuning_size() ints: leaf FP64, leaf complex64, then
  * per precision one propagation entry per level (0 = the most cones per block), then a bit
- * mask of the batched complex64 kernels that run in 3xTF32 on the tcgen05 tensor cores
- * (IFGF2D_BATCH_TC_*; FP32 FMA otherwise) and of the other batched kernel choices below;
- * the default is IFGF2D_BATCH_TC_LEAF | IFGF2D_BATCH_GROUPED_INTERP.  get / set read and restore
- * it (e.g. from an on-disk cache); applies use the context's current table. */
+ * mask of kernel choices: the batched complex64 kernels that run in 3xTF32 on the tcgen05
+ * tensor cores (IFGF2D_BATCH_TC_*; FP32 FMA otherwise), the other batched choices and the
+ * single-vector interpolation by leaf box (IFGF2D_SINGLE_INTERP_BY_BOX_*); the default is
+ * IFGF2D_BATCH_TC_LEAF | IFGF2D_BATCH_GROUPED_INTERP | IFGF2D_SINGLE_INTERP_BY_BOX_C64.
+ * get / set read and restore it (e.g. from an on-disk cache); applies use the context's
+ * current table. */
 #define IFGF2D_BATCH_TC_LEAF 1          /* leaf-cone sums, 3xTF32 (two TF32 terms per operand) */
 #define IFGF2D_BATCH_TC_PROPAGATION 2   /* propagation, 3xTF32 */
 #define IFGF2D_BATCH_TC_LEAF_FP32 4     /* leaf-cone sums, three TF32 terms per operand (6 products) */
 #define IFGF2D_BATCH_BULK_PROPAGATION 8 /* FP32 FMA propagation, child coefficients staged by TMA bulk copies */
 #define IFGF2D_BATCH_GROUPED_INTERP 16  /* complex64 interpolation grouped by cone per leaf box */
+#define IFGF2D_SINGLE_INTERP_BY_BOX_FP64 32  /* single vector, FP64: interpolation by leaf box, a lane per target */
+#define IFGF2D_SINGLE_INTERP_BY_BOX_C64 64   /* single vector, complex64: the same */
 int ifgf2d_tuning_size(void);
 int ifgf2d_autotune(ifgf2d_ctx* ctx, int reps, int* choices);
 int ifgf2d_get_tuning(const ifgf2d_ctx* ctx, int* choices);

@@ -400,6 +400,14 @@ def test_gpu_autotune_keeps_results_and_caches(lib, oracle, tmp_path):
         assert L.ifgf2d_set_tuning(fm.handle, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
         assert rel(fm.compute_Ax_acc(d), y64) < 1e-14
         assert rel(fm.compute_Ax_acc(d, mixed=True), y32) < 1e-6
+    # the interpolation by leaf box (a lane per target, pieces summed in order) against by target
+    c = np.asarray(fm.get_tuning()).copy()
+    for bits in (0, fm.SINGLE_INTERP_BY_BOX_FP64, fm.SINGLE_INTERP_BY_BOX_C64,
+                 fm.SINGLE_INTERP_BY_BOX_FP64 | fm.SINGLE_INTERP_BY_BOX_C64):
+        c[-1] = (int(c[-1]) & ~(fm.SINGLE_INTERP_BY_BOX_FP64 | fm.SINGLE_INTERP_BY_BOX_C64)) | bits
+        fm.set_tuning(c)
+        assert rel(fm.compute_Ax_acc(d), y64) < 1e-14
+        assert rel(fm.compute_Ax_acc(d, mixed=True), y32) < 1e-6
     # the staged propagation does the arithmetic of the default one in the same order
     c = np.asarray(fm.get_tuning()).copy()
     c[2:-1] = 0
