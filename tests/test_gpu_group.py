@@ -75,3 +75,20 @@ def test_gpu_grouped_driver_matches_one_at_a_time(lib):
     for a, b, o, r in zip(xg, xr, obs, ref):
         assert abs(o.result["iters"] - r.result["iters"]) <= 1
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-6
+
+
+def test_gpu_group_of_one_equals_its_member(lib, oracle):
+    """The degenerate group: one member's merged tables give that member's own apply and solve."""
+    k = 150.0
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=128, formulation="combined")
+    fm.prepare(k, 0)
+    g = lib.Group([fm])
+    assert g.N == fm.total_num_unknowns_ and list(g.offsets) == [0, g.N]
+    x = oracle.seeded_density(g.N)
+    fm.precomps_and_setup(k, 0)
+    assert rel(g.apply(x), fm.compute_Ax_acc(x)) < 1e-13
+    rhs = -np.exp(1j * k * fm.xs_)
+    xg = g.solve(rhs, tol=1e-8, restart=300, max_iters=500)
+    xm = fm.gmres(rhs, tol=1e-8, restart=300, max_iters=500)
+    assert g.last_solve["converged"] and abs(g.last_solve["iters"][0] - fm.last_solve["iters"]) <= 1
+    assert rel(xg, xm) < 1e-6

@@ -147,3 +147,31 @@ def test_prepare_tree_equals_oracle_at_full_size(lib, oracle, k, patches):
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=64)
     assert L.ifgf2d_prepare(fm.handle, k, 2) == 4          # IFGF2D_ERR_NLEVELS, BoxTree.h:1117
     assert L.ifgf2d_prepare(fm.handle, -1.0, 0) == 1
+
+
+def test_group_create_checks_its_members_before_any_gpu_work(lib):
+    """ifgf2d_group_create rejects a NULL or empty member list, an unprepared member and members
+    of different Np / Ps / Pang / formulation with a status and a message, before it touches the
+    GPU, and the half-built group is destroyed cleanly."""
+    L = lib._lib.load()
+    h = ctypes.c_void_p()
+    assert L.ifgf2d_group_create(None, 1, ctypes.byref(h)) == 1
+    arr = (ctypes.c_void_p * 1)()
+    assert L.ifgf2d_group_create(arr, 0, ctypes.byref(h)) == 1
+    assert L.ifgf2d_group_create(arr, 1025, ctypes.byref(h)) == 1
+    with pytest.raises(ValueError):
+        lib.Group([])
+    kite = lambda k, **kw: lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, **{"Np": 16, "patches_per_curve": 128,
+                                                                           "formulation": "combined", **kw})
+    a, b = kite(100.0), kite(150.0)
+    with pytest.raises(lib.IFGF2DError, match="prepared"):
+        lib.Group([a, b])                       # neither member prepared
+    a.prepare(100.0, 0)
+    c = kite(150.0, Np=10)
+    c.prepare(150.0, 0)
+    with pytest.raises(ValueError, match="Np"):
+        lib.Group([a, c])                       # different Np
+    d = kite(150.0, formulation="single_layer")
+    d.prepare(150.0, 0)
+    with pytest.raises(ValueError, match="formulation"):
+        lib.Group([a, d])                       # different formulation
