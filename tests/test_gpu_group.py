@@ -88,7 +88,7 @@ def test_gpu_group_of_one_equals_its_member(lib, oracle):
     fm.precomps_and_setup(k, 0)
     assert rel(g.apply(x), fm.compute_Ax_acc(x)) < 1e-13
     rhs = -np.exp(1j * k * fm.xs_)
-    xg = g.solve(rhs, tol=1e-8, restart=300, max_iters=500)
+    xg = g.solve(rhs, tol=1e-8, restart=300, max_iters=500, mixed=False)
     xm = fm.gmres(rhs, tol=1e-8, restart=300, max_iters=500)
     assert g.last_solve["converged"] and abs(g.last_solve["iters"][0] - fm.last_solve["iters"]) <= 1
     assert rel(xg, xm) < 1e-6
