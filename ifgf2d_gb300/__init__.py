@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED
+from ._lib import APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED, PRECOND_NET, PRECOND_SPECTRAL
 
 __all__ = ["ForwardMap", "LinearOperator", "Circle", "Kite", "Line", "Star", "Junction", "hankel1", "Group",
            "IFGF2DError", "NeighbourhoodError", "NoConvergence", "load_library"]
@@ -512,6 +512,49 @@ class ForwardMap:
         rc = _lib.load().ifgf2d_solve_precond(self._h, net.handle, _dp(b.view(np.float64)), _dp(x.view(np.float64)), mode,
                                               float(tol), int(restart), int(max_iters), ctypes.byref(it), ctypes.byref(err))
         self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0))
+        if rc == 8:
+            if raise_on_noconv:
+                raise NoConvergence(f"FGMRES: {it.value} iterations, error {err.value:.3e}")
+        else:
+            _check(rc, self._h)
+        return x
+
+    def spectral_setup(self, scale=None):
+        """Tables of the spectral right preconditioner (combined field, closed curves): the
+        flat-boundary symbol's inverse along each curve, glancing damping eps = scale k^(1/3)
+        (default IFGF2D_SPECTRAL_DEFAULT_SCALE).  After precompute."""
+        _check(_lib.load().ifgf2d_spectral_setup(self._h, 0.0 if scale is None else float(scale)), self._h)
+
+    def spectral_apply(self, r):
+        """z = M r with the spectral preconditioner (host vectors)"""
+        n = self.total_num_unknowns_
+        rin = _cview(r, n)
+        z = np.empty(n, dtype=np.complex128)
+        _check(_lib.load().ifgf2d_spectral_apply(self._h, _dp(rin.view(np.float64)), _dp(z.view(np.float64))), self._h)
+        return z
+
+    def solve_flexible(self, rhs, precond="spectral", net=None, accelerated=True, tol=None, restart=None, max_iters=None,
+                       mixed=False, raise_on_noconv=False):
+        """Flexible GMRES inside FP64 iterative refinement with a right preconditioner:
+        ``precond`` "spectral", "net" (``net`` a learned.PreconditionerNet) or "spectral+net" (the
+        network's correction on top of the spectral preconditioner)."""
+        kinds = {"net": PRECOND_NET, "spectral": PRECOND_SPECTRAL, "spectral+net": PRECOND_NET | PRECOND_SPECTRAL}
+        if precond not in kinds:
+            raise ValueError(f"precond must be one of {sorted(kinds)}")
+        n = self.total_num_unknowns_
+        b = _cview(rhs, n)
+        x = np.empty(n, dtype=np.complex128)
+        it = ctypes.c_int(0)
+        err = ctypes.c_double(0.0)
+        tol = self.GMRES_TOLERANCE_ if tol is None else tol
+        restart = self.GMRES_MAX_ITER_ if restart is None else restart
+        max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
+        mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
+        rc = _lib.load().ifgf2d_solve_flexible(self._h, net.handle if net is not None else None, kinds[precond],
+                                               _dp(b.view(np.float64)), _dp(x.view(np.float64)), mode, float(tol), int(restart),
+                                               int(max_iters), ctypes.byref(it), ctypes.byref(err))
+        self.last_solve = dict(iters=it.value, error=err.value, converged=(rc == 0),
+                               refinements=int(_lib.load().ifgf2d_last_refinements(self._h)))
         if rc == 8:
             if raise_on_noconv:
                 raise NoConvergence(f"FGMRES: {it.value} iterations, error {err.value:.3e}")

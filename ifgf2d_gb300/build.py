@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libifgf2d.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["geometry.cpp", "tree.cpp", "ifgf2d_kernels.cu", "ifgf_apply.cu", "ifgf_batch.cu", "rp_precompute.cu", "ifgf2d_capi.cu",
-           "batch.cu", "batch_tcgen05.cu", "offsurface.cu", "precond_net.cu", "precond_capi.cu", "noalloc.cu", "gmres_device.cu", "plan_device.cu", "geometry_device.cu", "group.cu"]
+           "batch.cu", "batch_tcgen05.cu", "offsurface.cu", "precond_net.cu", "precond_capi.cu", "noalloc.cu", "gmres_device.cu", "plan_device.cu", "geometry_device.cu", "group.cu", "spectral_precond.cu"]
 # translation units whose arithmetic must round like the host restatement (no FMA contraction)
 NO_FMAD = {"rp_precompute.cu", "plan_device.cu", "geometry_device.cu"}
 

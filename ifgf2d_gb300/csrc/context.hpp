@@ -19,6 +19,7 @@
 
 struct BatchWork;
 struct EvalWork;
+struct SpectralWork;
 constexpr int kTuneLevels = 24;   // levels covered by the launch-shape table
 constexpr int kBatchTcLeaf = 1;   // leaf-cone sums (k_leaf_t5)
 constexpr int kBatchTcProp = 2;   // propagation (k_prop_t5)
@@ -109,7 +110,7 @@ struct GmresWork {
     long long sn = 0;
     // flexible GMRES with the learned preconditioner: z_j = M(v_j) for every column, and the
     // preconditioner's output buffer the captured iteration writes before copying it into Z
-    DBuf<double2> Z, zt;
+    DBuf<double2> Z, zt, zt2;   // zt2: the network's output when it corrects the spectral preconditioner
     DBuf<double> nrm2;
     DBuf<int> jdev;
     // least squares on the device (LsqDev): rotated columns, rotated right-hand side, rotations,
@@ -119,7 +120,8 @@ struct GmresWork {
     DBuf<int> lsst;
     long long n = 0;
     int m = 0;
-    cudaGraphExec_t exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // mode x (plain, preconditioned)
+    // mode x preconditioner (none, network, spectral, spectral corrected by the network)
+    cudaGraphExec_t exec[12] = {};
     cudaGraphExec_t apply_exec[3] = {nullptr, nullptr, nullptr};   // per mode: one apply, vin -> vout
     void drop_graphs() {
         for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
@@ -205,6 +207,7 @@ struct ifgf2d_ctx {
     std::unique_ptr<GmresWork> gw;
     BatchWork* bw = nullptr;        // batched apply / solve workspace (batch.cu), freed by destroy
     EvalWork* ew = nullptr;         // off-surface evaluation plan (offsurface.cu), freed by destroy
+    SpectralWork* sw = nullptr;     // spectral right preconditioner (spectral_precond.cu), freed by destroy and precompute
     long long counts[8] = {0};
     int last_passes = 0;            // FP64 refinement passes of the last mixed solve (batched: of the batch)
     int nsm = 0;                    // SMs of the context's device
@@ -265,6 +268,14 @@ int apply_single(ifgf2d_ctx* ctx, const double2* x, double2* y, int mode);
 void free_batch(ifgf2d_ctx* ctx);
 // off-surface evaluation plan release (offsurface.cu)
 void free_eval(ifgf2d_ctx* ctx);
+// the spectral right preconditioner (spectral_precond.cu): set-up of its tables for the context's
+// k and coupling, with glancing damping eps = scale k^(1/3); release; z = M r queued on s
+// (capturable: the tables stay fixed until the next set-up)
+int spectral_setup(ifgf2d_ctx* ctx, double scale);
+void free_spectral(ifgf2d_ctx* ctx);
+void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s);
+// z += zn - 2 r (the learned network's output zn correcting the spectral preconditioner's z)
+void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s);
 // the learned preconditioner on one curve of N points (precond_capi.cu): prepare lays the
 // network out for N points with the curve's geometry (host call, synchronous, not capturable);
 // launch queues z = M(r) on stream s (capturable; the buffers stay fixed until the next prepare)

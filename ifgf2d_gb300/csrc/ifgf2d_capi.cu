@@ -161,6 +161,7 @@ extern "C" int ifgf2d_destroy(ifgf2d_ctx* ctx) {
         AllocStream guard(s);
         free_batch(ctx);
         free_eval(ctx);
+        free_spectral(ctx);
         delete ctx;   // buffers allocated on s are freed on s, before s goes
     }
     if (s) cudaStreamDestroy(s);
@@ -226,6 +227,7 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     if (ctx->gw) ctx->gw->drop_graphs();
     free_batch(ctx);
     free_eval(ctx);
+    free_spectral(ctx);
     ctx->counts[6] = (long long)ncols * D.Np;
     return IFGF2D_OK;
 }
@@ -843,8 +845,17 @@ extern "C" int ifgf2d_propagate(ifgf2d_ctx* ctx, long long m, const double* xp, 
 // triangular system, x += V y, and the host reads the cycle's state (a few bytes) once.  Stops
 // when |g_{j+1}| / ||r0|| < tol (the first ||r0||, opGMRES.hpp:207) or after max_iters
 // iterations.
+// The right preconditioner of a flexible GMRES: the learned network, the spectral preconditioner
+// (spectral_precond.cu), or the spectral one corrected by the network (z = M_s r + N(r) - 2 r:
+// the network trained on the spectral preconditioner's errors)
+struct RightPrecond {
+    ifgf2d_net* net = nullptr;
+    SpectralWork* spec = nullptr;
+    int kind() const { return (net ? 1 : 0) | (spec ? 2 : 0); }
+};
+
 static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, double tol, int restart,
-                      int max_iters, int& iters, double& est, ifgf2d_net* net = nullptr) {
+                      int max_iters, int& iters, double& est, const RightPrecond* P = nullptr) {
     const long long N = ctx->D.N;
     const int m = restart, ldh = m + 1;
     cudaStream_t s = ctx->stream;
@@ -857,12 +868,14 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         CK(G.part.alloc((size_t)arnoldi_part_size(N, m)));
         CK(G.lsR.alloc((size_t)ldh * m)); CK(G.lsg.alloc(m + 1)); CK(G.lsgc.alloc(m)); CK(G.lsgs.alloc(m));
         CK(G.lsst.alloc(4)); CK(G.lssc.alloc(3));
-        G.Z.release(); G.zt.release();
+        G.Z.release(); G.zt.release(); G.zt2.release();
         G.n = N; G.m = m;
     }
-    if (net && !G.Z.p) { CK(G.Z.alloc((size_t)N * m)); CK(G.zt.alloc(N)); }
+    const int pk = P ? P->kind() : 0;
+    if (pk && !G.Z.p) { CK(G.Z.alloc((size_t)N * m)); CK(G.zt.alloc(N)); }
+    if (pk == 3 && !G.zt2.p) CK(G.zt2.alloc(N));
     const LsqDev L{G.lsR.p, G.lsg.p, G.lsgc.p, G.lsgs.p, G.lsst.p, G.lssc.p, m};
-    const int gi = mode + (net ? 3 : 0);
+    const int gi = mode + 3 * pk;
     if (!G.exec[gi]) {
         cudaGraph_t graph;
         CK(cudaGraphCreate(&graph, 0));
@@ -883,9 +896,17 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         }
         launch_copy_col(G.V.p, N, G.jdev.p, G.vin.p, G.nrm2.p, s);
         int rc;
-        if (net) {
+        if (pk) {
             // flexible GMRES: z_j = M(v_j) into Z[:, j], then w = A z_j
-            net_precondition_launch(net, G.vin.p, G.zt.p, s);
+            if (pk == 1) {
+                net_precondition_launch(P->net, G.vin.p, G.zt.p, s);
+            } else {
+                spectral_launch(P->spec, G.vin.p, G.zt.p, ctx->D.Np, s);
+                if (pk == 3) {
+                    net_precondition_launch(P->net, G.vin.p, G.zt2.p, s);
+                    launch_precond_sum(G.zt.p, G.zt2.p, G.vin.p, N, s);   // zt += zt2 - 2 v
+                }
+            }
             launch_store_col(G.zt.p, N, G.jdev.p, G.Z.p, s);
             rc = apply_dev(ctx, G.zt.p, G.w.p, mode);
         } else {
@@ -941,7 +962,7 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         launch_lsq_init(L, G.jdev.p, beta, r0n, tol, (int)std::min<long long>(limit, 1 << 30), s);
         CK(cudaGraphLaunch(G.exec[gi], s));
         launch_lsq_solve(L, ldh, G.y.p, s);
-        launch_multi_axpy_dyn(net ? G.Z.p : V, N, G.lsst.p + 1, G.y.p, N, x, s);   // x += V y, or Z y (flexible)
+        launch_multi_axpy_dyn(pk ? G.Z.p : V, N, G.lsst.p + 1, G.y.p, N, x, s);   // x += V y, or Z y (flexible)
         CK(cudaMemcpyAsync(rb_est, G.lssc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(rb_st, G.lsst.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -1031,15 +1052,13 @@ extern "C" int ifgf2d_solve(ifgf2d_ctx* ctx, const double* rhs, double* xout, in
     return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
 }
 
-// ------------------------------------------------------------------ learned right preconditioner
-// Flexible GMRES with z_j = M(v_j) from the network, inside FP64 iterative refinement: the
-// residual b - A x with the FP64 operator (the stop test), corrections from flexible GMRES on
-// the operator of `mode`.  A preconditioned correction that misses its tolerance (a stall)
-// switches the rest of the solve to plain GMRES.
-extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* xout, int mode, double tol,
-                                    int restart, int max_iters, int* iters_out, double* err_out) {
-    if (!ctx || !net || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
-    AllocStream guard(ctx->stream);
+// ------------------------------------------------------------------ right preconditioners
+// Flexible GMRES with z_j = M(v_j) (the network, the spectral preconditioner or both) inside FP64
+// iterative refinement: the residual b - A x with the FP64 operator (the stop test), corrections
+// from flexible GMRES on the operator of `mode`.  A preconditioned correction that misses its
+// tolerance (a stall) switches the rest of the solve to plain GMRES.
+static int solve_flexible(ifgf2d_ctx* ctx, RightPrecond P, const double* rhs, double* xout, int mode, double tol, int restart,
+                          int max_iters, int* iters_out, double* err_out) {
     if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before solve");
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_DIRECT && mode != IFGF2D_APPLY_IFGF_MIXED)
         return fail(ctx, IFGF2D_ERR_ARG, "unknown solve mode");
@@ -1048,20 +1067,21 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
     const long long N = D.N;
     if (!all_finite(rhs, 2 * N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the right-hand side");
     cudaStream_t s = ctx->stream;
-    {
+    if (!ctx->gw) ctx->gw.reset(new GmresWork);
+    GmresWork& GW = *ctx->gw;
+    if (P.net) {
         std::vector<double> geom((size_t)N * 4);
         for (long long i = 0; i < N; ++i) {
             geom[4 * i] = D.kappa[i]; geom[4 * i + 1] = -D.ny[i]; geom[4 * i + 2] = D.nx[i]; geom[4 * i + 3] = D.wq[i];
         }
         CK(cudaStreamSynchronize(s));
         std::string msg;
-        int rc = net_prepare_single(net, N, geom.data(), ctx->k, msg);
+        int rc = net_prepare_single(P.net, N, geom.data(), ctx->k, msg);
         if (rc != IFGF2D_OK) return fail(ctx, rc, msg);
+        // the network's buffers may have moved since the last capture: recapture its iterations
+        for (int q = 3; q < 12; ++q)
+            if (((q / 3) & 1) && GW.exec[q]) { cudaGraphExecDestroy(GW.exec[q]); GW.exec[q] = nullptr; }
     }
-    if (!ctx->gw) ctx->gw.reset(new GmresWork);
-    GmresWork& GW = *ctx->gw;
-    // the network's buffers may have moved since the last capture: recapture the flexible iterations
-    for (int q = 3; q < 6; ++q) if (GW.exec[q]) { cudaGraphExecDestroy(GW.exec[q]); GW.exec[q] = nullptr; }
     if (GW.sn != N) {
         CK(GW.sb.alloc(N)); CK(GW.sx.alloc(N)); CK(GW.sr.alloc(N)); CK(GW.sd.alloc(N)); CK(GW.st.alloc(N)); CK(GW.shb.alloc(1));
         GW.sn = N;
@@ -1081,14 +1101,16 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
     double bn; if ((rc = nrm(b, bn))) return rc;
     CK(cudaMemcpyAsync(r, b, sizeof(double2) * N, cudaMemcpyDeviceToDevice, s));
     double rn = bn, est = bn > 0 ? 1.0 : 0.0;
-    bool use_net = true;
+    bool use_p = true;
+    ctx->last_passes = 0;
     for (int outer = 0; outer < 30 && est >= tol && iters < max_iters; ++outer) {
+        ++ctx->last_passes;
         const double want = tol * bn / rn;
         const double inner_tol = mode == IFGF2D_APPLY_IFGF_MIXED ? std::max(2e-7, 0.3 * want) : 0.5 * want;
         int it = 0; double e = 0.0;
-        if ((rc = gmres_core(ctx, r, d, mode, inner_tol, restart, max_iters - iters, it, e, use_net ? net : nullptr))) return rc;
+        if ((rc = gmres_core(ctx, r, d, mode, inner_tol, restart, max_iters - iters, it, e, use_p ? &P : nullptr))) return rc;
         iters += it;
-        if (use_net && e >= inner_tol) use_net = false;   // stalled: plain GMRES from here on
+        if (use_p && e >= inner_tol) use_p = false;   // stalled: plain GMRES from here on
         double2 one = make_double2(1.0, 0.0);
         CK(cudaMemcpyAsync(hb, &one, sizeof(double2), cudaMemcpyHostToDevice, s));
         launch_multi_axpy(d, N, 1, hb, 1.0, N, x, s);   // x += d
@@ -1103,6 +1125,34 @@ extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const doub
     if (err_out) *err_out = est;
     if (int rk = check_kerr(ctx)) return rk;
     return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}
+
+extern "C" int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* xout, int mode, double tol,
+                                    int restart, int max_iters, int* iters_out, double* err_out) {
+    if (!ctx || !net || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
+    RightPrecond P;
+    P.net = net;
+    return solve_flexible(ctx, P, rhs, xout, mode, tol, restart, max_iters, iters_out, err_out);
+}
+
+extern "C" int ifgf2d_solve_flexible(ifgf2d_ctx* ctx, ifgf2d_net* net, int precond, const double* rhs, double* xout, int mode,
+                                     double tol, int restart, int max_iters, int* iters_out, double* err_out) {
+    if (!ctx || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (precond <= 0 || (precond & ~(IFGF2D_PRECOND_NET | IFGF2D_PRECOND_SPECTRAL)))
+        return fail(ctx, IFGF2D_ERR_ARG, "precond: IFGF2D_PRECOND_NET, IFGF2D_PRECOND_SPECTRAL or both");
+    if ((precond & IFGF2D_PRECOND_NET) && !net) return fail(ctx, IFGF2D_ERR_ARG, "IFGF2D_PRECOND_NET needs a network");
+    AllocStream guard(ctx->stream);
+    RightPrecond P;
+    if (precond & IFGF2D_PRECOND_NET) P.net = net;
+    if (precond & IFGF2D_PRECOND_SPECTRAL) {
+        if (!ctx->sw) {
+            const int rc = spectral_setup(ctx, IFGF2D_SPECTRAL_DEFAULT_SCALE);
+            if (rc != IFGF2D_OK) return rc;
+        }
+        P.spec = ctx->sw;
+    }
+    return solve_flexible(ctx, P, rhs, xout, mode, tol, restart, max_iters, iters_out, err_out);
 }
 
 // ------------------------------------------------------------------ Hankel test entry

@@ -1,0 +1,413 @@
+// spectral_precond.cu -- the spectral right preconditioner of the combined-field operator.
+//
+// The reference's GMRES is unpreconditioned (ForwardMap/ForwardMap.tpp:658-697,
+// ForwardMap/opGMRES.hpp:68-269).  This file adds a right preconditioner for the sound-soft
+// combined field A = 1/2 I + K - i eta S on closed curves.  Along a curve, A acts on a wave
+// e^{i xi s} (s arc length) approximately as the flat boundary's symbol
+//
+//     sigma(xi) = 1/2 + eta / (2 sqrt(k_eps^2 - xi^2)),   k_eps = k + i eps,  Im sqrt >= 0,
+//
+// (the single layer's flat symbol is i / (2 sqrt(k^2 - xi^2)) and the flat double layer
+// vanishes); the complex wavenumber smooths the square-root singularity at glancing
+// incidence xi = k (the on-surface radiation condition device of Antoine and Darbas, M2AN
+// 2005), eps = scale k^(1/3).  The preconditioner applies the inverse symbol:
+//
+//     z = M r = 2 r + B F^{-1} [ (1/sigma - 2) F (W r) ].
+//
+// 1/sigma -> 2 at high frequency, so the part that goes through the resampling decays like
+// k / xi and the identity part 2 r stays exact at the nodes.
+//   W  resamples each closed curve's node values onto a uniform arc-length grid of
+//      nu = 2^m >= n points: per grid point the Lagrange interpolant (barycentric form) of the
+//      Np nodes of its patch;
+//   F  is the length-nu discrete Fourier transform, computed in four steps (nu = N1 N2):
+//      FFTs of length N1 down the columns of the N1 x N2 view, a twiddle factor, FFTs of
+//      length N2 along the rows.  The spectrum stays in that transposed order; the multiplier
+//      table is stored in it, so the inverse runs the same steps backwards with no transpose;
+//   B  interpolates back to each node from the 8 uniform grid points around it.
+// Everything runs in FP32 (a preconditioner only has to be a fixed linear map); the solver's
+// vectors stay FP64.  Per application: four launches, O(nu log nu) work, a few hundred KB of
+// traffic at nu = 32768.
+#include "context.hpp"
+#include "host_threads.hpp"
+
+#include <algorithm>
+#include <complex>
+#include <memory>
+
+namespace ifgf {
+
+constexpr int kSpecTile = 4;      // grid columns per block of the column FFTs
+constexpr int kSpecTaps = 8;      // back-interpolation taps
+constexpr int kSpecThreads = 256;
+constexpr int kSpecMinLog = 6;    // smallest grid: 64 points
+constexpr int kSpecMaxLog = 20;   // largest grid: 2^20 points per curve
+
+struct SpecCurve {
+    long long off = 0;            // the curve's points: [off, off + n) of the context (patch-major)
+    int n = 0;
+    int lg = 0, lg1 = 0, lg2 = 0; // nu = 2^lg = N1 N2, N1 = 2^lg1, N2 = 2^lg2
+    double length = 0.0;
+    DBuf<int> fw_base;            // per grid point: first point of its patch
+    DBuf<float> fw_w;             // per grid point: Np Lagrange weights
+    DBuf<int> bk_base;            // per node: first of its kSpecTaps grid points (mod nu)
+    DBuf<float> bk_w;             // per node: kSpecTaps weights
+    DBuf<float2> mult;            // 1/sigma - 2 per frequency, in the transposed order k1 N2 + k2
+    DBuf<float2> twN;             // e^{-2 pi i k1 n2 / nu} at k1 N2 + n2
+    DBuf<float2> tw1, tw2;        // e^{-2 pi i j / N1}, j < N1 / 2; the same for N2
+};
+
+}  // namespace ifgf
+
+struct SpectralWork {
+    std::vector<std::unique_ptr<ifgf::SpecCurve>> curves;
+    DBuf<float2> u;               // the grid values of the largest curve
+    double scale = 0.0, eps_used = 0.0;
+};
+
+namespace ifgf {
+namespace {
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ int brev(int i, int lg) { return lg ? (int)(__brev((unsigned)i) >> (32 - lg)) : 0; }
+
+// radix-2 decimation-in-time FFT, in place, of `cols` interleaved columns of length 2^lg held
+// in bit-reversed order: element i of column c at s[i * cols + c].  tw[j] = e^{-2 pi i j / L};
+// inv: conjugate twiddles (unnormalised inverse).  Ends with a barrier.
+__device__ void fft_shared(float2* s, int lg, int cols, const float2* __restrict__ tw, bool inv) {
+    const int half = 1 << (lg - 1);
+    for (int st = 0; st < lg; ++st) {
+        const int hs = 1 << st;
+        for (int b = threadIdx.x; b < half * cols; b += blockDim.x) {
+            const int c = b % cols, q = b / cols;
+            const int j = q & (hs - 1);
+            const int i0 = ((q >> st) << (st + 1)) + j, i1 = i0 + hs;
+            float2 w = tw[j << (lg - 1 - st)];
+            if (inv) w.y = -w.y;
+            const float2 a = s[i0 * cols + c], t = cmulf(w, s[i1 * cols + c]);
+            s[i0 * cols + c] = make_float2(a.x + t.x, a.y + t.y);
+            s[i1 * cols + c] = make_float2(a.x - t.x, a.y - t.y);
+        }
+        __syncthreads();
+    }
+}
+
+// W r and the column FFTs: grid point g = n1 N2 + n2 takes its patch's Np node values; each
+// block transforms kSpecTile columns n2 over n1, multiplies by the twiddle and writes
+// Y[k1 N2 + n2].
+__global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* __restrict__ r, const int* __restrict__ fw_base,
+                                                                const float* __restrict__ fw_w, int Np, int lg1, int lg2,
+                                                                const float2* __restrict__ tw1, const float2* __restrict__ twN,
+                                                                float2* __restrict__ Y) {
+    extern __shared__ float2 sm[];
+    const int N1 = 1 << lg1, N2 = 1 << lg2;
+    const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
+    for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
+        const int n1 = e / cols, c = e - n1 * cols;
+        const int g = n1 * N2 + c0 + c;
+        const double2* src = r + fw_base[g];
+        const float* w = fw_w + (size_t)g * Np;
+        float re = 0.f, im = 0.f;
+        for (int j = 0; j < Np; ++j) {
+            const double2 v = src[j];
+            re = fmaf(w[j], (float)v.x, re);
+            im = fmaf(w[j], (float)v.y, im);
+        }
+        sm[brev(n1, lg1) * cols + c] = make_float2(re, im);
+    }
+    __syncthreads();
+    fft_shared(sm, lg1, cols, tw1, false);
+    for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
+        const int k1 = e / cols, c = e - k1 * cols;
+        const int o = k1 * N2 + c0 + c;
+        Y[o] = cmulf(sm[k1 * cols + c], twN[o]);
+    }
+}
+
+// per row k1: the row FFT, the multiplier, the inverse row FFT and the inverse twiddle, in place
+__global__ void __launch_bounds__(kSpecThreads) k_spec_rows(float2* __restrict__ Y, const float2* __restrict__ mult, int lg2,
+                                                            const float2* __restrict__ tw2, const float2* __restrict__ twN) {
+    extern __shared__ float2 sm[];
+    const int N2 = 1 << lg2;
+    float2* row = Y + (size_t)blockIdx.x * N2;
+    const float2* mrow = mult + (size_t)blockIdx.x * N2;
+    const float2* trow = twN + (size_t)blockIdx.x * N2;
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[brev(i, lg2)] = row[i];
+    __syncthreads();
+    if (lg2 > 0) fft_shared(sm, lg2, 1, tw2, false);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[i] = cmulf(sm[i], mrow[i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) {   // back to bit-reversed order: disjoint swaps
+        const int j = brev(i, lg2);
+        if (i < j) { const float2 t = sm[i]; sm[i] = sm[j]; sm[j] = t; }
+    }
+    __syncthreads();
+    if (lg2 > 0) fft_shared(sm, lg2, 1, tw2, true);
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) {
+        const float2 t = trow[i];
+        row[i] = cmulf(sm[i], make_float2(t.x, -t.y));
+    }
+}
+
+// the inverse column FFTs, scaled by 1/nu: u[n1 N2 + n2] on the uniform grid (U and u may be
+// the same buffer: a block reads all of its columns before it writes them)
+__global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const float2* U, int lg1, int lg2,
+                                                                const float2* __restrict__ tw1, float scale, float2* u) {
+    extern __shared__ float2 sm[];
+    const int N1 = 1 << lg1, N2 = 1 << lg2;
+    const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
+    for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
+        const int k1 = e / cols, c = e - k1 * cols;
+        sm[brev(k1, lg1) * cols + c] = U[k1 * N2 + c0 + c];
+    }
+    __syncthreads();
+    fft_shared(sm, lg1, cols, tw1, true);
+    for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
+        const int n1 = e / cols, c = e - n1 * cols;
+        const float2 v = sm[n1 * cols + c];
+        u[n1 * N2 + c0 + c] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+// z = 2 r + B u on the curve's nodes
+__global__ void k_spec_back(const double2* __restrict__ r, const float2* __restrict__ u, const int* __restrict__ bk_base,
+                            const float* __restrict__ bk_w, int n, int mask, double2* __restrict__ z) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int b = bk_base[j];
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int t = 0; t < kSpecTaps; ++t) {
+        const float w = bk_w[(size_t)j * kSpecTaps + t];
+        const float2 v = u[(b + t) & mask];
+        re = fmaf(w, v.x, re);
+        im = fmaf(w, v.y, im);
+    }
+    const double2 x = r[j];
+    z[j] = make_double2(2.0 * x.x + (double)re, 2.0 * x.y + (double)im);
+}
+
+// z += zn - 2 r: the network's correction on top of the spectral preconditioner
+__global__ void k_precond_sum(double2* __restrict__ z, const double2* __restrict__ zn, const double2* __restrict__ r, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 a = z[i], b = zn[i], c = r[i];
+    z[i] = make_double2(a.x + b.x - 2.0 * c.x, a.y + b.y - 2.0 * c.y);
+}
+
+// ---------------------------------------------------------------- host tables
+
+struct GaussLegendre {
+    std::vector<double> x, w;
+    explicit GaussLegendre(int n) : x(n), w(n) {
+        for (int i = 0; i < n; ++i) {
+            double z = std::cos(kPiH * (i + 0.75) / (n + 0.5)), dp = 1.0;
+            for (int it = 0; it < 100; ++it) {
+                double p0 = 1.0, p1 = z;
+                for (int m = 2; m <= n; ++m) { const double p2 = ((2 * m - 1) * z * p1 - (m - 1) * p0) / m; p0 = p1; p1 = p2; }
+                dp = n * (z * p1 - p0) / (z * z - 1.0);
+                const double dz = p1 / dp;
+                z -= dz;
+                if (std::fabs(dz) < 1e-16) break;
+            }
+            x[i] = z;
+            w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+        }
+    }
+};
+
+int build_curve(const Discretisation& D, int c, double k, double eta, double eps, SpecCurve& out, std::string& err) {
+    const HostCurve& C = D.curves[c];
+    if (!C.closed) { err = "the spectral preconditioner needs closed curves"; return IFGF2D_ERR_ARG; }
+    const int Np = D.Np;
+    std::vector<int> pats;
+    for (long long p = 0; p < D.num_patches; ++p) if (D.curve_of[p] == c) pats.push_back((int)p);
+    if (pats.empty()) { err = "a curve without patches"; return IFGF2D_ERR_ARG; }
+    std::sort(pats.begin(), pats.end(), [&](int a, int b) { return D.t1[a] < D.t1[b]; });
+    for (size_t i = 1; i < pats.size(); ++i)
+        if (pats[i] != pats[0] + (int)i) { err = "the spectral preconditioner needs each curve's patches stored in parameter order"; return IFGF2D_ERR_ARG; }
+    const int P = (int)pats.size();
+    const long long n = (long long)P * Np;
+    int lg = kSpecMinLog;
+    while ((1LL << lg) < n) ++lg;
+    if (lg > kSpecMaxLog) { err = "the spectral preconditioner takes at most 2^20 points per curve"; return IFGF2D_ERR_ARG; }
+    out.off = (long long)pats[0] * Np;
+    out.n = (int)n;
+    out.lg = lg; out.lg1 = (lg + 1) / 2; out.lg2 = lg / 2;
+    const long long nu = 1LL << lg;
+    const int N1 = 1 << out.lg1, N2 = 1 << out.lg2;
+    static const GaussLegendre gl(32);
+    auto speed = [&](double t) { return std::hypot(C.xp(t), C.yp(t)); };
+    auto seg = [&](double a, double b) {
+        const double h = 0.5 * (b - a), m = 0.5 * (a + b);
+        double s = 0.0;
+        for (size_t i = 0; i < gl.x.size(); ++i) s += gl.w[i] * speed(m + h * gl.x[i]);
+        return h * s;
+    };
+    std::vector<double> S(P + 1, 0.0);
+    for (int i = 0; i < P; ++i) S[i + 1] = S[i] + seg(D.t1[pats[i]], D.t2[pats[i]]);
+    const double L = S[P];
+    out.length = L;
+    const double h = L / (double)nu;
+    // barycentric weights of each patch's nodes in the patch's local coordinate
+    std::vector<double> loc((size_t)n), lam((size_t)n);
+    for (int i = 0; i < P; ++i) {
+        const int p = pats[i];
+        const double a = D.t1[p], b = D.t2[p];
+        for (int j = 0; j < Np; ++j) loc[(size_t)i * Np + j] = (2.0 * D.t[out.off + (long long)i * Np + j] - a - b) / (b - a);
+        for (int j = 0; j < Np; ++j) {
+            double q = 1.0;
+            for (int m = 0; m < Np; ++m) if (m != j) q *= loc[(size_t)i * Np + j] - loc[(size_t)i * Np + m];
+            lam[(size_t)i * Np + j] = 1.0 / q;
+        }
+    }
+    // forward: the grid point's parameter by Newton on its patch's arc length, then the weights
+    std::vector<int> fb((size_t)nu);
+    std::vector<float> fw((size_t)nu * Np);
+    parallel_for(nu, [&](long long g0, long long g1) {
+        for (long long g = g0; g < g1; ++g) {
+            const double sg = h * (double)g;
+            int i = (int)(std::upper_bound(S.begin(), S.end(), sg) - S.begin()) - 1;
+            i = std::min(std::max(i, 0), P - 1);
+            const int p = pats[i];
+            const double a = D.t1[p], b = D.t2[p];
+            double t = a + (sg - S[i]) / (S[i + 1] - S[i]) * (b - a);
+            for (int it = 0; it < 12; ++it) {
+                const double dt = (S[i] + seg(a, t) - sg) / speed(t);
+                t = std::min(std::max(t - dt, a), b);
+                if (std::fabs(dt) < 1e-15 * (b - a)) break;
+            }
+            const double x = (2.0 * t - a - b) / (b - a);
+            fb[(size_t)g] = (int)(out.off + (long long)i * Np);
+            const double* ln = &loc[(size_t)i * Np];
+            const double* lm = &lam[(size_t)i * Np];
+            int exact = -1;
+            double den = 0.0;
+            for (int j = 0; j < Np; ++j) {
+                if (x == ln[j]) { exact = j; break; }
+                den += lm[j] / (x - ln[j]);
+            }
+            for (int j = 0; j < Np; ++j)
+                fw[(size_t)g * Np + j] = exact >= 0 ? (j == exact ? 1.f : 0.f) : (float)(lm[j] / (x - ln[j]) / den);
+        }
+    }, 256);
+    // back: each node's arc length, kSpecTaps-point Lagrange weights on the grid
+    std::vector<int> bb((size_t)n);
+    std::vector<float> bw((size_t)n * kSpecTaps);
+    parallel_for(n, [&](long long j0, long long j1) {
+        for (long long j = j0; j < j1; ++j) {
+            const int i = (int)(j / Np);
+            const double sj = S[i] + seg(D.t1[pats[i]], D.t[out.off + j]);
+            const double x = sj / h;
+            const long long q0 = (long long)std::floor(x) - (kSpecTaps / 2 - 1);
+            const double xr = x - (double)q0;
+            bb[(size_t)j] = (int)(((q0 % nu) + nu) % nu);
+            for (int a = 0; a < kSpecTaps; ++a) {
+                double v = 1.0;
+                for (int m = 0; m < kSpecTaps; ++m) if (m != a) v *= (xr - m) / (double)(a - m);
+                bw[(size_t)j * kSpecTaps + a] = (float)v;
+            }
+        }
+    }, 256);
+    // the multiplier in transposed order, and the twiddles
+    std::vector<float2> mult((size_t)nu), twN((size_t)nu), tw1(std::max(1, N1 / 2)), tw2(std::max(1, N2 / 2));
+    const std::complex<double> ke(k, eps);
+    for (int k1 = 0; k1 < N1; ++k1)
+        for (int k2 = 0; k2 < N2; ++k2) {
+            const long long q = k1 + (long long)N1 * k2;
+            const double f = (double)(q < nu / 2 ? q : q - nu);
+            const double xi = 2.0 * kPiH * f / L;
+            const std::complex<double> sig = 0.5 + eta / (2.0 * std::sqrt(ke * ke - xi * xi));
+            const std::complex<double> m = 1.0 / sig - 2.0;
+            mult[(size_t)k1 * N2 + k2] = make_float2((float)m.real(), (float)m.imag());
+            const long long a = ((long long)k1 * k2) % nu;
+            const double th = -2.0 * kPiH * (double)a / (double)nu;
+            twN[(size_t)k1 * N2 + k2] = make_float2((float)std::cos(th), (float)std::sin(th));
+        }
+    for (int j = 0; j < N1 / 2; ++j) { const double th = -2.0 * kPiH * j / N1; tw1[j] = make_float2((float)std::cos(th), (float)std::sin(th)); }
+    for (int j = 0; j < N2 / 2; ++j) { const double th = -2.0 * kPiH * j / N2; tw2[j] = make_float2((float)std::cos(th), (float)std::sin(th)); }
+    if (out.fw_base.upload(fb.data(), fb.size()) != cudaSuccess || out.fw_w.upload(fw.data(), fw.size()) != cudaSuccess ||
+        out.bk_base.upload(bb.data(), bb.size()) != cudaSuccess || out.bk_w.upload(bw.data(), bw.size()) != cudaSuccess ||
+        out.mult.upload(mult.data(), mult.size()) != cudaSuccess || out.twN.upload(twN.data(), twN.size()) != cudaSuccess ||
+        out.tw1.upload(tw1.data(), tw1.size()) != cudaSuccess || out.tw2.upload(tw2.data(), tw2.size()) != cudaSuccess) {
+        err = "uploading the spectral preconditioner's tables failed";
+        return IFGF2D_ERR_CUDA;
+    }
+    return IFGF2D_OK;
+}
+
+}  // namespace
+
+void free_spectral(ifgf2d_ctx* ctx) {
+    delete ctx->sw;
+    ctx->sw = nullptr;
+}
+
+// z = M r on the context's stream (capturable; the tables stay fixed until the next set-up)
+void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s) {
+    for (auto& cp : sw->curves) {
+        const SpecCurve& c = *cp;
+        const int N1 = 1 << c.lg1, N2 = 1 << c.lg2, cols = std::min(kSpecTile, N2);
+        const size_t smc = sizeof(float2) * (size_t)N1 * cols;
+        k_spec_fwd_cols<<<N2 / cols, kSpecThreads, smc, s>>>(r, c.fw_base.p, c.fw_w.p, Np, c.lg1, c.lg2, c.tw1.p, c.twN.p, sw->u.p);
+        k_spec_rows<<<N1, kSpecThreads, sizeof(float2) * N2, s>>>(sw->u.p, c.mult.p, c.lg2, c.tw2.p, c.twN.p);
+        k_spec_inv_cols<<<N2 / cols, kSpecThreads, smc, s>>>(sw->u.p, c.lg1, c.lg2, c.tw1.p, 1.0f / (float)(1LL << c.lg), sw->u.p);
+        k_spec_back<<<(c.n + 255) / 256, 256, 0, s>>>(r + c.off, sw->u.p, c.bk_base.p, c.bk_w.p, c.n, (1 << c.lg) - 1, z + c.off);
+    }
+}
+
+void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s) {
+    k_precond_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(z, zn, r, n);
+}
+
+int spectral_setup(ifgf2d_ctx* ctx, double scale) {
+    const Discretisation& D = ctx->D;
+    if (ctx->form != IFGF2D_COMBINED) return fail(ctx, IFGF2D_ERR_ARG, "the spectral preconditioner is for the combined-field formulation");
+    if (!(scale > 0.0) || !std::isfinite(scale)) return fail(ctx, IFGF2D_ERR_ARG, "the glancing damping scale must be positive");
+    if (!ctx->precomputed) return fail(ctx, IFGF2D_ERR_STATE, "precompute (or setup) before the spectral preconditioner");
+    if (ctx->sw && ctx->sw->scale == scale) return IFGF2D_OK;
+    AllocStream guard(ctx->stream);
+    if (ctx->gw) ctx->gw->drop_graphs();
+    free_spectral(ctx);
+    std::unique_ptr<SpectralWork> sw(new SpectralWork);
+    const double eps = scale * std::cbrt(ctx->k);
+    long long covered = 0, biggest = 0;
+    for (int c = 0; c < (int)D.curves.size(); ++c) {
+        std::unique_ptr<SpecCurve> sc(new SpecCurve);
+        std::string err;
+        const int rc = build_curve(D, c, ctx->k, ctx->eta, eps, *sc, err);
+        if (rc != IFGF2D_OK) return fail(ctx, rc, err);
+        covered += sc->n;
+        biggest = std::max(biggest, 1LL << sc->lg);
+        sw->curves.push_back(std::move(sc));
+    }
+    if (covered != D.N) return fail(ctx, IFGF2D_ERR_ARG, "the spectral preconditioner needs every point on a closed curve");
+    CK(sw->u.alloc((size_t)biggest));
+    sw->scale = scale;
+    sw->eps_used = eps;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->sw = sw.release();
+    return IFGF2D_OK;
+}
+
+}  // namespace ifgf
+
+extern "C" int ifgf2d_spectral_setup(ifgf2d_ctx* ctx, double scale) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    return ifgf::spectral_setup(ctx, scale <= 0.0 ? IFGF2D_SPECTRAL_DEFAULT_SCALE : scale);
+}
+
+extern "C" int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z) {
+    if (!ctx || !r || !z) return IFGF2D_ERR_ARG;
+    if (!ctx->sw) return fail(ctx, IFGF2D_ERR_STATE, "ifgf2d_spectral_setup first");
+    const long long N = ctx->D.N;
+    if (!all_finite(r, 2 * N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the residual");
+    AllocStream guard(ctx->stream);
+    DBuf<double2> dr, dz;
+    CK(dr.alloc(N)); CK(dz.alloc(N));
+    CK(cudaMemcpyAsync(dr.p, r, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
+    ifgf::spectral_launch(ctx->sw, dr.p, dz.p, ctx->D.Np, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(z, dz.p, sizeof(double2) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return IFGF2D_OK;
+}

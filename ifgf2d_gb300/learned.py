@@ -26,6 +26,9 @@ from . import _lib
 
 MAGIC = b"IFGFNET\x01"
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "cfie_conv6x64.bin")
+# the network trained as a correction of the spectral preconditioner (ForwardMap.solve_flexible
+# with precond="spectral+net"): targets e - M_s r instead of e - 2 r
+SPECTRAL_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "cfie_conv6x64_spectral.bin")
 
 
 def _dp(a):
@@ -147,18 +150,25 @@ class PreconditionerNet:
 
 
 # ---------------------------------------------------------------- training data
-def harvest(fm, k, rhs, stops=(1, 2, 4, 8, 16, 32), tol=1e-9):
+def harvest(fm, k, rhs, stops=(1, 2, 4, 8, 16, 32), tol=1e-9, base=None):
     """(r, e, geom, k) pairs from the plain FP64 IFGF GMRES of one problem: the converged
-    solution x*, then GMRES stopped after j iterations for every j in `stops`"""
+    solution x*, then GMRES stopped after j iterations for every j in `stops`.  base="spectral":
+    the network is to correct the spectral preconditioner M_s, so the stored error is
+    e - (M_s r - 2 r), whose target (e' - 2 r) is what M_s leaves of e."""
     xs = fm.gmres(rhs, accelerated=True, tol=tol, restart=300, max_iters=1000)
     geom = fm.geometry_features()
+    if base == "spectral":
+        fm.spectral_setup()
     out = []
     for j in stops:
         xj = fm.gmres(rhs, accelerated=True, tol=1e-15, restart=max(j, 1), max_iters=j)
         r = rhs - fm.compute_Ax_acc(xj)
         if np.linalg.norm(r) <= 1e-12 * np.linalg.norm(rhs):
             break
-        out.append((r, xs - xj, geom, k))
+        e = xs - xj
+        if base == "spectral":
+            e = e - (fm.spectral_apply(r) - 2.0 * r)
+        out.append((r, e, geom, k))
     return out
 
 
@@ -180,7 +190,7 @@ def training_problems(n=160, seed=0, kmin=50.0, kmax=400.0, kite_every=4):
     return probs
 
 
-def harvest_set(problems, stops=(1, 2, 4, 8, 16, 32), log=None):
+def harvest_set(problems, stops=(1, 2, 4, 8, 16, 32), log=None, base=None):
     import ifgf2d_gb300 as G
     pairs = []
     for name, curve, k, ang, npts in problems:
@@ -190,7 +200,7 @@ def harvest_set(problems, stops=(1, 2, 4, 8, 16, 32), log=None):
         except G.NeighbourhoodError:
             continue
         rhs = -np.exp(1j * k * (math.cos(ang) * fm.xs_ + math.sin(ang) * fm.ys_))
-        pairs += harvest(fm, k, rhs, stops)
+        pairs += harvest(fm, k, rhs, stops, base=base)
         if log:
             log(f"{name} k={k:.1f} N={fm.total_num_unknowns_}: {len(pairs)} pairs")
     return pairs
@@ -225,13 +235,17 @@ def main(argv=None):
     import argparse
     import time
     ap = argparse.ArgumentParser(description="harvest (residual, error) pairs from plain GMRES and train the network")
-    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--base", choices=("none", "spectral"), default="none",
+                    help="spectral: train the correction of the spectral preconditioner")
     ap.add_argument("--problems", type=int, default=160)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args(argv)
     t0 = time.perf_counter()
-    pairs = harvest_set(training_problems(args.problems, seed=args.seed))
+    base = None if args.base == "none" else args.base
+    out = args.out or (SPECTRAL_WEIGHTS if base == "spectral" else DEFAULT_WEIGHTS)
+    pairs = harvest_set(training_problems(args.problems, seed=args.seed), base=base)
     rng = np.random.default_rng(args.seed)
     idx = rng.permutation(len(pairs))
     nval = max(4, len(pairs) // 10)
@@ -241,8 +255,8 @@ def main(argv=None):
     t0 = time.perf_counter()
     train(net, tr, steps=args.steps, seed=args.seed, val=val, log=lambda m: print(m, flush=True))
     print(f"trained in {time.perf_counter() - t0:.1f} s", flush=True)
-    net.save(args.out)
-    print("saved", args.out)
+    net.save(out)
+    print("saved", out)
 
 
 if __name__ == "__main__":

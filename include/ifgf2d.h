@@ -212,6 +212,29 @@ int ifgf2d_net_apply(ifgf2d_net* net, int nseg, const int* len, const double* r,
  * GMRES.  *iters counts inner iterations. */
 int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, double* x, int mode, double tol, int restart,
                          int max_iters, int* iters, double* est_error);
+
+/* Spectral right preconditioner of the combined-field operator on closed curves (no
+ * counterpart in the reference, whose GMRES, ForwardMap/opGMRES.hpp:68-269, is
+ * unpreconditioned).  M r = 2 r + B F^-1 [(1/sigma - 2) F (W r)]: W resamples each curve's node
+ * values onto a uniform arc-length grid, F is the FFT along the curve, sigma(xi) =
+ * 1/2 + eta / (2 sqrt((k + i eps)^2 - xi^2)) the flat-boundary symbol of 1/2 I + K - i eta S with
+ * the glancing damping eps = scale k^(1/3), and B interpolates back to the nodes.  FP32 on the
+ * device.  Set-up (after precompute; host tables, uploaded; a new precompute drops them):
+ * scale <= 0 takes IFGF2D_SPECTRAL_DEFAULT_SCALE.  Needs the combined formulation and closed
+ * curves of at most 2^20 points each. */
+#define IFGF2D_SPECTRAL_DEFAULT_SCALE 0.25
+int ifgf2d_spectral_setup(ifgf2d_ctx* ctx, double scale);
+/* z = M r on host vectors (complex interleaved, N entries), for tests */
+int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z);
+/* ifgf2d_solve_precond with the preconditioner chosen by `precond`: IFGF2D_PRECOND_NET (net
+ * required), IFGF2D_PRECOND_SPECTRAL (set up with the default scale on first use when
+ * ifgf2d_spectral_setup was not called), or both: the spectral preconditioner plus the
+ * network's correction, z = M_s r + (N(r) - 2 r), for a network trained on the spectral
+ * preconditioner's errors. */
+#define IFGF2D_PRECOND_NET 1
+#define IFGF2D_PRECOND_SPECTRAL 2
+int ifgf2d_solve_flexible(ifgf2d_ctx* ctx, ifgf2d_net* net, int precond, const double* rhs, double* x, int mode, double tol,
+                          int restart, int max_iters, int* iters, double* est_error);
 /* per point of the context (patch order): curvature, unit tangent x, y, quadrature weight */
 int ifgf2d_get_geometry_features(const ifgf2d_ctx* ctx, double* geom);
 
