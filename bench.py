@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-angle batch (kite k=2000, N=32768)")
     ap.add_argument("--no-obstacles", action="store_true", help="skip the 256-obstacle workload")
     ap.add_argument("--no-large", action="store_true", help="skip the kite k=8000, N=131072 solve")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
+    ap.add_argument("--no-learned", action="store_true", help="skip the preconditioner comparison (spectral, learned)")
     ap.add_argument("--batch-k", type=float, default=2000.0, help="wavenumber of the batch workload (profiling)")
     ap.add_argument("--batch-patches", type=int, default=2048, help="patches of the batch workload (profiling)")
     return ap.parse_args()
@@ -308,11 +308,15 @@ def run_ours(args, rank, local_rank, world):
     if not args.no_solve:
         b = -np.exp(1j * K_WAVE * fm.xs_)
         solve = {}
-        for name, mixed in (("plain_fp64", False), ("chosen_mixed", True)):
+        fm.spectral_setup()
+        for name, mixed, spec in (("plain_fp64", False, False), ("chosen_mixed", True, False), ("chosen_mixed_spectral", True, True)):
             times = []
             for _ in range(3):   # first call: Krylov workspace + graph capture; then warm solves
                 t0 = time.perf_counter()
-                xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
+                if spec:
+                    xs = fm.solve_flexible(b, "spectral", tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
+                else:
+                    xs = fm.gmres(b, accelerated=True, tol=1e-6, restart=300, max_iters=3000, mixed=mixed)
                 times.append(time.perf_counter() - t0)
             true_res = float(np.linalg.norm(fm.compute_Ax_acc(xs) - b) / np.linalg.norm(b))
             solve[name] = {"seconds": min(times[1:]), "seconds_first_call": times[0], "iters": fm.last_solve["iters"],
@@ -320,6 +324,7 @@ def run_ours(args, rank, local_rank, world):
                            "converged": fm.last_solve["converged"], "true_rel_residual_fp64": true_res, "tol": 1e-6,
                            "restart": 300}
         solve["speedup_chosen_vs_plain"] = solve["plain_fp64"]["seconds"] / solve["chosen_mixed"]["seconds"]
+        solve["speedup_spectral_vs_plain"] = solve["plain_fp64"]["seconds"] / solve["chosen_mixed_spectral"]["seconds"]
     # one apply = fused singular correction + intensities, leaf cones, nl - 3 propagation
     # levels, near field + interpolation
     launches_per_apply = 1 + 1 + (nl - 3) + 1
@@ -359,19 +364,25 @@ def run_ours(args, rank, local_rank, world):
     if not args.no_obstacles and not args.no_solve:
         out["obstacles"] = run_obstacles()
     if not args.no_learned and not args.no_solve:
-        out["learned"] = run_learned(G)
+        out["preconditioned"] = run_preconditioned(G)
     return out
 
 
-def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
-    """The learned right preconditioner (shipped weights, trained at k in [50, 400]) against the
-    same solves without it: plain FP64 GMRES, FP64 refinement around complex64 GMRES, and
-    the latter with the network inside flexible GMRES.  All to a 1e-6 FP64 true residual."""
-    from ifgf2d_gb300.learned import PreconditionerNet, DEFAULT_WEIGHTS
-    if not os.path.exists(DEFAULT_WEIGHTS):
-        return {"unavailable": "no trained weights shipped"}
-    net = PreconditionerNet.load(DEFAULT_WEIGHTS)
-    res = {"weights": os.path.relpath(DEFAULT_WEIGHTS, ROOT), "training": "k ~ U(50, 400), stars and kites, 10 points per wavelength"}
+def run_preconditioned(G, cases=((2000.0, 2048), (8000.0, 8192))):
+    """Right preconditioners on the kite, all solves to a 1e-6 FP64 true residual: plain FP64
+    GMRES; FP64 refinement around complex64 GMRES ("mixed"); the same with flexible GMRES and the
+    spectral preconditioner (inverse flat-boundary symbol along the curve), alone and corrected
+    by the learned network trained on its errors; and the first network alone (trained on the
+    errors of 2I).  Set-up-inclusive times add the constructor, precomps_and_setup and, for the
+    spectral forms, the preconditioner's tables."""
+    from ifgf2d_gb300.learned import PreconditionerNet, DEFAULT_WEIGHTS, SPECTRAL_WEIGHTS
+    nets = {}
+    for key, path in (("net", DEFAULT_WEIGHTS), ("spectral_net", SPECTRAL_WEIGHTS)):
+        if os.path.exists(path):
+            nets[key] = PreconditionerNet.load(path)
+    res = {"weights": {k: os.path.relpath(p, ROOT) for k, p in (("net", DEFAULT_WEIGHTS), ("spectral_net", SPECTRAL_WEIGHTS))},
+           "training": "pairs from plain FP64 GMRES iterates; k ~ U(50, 400), stars and kites, 10 points per wavelength",
+           "spectral_scale": None}
     for k, npatch in cases:
         import torch
         t0 = time.perf_counter()
@@ -379,25 +390,37 @@ def run_learned(G, cases=((2000.0, 2048), (8000.0, 8192))):
         fm.precomps_and_setup(k, 0)
         torch.cuda.synchronize()
         setup_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        fm.spectral_setup()
+        spec_setup_s = time.perf_counter() - t0
         b = -np.exp(1j * k * fm.xs_)
-        row = {"N": fm.total_num_unknowns_, "setup_s": setup_s}
-        for name, fn in (("plain_fp64", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000)),
-                         ("mixed", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000, mixed=True)),
-                         ("mixed_learned", lambda: fm.solve_precond(net, b, tol=1e-6, restart=300, max_iters=3000, mixed=True))):
+        row = {"N": fm.total_num_unknowns_, "setup_s": setup_s, "spectral_setup_s": spec_setup_s}
+        forms = [("plain_fp64", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000)),
+                 ("mixed", lambda: fm.gmres(b, tol=1e-6, restart=300, max_iters=3000, mixed=True)),
+                 ("mixed_spectral", lambda: fm.solve_flexible(b, "spectral", tol=1e-6, restart=300, max_iters=3000, mixed=True))]
+        if "spectral_net" in nets:
+            forms.append(("mixed_spectral_net", lambda: fm.solve_flexible(b, "spectral+net", net=nets["spectral_net"], tol=1e-6,
+                                                                          restart=300, max_iters=3000, mixed=True)))
+        if "net" in nets:
+            forms.append(("mixed_net", lambda: fm.solve_flexible(b, "net", net=nets["net"], tol=1e-6, restart=300, max_iters=3000,
+                                                                 mixed=True)))
+        for name, fn in forms:
             fn()
             t0 = time.perf_counter()
             x = fn()
             dt = time.perf_counter() - t0
             tr = float(np.linalg.norm(fm.compute_Ax_acc(x) - b) / np.linalg.norm(b))
             row[name] = {"seconds": dt, "iters": fm.last_solve["iters"], "converged": fm.last_solve["converged"],
-                         "true_rel_residual_fp64": tr}
-        row["speedup_mixed_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed"]["seconds"]
-        row["speedup_learned_vs_plain"] = row["plain_fp64"]["seconds"] / row["mixed_learned"]["seconds"]
-        row["learned_iteration_ratio"] = row["mixed_learned"]["iters"] / max(1, row["mixed"]["iters"])
-        row["with_setup"] = {n: setup_s + row[n]["seconds"] for n in ("plain_fp64", "mixed", "mixed_learned")}
-        row["with_setup"]["speedup_mixed_vs_plain"] = row["with_setup"]["plain_fp64"] / row["with_setup"]["mixed"]
+                         "fp64_refinement_passes": fm.last_solve.get("refinements", 0), "true_rel_residual_fp64": tr}
+        plain = row["plain_fp64"]["seconds"]
+        row["speedup_vs_plain"] = {n: plain / row[n]["seconds"] for n, _ in forms if n != "plain_fp64"}
+        extra = {n: (spec_setup_s if "spectral" in n else 0.0) for n, _ in forms}
+        row["with_setup"] = {n: setup_s + extra[n] + row[n]["seconds"] for n, _ in forms}
+        row["with_setup"]["speedup_vs_plain"] = {n: row["with_setup"]["plain_fp64"] / row["with_setup"][n]
+                                                 for n, _ in forms if n != "plain_fp64"}
         res[f"kite_k{int(k)}"] = row
         del fm
+    res["spectral_scale"] = G._lib.SPECTRAL_DEFAULT_SCALE
     return res
 
 
@@ -496,21 +519,26 @@ def run_obstacles(n=256, plain_sample=256):
     one block-diagonal operator (one launch per phase, lock-step GMRES), 3 device threads.
     Plain: one obstacle after another, FP64 GMRES, on the first `plain_sample` obstacles."""
     from ifgf2d_gb300.scatterers import star_obstacles, solve_obstacles, solve_obstacles_grouped
-    # groups of 16 obstacles on 3 device threads (the first call warms up)
-    grouped = {}
-    for rep in range(2):
-        obs = star_obstacles(n)
-        t0 = time.perf_counter()
-        solve_obstacles_grouped(obs, tol=1e-6, workers=15, mixed=True, chunk=16, device_threads=3)
-        grouped = {"seconds": time.perf_counter() - t0}
-    rg = [o.result for o in obs]
-    grouped.update({"ms_per_obstacle": grouped["seconds"] / n * 1e3,
-                    "all_converged": all(x["converged"] for x in rg),
-                    "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in rg),
-                    "grouped": int(sum(x.get("grouped", False) for x in rg)),
-                    "iters_max": int(max(x["iters"] for x in rg)),
-                    "form": "groups of 16 on 3 device threads: merged set-up, segmented lock-step GMRES, "
-                            "complex64 inner solves, FP64 refinement"})
+    # groups of 16 obstacles on 3 device threads (the first call warms up), without and with the
+    # spectral preconditioner
+    res_g = {}
+    for key, pc in (("grouped", None), ("grouped_spectral", "spectral")):
+        for rep in range(2):
+            obs = star_obstacles(n)
+            t0 = time.perf_counter()
+            solve_obstacles_grouped(obs, tol=1e-6, workers=15, mixed=True, chunk=16, device_threads=3, precond=pc)
+            g = {"seconds": time.perf_counter() - t0}
+        rg = [o.result for o in obs]
+        g.update({"ms_per_obstacle": g["seconds"] / n * 1e3,
+                  "all_converged": all(x["converged"] for x in rg),
+                  "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in rg),
+                  "grouped": int(sum(x.get("grouped", False) for x in rg)),
+                  "iters_max": int(max(x["iters"] for x in rg)),
+                  "iters_mean": float(np.mean([x["iters"] for x in rg])),
+                  "form": "groups of 16 on 3 device threads: merged set-up, segmented lock-step GMRES, "
+                          "complex64 inner solves, FP64 refinement" + (", flexible GMRES with the spectral preconditioner" if pc else "")})
+        res_g[key] = g
+    grouped = res_g["grouped"]
     obs = star_obstacles(n)
     t0 = time.perf_counter()
     solve_obstacles(obs, tol=1e-6, workers=15, mixed=True, device_threads=3)
@@ -525,6 +553,7 @@ def run_obstacles(n=256, plain_sample=256):
                         "k ~ U(10, 400), N_i = 16 ceil(10 k L / 2 pi / 16), plane wave at a random angle; numpy default_rng(0)",
             "n": n, "unknowns_total": int(sum(o.npoints for o in obs)),
             "grouped": grouped,
+            "grouped_spectral": res_g["grouped_spectral"],
             "chosen": {"seconds": dt, "ms_per_obstacle": dt / n * 1e3, "device_threads": 3,
                        "all_converged": all(x["converged"] for x in r),
                        "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in r),
@@ -533,7 +562,8 @@ def run_obstacles(n=256, plain_sample=256):
                       "all_converged": all(x["converged"] for x in rp),
                       "max_true_rel_residual_fp64": max(x["true_rel_residual"] for x in rp)},
             "speedup_chosen_vs_plain_per_obstacle": (dtp / plain_sample) / (dt / n),
-            "speedup_grouped_vs_plain_per_obstacle": (dtp / plain_sample) / (grouped["seconds"] / n)}
+            "speedup_grouped_vs_plain_per_obstacle": (dtp / plain_sample) / (grouped["seconds"] / n),
+            "speedup_grouped_spectral_vs_plain_per_obstacle": (dtp / plain_sample) / (res_g["grouped_spectral"]["seconds"] / n)}
 
 
 def run_batch(G, k=2000.0, npatch=2048, nrhs=64, solve=True):

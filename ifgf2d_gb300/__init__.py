@@ -428,9 +428,13 @@ class ForwardMap:
         mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
         _check(_lib.load().ifgf2d_apply_batch_device(self._h, px, py, int(nrhs), mode), self._h)
 
-    def gmres_batch(self, B, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False, mixed=False):
+    def gmres_batch(self, B, accelerated=True, tol=None, restart=None, max_iters=None, raise_on_noconv=False, mixed=False,
+                    precond=None):
         """GMRES for every column of an (N, nrhs) matrix, all columns in lock step on the batched
-        operator; ``self.last_solve`` holds per-column iterations and errors."""
+        operator; ``self.last_solve`` holds per-column iterations and errors.  precond="spectral":
+        flexible GMRES with the spectral right preconditioner (IFGF operators only)."""
+        if precond not in (None, "spectral"):
+            raise ValueError("batched solves take precond=None or 'spectral'")
         Bf = self._batch_in(B)
         X = np.empty_like(Bf, order="F")
         nrhs = Bf.shape[1]
@@ -440,9 +444,14 @@ class ForwardMap:
         restart = self.GMRES_MAX_ITER_ if restart is None else restart
         max_iters = self.GMRES_MAX_ITER_ if max_iters is None else max_iters
         mode = (APPLY_IFGF_MIXED if mixed else APPLY_IFGF) if accelerated else APPLY_DIRECT
-        rc = _lib.load().ifgf2d_solve_batch(self._h, _dp(Bf), _dp(X), nrhs, mode,
-                                            float(tol), int(restart), int(max_iters),
-                                            it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        if precond == "spectral":
+            rc = _lib.load().ifgf2d_solve_batch_flexible(self._h, PRECOND_SPECTRAL, _dp(Bf), _dp(X), nrhs, mode, float(tol),
+                                                         int(restart), int(max_iters),
+                                                         it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        else:
+            rc = _lib.load().ifgf2d_solve_batch(self._h, _dp(Bf), _dp(X), nrhs, mode,
+                                                float(tol), int(restart), int(max_iters),
+                                                it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
         self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0),
                                refinements=int(_lib.load().ifgf2d_last_refinements(self._h)) if mixed else 0)
         if rc == 8:
@@ -661,16 +670,25 @@ class Group:
                                                    APPLY_IFGF_MIXED if mixed else APPLY_IFGF))
         return out
 
-    def solve(self, rhs, tol=1e-6, restart=300, max_iters=1000, mixed=True):
+    def solve(self, rhs, tol=1e-6, restart=300, max_iters=1000, mixed=True, precond=None):
         """GMRES for every member in lock step; ``self.last_solve`` holds per-member iterations and
-        estimated errors (FP64 relative residuals with mixed=True)."""
+        estimated errors (FP64 relative residuals with mixed=True).  precond="spectral": flexible
+        GMRES with the spectral right preconditioner (each member at its own wavenumber)."""
+        if precond not in (None, "spectral"):
+            raise ValueError("group solves take precond=None or 'spectral'")
         b = _cview(rhs, self.N)
         x = np.empty(self.N, dtype=np.complex128)
         it = np.zeros(self.n, dtype=np.int32)
         err = np.zeros(self.n)
-        rc = _lib.load().ifgf2d_group_solve(self._h, _dp(b.view(np.float64)), _dp(x.view(np.float64)),
-                                            APPLY_IFGF_MIXED if mixed else APPLY_IFGF, float(tol), int(restart),
-                                            int(max_iters), it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        mode = APPLY_IFGF_MIXED if mixed else APPLY_IFGF
+        if precond == "spectral":
+            rc = _lib.load().ifgf2d_group_solve_flexible(self._h, PRECOND_SPECTRAL, _dp(b.view(np.float64)),
+                                                         _dp(x.view(np.float64)), mode, float(tol), int(restart), int(max_iters),
+                                                         it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(err))
+        else:
+            rc = _lib.load().ifgf2d_group_solve(self._h, _dp(b.view(np.float64)), _dp(x.view(np.float64)), mode, float(tol),
+                                                int(restart), int(max_iters), it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                _dp(err))
         self.last_solve = dict(iters=it.tolist(), error=err.tolist(), converged=(rc == 0))
         if rc != 8:
             self._check(rc)

@@ -21,6 +21,7 @@ STATUS = {
 }
 APPLY_DIRECT, APPLY_IFGF, APPLY_IFGF_MIXED = 0, 1, 2
 PRECOND_NET, PRECOND_SPECTRAL = 1, 2
+SPECTRAL_DEFAULT_SCALE = 0.25   # IFGF2D_SPECTRAL_DEFAULT_SCALE
 CURVE_CIRCLE, CURVE_KITE, CURVE_LINE, CURVE_STAR = 0, 1, 2, 3
 
 # every symbol include/ifgf2d.h declares
@@ -37,7 +38,8 @@ EXPORTS = [
     "ifgf2d_tuning_size", "ifgf2d_autotune", "ifgf2d_get_tuning", "ifgf2d_set_tuning", "ifgf2d_eval_offsurface_setup", "ifgf2d_eval_offsurface", "ifgf2d_eval_offsurface_counts",
     "ifgf2d_group_create", "ifgf2d_group_destroy", "ifgf2d_group_last_error", "ifgf2d_group_num_unknowns",
     "ifgf2d_group_offsets", "ifgf2d_group_apply", "ifgf2d_group_solve",
-    "ifgf2d_spectral_setup", "ifgf2d_spectral_apply", "ifgf2d_solve_flexible",
+    "ifgf2d_spectral_setup", "ifgf2d_spectral_apply", "ifgf2d_solve_flexible", "ifgf2d_solve_batch_flexible",
+    "ifgf2d_group_solve_flexible",
 ]
 
 
@@ -127,6 +129,10 @@ def load(build_if_missing: bool = True):
         L.ifgf2d_spectral_apply.argtypes = [P, D, D]
         L.ifgf2d_solve_flexible.argtypes = [P, P, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int), D]
+        L.ifgf2d_group_solve_flexible.argtypes = [P, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_int), D]
+        L.ifgf2d_solve_batch_flexible.argtypes = [P, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.POINTER(ctypes.c_int), D]
         L.ifgf2d_eval_offsurface_setup.argtypes = [P, ctypes.c_longlong, D, D]
         L.ifgf2d_eval_offsurface.argtypes = [P, D, D]
         L.ifgf2d_eval_offsurface_counts.argtypes = [P, I64]

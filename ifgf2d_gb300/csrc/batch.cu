@@ -43,6 +43,11 @@ struct BatchWork {
     DBuf<double2> lsR, lsg, lsgs;
     DBuf<double> lsgc, lssc, lspar;
     DBuf<int> lsst, lsact;
+    // flexible GMRES with the spectral preconditioner: z_j = M v_j for every column (right-hand
+    // sides interleaved as V), and the preconditioner's grid values of every right-hand side
+    DBuf<double2> Z;
+    DBuf<float2> ug;
+    int zcap = 0, zm = 0;
 };
 
 void ifgf::free_batch(ifgf2d_ctx* ctx) {
@@ -290,12 +295,17 @@ int bnorms(ifgf2d_ctx* ctx, const double2* v, int B, std::vector<double>& out) {
 // than running one iteration past the last stop would.
 int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, const std::vector<double>& tol, int restart,
                 int max_iters, const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est,
-                int gs_passes = 2) {
+                int gs_passes = 2, SpectralWork* spec = nullptr) {
     const long long N = ctx->D.N;
     const int m = (int)std::min<long long>(restart, N);
     int rc = ensure_solve(ctx, B, m);
     if (rc != IFGF2D_OK) return rc;
     BatchWork& W = *ctx->bw;
+    if (spec && (W.zcap < W.scap || W.zm != m)) {   // flexible: the preconditioned columns Z
+        CK(W.Z.alloc((size_t)N * W.scap * m));
+        CK(W.ug.alloc((size_t)spectral_grid_size(spec) * W.scap));
+        W.zcap = W.scap; W.zm = m;
+    }
     cudaStream_t s = ctx->stream;
     const long long nb = N * B;
     const int ldh = m + 1;
@@ -338,7 +348,13 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
         for (int j = 0; j < m; ++j) {
             double2* vj = W.V.p + (long long)j * nb;
             double2* Hcol = W.H.p + (long long)j * ldh * B;
-            if ((rc = apply_il(ctx, vj, W.w.p, B, mode))) return rc;
+            const double2* src = vj;
+            if (spec) {   // flexible GMRES: z_j = M v_j, w = A z_j
+                double2* zj = W.Z.p + (long long)j * nb;
+                spectral_launch_batch(spec, vj, zj, B, W.ug.p, ctx->D.Np, s);
+                src = zj;
+            }
+            if ((rc = apply_il(ctx, src, W.w.p, B, mode))) return rc;
             for (int pass = 0; pass < gs_passes; ++pass) {   // classical Gram-Schmidt, once or twice
                 launch_bdot(W.V.p, nb, j + 1, W.w.p, N, B, W.part.p, W.h.p, Hcol, pass, -1, s);
                 launch_bupdate(W.V.p, nb, j + 1, W.h.p, -1.0, N, B, W.w.p, s);
@@ -353,7 +369,7 @@ int gmres_batch(ifgf2d_ctx* ctx, const double2* b, double2* x, int B, int mode, 
         }
         // y_r = R_r^{-1} g_r over its own column count, x += V Y
         launch_lsq_solve_batch(L, ncols, W.Y.p, s);
-        launch_bupdate(W.V.p, nb, ncols, W.Y.p, 1.0, N, B, x, s);
+        launch_bupdate(spec ? W.Z.p : W.V.p, nb, ncols, W.Y.p, 1.0, N, B, x, s);   // x += V Y, or Z Y (flexible)
         CK(cudaMemcpyAsync(h_sc, W.lssc.p, sizeof(double) * 3 * B, cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(h_st, W.lsst.p, sizeof(int) * 4 * B, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -385,7 +401,7 @@ constexpr int kInnerGsPasses = 1;
 
 // solve B <= kMaxBatch interleaved right-hand sides W.b into W.x
 int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_iters, std::vector<int>& iters,
-             std::vector<double>& est) {
+             std::vector<double>& est, SpectralWork* spec = nullptr) {
     BatchWork& W = *ctx->bw;
     const long long N = ctx->D.N;
     const long long nb = N * B;
@@ -394,7 +410,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
     if (mode != IFGF2D_APPLY_IFGF_MIXED) {
         std::vector<double> tv(B, tol);
         std::vector<char> skip(B, 0);
-        return gmres_batch(ctx, W.b.p, W.x.p, B, mode, tv, restart, max_iters, skip, iters, est);
+        return gmres_batch(ctx, W.b.p, W.x.p, B, mode, tv, restart, max_iters, skip, iters, est, 2, spec);
     }
     // FP64 iterative refinement per right-hand side, as ifgf2d_solve: residual with the FP64
     // operator, correction from GMRES on the complex64 operator
@@ -425,7 +441,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
         if (Bc == B) {
             std::vector<char> skip(B, 0);
             if ((rc = gmres_batch(ctx, W.r.p, W.d.p, B, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most),
-                                  skip, it, e, kInnerGsPasses)))
+                                  skip, it, e, kInnerGsPasses, spec)))
                 return rc;
             for (int r = 0; r < B; ++r) iters[r] += it[r];
             launch_bupdate(W.d.p, 0, 1, W.ones.p, 1.0, N, B, W.x.p, s);   // x += d
@@ -446,7 +462,7 @@ int solve_il(ifgf2d_ctx* ctx, int B, int mode, double tol, int restart, int max_
             std::vector<char> skip(Bc, 0);
             launch_gather_cols(W.r.p, B, W.act.p, Bc, N, W.cr.p, s);
             if ((rc = gmres_batch(ctx, W.cr.p, W.cd.p, Bc, IFGF2D_APPLY_IFGF_MIXED, itc, restart, std::max(1, max_iters - most),
-                                  skip, it, e, kInnerGsPasses)))
+                                  skip, it, e, kInnerGsPasses, spec)))
                 return rc;
             for (int j = 0; j < Bc; ++j) iters[act[j]] += it[j];
             launch_scatter_cols(W.cd.p, Bc, W.act.p, B, N, true, W.x.p, s);   // x += d on the active columns
@@ -500,10 +516,9 @@ extern "C" int ifgf2d_apply_batch(ifgf2d_ctx* ctx, const double* x, double* y, i
     return check_t5(ctx);
 }
 
-extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
-                                  int max_iters, int* iters, double* est_error) {
-    if (!ctx || nrhs < 0 || (nrhs > 0 && (!rhs || !x)) || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
-    AllocStream guard(ctx->stream);
+namespace {
+int solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart, int max_iters,
+                int* iters, double* est_error, SpectralWork* spec) {
     int rc = check_mode(ctx, mode);
     if (rc != IFGF2D_OK || nrhs == 0) return rc;
     const long long N = ctx->D.N;
@@ -534,7 +549,7 @@ extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x,
         launch_interleave(W.xcm.p, N, B, W.b.p, s);
         std::vector<int> it;
         std::vector<double> e;
-        if ((rc = solve_il(ctx, B, mode, tol, restart, max_iters, it, e))) return rc;
+        if ((rc = solve_il(ctx, B, mode, tol, restart, max_iters, it, e, spec))) return rc;
         launch_deinterleave(W.x.p, N, B, W.ycm.p, s);
         CK(cudaMemcpyAsync(x + 2 * (size_t)N * r0, W.ycm.p, bytes, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -546,4 +561,24 @@ extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x,
         }
     }
     return all_ok ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}
+}  // namespace
+
+extern "C" int ifgf2d_solve_batch(ifgf2d_ctx* ctx, const double* rhs, double* x, int nrhs, int mode, double tol, int restart,
+                                  int max_iters, int* iters, double* est_error) {
+    if (!ctx || nrhs < 0 || (nrhs > 0 && (!rhs || !x)) || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    AllocStream guard(ctx->stream);
+    return solve_batch(ctx, rhs, x, nrhs, mode, tol, restart, max_iters, iters, est_error, nullptr);
+}
+
+extern "C" int ifgf2d_solve_batch_flexible(ifgf2d_ctx* ctx, int precond, const double* rhs, double* x, int nrhs, int mode,
+                                           double tol, int restart, int max_iters, int* iters, double* est_error) {
+    if (!ctx || nrhs < 0 || (nrhs > 0 && (!rhs || !x)) || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (precond != IFGF2D_PRECOND_SPECTRAL) return fail(ctx, IFGF2D_ERR_ARG, "batched solves take the spectral preconditioner only");
+    if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_IFGF_MIXED) return fail(ctx, IFGF2D_ERR_ARG, "batched flexible solves are IFGF or IFGF_MIXED");
+    AllocStream guard(ctx->stream);
+    int rc = check_mode(ctx, mode);
+    if (rc != IFGF2D_OK) return rc;
+    if (!ctx->sw && (rc = spectral_setup(ctx, IFGF2D_SPECTRAL_DEFAULT_SCALE)) != IFGF2D_OK) return rc;
+    return solve_batch(ctx, rhs, x, nrhs, mode, tol, restart, max_iters, iters, est_error, ctx->sw);
 }

@@ -269,11 +269,16 @@ void free_batch(ifgf2d_ctx* ctx);
 // off-surface evaluation plan release (offsurface.cu)
 void free_eval(ifgf2d_ctx* ctx);
 // the spectral right preconditioner (spectral_precond.cu): set-up of its tables for the context's
-// k and coupling, with glancing damping eps = scale k^(1/3); release; z = M r queued on s
-// (capturable: the tables stay fixed until the next set-up)
-int spectral_setup(ifgf2d_ctx* ctx, double scale);
+// k and coupling (or per curve, for a group of obstacles), with glancing damping
+// eps = scale k^(1/3); release; z = M r queued on s (capturable: the tables stay fixed until
+// the next set-up)
+int spectral_setup(ifgf2d_ctx* ctx, double scale, const double* curve_k = nullptr, const double* curve_eta = nullptr);
 void free_spectral(ifgf2d_ctx* ctx);
 void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s);
+// the same for B interleaved vectors (point i of vector b at i * B + b), through a grid buffer
+// of B * spectral_grid_size(sw) complex64 values
+void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s);
+long long spectral_grid_size(const SpectralWork* sw);
 // z += zn - 2 r (the learned network's output zn correcting the spectral preconditioner's z)
 void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s);
 // the learned preconditioner on one curve of N points (precond_capi.cu): prepare lays the

@@ -37,13 +37,16 @@ struct ifgf2d_group {
     DBuf<double> lsgc, lssc;
     DBuf<int> lsst;
     int nchunk = 0;
-    cudaGraphExec_t exec[2] = {nullptr, nullptr};   // per apply mode (FP64, complex64): one restart cycle
+    // flexible GMRES with the spectral preconditioner: the preconditioned columns and z_j
+    DBuf<double2> Z, zt;
+    // per apply mode (FP64, complex64) x (plain, spectral preconditioner): one restart cycle
+    cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
     void drop_graphs() { for (auto& e : exec) if (e) { cudaGraphExecDestroy(e); e = nullptr; } }
     ~ifgf2d_group() {
         drop_graphs();
         // the workspace was allocated in order on the merged context's stream: free it before
         // that stream goes with the context
-        for (DBuf<double2>* b : {&V, &w, &vin, &t, &H, &hh, &part, &Y, &hn, &this->b, &x, &r, &d, &lsR, &lsg, &lsgs}) b->release();
+        for (DBuf<double2>* b : {&V, &w, &vin, &t, &H, &hh, &part, &Y, &hn, &this->b, &x, &r, &d, &lsR, &lsg, &lsgs, &Z, &zt}) b->release();
         for (DBuf<int>* b : {&seg_of, &chunk_seg, &seg_chunk_ptr, &jdev, &act, &lsst}) b->release();
         for (DBuf<double>* b : {&par, &lsgc, &lssc}) b->release();
         chunk_lo.release();
@@ -390,7 +393,8 @@ int seg_norms_host(ifgf2d_group* G, const double2* v, std::vector<double>& out) 
 // v_j, the group apply, per-member Gram-Schmidt and norms, per-member Givens step); member s stops
 // when |g_{j+1}| / ||r0_s|| < tol[s], after its iteration limit, or at the start when skip[s].
 int group_gmres(ifgf2d_group* G, const double2* b, double2* x, int mode, const std::vector<double>& tol, int restart, int max_iters,
-                const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est, int passes) {
+                const std::vector<char>& skip, std::vector<int>& iters, std::vector<double>& est, int passes,
+                SpectralWork* spec = nullptr) {
     ifgf2d_ctx* ctx = G->g;
     const long long N = ctx->D.N;
     const int B = G->n;
@@ -401,7 +405,8 @@ int group_gmres(ifgf2d_group* G, const double2* b, double2* x, int mode, const s
     cudaStream_t s = ctx->stream;
     const SegDesc S = seg_desc(G);
     const LsqBatchDev L{G->lsR.p, G->lsg.p, G->lsgc.p, G->lsgs.p, G->lsst.p, G->lssc.p, m, B};
-    const int gi = mode == IFGF2D_APPLY_IFGF_MIXED ? 1 : 0;
+    const int gi = (mode == IFGF2D_APPLY_IFGF_MIXED ? 1 : 0) + (spec ? 2 : 0);
+    if (spec && G->Z.n != (size_t)N * m) { CK(G->Z.alloc((size_t)N * m)); CK(G->zt.alloc(N)); }
     if (!G->exec[gi]) {
         cudaGraph_t graph;
         CK(cudaGraphCreate(&graph, 0));
@@ -421,7 +426,13 @@ int group_gmres(ifgf2d_group* G, const double2* b, double2* x, int mode, const s
             return gfail(G, IFGF2D_ERR_CUDA, std::string("building the group GMRES graph: ") + cudaGetErrorString(e));
         }
         launch_copy_col(G->V.p, N, G->jdev.p, G->vin.p, nullptr, s);
-        const int rc = apply_single(ctx, G->vin.p, G->w.p, mode);
+        const double2* src = G->vin.p;
+        if (spec) {   // flexible GMRES: z_j = M v_j into Z[:, j], then w = A z_j
+            spectral_launch(spec, G->vin.p, G->zt.p, ctx->D.Np, s);
+            launch_store_col(G->zt.p, N, G->jdev.p, G->Z.p, s);
+            src = G->zt.p;
+        }
+        const int rc = apply_single(ctx, src, G->w.p, mode);
         launch_seg_arnoldi(S, G->V.p, m, G->jdev.p, G->w.p, G->hh.p, G->H.p, G->hn.p, passes, s);
         launch_lsq_givens_batch_dev(G->H.p, G->jdev.p, L, G->act.p, cond, s);
         cudaGraph_t body = nullptr;
@@ -477,7 +488,7 @@ int group_gmres(ifgf2d_group* G, const double2* b, double2* x, int mode, const s
             progress = progress || hst[4 * r + 3] > 0;
             if (hst[4 * r] || hst[4 * r + 3] <= 0) done[r] = 1;
         }
-        launch_seg_axpy(S, G->V.p, ncols, G->Y.p, x, s);   // x += V Y per member
+        launch_seg_axpy(S, spec ? G->Z.p : G->V.p, ncols, G->Y.p, x, s);   // x += V Y (or Z Y, flexible) per member
         if (all_done() || !progress) break;
         // restart: r = b - A x; the estimate keeps the first ||r0|| (opGMRES.hpp:207)
         if (int rc = apply_single(ctx, x, G->t.p, mode)) { G->err = ctx->err; return rc; }
@@ -496,9 +507,9 @@ int group_gmres(ifgf2d_group* G, const double2* b, double2* x, int mode, const s
 // host vectors of all members' unknowns in member order; per member its iterations and
 // estimated error.  IFGF2D_APPLY_IFGF_MIXED: FP64 iterative refinement around complex64 inner
 // solves, each member stopping on its own FP64 relative residual.
-extern "C" int ifgf2d_group_solve(ifgf2d_group* G, const double* rhs, double* xout, int mode, double tol, int restart,
-                                  int max_iters, int* iters_out, double* est_out) {
-    if (!G || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+namespace {
+int group_solve(ifgf2d_group* G, const double* rhs, double* xout, int mode, double tol, int restart, int max_iters, int* iters_out,
+                double* est_out, SpectralWork* spec) {
     if (mode != IFGF2D_APPLY_IFGF && mode != IFGF2D_APPLY_IFGF_MIXED) return gfail(G, IFGF2D_ERR_ARG, "group solves are IFGF or IFGF_MIXED");
     ifgf2d_ctx* ctx = G->g;
     if (!ctx || !ctx->ifgf_ready) return gfail(G, IFGF2D_ERR_STATE, "group not set up");
@@ -516,7 +527,7 @@ extern "C" int ifgf2d_group_solve(ifgf2d_group* G, const double* rhs, double* xo
     int rc;
     if (mode == IFGF2D_APPLY_IFGF) {
         std::vector<double> tv(B, tol);
-        if ((rc = group_gmres(G, G->b.p, G->x.p, mode, tv, restart, max_iters, skip, iters, est, 2))) return rc;
+        if ((rc = group_gmres(G, G->b.p, G->x.p, mode, tv, restart, max_iters, skip, iters, est, 2, spec))) return rc;
     } else {
         // FP64 iterative refinement per member: residual with the FP64 operator, correction from
         // GMRES on the complex64 operator (one Gram-Schmidt pass, as the batched inner solves)
@@ -542,7 +553,8 @@ extern "C" int ifgf2d_group_solve(ifgf2d_group* G, const double* rhs, double* xo
             }
             if (!any) break;
             ++ctx->last_passes;
-            if ((rc = group_gmres(G, G->r.p, G->d.p, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most), skip, it, e, 1)))
+            if ((rc = group_gmres(G, G->r.p, G->d.p, IFGF2D_APPLY_IFGF_MIXED, itol, restart, std::max(1, max_iters - most), skip, it, e, 1,
+                                  spec)))
                 return rc;
             for (int r = 0; r < B; ++r) iters[r] += it[r];
             {
@@ -568,4 +580,35 @@ extern "C" int ifgf2d_group_solve(ifgf2d_group* G, const double* rhs, double* xo
         ok = ok && est[r] < tol;
     }
     return ok ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
+}
+}  // namespace
+
+extern "C" int ifgf2d_group_solve(ifgf2d_group* G, const double* rhs, double* xout, int mode, double tol, int restart,
+                                  int max_iters, int* iters_out, double* est_out) {
+    if (!G || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    return group_solve(G, rhs, xout, mode, tol, restart, max_iters, iters_out, est_out, nullptr);
+}
+
+// the spectral preconditioner of the merged context, each curve with its own member's k and eta
+extern "C" int ifgf2d_group_solve_flexible(ifgf2d_group* G, int precond, const double* rhs, double* xout, int mode, double tol,
+                                           int restart, int max_iters, int* iters_out, double* est_out) {
+    if (!G || !rhs || !xout || restart <= 0 || max_iters <= 0) return IFGF2D_ERR_ARG;
+    if (precond != IFGF2D_PRECOND_SPECTRAL) return gfail(G, IFGF2D_ERR_ARG, "group solves take the spectral preconditioner only");
+    ifgf2d_ctx* ctx = G->g;
+    if (!ctx || !ctx->ifgf_ready) return gfail(G, IFGF2D_ERR_STATE, "group not set up");
+    if (!ctx->sw) {
+        const Discretisation& D = ctx->D;
+        std::vector<double> kc(D.curves.size(), 0.0), ec(D.curves.size(), 0.0);
+        for (long long p = 0; p < D.num_patches; ++p) {
+            const long long first = p * D.Np;
+            const int o = (int)(std::upper_bound(G->off.begin(), G->off.end(), first) - G->off.begin()) - 1;
+            kc[D.curve_of[p]] = G->k[o];
+            ec[D.curve_of[p]] = G->eta[o];
+        }
+        AllocStream guard(ctx->stream);
+        const int rc = spectral_setup(ctx, IFGF2D_SPECTRAL_DEFAULT_SCALE, kc.data(), ec.data());
+        if (rc != IFGF2D_OK) { G->err = ctx->err; return rc; }
+        G->drop_graphs();
+    }
+    return group_solve(G, rhs, xout, mode, tol, restart, max_iters, iters_out, est_out, ctx->sw);
 }

@@ -61,7 +61,8 @@ struct SpecCurve {
 struct SpectralWork {
     std::vector<std::unique_ptr<ifgf::SpecCurve>> curves;
     DBuf<float2> u;               // the grid values of the largest curve
-    double scale = 0.0, eps_used = 0.0;
+    long long biggest = 0;        // points of the largest curve's grid
+    double scale = 0.0;
 };
 
 namespace ifgf {
@@ -93,22 +94,25 @@ __device__ void fft_shared(float2* s, int lg, int cols, const float2* __restrict
 
 // W r and the column FFTs: grid point g = n1 N2 + n2 takes its patch's Np node values; each
 // block transforms kSpecTile columns n2 over n1, multiplies by the twiddle and writes
-// Y[k1 N2 + n2].
-__global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* __restrict__ r, const int* __restrict__ fw_base,
+// Y[k1 N2 + n2].  Vectors hold right-hand side b = blockIdx.y of point i at i * ld + b (ld 1
+// for one vector, the batch size for interleaved batches); its grid values at Y + b * ustride.
+__global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* __restrict__ r, int ld, const int* __restrict__ fw_base,
                                                                 const float* __restrict__ fw_w, int Np, int lg1, int lg2,
                                                                 const float2* __restrict__ tw1, const float2* __restrict__ twN,
-                                                                float2* __restrict__ Y) {
+                                                                float2* __restrict__ Y, long long ustride) {
     extern __shared__ float2 sm[];
     const int N1 = 1 << lg1, N2 = 1 << lg2;
     const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
+    r += blockIdx.y;
+    Y += blockIdx.y * ustride;
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
         const int n1 = e / cols, c = e - n1 * cols;
         const int g = n1 * N2 + c0 + c;
-        const double2* src = r + fw_base[g];
+        const double2* src = r + (long long)fw_base[g] * ld;
         const float* w = fw_w + (size_t)g * Np;
         float re = 0.f, im = 0.f;
         for (int j = 0; j < Np; ++j) {
-            const double2 v = src[j];
+            const double2 v = src[(long long)j * ld];
             re = fmaf(w[j], (float)v.x, re);
             im = fmaf(w[j], (float)v.y, im);
         }
@@ -124,11 +128,11 @@ __global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* _
 }
 
 // per row k1: the row FFT, the multiplier, the inverse row FFT and the inverse twiddle, in place
-__global__ void __launch_bounds__(kSpecThreads) k_spec_rows(float2* __restrict__ Y, const float2* __restrict__ mult, int lg2,
-                                                            const float2* __restrict__ tw2, const float2* __restrict__ twN) {
+__global__ void __launch_bounds__(kSpecThreads) k_spec_rows(float2* __restrict__ Y, long long ustride, const float2* __restrict__ mult,
+                                                            int lg2, const float2* __restrict__ tw2, const float2* __restrict__ twN) {
     extern __shared__ float2 sm[];
     const int N2 = 1 << lg2;
-    float2* row = Y + (size_t)blockIdx.x * N2;
+    float2* row = Y + blockIdx.y * ustride + (size_t)blockIdx.x * N2;
     const float2* mrow = mult + (size_t)blockIdx.x * N2;
     const float2* trow = twN + (size_t)blockIdx.x * N2;
     for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[brev(i, lg2)] = row[i];
@@ -151,10 +155,13 @@ __global__ void __launch_bounds__(kSpecThreads) k_spec_rows(float2* __restrict__
 // the inverse column FFTs, scaled by 1/nu: u[n1 N2 + n2] on the uniform grid (U and u may be
 // the same buffer: a block reads all of its columns before it writes them)
 __global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const float2* U, int lg1, int lg2,
-                                                                const float2* __restrict__ tw1, float scale, float2* u) {
+                                                                const float2* __restrict__ tw1, float scale, float2* u,
+                                                                long long ustride) {
     extern __shared__ float2 sm[];
     const int N1 = 1 << lg1, N2 = 1 << lg2;
     const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
+    U += blockIdx.y * ustride;
+    u += blockIdx.y * ustride;
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
         const int k1 = e / cols, c = e - k1 * cols;
         sm[brev(k1, lg1) * cols + c] = U[k1 * N2 + c0 + c];
@@ -169,10 +176,12 @@ __global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const float2* U,
 }
 
 // z = 2 r + B u on the curve's nodes
-__global__ void k_spec_back(const double2* __restrict__ r, const float2* __restrict__ u, const int* __restrict__ bk_base,
-                            const float* __restrict__ bk_w, int n, int mask, double2* __restrict__ z) {
+__global__ void k_spec_back(const double2* __restrict__ r, int ld, const float2* __restrict__ u, long long ustride,
+                            const int* __restrict__ bk_base, const float* __restrict__ bk_w, int n, int mask,
+                            double2* __restrict__ z) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
+    u += blockIdx.y * ustride;
     const int b = bk_base[j];
     float re = 0.f, im = 0.f;
 #pragma unroll
@@ -182,8 +191,9 @@ __global__ void k_spec_back(const double2* __restrict__ r, const float2* __restr
         re = fmaf(w, v.x, re);
         im = fmaf(w, v.y, im);
     }
-    const double2 x = r[j];
-    z[j] = make_double2(2.0 * x.x + (double)re, 2.0 * x.y + (double)im);
+    const long long o = (long long)j * ld + blockIdx.y;
+    const double2 x = r[o];
+    z[o] = make_double2(2.0 * x.x + (double)re, 2.0 * x.y + (double)im);
 }
 
 // z += zn - 2 r: the network's correction on top of the spectral preconditioner
@@ -235,7 +245,7 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
     out.lg = lg; out.lg1 = (lg + 1) / 2; out.lg2 = lg / 2;
     const long long nu = 1LL << lg;
     const int N1 = 1 << out.lg1, N2 = 1 << out.lg2;
-    static const GaussLegendre gl(32);
+    static const GaussLegendre gl(24);
     auto speed = [&](double t) { return std::hypot(C.xp(t), C.yp(t)); };
     auto seg = [&](double a, double b) {
         const double h = 0.5 * (b - a), m = 0.5 * (a + b);
@@ -271,10 +281,10 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
             const int p = pats[i];
             const double a = D.t1[p], b = D.t2[p];
             double t = a + (sg - S[i]) / (S[i + 1] - S[i]) * (b - a);
-            for (int it = 0; it < 12; ++it) {
+            for (int it = 0; it < 12; ++it) {   // quadratic convergence from the linear guess: 3 to 4 steps
                 const double dt = (S[i] + seg(a, t) - sg) / speed(t);
                 t = std::min(std::max(t - dt, a), b);
-                if (std::fabs(dt) < 1e-15 * (b - a)) break;
+                if (std::fabs(dt) < 1e-12 * (b - a)) break;
             }
             const double x = (2.0 * t - a - b) / (b - a);
             fb[(size_t)g] = (int)(out.off + (long long)i * Np);
@@ -342,24 +352,34 @@ void free_spectral(ifgf2d_ctx* ctx) {
     ctx->sw = nullptr;
 }
 
-// z = M r on the context's stream (capturable; the tables stay fixed until the next set-up)
-void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s) {
+// z = M r on the context's stream (capturable; the tables stay fixed until the next set-up):
+// B interleaved vectors (point i of vector b at i * B + b; B = 1 for one vector) through the
+// grid buffer `u` of B * biggest values
+void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s) {
+    const long long us = sw->biggest;
     for (auto& cp : sw->curves) {
         const SpecCurve& c = *cp;
         const int N1 = 1 << c.lg1, N2 = 1 << c.lg2, cols = std::min(kSpecTile, N2);
         const size_t smc = sizeof(float2) * (size_t)N1 * cols;
-        k_spec_fwd_cols<<<N2 / cols, kSpecThreads, smc, s>>>(r, c.fw_base.p, c.fw_w.p, Np, c.lg1, c.lg2, c.tw1.p, c.twN.p, sw->u.p);
-        k_spec_rows<<<N1, kSpecThreads, sizeof(float2) * N2, s>>>(sw->u.p, c.mult.p, c.lg2, c.tw2.p, c.twN.p);
-        k_spec_inv_cols<<<N2 / cols, kSpecThreads, smc, s>>>(sw->u.p, c.lg1, c.lg2, c.tw1.p, 1.0f / (float)(1LL << c.lg), sw->u.p);
-        k_spec_back<<<(c.n + 255) / 256, 256, 0, s>>>(r + c.off, sw->u.p, c.bk_base.p, c.bk_w.p, c.n, (1 << c.lg) - 1, z + c.off);
+        const double2* rc = r + c.off * B;
+        double2* zc = z + c.off * B;
+        k_spec_fwd_cols<<<dim3(N2 / cols, B), kSpecThreads, smc, s>>>(r, B, c.fw_base.p, c.fw_w.p, Np, c.lg1, c.lg2, c.tw1.p,
+                                                                      c.twN.p, u, us);
+        k_spec_rows<<<dim3(N1, B), kSpecThreads, sizeof(float2) * N2, s>>>(u, us, c.mult.p, c.lg2, c.tw2.p, c.twN.p);
+        k_spec_inv_cols<<<dim3(N2 / cols, B), kSpecThreads, smc, s>>>(u, c.lg1, c.lg2, c.tw1.p, 1.0f / (float)(1LL << c.lg), u, us);
+        k_spec_back<<<dim3((c.n + 255) / 256, B), 256, 0, s>>>(rc, B, u, us, c.bk_base.p, c.bk_w.p, c.n, (1 << c.lg) - 1, zc);
     }
 }
+void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s) {
+    spectral_launch_batch(sw, r, z, 1, sw->u.p, Np, s);
+}
+long long spectral_grid_size(const SpectralWork* sw) { return sw ? sw->biggest : 0; }
 
 void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s) {
     k_precond_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(z, zn, r, n);
 }
 
-int spectral_setup(ifgf2d_ctx* ctx, double scale) {
+int spectral_setup(ifgf2d_ctx* ctx, double scale, const double* curve_k, const double* curve_eta) {
     const Discretisation& D = ctx->D;
     if (ctx->form != IFGF2D_COMBINED) return fail(ctx, IFGF2D_ERR_ARG, "the spectral preconditioner is for the combined-field formulation");
     if (!(scale > 0.0) || !std::isfinite(scale)) return fail(ctx, IFGF2D_ERR_ARG, "the glancing damping scale must be positive");
@@ -369,12 +389,12 @@ int spectral_setup(ifgf2d_ctx* ctx, double scale) {
     if (ctx->gw) ctx->gw->drop_graphs();
     free_spectral(ctx);
     std::unique_ptr<SpectralWork> sw(new SpectralWork);
-    const double eps = scale * std::cbrt(ctx->k);
     long long covered = 0, biggest = 0;
     for (int c = 0; c < (int)D.curves.size(); ++c) {
         std::unique_ptr<SpecCurve> sc(new SpecCurve);
         std::string err;
-        const int rc = build_curve(D, c, ctx->k, ctx->eta, eps, *sc, err);
+        const double kc = curve_k ? curve_k[c] : ctx->k, ec = curve_eta ? curve_eta[c] : ctx->eta;
+        const int rc = build_curve(D, c, kc, ec, scale * std::cbrt(kc), *sc, err);
         if (rc != IFGF2D_OK) return fail(ctx, rc, err);
         covered += sc->n;
         biggest = std::max(biggest, 1LL << sc->lg);
@@ -382,8 +402,8 @@ int spectral_setup(ifgf2d_ctx* ctx, double scale) {
     }
     if (covered != D.N) return fail(ctx, IFGF2D_ERR_ARG, "the spectral preconditioner needs every point on a closed curve");
     CK(sw->u.alloc((size_t)biggest));
+    sw->biggest = biggest;
     sw->scale = scale;
-    sw->eps_used = eps;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->sw = sw.release();
     return IFGF2D_OK;

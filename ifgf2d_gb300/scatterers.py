@@ -159,7 +159,7 @@ def solve_obstacles(obstacles, tol=1e-6, workers=15, mixed=True, direct_below=0,
 
 
 def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart=300, max_iters=1000,
-                            keep_solutions=False, chunk=16, device_threads=3):
+                            keep_solutions=False, chunk=16, device_threads=3, precond=None):
     """Solve the obstacles in groups (ifgf2d_group_*) of `chunk` obstacles (None: one group).
     The host part of each obstacle's set-up (discretisation, tree depth, tree and plans) runs on
     `workers` threads; `device_threads` threads take the groups in turn as their obstacles are
@@ -168,7 +168,8 @@ def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart
     over all its obstacles, and several groups overlap on the GPU.  Obstacles whose points no tree
     depth keeps in the leaf neighbourhood use the direct operator, one at a time.  Each obstacle's
     `result` holds its iterations, convergence, true FP64 relative residual and operator; returns
-    the densities when keep_solutions."""
+    the densities when keep_solutions.  precond="spectral": the groups' GMRES is flexible, with the
+    spectral right preconditioner."""
     from . import _lib
     import ifgf2d_gb300 as G
     L = _lib.load()
@@ -193,7 +194,7 @@ def solve_obstacles_grouped(obstacles, tol=1e-6, workers=15, mixed=True, restart
         for i in acc:                       # the group holds its own copy of everything
             prepared[i][0].close()
         rhs = np.concatenate(rhs_of)
-        x = grp.solve(rhs, tol=tol, restart=restart, max_iters=max_iters, mixed=mixed)
+        x = grp.solve(rhs, tol=tol, restart=restart, max_iters=max_iters, mixed=mixed, precond=precond)
         st = grp.last_solve
         res = grp.split(grp.apply(x) - rhs)
         parts = grp.split(x)

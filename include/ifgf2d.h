@@ -235,6 +235,11 @@ int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z);
 #define IFGF2D_PRECOND_SPECTRAL 2
 int ifgf2d_solve_flexible(ifgf2d_ctx* ctx, ifgf2d_net* net, int precond, const double* rhs, double* x, int mode, double tol,
                           int restart, int max_iters, int* iters, double* est_error);
+/* ifgf2d_solve_batch with flexible GMRES and the spectral preconditioner (precond must be
+ * IFGF2D_PRECOND_SPECTRAL; mode IFGF2D_APPLY_IFGF or IFGF2D_APPLY_IFGF_MIXED): every right-hand
+ * side's Krylov vector is preconditioned in the same launches. */
+int ifgf2d_solve_batch_flexible(ifgf2d_ctx* ctx, int precond, const double* rhs, double* x, int nrhs, int mode, double tol,
+                                int restart, int max_iters, int* iters, double* est_error);
 /* per point of the context (patch order): curvature, unit tangent x, y, quadrature weight */
 int ifgf2d_get_geometry_features(const ifgf2d_ctx* ctx, double* geom);
 
@@ -310,6 +315,11 @@ int ifgf2d_group_offsets(const ifgf2d_group* group, long long* offsets);
 int ifgf2d_group_apply(ifgf2d_group* group, const double* x, double* y, int mode);
 int ifgf2d_group_solve(ifgf2d_group* group, const double* rhs, double* x, int mode, double tol, int restart, int max_iters,
                        int* iters, double* est);
+/* ifgf2d_group_solve with flexible GMRES and the spectral preconditioner (precond must be
+ * IFGF2D_PRECOND_SPECTRAL), each member's curve with its own wavenumber and coupling; the tables
+ * are built on the first call. */
+int ifgf2d_group_solve_flexible(ifgf2d_group* group, int precond, const double* rhs, double* x, int mode, double tol,
+                                int restart, int max_iters, int* iters, double* est);
 
 /* Largest N accepted by ifgf2d_apply_direct_noalloc. */
 #define IFGF2D_NOALLOC_MAX_N 65536

@@ -106,27 +106,36 @@ def test_gpu_fgmres_identity_is_gmres_and_converges(lib, tmp_path):
     assert np.array_equal(PreconditionerNet.load(path).params, net.params)
 
 
-def test_gpu_shipped_network_effect_is_measured(lib):
-    """The shipped weights (trained at k in [50, 400]) inside flexible GMRES on a kite outside
-    the training set: the FP64 tolerance is reached, and the iteration count with and without
-    the network is measured.  The network does not reduce the count on the kite (about 1.7x
-    more iterations at k = 300 and 2x at k = 2000): its errors fall on the components that set
-    GMRES's rate, and the solver keeps plain GMRES as the default."""
+def test_gpu_learned_preconditioner_beats_plain_gmres(lib):
+    """The shipped networks inside flexible GMRES on a kite outside their training set (k = 300;
+    trained at k in [50, 400] on stars and kites of other sizes), all to the FP64 tolerance:
+    * the network trained on the spectral preconditioner's errors, on top of that preconditioner
+      ("spectral+net"), needs at most 0.7 of plain GMRES's iterations, and no more than two
+      iterations beyond the spectral preconditioner alone (it must not spoil it);
+    * the first network alone (trained on the errors of 2I) is measured: it needs more
+      iterations than plain GMRES (about 1.7x), which the printout records."""
     import os
-    from ifgf2d_gb300.learned import PreconditionerNet, DEFAULT_WEIGHTS
-    if not os.path.exists(DEFAULT_WEIGHTS):
+    from ifgf2d_gb300.learned import PreconditionerNet, DEFAULT_WEIGHTS, SPECTRAL_WEIGHTS
+    if not (os.path.exists(DEFAULT_WEIGHTS) and os.path.exists(SPECTRAL_WEIGHTS)):
         pytest.skip("no shipped weights")
-    net = PreconditionerNet.load(DEFAULT_WEIGHTS)
     k = 300.0
     fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=320, formulation="combined")
     fm.precomps_and_setup(k, 0)
     b = -np.exp(1j * k * fm.xs_)
     fm.gmres(b, tol=1e-6, restart=300, max_iters=1000, mixed=True)
-    it0 = fm.last_solve["iters"]
-    x = fm.solve_precond(net, b, tol=1e-6, restart=300, max_iters=1000, mixed=True)
-    it1 = fm.last_solve["iters"]
+    it_plain = fm.last_solve["iters"]
+    fm.solve_flexible(b, "spectral", tol=1e-6, restart=300, max_iters=1000, mixed=True)
+    it_spec = fm.last_solve["iters"]
+    x = fm.solve_flexible(b, "spectral+net", net=PreconditionerNet.load(SPECTRAL_WEIGHTS), tol=1e-6, restart=300,
+                          max_iters=1000, mixed=True)
+    it_learned = fm.last_solve["iters"]
     assert fm.last_solve["converged"]
     assert np.linalg.norm(fm.compute_Ax_acc(x) - b) / np.linalg.norm(b) < 1e-6
-    ratio = it1 / it0
-    print(f"learned preconditioner, kite k=300: {it1} iterations against {it0} without it (x{ratio:.2f})")
-    assert 0.2 < ratio < 3.0
+    x = fm.solve_flexible(b, "net", net=PreconditionerNet.load(DEFAULT_WEIGHTS), tol=1e-6, restart=300, max_iters=1000,
+                          mixed=True)
+    it_net = fm.last_solve["iters"]
+    assert fm.last_solve["converged"]
+    assert np.linalg.norm(fm.compute_Ax_acc(x) - b) / np.linalg.norm(b) < 1e-6
+    print(f"kite k=300 iterations: plain {it_plain}, spectral {it_spec}, spectral+net {it_learned}, net alone {it_net}")
+    assert it_learned <= 0.7 * it_plain
+    assert it_learned <= it_spec + 2
