@@ -18,7 +18,8 @@
 // k / xi and the identity part 2 r stays exact at the nodes.
 //   W  resamples each closed curve's node values onto a uniform arc-length grid of
 //      nu = 2^m >= n points: per grid point the Lagrange interpolant (barycentric form) of the
-//      Np nodes of its patch;
+//      Np nodes of its patch, at the local coordinate that the same interpolation through the
+//      nodes' arc lengths (spectral integrals of |x'| from the quadrature factors) gives;
 //   F  is the length-nu discrete Fourier transform, computed in four steps (nu = N1 N2):
 //      FFTs of length N1 down the columns of the N1 x N2 view, a twiddle factor, FFTs of
 //      length N2 along the rows.  The spectrum stays in that transposed order; the multiplier
@@ -56,12 +57,27 @@ struct SpecCurve {
     DBuf<float2> tw1, tw2;        // e^{-2 pi i j / N1}, j < N1 / 2; the same for N2
 };
 
+// a curve's tables as the kernels see them
+struct SpecDesc {
+    long long off, uoff;          // first point of the curve; first grid value in the work buffer
+    int n, lg, lg1, lg2;
+    const int* fw_base;
+    const float* fw_w;
+    const int* bk_base;
+    const float* bk_w;
+    const float2 *mult, *twN, *tw1, *tw2;
+};
+
 }  // namespace ifgf
 
 struct SpectralWork {
     std::vector<std::unique_ptr<ifgf::SpecCurve>> curves;
-    DBuf<float2> u;               // the grid values of the largest curve
-    long long biggest = 0;        // points of the largest curve's grid
+    DBuf<ifgf::SpecDesc> desc;    // per curve: its tables
+    DBuf<int> pre;                // per kernel (columns, rows, nodes): the curves' block-count prefix, ncurves + 1 each
+    int ncurves = 0, blocks_cols = 0, blocks_rows = 0, blocks_back = 0;
+    size_t smem_cols = 0, smem_rows = 0;
+    DBuf<float2> u;               // the grid values of every curve, one right-hand side
+    long long grid_total = 0;     // grid points of all curves
     double scale = 0.0;
 };
 
@@ -92,106 +108,125 @@ __device__ void fft_shared(float2* s, int lg, int cols, const float2* __restrict
     }
 }
 
+// Every kernel serves all curves of the context in one launch: block b of a launch belongs to
+// the curve c with pre[c] <= b < pre[c + 1] (pre: the curves' block-count prefix for that kernel),
+// and works on that curve's tables (SpecDesc).  Vectors hold right-hand side q = blockIdx.y of
+// point i at i * ld + q (ld 1 for one vector, the batch size for interleaved batches); its grid
+// values at u + q * ustride + desc.uoff.
+__device__ __forceinline__ int spec_curve_of(const int* __restrict__ pre, int ncurves, int b) {
+    int lo = 0, hi = ncurves - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // W r and the column FFTs: grid point g = n1 N2 + n2 takes its patch's Np node values; each
 // block transforms kSpecTile columns n2 over n1, multiplies by the twiddle and writes
-// Y[k1 N2 + n2].  Vectors hold right-hand side b = blockIdx.y of point i at i * ld + b (ld 1
-// for one vector, the batch size for interleaved batches); its grid values at Y + b * ustride.
-__global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* __restrict__ r, int ld, const int* __restrict__ fw_base,
-                                                                const float* __restrict__ fw_w, int Np, int lg1, int lg2,
-                                                                const float2* __restrict__ tw1, const float2* __restrict__ twN,
-                                                                float2* __restrict__ Y, long long ustride) {
+// Y[k1 N2 + n2].
+__global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* __restrict__ r, int ld, const SpecDesc* __restrict__ cd,
+                                                                const int* __restrict__ pre, int ncurves, int Np,
+                                                                float2* __restrict__ u, long long ustride) {
     extern __shared__ float2 sm[];
-    const int N1 = 1 << lg1, N2 = 1 << lg2;
-    const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
+    const int c = spec_curve_of(pre, ncurves, blockIdx.x);
+    const SpecDesc d = cd[c];
+    const int N1 = 1 << d.lg1, N2 = 1 << d.lg2;
+    const int cols = min(kSpecTile, N2), c0 = (blockIdx.x - pre[c]) * cols;
     r += blockIdx.y;
-    Y += blockIdx.y * ustride;
+    float2* Y = u + blockIdx.y * ustride + d.uoff;
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
-        const int n1 = e / cols, c = e - n1 * cols;
-        const int g = n1 * N2 + c0 + c;
-        const double2* src = r + (long long)fw_base[g] * ld;
-        const float* w = fw_w + (size_t)g * Np;
+        const int n1 = e / cols, cc = e - n1 * cols;
+        const int g = n1 * N2 + c0 + cc;
+        const double2* src = r + (long long)d.fw_base[g] * ld;
+        const float* w = d.fw_w + (size_t)g * Np;
         float re = 0.f, im = 0.f;
         for (int j = 0; j < Np; ++j) {
             const double2 v = src[(long long)j * ld];
             re = fmaf(w[j], (float)v.x, re);
             im = fmaf(w[j], (float)v.y, im);
         }
-        sm[brev(n1, lg1) * cols + c] = make_float2(re, im);
+        sm[brev(n1, d.lg1) * cols + cc] = make_float2(re, im);
     }
     __syncthreads();
-    fft_shared(sm, lg1, cols, tw1, false);
+    fft_shared(sm, d.lg1, cols, d.tw1, false);
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
-        const int k1 = e / cols, c = e - k1 * cols;
-        const int o = k1 * N2 + c0 + c;
-        Y[o] = cmulf(sm[k1 * cols + c], twN[o]);
+        const int k1 = e / cols, cc = e - k1 * cols;
+        const int o = k1 * N2 + c0 + cc;
+        Y[o] = cmulf(sm[k1 * cols + cc], d.twN[o]);
     }
 }
 
 // per row k1: the row FFT, the multiplier, the inverse row FFT and the inverse twiddle, in place
-__global__ void __launch_bounds__(kSpecThreads) k_spec_rows(float2* __restrict__ Y, long long ustride, const float2* __restrict__ mult,
-                                                            int lg2, const float2* __restrict__ tw2, const float2* __restrict__ twN) {
+__global__ void __launch_bounds__(kSpecThreads) k_spec_rows(const SpecDesc* __restrict__ cd, const int* __restrict__ pre, int ncurves,
+                                                            float2* __restrict__ u, long long ustride) {
     extern __shared__ float2 sm[];
-    const int N2 = 1 << lg2;
-    float2* row = Y + blockIdx.y * ustride + (size_t)blockIdx.x * N2;
-    const float2* mrow = mult + (size_t)blockIdx.x * N2;
-    const float2* trow = twN + (size_t)blockIdx.x * N2;
-    for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[brev(i, lg2)] = row[i];
+    const int c = spec_curve_of(pre, ncurves, blockIdx.x);
+    const SpecDesc d = cd[c];
+    const int N2 = 1 << d.lg2, k1 = blockIdx.x - pre[c];
+    float2* row = u + blockIdx.y * ustride + d.uoff + (size_t)k1 * N2;
+    const float2* mrow = d.mult + (size_t)k1 * N2;
+    const float2* trow = d.twN + (size_t)k1 * N2;
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[brev(i, d.lg2)] = row[i];
     __syncthreads();
-    if (lg2 > 0) fft_shared(sm, lg2, 1, tw2, false);
+    fft_shared(sm, d.lg2, 1, d.tw2, false);
     for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[i] = cmulf(sm[i], mrow[i]);
     __syncthreads();
     for (int i = threadIdx.x; i < N2; i += blockDim.x) {   // back to bit-reversed order: disjoint swaps
-        const int j = brev(i, lg2);
+        const int j = brev(i, d.lg2);
         if (i < j) { const float2 t = sm[i]; sm[i] = sm[j]; sm[j] = t; }
     }
     __syncthreads();
-    if (lg2 > 0) fft_shared(sm, lg2, 1, tw2, true);
+    fft_shared(sm, d.lg2, 1, d.tw2, true);
     for (int i = threadIdx.x; i < N2; i += blockDim.x) {
         const float2 t = trow[i];
         row[i] = cmulf(sm[i], make_float2(t.x, -t.y));
     }
 }
 
-// the inverse column FFTs, scaled by 1/nu: u[n1 N2 + n2] on the uniform grid (U and u may be
-// the same buffer: a block reads all of its columns before it writes them)
-__global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const float2* U, int lg1, int lg2,
-                                                                const float2* __restrict__ tw1, float scale, float2* u,
-                                                                long long ustride) {
+// the inverse column FFTs, scaled by 1/nu, in place: u[n1 N2 + n2] on the uniform grid (a block
+// reads all of its columns before it writes them)
+__global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const SpecDesc* __restrict__ cd, const int* __restrict__ pre, int ncurves,
+                                                                float2* __restrict__ u, long long ustride) {
     extern __shared__ float2 sm[];
-    const int N1 = 1 << lg1, N2 = 1 << lg2;
-    const int cols = min(kSpecTile, N2), c0 = blockIdx.x * cols;
-    U += blockIdx.y * ustride;
-    u += blockIdx.y * ustride;
+    const int c = spec_curve_of(pre, ncurves, blockIdx.x);
+    const SpecDesc d = cd[c];
+    const int N1 = 1 << d.lg1, N2 = 1 << d.lg2;
+    const int cols = min(kSpecTile, N2), c0 = (blockIdx.x - pre[c]) * cols;
+    float2* U = u + blockIdx.y * ustride + d.uoff;
+    const float scale = 1.0f / (float)(N1 * N2);
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
-        const int k1 = e / cols, c = e - k1 * cols;
-        sm[brev(k1, lg1) * cols + c] = U[k1 * N2 + c0 + c];
+        const int k1 = e / cols, cc = e - k1 * cols;
+        sm[brev(k1, d.lg1) * cols + cc] = U[k1 * N2 + c0 + cc];
     }
     __syncthreads();
-    fft_shared(sm, lg1, cols, tw1, true);
+    fft_shared(sm, d.lg1, cols, d.tw1, true);
     for (int e = threadIdx.x; e < N1 * cols; e += blockDim.x) {
-        const int n1 = e / cols, c = e - n1 * cols;
-        const float2 v = sm[n1 * cols + c];
-        u[n1 * N2 + c0 + c] = make_float2(v.x * scale, v.y * scale);
+        const int n1 = e / cols, cc = e - n1 * cols;
+        const float2 v = sm[n1 * cols + cc];
+        U[n1 * N2 + c0 + cc] = make_float2(v.x * scale, v.y * scale);
     }
 }
 
-// z = 2 r + B u on the curve's nodes
-__global__ void k_spec_back(const double2* __restrict__ r, int ld, const float2* __restrict__ u, long long ustride,
-                            const int* __restrict__ bk_base, const float* __restrict__ bk_w, int n, int mask,
-                            double2* __restrict__ z) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    u += blockIdx.y * ustride;
-    const int b = bk_base[j];
+// z = 2 r + B u on every curve's nodes
+__global__ void k_spec_back(const double2* __restrict__ r, int ld, const SpecDesc* __restrict__ cd, const int* __restrict__ pre,
+                            int ncurves, const float2* __restrict__ u, long long ustride, double2* __restrict__ z) {
+    const int c = spec_curve_of(pre, ncurves, blockIdx.x);
+    const SpecDesc d = cd[c];
+    const int j = (blockIdx.x - pre[c]) * blockDim.x + threadIdx.x;
+    if (j >= d.n) return;
+    const float2* uc = u + blockIdx.y * ustride + d.uoff;
+    const int mask = (1 << d.lg) - 1;
+    const int b = d.bk_base[j];
     float re = 0.f, im = 0.f;
 #pragma unroll
     for (int t = 0; t < kSpecTaps; ++t) {
-        const float w = bk_w[(size_t)j * kSpecTaps + t];
-        const float2 v = u[(b + t) & mask];
+        const float w = d.bk_w[(size_t)j * kSpecTaps + t];
+        const float2 v = uc[(b + t) & mask];
         re = fmaf(w, v.x, re);
         im = fmaf(w, v.y, im);
     }
-    const long long o = (long long)j * ld + blockIdx.y;
+    const long long o = (d.off + j) * ld + blockIdx.y;
     const double2 x = r[o];
     z[o] = make_double2(2.0 * x.x + (double)re, 2.0 * x.y + (double)im);
 }
@@ -206,24 +241,26 @@ __global__ void k_precond_sum(double2* __restrict__ z, const double2* __restrict
 
 // ---------------------------------------------------------------- host tables
 
-struct GaussLegendre {
-    std::vector<double> x, w;
-    explicit GaussLegendre(int n) : x(n), w(n) {
-        for (int i = 0; i < n; ++i) {
-            double z = std::cos(kPiH * (i + 0.75) / (n + 0.5)), dp = 1.0;
-            for (int it = 0; it < 100; ++it) {
-                double p0 = 1.0, p1 = z;
-                for (int m = 2; m <= n; ++m) { const double p2 = ((2 * m - 1) * z * p1 - (m - 1) * p0) / m; p0 = p1; p1 = p2; }
-                dp = n * (z * p1 - p0) / (z * z - 1.0);
-                const double dz = p1 / dp;
-                z -= dz;
-                if (std::fabs(dz) < 1e-16) break;
-            }
-            x[i] = z;
-            w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+// Q[j][m] = integral from -1 to z_j of the m-th Lagrange basis polynomial of the n first-kind
+// Chebyshev (Fejer) nodes z: node m's weight in the arc length from the patch's start to node j
+std::vector<double> cumulative_weights(const std::vector<double>& z) {
+    const int n = (int)z.size();
+    std::vector<double> Q((size_t)n * n, 0.0);
+    auto T = [](int k, double x) { return std::cos(k * std::acos(std::min(1.0, std::max(-1.0, x)))); };
+    auto I = [&](int k, double x) {   // integral of T_k from -1 to x
+        if (k == 0) return x + 1.0;
+        if (k == 1) return 0.5 * (x * x - 1.0);
+        const double lo = 0.5 * ((k % 2 ? 1.0 : -1.0) / (k + 1) - (k % 2 ? 1.0 : -1.0) / (k - 1));
+        return 0.5 * (T(k + 1, x) / (k + 1) - T(k - 1, x) / (k - 1)) - lo;
+    };
+    for (int j = 0; j < n; ++j)
+        for (int m = 0; m < n; ++m) {
+            double q = 0.0;
+            for (int k = 0; k < n; ++k) q += (k == 0 ? 1.0 : 2.0) / n * T(k, z[m]) * I(k, z[j]);
+            Q[(size_t)j * n + m] = q;
         }
-    }
-};
+    return Q;
+}
 
 int build_curve(const Discretisation& D, int c, double k, double eta, double eps, SpecCurve& out, std::string& err) {
     const HostCurve& C = D.curves[c];
@@ -245,32 +282,59 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
     out.lg = lg; out.lg1 = (lg + 1) / 2; out.lg2 = lg / 2;
     const long long nu = 1LL << lg;
     const int N1 = 1 << out.lg1, N2 = 1 << out.lg2;
-    static const GaussLegendre gl(24);
-    auto speed = [&](double t) { return std::hypot(C.xp(t), C.yp(t)); };
-    auto seg = [&](double a, double b) {
-        const double h = 0.5 * (b - a), m = 0.5 * (a + b);
-        double s = 0.0;
-        for (size_t i = 0; i < gl.x.size(); ++i) s += gl.w[i] * speed(m + h * gl.x[i]);
-        return h * s;
-    };
+    // arc lengths from the nodes' quadrature factors: a closed curve's node j of a patch on
+    // [a, b] has wq_j = (b - a) / 2 w_j |x'(t_j)| (Fejer weight w_j), so the patch length is
+    // sum_j wq_j and the length up to node j is sum_m Q[j][m] wq_m / w_m (spectral integration
+    // of the interpolant of |x'|)
+    const std::vector<double> Q = cumulative_weights(D.fej_n);
     std::vector<double> S(P + 1, 0.0);
-    for (int i = 0; i < P; ++i) S[i + 1] = S[i] + seg(D.t1[pats[i]], D.t2[pats[i]]);
+    for (int i = 0; i < P; ++i) {
+        double l = 0.0;
+        for (int j = 0; j < Np; ++j) l += D.wq[out.off + (long long)i * Np + j];
+        S[i + 1] = S[i] + l;
+    }
     const double L = S[P];
     out.length = L;
     const double h = L / (double)nu;
-    // barycentric weights of each patch's nodes in the patch's local coordinate
-    std::vector<double> loc((size_t)n), lam((size_t)n);
-    for (int i = 0; i < P; ++i) {
-        const int p = pats[i];
-        const double a = D.t1[p], b = D.t2[p];
-        for (int j = 0; j < Np; ++j) loc[(size_t)i * Np + j] = (2.0 * D.t[out.off + (long long)i * Np + j] - a - b) / (b - a);
-        for (int j = 0; j < Np; ++j) {
-            double q = 1.0;
-            for (int m = 0; m < Np; ++m) if (m != j) q *= loc[(size_t)i * Np + j] - loc[(size_t)i * Np + m];
-            lam[(size_t)i * Np + j] = 1.0 / q;
+    // per patch: its nodes' local coordinates and arc lengths, and the barycentric weights of
+    // both node sets (the grid point's local coordinate is interpolated from its arc length
+    // through the nodes, then its value from the nodes' values)
+    std::vector<double> loc((size_t)n), lam((size_t)n), sn((size_t)n), lams((size_t)n);
+    parallel_for(P, [&](long long i0, long long i1) {
+        for (long long i = i0; i < i1; ++i) {
+            const int p = pats[i];
+            const double a = D.t1[p], b = D.t2[p];
+            double* ln = &loc[(size_t)i * Np];
+            double* sl = &sn[(size_t)i * Np];
+            const double* wq = &D.wq[out.off + i * Np];
+            for (int j = 0; j < Np; ++j) {
+                const double t = D.t[out.off + i * Np + j];
+                ln[j] = (2.0 * t - a - b) / (b - a);
+                double acc = 0.0;
+                for (int m = 0; m < Np; ++m) acc += Q[(size_t)j * Np + m] * wq[m] / D.fej_w[m];
+                sl[j] = S[i] + acc;
+            }
+            for (int j = 0; j < Np; ++j) {
+                double q = 1.0, qs = 1.0;
+                for (int m = 0; m < Np; ++m)
+                    if (m != j) { q *= ln[j] - ln[m]; qs *= sl[j] - sl[m]; }
+                lam[(size_t)i * Np + j] = 1.0 / q;
+                lams[(size_t)i * Np + j] = 1.0 / qs;
+            }
         }
-    }
-    // forward: the grid point's parameter by Newton on its patch's arc length, then the weights
+    }, 16);
+    // barycentric interpolation through the nodes xs (weights lw) of values v, at x
+    auto bary = [&](const double* xs, const double* lw, double x, auto&& value) {
+        double num = 0.0, den = 0.0;
+        for (int j = 0; j < Np; ++j) {
+            if (x == xs[j]) return value(j);
+            const double c = lw[j] / (x - xs[j]);
+            num += c * value(j);
+            den += c;
+        }
+        return num / den;
+    };
+    // forward: each grid point's local coordinate in its patch, then its Np weights
     std::vector<int> fb((size_t)nu);
     std::vector<float> fw((size_t)nu * Np);
     parallel_for(nu, [&](long long g0, long long g1) {
@@ -278,36 +342,21 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
             const double sg = h * (double)g;
             int i = (int)(std::upper_bound(S.begin(), S.end(), sg) - S.begin()) - 1;
             i = std::min(std::max(i, 0), P - 1);
-            const int p = pats[i];
-            const double a = D.t1[p], b = D.t2[p];
-            double t = a + (sg - S[i]) / (S[i + 1] - S[i]) * (b - a);
-            for (int it = 0; it < 12; ++it) {   // quadratic convergence from the linear guess: 3 to 4 steps
-                const double dt = (S[i] + seg(a, t) - sg) / speed(t);
-                t = std::min(std::max(t - dt, a), b);
-                if (std::fabs(dt) < 1e-12 * (b - a)) break;
-            }
-            const double x = (2.0 * t - a - b) / (b - a);
-            fb[(size_t)g] = (int)(out.off + (long long)i * Np);
             const double* ln = &loc[(size_t)i * Np];
             const double* lm = &lam[(size_t)i * Np];
-            int exact = -1;
-            double den = 0.0;
-            for (int j = 0; j < Np; ++j) {
-                if (x == ln[j]) { exact = j; break; }
-                den += lm[j] / (x - ln[j]);
-            }
+            const double x = std::min(1.0, std::max(-1.0, bary(&sn[(size_t)i * Np], &lams[(size_t)i * Np], sg,
+                                                               [&](int j) { return ln[j]; })));
+            fb[(size_t)g] = (int)(out.off + (long long)i * Np);
             for (int j = 0; j < Np; ++j)
-                fw[(size_t)g * Np + j] = exact >= 0 ? (j == exact ? 1.f : 0.f) : (float)(lm[j] / (x - ln[j]) / den);
+                fw[(size_t)g * Np + j] = (float)bary(ln, lm, x, [&](int m) { return m == j ? 1.0 : 0.0; });
         }
     }, 256);
-    // back: each node's arc length, kSpecTaps-point Lagrange weights on the grid
+    // back: kSpecTaps-point Lagrange weights on the grid at each node's arc length
     std::vector<int> bb((size_t)n);
     std::vector<float> bw((size_t)n * kSpecTaps);
     parallel_for(n, [&](long long j0, long long j1) {
         for (long long j = j0; j < j1; ++j) {
-            const int i = (int)(j / Np);
-            const double sj = S[i] + seg(D.t1[pats[i]], D.t[out.off + j]);
-            const double x = sj / h;
+            const double x = sn[(size_t)j] / h;
             const long long q0 = (long long)std::floor(x) - (kSpecTaps / 2 - 1);
             const double xr = x - (double)q0;
             bb[(size_t)j] = (int)(((q0 % nu) + nu) % nu);
@@ -354,26 +403,20 @@ void free_spectral(ifgf2d_ctx* ctx) {
 
 // z = M r on the context's stream (capturable; the tables stay fixed until the next set-up):
 // B interleaved vectors (point i of vector b at i * B + b; B = 1 for one vector) through the
-// grid buffer `u` of B * biggest values
+// grid buffer `u` of B * spectral_grid_size(sw) values; four launches for all curves
 void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s) {
-    const long long us = sw->biggest;
-    for (auto& cp : sw->curves) {
-        const SpecCurve& c = *cp;
-        const int N1 = 1 << c.lg1, N2 = 1 << c.lg2, cols = std::min(kSpecTile, N2);
-        const size_t smc = sizeof(float2) * (size_t)N1 * cols;
-        const double2* rc = r + c.off * B;
-        double2* zc = z + c.off * B;
-        k_spec_fwd_cols<<<dim3(N2 / cols, B), kSpecThreads, smc, s>>>(r, B, c.fw_base.p, c.fw_w.p, Np, c.lg1, c.lg2, c.tw1.p,
-                                                                      c.twN.p, u, us);
-        k_spec_rows<<<dim3(N1, B), kSpecThreads, sizeof(float2) * N2, s>>>(u, us, c.mult.p, c.lg2, c.tw2.p, c.twN.p);
-        k_spec_inv_cols<<<dim3(N2 / cols, B), kSpecThreads, smc, s>>>(u, c.lg1, c.lg2, c.tw1.p, 1.0f / (float)(1LL << c.lg), u, us);
-        k_spec_back<<<dim3((c.n + 255) / 256, B), 256, 0, s>>>(rc, B, u, us, c.bk_base.p, c.bk_w.p, c.n, (1 << c.lg) - 1, zc);
-    }
+    const long long us = sw->grid_total;
+    const int nc = sw->ncurves;
+    const int* pre = sw->pre.p;
+    k_spec_fwd_cols<<<dim3(sw->blocks_cols, B), kSpecThreads, sw->smem_cols, s>>>(r, B, sw->desc.p, pre, nc, Np, u, us);
+    k_spec_rows<<<dim3(sw->blocks_rows, B), kSpecThreads, sw->smem_rows, s>>>(sw->desc.p, pre + (nc + 1), nc, u, us);
+    k_spec_inv_cols<<<dim3(sw->blocks_cols, B), kSpecThreads, sw->smem_cols, s>>>(sw->desc.p, pre, nc, u, us);
+    k_spec_back<<<dim3(sw->blocks_back, B), 256, 0, s>>>(r, B, sw->desc.p, pre + 2 * (nc + 1), nc, u, us, z);
 }
 void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s) {
     spectral_launch_batch(sw, r, z, 1, sw->u.p, Np, s);
 }
-long long spectral_grid_size(const SpectralWork* sw) { return sw ? sw->biggest : 0; }
+long long spectral_grid_size(const SpectralWork* sw) { return sw ? sw->grid_total : 0; }
 
 void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s) {
     k_precond_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(z, zn, r, n);
@@ -389,7 +432,7 @@ int spectral_setup(ifgf2d_ctx* ctx, double scale, const double* curve_k, const d
     if (ctx->gw) ctx->gw->drop_graphs();
     free_spectral(ctx);
     std::unique_ptr<SpectralWork> sw(new SpectralWork);
-    long long covered = 0, biggest = 0;
+    long long covered = 0;
     for (int c = 0; c < (int)D.curves.size(); ++c) {
         std::unique_ptr<SpecCurve> sc(new SpecCurve);
         std::string err;
@@ -397,12 +440,31 @@ int spectral_setup(ifgf2d_ctx* ctx, double scale, const double* curve_k, const d
         const int rc = build_curve(D, c, kc, ec, scale * std::cbrt(kc), *sc, err);
         if (rc != IFGF2D_OK) return fail(ctx, rc, err);
         covered += sc->n;
-        biggest = std::max(biggest, 1LL << sc->lg);
         sw->curves.push_back(std::move(sc));
     }
     if (covered != D.N) return fail(ctx, IFGF2D_ERR_ARG, "the spectral preconditioner needs every point on a closed curve");
-    CK(sw->u.alloc((size_t)biggest));
-    sw->biggest = biggest;
+    const int nc = (int)sw->curves.size();
+    std::vector<SpecDesc> desc(nc);
+    std::vector<int> pre(3 * (nc + 1), 0);
+    long long uoff = 0, bc = 0, br = 0, bb = 0;
+    for (int c = 0; c < nc; ++c) {
+        const SpecCurve& sc = *sw->curves[c];
+        const int N1 = 1 << sc.lg1, N2 = 1 << sc.lg2, cols = std::min(kSpecTile, N2);
+        desc[c] = SpecDesc{sc.off, uoff, sc.n, sc.lg, sc.lg1, sc.lg2, sc.fw_base.p, sc.fw_w.p, sc.bk_base.p, sc.bk_w.p,
+                           sc.mult.p, sc.twN.p, sc.tw1.p, sc.tw2.p};
+        pre[c] = (int)bc; pre[(nc + 1) + c] = (int)br; pre[2 * (nc + 1) + c] = (int)bb;
+        bc += N2 / cols; br += N1; bb += (sc.n + 255) / 256;
+        uoff += 1LL << sc.lg;
+        sw->smem_cols = std::max(sw->smem_cols, sizeof(float2) * (size_t)N1 * cols);
+        sw->smem_rows = std::max(sw->smem_rows, sizeof(float2) * (size_t)N2);
+    }
+    if (bc > (1LL << 30) || br > (1LL << 30) || bb > (1LL << 30)) return fail(ctx, IFGF2D_ERR_ARG, "too many curves for the spectral preconditioner");
+    pre[nc] = (int)bc; pre[2 * nc + 1] = (int)br; pre[3 * nc + 2] = (int)bb;
+    sw->ncurves = nc; sw->blocks_cols = (int)bc; sw->blocks_rows = (int)br; sw->blocks_back = (int)bb;
+    sw->grid_total = uoff;
+    CK(sw->desc.upload(desc));
+    CK(sw->pre.upload(pre));
+    CK(sw->u.alloc((size_t)uoff));
     sw->scale = scale;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->sw = sw.release();
