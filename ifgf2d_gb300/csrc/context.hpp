@@ -303,4 +303,7 @@ void launch_sort_plan(const long long* pp_ptr, int ncones, const PropE<double>* 
 // the complex64 copy of the interpolation plan
 void launch_interp_to_c64(const InterpE<double>* in, long long n, InterpE<float>* out, cudaStream_t s);
 void net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cudaStream_t s);
+// after a synchronisation: IFGF2D_ERR_CUDA (and the flag cleared) when one of the network's
+// tensor-core convolutions gave up waiting for its MMAs, else IFGF2D_OK
+int net_kernel_error(ifgf2d_net* net);
 }  // namespace ifgf

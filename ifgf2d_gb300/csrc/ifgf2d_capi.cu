@@ -1124,6 +1124,8 @@ static int solve_flexible(ifgf2d_ctx* ctx, RightPrecond P, const double* rhs, do
     if (iters_out) *iters_out = iters;
     if (err_out) *err_out = est;
     if (int rk = check_kerr(ctx)) return rk;
+    if (P.net && net_kernel_error(P.net) != IFGF2D_OK)
+        return fail(ctx, IFGF2D_ERR_CUDA, "learned preconditioner: a tensor-core completion wait ran out");
     return est < tol ? IFGF2D_OK : IFGF2D_ERR_NOCONV;
 }
 

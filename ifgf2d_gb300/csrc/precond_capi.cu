@@ -26,6 +26,7 @@ struct ifgf2d_net {
     DBuf<__nv_bfloat16> X[kNetLayers], Y[kNetLayers], gbf;
     DBuf<float> O, T, gO, G, dpre, dX, part, sigma;
     DBuf<double> loss;
+    DBuf<int> kerr;                 // set by a convolution whose bounded tensor-core wait ran out
     DBuf<double2> r, e, z;
     DBuf<double4> geom;
     DBuf<double> kseg;
@@ -117,21 +118,21 @@ void net_forward(ifgf2d_net* net, const double2* r, const double4* geom, bool ke
     launch_halo(net->X[0].p, kNetInPad, net->seg_start.p, net->seg_len.p, net->nseg, s);
     const float* p = net->p.p;
     launch_conv_fwd(net->X[0].p, (int)R, kNetInPad, net->Wt[0].p, p + net->off_b[0], kNetHidden, true, false, net->X[1].p,
-                    nullptr, s);
+                    nullptr, net->kerr.p, s);
     launch_halo(net->X[1].p, kNetHidden, net->seg_start.p, net->seg_len.p, net->nseg, s);
     for (int l = 1; l < kNetLayers - 1; ++l) {
         if (keep_relu) {
             launch_conv_fwd(net->X[l].p, (int)R, kNetHidden, net->Wt[l].p, p + net->off_b[l], kNetHidden, true, false, net->Y[l].p,
-                            nullptr, s);
+                            nullptr, net->kerr.p, s);
             launch_add_bf(net->Y[l].p, net->X[l].p, R * kNetHidden, net->X[l + 1].p, s);
         } else {
             launch_conv_fwd(net->X[l].p, (int)R, kNetHidden, net->Wt[l].p, p + net->off_b[l], kNetHidden, true, true,
-                            net->X[l + 1].p, nullptr, s);
+                            net->X[l + 1].p, nullptr, net->kerr.p, s);
         }
         launch_halo(net->X[l + 1].p, kNetHidden, net->seg_start.p, net->seg_len.p, net->nseg, s);
     }
     const int L = kNetLayers - 1;
-    launch_conv_fwd(net->X[L].p, (int)R, kNetHidden, net->Wt[L].p, p + net->off_b[L], kNetOutPad, false, false, nullptr, net->O.p,
+    launch_conv_fwd(net->X[L].p, (int)R, kNetHidden, net->Wt[L].p, p + net->off_b[L], kNetOutPad, false, false, nullptr, net->O.p, net->kerr.p,
                     s);
 }
 
@@ -148,7 +149,7 @@ void net_backward(ifgf2d_net* net, cudaStream_t s) {
     launch_conv_wgrad(net->X[L].p, net->gO.p, nullptr, (int)R, kNetHidden, kNetOutPad, net->part.p, g + net->off_w[L],
                       g + net->off_b[L], s);
     launch_f2bf(net->gO.p, R * kNetOutPad, net->gbf.p, s);
-    launch_conv_fwd(net->gbf.p, (int)R, kNetOutPad, net->Wb[L].p, net->zero_bias.p, kNetHidden, false, false, nullptr, net->G.p, s);
+    launch_conv_fwd(net->gbf.p, (int)R, kNetOutPad, net->Wb[L].p, net->zero_bias.p, kNetHidden, false, false, nullptr, net->G.p, net->kerr.p, s);
     launch_halo_fold(net->G.p, kNetHidden, net->seg_start.p, net->seg_len.p, net->nseg, s);
     for (int l = L - 1; l >= 1; --l) {
         // X[l+1] = relu(conv_l(X[l])) + X[l]: G holds dL/dX[l+1]
@@ -156,7 +157,7 @@ void net_backward(ifgf2d_net* net, cudaStream_t s) {
         launch_conv_wgrad(net->X[l].p, net->dpre.p, nullptr, (int)R, kNetHidden, kNetHidden, net->part.p, g + net->off_w[l],
                           g + net->off_b[l], s);
         launch_conv_fwd(net->gbf.p, (int)R, kNetHidden, net->Wb[l].p, net->zero_bias.p, kNetHidden, false, false, nullptr,
-                        net->dX.p, s);
+                        net->dX.p, net->kerr.p, s);
         launch_halo_fold(net->dX.p, kNetHidden, net->seg_start.p, net->seg_len.p, net->nseg, s);
         launch_axpy_f(net->dX.p, R * kNetHidden, net->G.p, s);
     }
@@ -177,6 +178,16 @@ int net_stage(ifgf2d_net* net, int nseg, const int* len, const double* r, const 
     return IFGF2D_OK;
 }
 
+// after a synchronisation: did a convolution give up waiting for its tensor-core MMAs?
+int net_check_kerr(ifgf2d_net* net) {
+    int v = 0;
+    NK(cudaMemcpy(&v, net->kerr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!v) return IFGF2D_OK;
+    NK(cudaMemset(net->kerr.p, 0, sizeof(int)));
+    net->err = "network convolution: a tensor-core completion wait ran out";
+    return IFGF2D_ERR_CUDA;
+}
+
 }  // namespace
 
 int ifgf::net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, double k, std::string& err) {
@@ -192,6 +203,7 @@ int ifgf::net_prepare_single(ifgf2d_net* net, long long N, const double* geom_ho
     }
     return IFGF2D_OK;
 }
+int ifgf::net_kernel_error(ifgf2d_net* net) { return net_check_kerr(net); }
 void ifgf::net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cudaStream_t s) {
     net_forward(net, r, net->geom.p, false, s);
     launch_combine(r, net->O.p, net->sigma.p, net->pt_row.p, net->pt_seg.p, (int)net->npts, z, s);
@@ -228,8 +240,9 @@ extern "C" int ifgf2d_net_create(unsigned long long seed, ifgf2d_net** out) {
                 for (int ci = 0; ci < cin_real; ++ci) h[net->off_w[l] + ((long long)co * kNetTaps + tap) * cin + ci] = (float)nd(rng);
     }
     if (bad(net->p.upload(h)) || bad(net->g.alloc(off)) || bad(net->m.alloc(off)) || bad(net->v.alloc(off)) ||
-        bad(net->zero_bias.alloc(kNetHidden)) || bad(net->loss.alloc(1)))
+        bad(net->zero_bias.alloc(kNetHidden)) || bad(net->loss.alloc(1)) || bad(net->kerr.alloc(1)))
         return IFGF2D_ERR_CUDA;
+    cudaMemsetAsync(net->kerr.p, 0, sizeof(int), net->stream);
     cudaMemsetAsync(net->m.p, 0, sizeof(float) * off, net->stream);
     cudaMemsetAsync(net->v.p, 0, sizeof(float) * off, net->stream);
     cudaMemsetAsync(net->zero_bias.p, 0, sizeof(float) * kNetHidden, net->stream);
@@ -282,7 +295,7 @@ extern "C" int ifgf2d_net_gradient(ifgf2d_net* net, int nseg, const int* len, co
     NK(cudaMemcpyAsync(loss, net->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     if (grad) NK(cudaMemcpyAsync(grad, net->g.p, sizeof(float) * net->nparam, cudaMemcpyDeviceToHost, s));
     NK(cudaStreamSynchronize(s));
-    return IFGF2D_OK;
+    return net_check_kerr(net);
 }
 
 extern "C" int ifgf2d_net_train_step(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* e, const double* geom,
@@ -298,7 +311,7 @@ extern "C" int ifgf2d_net_train_step(ifgf2d_net* net, int nseg, const int* len, 
     NK(cudaGetLastError());
     if (loss) NK(cudaMemcpyAsync(loss, net->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     NK(cudaStreamSynchronize(s));
-    return IFGF2D_OK;
+    return net_check_kerr(net);
 }
 
 extern "C" int ifgf2d_net_apply(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* geom, const double* k,
@@ -325,7 +338,7 @@ extern "C" int ifgf2d_net_apply(ifgf2d_net* net, int nseg, const int* len, const
         }
     }
     NK(cudaStreamSynchronize(s));
-    return IFGF2D_OK;
+    return net_check_kerr(net);
 }
 
 // per point of the context, patch order: curvature, unit tangent (x, y), quadrature weight

@@ -1,94 +1,154 @@
 // precond_net.cu -- kernels of the learned right preconditioner (see precond_net.cuh).
 //
-// The convolutions are implicit GEMMs on the tensor cores: M = 64 rows per block (16 per
-// warp), N = the output channels, K = 7 taps x input channels, BF16 operands with FP32
-// accumulation through mma.sync m16n8k16.  A block stages its input rows (with the 3-row
-// reach on either side) and the whole packed weight matrix in shared memory, rows padded by
-// 8 elements so the fragment loads are free of bank conflicts.  The backward data pass is the
-// same kernel on the packed transposed weights (taps flipped, channels swapped).  Weight
-// gradients are FP32 sums over rows: per-block partials of a 4 x 4 (co, ci) tile per tap,
-// then a reduction.
+// The convolutions are implicit GEMMs on the fifth-generation tensor cores (tcgen05.mma
+// kind::f16, BF16 operands, FP32 accumulation in tensor memory): per CTA M = 128 rows, N = the
+// output channels, K = 7 taps x input channels.  The CTA stages its input rows (with the 3-row
+// reach on either side) and the packed weight matrix in shared memory in the K-major
+// no-swizzle core-matrix layout; because each 8-channel slab of the input tile stores its rows
+// contiguously (16 bytes per row), the operand of tap t is the same tile with its descriptor's
+// start moved by t rows, so no im2col copy is made.  One thread issues the 7 x CIN/16 MMAs and
+// commits them to an mbarrier (bounded wait); the four warps read the accumulator rows back
+// from tensor memory for the epilogue (bias, ReLU, residual).  The backward data pass is the same
+// kernel on the packed transposed weights (taps flipped, channels swapped).  Weight gradients
+// are FP32 sums over rows: per-block partials of a 4 x 4 (co, ci) tile per tap, then a
+// reduction.
 #include "precond_net.cuh"
+#include "tcgen05.cuh"
 #include <cstdint>
 
 namespace ifgf {
 
 static inline unsigned nblk_n(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-__device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                         uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-        "{%0, %1, %2, %3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+constexpr int kConvRows = 128;                        // rows per CTA: the MMA's M
+constexpr int kConvIRows = kConvRows + 2 * kHalo;     // staged input rows
+constexpr long long kConvWaitCycles = 2000000000ll;   // about one second at 2 GHz
+
+template <int CIN> __host__ __device__ constexpr int conv_in_bytes() { return kConvIRows * CIN * 2; }
+template <int CIN, int COUT> __host__ __device__ constexpr int conv_w_bytes() { return COUT * kNetTaps * CIN * 2; }
+// dynamic shared memory per CTA: the tiles, the mbarrier and the TMEM address, and at least 29 KB,
+// so that at most 7 CTAs share an SM and their tensor memory (at most 64 columns each) never
+// exceeds the SM's 512 columns: tcgen05.alloc never has to wait
+template <int CIN, int COUT> __host__ __device__ constexpr int conv_smem() {
+    return conv_in_bytes<CIN>() + conv_w_bytes<CIN, COUT>() + 16 > 29 * 1024 ? conv_in_bytes<CIN>() + conv_w_bytes<CIN, COUT>() + 16
+                                                                              : 29 * 1024;
 }
 
-constexpr int kConvRows = 64;   // rows per block (4 warps x 16)
+// instruction descriptor of kind::f16 with BF16 operands: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 in bits 17-22, M / 16 in bits 24-28
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// D (+)= A B^T, K = 16, issued by one thread
+__device__ __forceinline__ void mma_bf16_tc(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
 
+// out[r][co] = act(bias[co] + sum_{tap, ci} Wt[co][tap * CIN + ci] in[r + tap - 3][ci]) (+ in[r][co])
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16* __restrict__ in, int rows,
-                                                  const __nv_bfloat16* __restrict__ Wt, const float* __restrict__ bias,
-                                                  int relu, int residual, __nv_bfloat16* __restrict__ out_bf,
-                                                  float* __restrict__ out_f32) {
+__global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict__ in, int rows,
+                                                 const __nv_bfloat16* __restrict__ Wt, const float* __restrict__ bias,
+                                                 int relu, int residual, __nv_bfloat16* __restrict__ out_bf,
+                                                 float* __restrict__ out_f32, int* __restrict__ err) {
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "K steps of 16, N a multiple of 16");
     constexpr int K = kNetTaps * CIN;
-    constexpr int SIN = CIN + 8, SW = K + 8, NT = COUT / 8;
-    constexpr int IROWS = kConvRows + 2 * kHalo;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* s_in = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    __nv_bfloat16* s_w = s_in + IROWS * SIN;
-    const int tid = threadIdx.x;
+    constexpr uint32_t LBO_A = kConvIRows * 16;          // between the input tile's 8-channel slabs
+    constexpr uint32_t LBO_B = (COUT / 8) * 128;         // between the weights' 8-wide K slabs
+    constexpr uint32_t TCOLS = COUT < 32 ? 32 : COUT;    // tensor-memory columns (a power of 2, >= 32)
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char* s_in = sm;                                          // [CIN/8][IROWS][8] BF16
+    unsigned char* s_w = sm + conv_in_bytes<CIN>();                    // [K/8][COUT/8][8][8] BF16
+    unsigned char* s_bar = s_w + conv_w_bytes<CIN, COUT>();            // mbarrier, then the TMEM address
+    const uint32_t bar = tc5::smem_u32(s_bar), tslot = tc5::smem_u32(s_bar + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
     const long long n0 = (long long)blockIdx.x * kConvRows;
-    // input rows n0 - 3 .. n0 + 66, 16-byte chunks; rows outside [0, rows) are zero
-    for (int q = tid; q < IROWS * (CIN / 8); q += blockDim.x) {
+    if (tid == 0) tc5::mbar_init(bar, 1);
+    if (warp == 0) tc5::tmem_alloc(tslot, TCOLS);
+    // input rows n0 - 3 .. n0 + 130 in 16-byte chunks; rows outside [0, rows) are zero
+    for (int q = tid; q < kConvIRows * (CIN / 8); q += blockDim.x) {
         const int r = q / (CIN / 8), c8 = q % (CIN / 8);
         const long long gr = n0 - kHalo + r;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (gr >= 0 && gr < rows) v = *reinterpret_cast<const uint4*>(in + gr * CIN + c8 * 8);
-        *reinterpret_cast<uint4*>(s_in + r * SIN + c8 * 8) = v;
+        *reinterpret_cast<uint4*>(s_in + c8 * LBO_A + r * 16) = v;
     }
     for (int q = tid; q < COUT * (K / 8); q += blockDim.x) {
         const int co = q / (K / 8), k8 = q % (K / 8);
-        *reinterpret_cast<uint4*>(s_w + co * SW + k8 * 8) = *reinterpret_cast<const uint4*>(Wt + (long long)co * K + k8 * 8);
+        *reinterpret_cast<uint4*>(s_w + k8 * LBO_B + (co >> 3) * 128 + (co & 7) * 16) =
+            *reinterpret_cast<const uint4*>(Wt + (long long)co * K + k8 * 8);
     }
+    tc5::fence_async_smem();
+    tc5::fence_before_sync();
     __syncthreads();
-    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, tig = lane & 3;
-    float acc[NT][4];
+    tc5::fence_after_sync();
+    const uint32_t tmem = *(volatile uint32_t*)(s_bar + 8);
+    bool ok = true;
+    if (tid == 0) {
+        const uint32_t idesc = idesc_bf16(kConvRows, COUT);
+        const uint32_t a0 = tc5::smem_u32(s_in), b0 = tc5::smem_u32(s_w);
+        uint32_t acc = 0;
+#pragma unroll 1
+        for (int tap = 0; tap < kNetTaps; ++tap)
 #pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-#pragma unroll 4
-    for (int ks = 0; ks < K / 16; ++ks) {
-        const int kk0 = ks * 16;
-        const int tap = kk0 / CIN, ci0 = kk0 % CIN;
-        // A[row][k] = input row (row + tap) of the staged window, channel ci0 + k
-        const __nv_bfloat16* a = s_in + (warp * 16 + g + tap) * SIN + ci0 + tig * 2;
-        const uint32_t a0 = *reinterpret_cast<const uint32_t*>(a);
-        const uint32_t a1 = *reinterpret_cast<const uint32_t*>(a + 8 * SIN);
-        const uint32_t a2 = *reinterpret_cast<const uint32_t*>(a + 8);
-        const uint32_t a3 = *reinterpret_cast<const uint32_t*>(a + 8 * SIN + 8);
+            for (int c = 0; c < CIN / 16; ++c) {
+                const uint32_t a = a0 + 2 * c * LBO_A + tap * 16;                 // rows shifted by the tap
+                const uint32_t b = b0 + ((tap * CIN + 16 * c) / 8) * LBO_B;
+                mma_bf16_tc(tmem, tc5::smem_desc(a, LBO_A, 128), tc5::smem_desc(b, LBO_B, 128), idesc, acc);
+                acc = 1u;
+            }
+        tc5::commit(bar);
+        ok = tc5::mbar_wait(bar, 0, kConvWaitCycles);
+    }
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) {
+            atomicExch(err, 1);
+            tc5::mbar_wait(bar, 0, kConvWaitCycles);   // the MMAs in flight, before the memory goes
+        }
+        tc5::fence_before_sync();
+        __syncthreads();
+        if (warp == 0) tc5::tmem_dealloc(tmem, TCOLS);
+        return;
+    }
+    tc5::fence_after_sync();
+    // warp w reads accumulator rows 32 w .. 32 w + 31 (its tensor-memory lanes): one row per thread
+    const int row = 32 * warp + (tid & 31);
+    const long long gr = n0 + row;
+    const uint32_t tread = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+        float v[16];
+        tc5::tmem_ld16(tread + c0, v);   // warp-collective: every lane loads, then rows past the end skip the stores
+        if (gr < rows) {
 #pragma unroll
-        for (int j = 0; j < NT; ++j) {
-            const __nv_bfloat16* b = s_w + (j * 8 + g) * SW + kk0 + tig * 2;
-            mma_bf16(acc[j], a0, a1, a2, a3, *reinterpret_cast<const uint32_t*>(b), *reinterpret_cast<const uint32_t*>(b + 8));
+            for (int j = 0; j < 16; ++j) {
+                const int col = c0 + j;
+                float x = v[j] + bias[col];
+                if (relu) x = fmaxf(x, 0.f);
+                if (residual)   // CIN == COUT
+                    x += __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(s_in + (col >> 3) * LBO_A + (row + kHalo) * 16 +
+                                                                                   (col & 7) * 2));
+                v[j] = x;
+            }
+            if (out_f32) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 4)
+                    *reinterpret_cast<float4*>(out_f32 + gr * COUT + c0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            }
+            if (out_bf) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 2)
+                    *reinterpret_cast<__nv_bfloat162*>(out_bf + gr * COUT + c0 + j) = __floats2bfloat162_rn(v[j], v[j + 1]);
+            }
         }
     }
-#pragma unroll
-    for (int j = 0; j < NT; ++j)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int row = warp * 16 + g + 8 * h;
-            const long long gr = n0 + row;
-            if (gr >= rows) continue;
-            const int col = j * 8 + tig * 2;
-            float v0 = acc[j][2 * h] + bias[col], v1 = acc[j][2 * h + 1] + bias[col + 1];
-            if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-            if (residual) {   // CIN == COUT
-                const __nv_bfloat16* xr = s_in + (row + kHalo) * SIN + col;
-                v0 += __bfloat162float(xr[0]); v1 += __bfloat162float(xr[1]);
-            }
-            if (out_f32) { out_f32[gr * COUT + col] = v0; out_f32[gr * COUT + col + 1] = v1; }
-            if (out_bf) *reinterpret_cast<__nv_bfloat162*>(out_bf + gr * COUT + col) = __floats2bfloat162_rn(v0, v1);
-        }
+    tc5::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc5::tmem_dealloc(tmem, TCOLS);
 }
 
 __global__ void k_halo(__nv_bfloat16* __restrict__ buf, int C, const int* __restrict__ seg_start, const int* __restrict__ seg_len,
@@ -331,16 +391,15 @@ __global__ void k_halo_fold(float* __restrict__ G, int C, const int* __restrict_
 
 // ------------------------------------------------------------------ launchers
 void launch_conv_fwd(const __nv_bfloat16* in, int rows, int cin, const __nv_bfloat16* Wt, const float* bias, int cout,
-                     bool relu, bool residual, __nv_bfloat16* out_bf, float* out_f32, cudaStream_t s) {
+                     bool relu, bool residual, __nv_bfloat16* out_bf, float* out_f32, int* err, cudaStream_t s) {
     if (rows <= 0) return;
     const unsigned grid = nblk_n(rows, kConvRows);
-    auto smem = [](int ci, int co) { return (size_t)((kConvRows + 2 * kHalo) * (ci + 8) + co * (kNetTaps * ci + 8)) * 2; };
     if (cin == 16 && cout == 64) {
-        k_conv_fwd<16, 64><<<grid, 128, smem(16, 64), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32);
+        k_conv_tc<16, 64><<<grid, 128, conv_smem<16, 64>(), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32, err);
     } else if (cin == 64 && cout == 64) {
-        k_conv_fwd<64, 64><<<grid, 128, smem(64, 64), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32);
+        k_conv_tc<64, 64><<<grid, 128, conv_smem<64, 64>(), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32, err);
     } else if (cin == 64 && cout == 16) {
-        k_conv_fwd<64, 16><<<grid, 128, smem(64, 16), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32);
+        k_conv_tc<64, 16><<<grid, 128, conv_smem<64, 16>(), s>>>(in, rows, Wt, bias, relu, residual, out_bf, out_f32, err);
     }
 }
 void launch_halo(__nv_bfloat16* buf, int C, const int* seg_start, const int* seg_len, int nseg, cudaStream_t s) {
@@ -349,8 +408,10 @@ void launch_halo(__nv_bfloat16* buf, int C, const int* seg_start, const int* seg
 }
 cudaError_t conv_init_attributes() {
     // dynamic shared memory above 48 KB needs the opt-in (a per-device function attribute)
-    const int bytes = ((kConvRows + 2 * kHalo) * (64 + 8) + 64 * (kNetTaps * 64 + 8)) * 2;
-    return cudaFuncSetAttribute(k_conv_fwd<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_conv_tc<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem<64, 64>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv_tc<64, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem<64, 16>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv_tc<16, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem<16, 64>());
+    return e;
 }
 int conv_wgrad_chunks(int rows) { return (int)nblk_n(rows, kWgRows); }
 void launch_conv_wgrad(const __nv_bfloat16* x, const float* g, const unsigned char* /*row_mask*/, int rows, int cin, int cout,

@@ -41,8 +41,9 @@ inline int net_cout(int l) { return l == kNetLayers - 1 ? kNetOutPad : kNetHidde
 // one convolution over padded rows [0, rows): out[r][co] = act(b[co] + sum_{tap, ci}
 // Wt[co][tap * CIN + ci] in[r + tap - 3][ci]) (+ in[r][co] when residual); rows outside
 // [0, rows) read as zero.  out_f32 (optional) receives the FP32 values, out_bf (optional) BF16.
+// On tcgen05 tensor cores; *err is set when a CTA's bounded wait for its MMAs ran out.
 void launch_conv_fwd(const __nv_bfloat16* in, int rows, int cin, const __nv_bfloat16* Wt, const float* bias, int cout,
-                     bool relu, bool residual, __nv_bfloat16* out_bf, float* out_f32, cudaStream_t s);
+                     bool relu, bool residual, __nv_bfloat16* out_bf, float* out_f32, int* err, cudaStream_t s);
 // the per-device kernel attributes the convolutions need (call on the device before use,
 // outside stream capture)
 cudaError_t conv_init_attributes();

@@ -37,7 +37,7 @@
 
 namespace ifgf {
 
-constexpr int kSpecTile = 4;      // grid columns per block of the column FFTs
+constexpr int kSpecTile = 2;      // grid columns per block of the column FFTs (more blocks: these kernels are latency-bound)
 constexpr int kSpecTaps = 8;      // back-interpolation taps
 constexpr int kSpecThreads = 256;
 constexpr int kSpecMinLog = 6;    // smallest grid: 64 points
@@ -279,7 +279,7 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
     if (lg > kSpecMaxLog) { err = "the spectral preconditioner takes at most 2^20 points per curve"; return IFGF2D_ERR_ARG; }
     out.off = (long long)pats[0] * Np;
     out.n = (int)n;
-    out.lg = lg; out.lg1 = (lg + 1) / 2; out.lg2 = lg / 2;
+    out.lg = lg; out.lg1 = lg / 2; out.lg2 = lg - lg / 2;   // N2 >= N1: N2 / kSpecTile column blocks
     const long long nu = 1LL << lg;
     const int N1 = 1 << out.lg1, N2 = 1 << out.lg2;
     // arc lengths from the nodes' quadrature factors: a closed curve's node j of a patch on
