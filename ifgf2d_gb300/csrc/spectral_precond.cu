@@ -340,7 +340,8 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
     parallel_for(nu, [&](long long g0, long long g1) {
         for (long long g = g0; g < g1; ++g) {
             const double sg = h * (double)g;
-            int i = (int)(std::upper_bound(S.begin(), S.end(), sg) - S.begin()) - 1;
+            // a grid point on a patch boundary (up to rounding) belongs to the patch that starts there
+            int i = (int)(std::upper_bound(S.begin(), S.end(), sg + 1e-10 * L) - S.begin()) - 1;
             i = std::min(std::max(i, 0), P - 1);
             const double* ln = &loc[(size_t)i * Np];
             const double* lm = &lam[(size_t)i * Np];

@@ -73,10 +73,12 @@ class CurveTables:
         self.L = L = S[-1]
         patch = np.repeat(np.arange(P), Np)
         self.s_nodes = S[patch] + seg(t1[patch], tp)
-        # uniform grid: parameter by Newton on the patch's arc length
+        # uniform grid: parameter by Newton on the patch's arc length (the device interpolates it
+        # through the nodes' arc lengths instead; both agree to rounding)
         h = L / self.nu
         su = h * np.arange(self.nu)
-        pu = np.clip(np.searchsorted(S, su, side="right") - 1, 0, P - 1)
+        # a grid point on a patch boundary (up to rounding) belongs to the patch that starts there
+        pu = np.clip(np.searchsorted(S, su + 1e-10 * L, side="right") - 1, 0, P - 1)
         a, b = t1[pu], t2[pu]
         t = a + (su - S[pu]) / Lp[pu] * (b - a)
         for _ in range(12):
@@ -128,8 +130,8 @@ class CurveTables:
         return 1.0 / sig - 2.0
 
 
-def eps_default(k, scale=0.4):
-    """The glancing damping eps = scale k^(1/3) (curvature 1)."""
+def eps_default(k, scale=0.25):
+    """The glancing damping eps = scale k^(1/3), the device's default scale."""
     return scale * k ** (1.0 / 3.0)
 
 
