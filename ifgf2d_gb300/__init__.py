@@ -536,10 +536,18 @@ class ForwardMap:
 
     def spectral_apply(self, r):
         """z = M r with the spectral preconditioner (host vectors)"""
+        return self.spectral_symbol(r, "preconditioner")
+
+    def spectral_symbol(self, r, which="preconditioner"):
+        """z = Op(m) r along the curves with the spectral tables: m = the preconditioner's
+        1/sigma ("preconditioner"), the flat symbol's magnitude |sigma| ("magnitude") or its
+        inverse ("inverse_magnitude")"""
+        kinds = {"preconditioner": 0, "magnitude": 1, "inverse_magnitude": 2}
         n = self.total_num_unknowns_
         rin = _cview(r, n)
         z = np.empty(n, dtype=np.complex128)
-        _check(_lib.load().ifgf2d_spectral_apply(self._h, _dp(rin.view(np.float64)), _dp(z.view(np.float64))), self._h)
+        _check(_lib.load().ifgf2d_spectral_symbol(self._h, kinds[which], _dp(rin.view(np.float64)), _dp(z.view(np.float64))),
+               self._h)
         return z
 
     def solve_flexible(self, rhs, precond="spectral", net=None, accelerated=True, tol=None, restart=None, max_iters=None,

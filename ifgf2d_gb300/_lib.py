@@ -39,7 +39,8 @@ EXPORTS = [
     "ifgf2d_group_create", "ifgf2d_group_destroy", "ifgf2d_group_last_error", "ifgf2d_group_num_unknowns",
     "ifgf2d_group_offsets", "ifgf2d_group_apply", "ifgf2d_group_solve",
     "ifgf2d_spectral_setup", "ifgf2d_spectral_apply", "ifgf2d_solve_flexible", "ifgf2d_solve_batch_flexible",
-    "ifgf2d_group_solve_flexible",
+    "ifgf2d_group_solve_flexible", "ifgf2d_spectral_symbol", "ifgf2d_net_set_output_weighting",
+    "ifgf2d_net_output_weighting",
 ]
 
 
@@ -127,6 +128,9 @@ def load(build_if_missing: bool = True):
                                            ctypes.POINTER(ctypes.c_int), D]
         L.ifgf2d_spectral_setup.argtypes = [P, ctypes.c_double]
         L.ifgf2d_spectral_apply.argtypes = [P, D, D]
+        L.ifgf2d_spectral_symbol.argtypes = [P, ctypes.c_int, D, D]
+        L.ifgf2d_net_set_output_weighting.argtypes = [P, ctypes.c_int]
+        L.ifgf2d_net_output_weighting.argtypes = [P]
         L.ifgf2d_solve_flexible.argtypes = [P, P, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int), D]
         L.ifgf2d_group_solve_flexible.argtypes = [P, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,

@@ -110,7 +110,7 @@ struct GmresWork {
     long long sn = 0;
     // flexible GMRES with the learned preconditioner: z_j = M(v_j) for every column, and the
     // preconditioner's output buffer the captured iteration writes before copying it into Z
-    DBuf<double2> Z, zt, zt2;   // zt2: the network's output when it corrects the spectral preconditioner
+    DBuf<double2> Z, zt, zt2, zt3;   // zt2, zt3: the network's output and its weighting, when it corrects the spectral preconditioner
     DBuf<double> nrm2;
     DBuf<int> jdev;
     // least squares on the device (LsqDev): rotated columns, rotated right-hand side, rotations,
@@ -274,10 +274,11 @@ void free_eval(ifgf2d_ctx* ctx);
 // the next set-up)
 int spectral_setup(ifgf2d_ctx* ctx, double scale, const double* curve_k = nullptr, const double* curve_eta = nullptr);
 void free_spectral(ifgf2d_ctx* ctx);
-void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s);
+// which: 0 the preconditioner z = M r, 1 the flat symbol's magnitude |sigma|, 2 its inverse
+void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s, int which = 0);
 // the same for B interleaved vectors (point i of vector b at i * B + b), through a grid buffer
 // of B * spectral_grid_size(sw) complex64 values
-void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s);
+void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s, int which = 0);
 long long spectral_grid_size(const SpectralWork* sw);
 // z += zn - 2 r (the learned network's output zn correcting the spectral preconditioner's z)
 void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s);
@@ -306,4 +307,8 @@ void net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cuda
 // after a synchronisation: IFGF2D_ERR_CUDA (and the flag cleared) when one of the network's
 // tensor-core convolutions gave up waiting for its MMAs, else IFGF2D_OK
 int net_kernel_error(ifgf2d_net* net);
+// the network's output is |sigma|-weighted (ifgf2d_net_set_output_weighting)
+bool net_weighted(const ifgf2d_net* net);
+// z = a x + b y (z may be x or y)
+void launch_axpby(double2* z, double a, const double2* x, double b, const double2* y, long long n, cudaStream_t s);
 }  // namespace ifgf

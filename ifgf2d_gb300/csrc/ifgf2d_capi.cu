@@ -868,12 +868,12 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
         CK(G.part.alloc((size_t)arnoldi_part_size(N, m)));
         CK(G.lsR.alloc((size_t)ldh * m)); CK(G.lsg.alloc(m + 1)); CK(G.lsgc.alloc(m)); CK(G.lsgs.alloc(m));
         CK(G.lsst.alloc(4)); CK(G.lssc.alloc(3));
-        G.Z.release(); G.zt.release(); G.zt2.release();
+        G.Z.release(); G.zt.release(); G.zt2.release(); G.zt3.release();
         G.n = N; G.m = m;
     }
     const int pk = P ? P->kind() : 0;
     if (pk && !G.Z.p) { CK(G.Z.alloc((size_t)N * m)); CK(G.zt.alloc(N)); }
-    if (pk == 3 && !G.zt2.p) CK(G.zt2.alloc(N));
+    if (pk == 3 && !G.zt2.p) { CK(G.zt2.alloc(N)); CK(G.zt3.alloc(N)); }
     const LsqDev L{G.lsR.p, G.lsg.p, G.lsgc.p, G.lsgs.p, G.lsst.p, G.lssc.p, m};
     const int gi = mode + 3 * pk;
     if (!G.exec[gi]) {
@@ -904,7 +904,13 @@ static int gmres_core(ifgf2d_ctx* ctx, const double2* b, double2* x, int mode, d
                 spectral_launch(P->spec, G.vin.p, G.zt.p, ctx->D.Np, s);
                 if (pk == 3) {
                     net_precondition_launch(P->net, G.vin.p, G.zt2.p, s);
-                    launch_precond_sum(G.zt.p, G.zt2.p, G.vin.p, N, s);   // zt += zt2 - 2 v
+                    if (net_weighted(P->net)) {   // zt += Op(1/|sigma|) (zt2 - 2 v)
+                        launch_axpby(G.zt2.p, 1.0, G.zt2.p, -2.0, G.vin.p, N, s);
+                        spectral_launch(P->spec, G.zt2.p, G.zt3.p, ctx->D.Np, s, 2);
+                        launch_axpby(G.zt.p, 1.0, G.zt.p, 1.0, G.zt3.p, N, s);
+                    } else {
+                        launch_precond_sum(G.zt.p, G.zt2.p, G.vin.p, N, s);   // zt += zt2 - 2 v
+                    }
                 }
             }
             launch_store_col(G.zt.p, N, G.jdev.p, G.Z.p, s);

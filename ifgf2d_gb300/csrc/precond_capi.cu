@@ -20,6 +20,9 @@ struct ifgf2d_net {
     DBuf<float> p, g, m, v, zero_bias;
     DBuf<__nv_bfloat16> Wt[kNetLayers], Wb[kNetLayers];
     int step = 0;
+    // 1: the output is the correction weighted by the operator's flat symbol magnitude |sigma|
+    // (trained on Op(|sigma|) e targets); the preconditioner applies Op(1/|sigma|) to it
+    int weighted = 0;
     // batch workspace for `rows_cap` padded rows, `pts_cap` points, `seg_cap` samples
     long long rows_cap = 0, pts_cap = 0;
     int seg_cap = 0;
@@ -204,6 +207,7 @@ int ifgf::net_prepare_single(ifgf2d_net* net, long long N, const double* geom_ho
     return IFGF2D_OK;
 }
 int ifgf::net_kernel_error(ifgf2d_net* net) { return net_check_kerr(net); }
+bool ifgf::net_weighted(const ifgf2d_net* net) { return net && net->weighted; }
 void ifgf::net_precondition_launch(ifgf2d_net* net, const double2* r, double2* z, cudaStream_t s) {
     net_forward(net, r, net->geom.p, false, s);
     launch_combine(r, net->O.p, net->sigma.p, net->pt_row.p, net->pt_seg.p, (int)net->npts, z, s);
@@ -262,6 +266,13 @@ extern "C" int ifgf2d_net_destroy(ifgf2d_net* net) {
 }
 
 extern "C" const char* ifgf2d_net_last_error(const ifgf2d_net* net) { return net ? net->err.c_str() : "null network"; }
+
+extern "C" int ifgf2d_net_set_output_weighting(ifgf2d_net* net, int weighted) {
+    if (!net || (weighted != 0 && weighted != 1)) return IFGF2D_ERR_ARG;
+    net->weighted = weighted;
+    return IFGF2D_OK;
+}
+extern "C" int ifgf2d_net_output_weighting(const ifgf2d_net* net) { return net ? net->weighted : -1; }
 
 extern "C" int ifgf2d_net_get_params(ifgf2d_net* net, float* out) {
     if (!net || !out) return IFGF2D_ERR_ARG;

@@ -52,7 +52,11 @@ struct SpecCurve {
     DBuf<float> fw_w;             // per grid point: Np Lagrange weights
     DBuf<int> bk_base;            // per node: first of its kSpecTaps grid points (mod nu)
     DBuf<float> bk_w;             // per node: kSpecTaps weights
-    DBuf<float2> mult;            // 1/sigma - 2 per frequency, in the transposed order k1 N2 + k2
+    // per frequency, in the transposed order k1 N2 + k2, three multipliers m, nu values each, each
+    // with the base b it is paired with (z = b v + B F^-1 [m F W v]):
+    //   0: 1/sigma - 2 (b = 2), the preconditioner;  1: |sigma| - 1/2 (b = 1/2), the operator's
+    //   magnitude;  2: 1/|sigma| - 2 (b = 2), its inverse
+    DBuf<float2> mult;
     DBuf<float2> twN;             // e^{-2 pi i k1 n2 / nu} at k1 N2 + n2
     DBuf<float2> tw1, tw2;        // e^{-2 pi i j / N1}, j < N1 / 2; the same for N2
 };
@@ -159,13 +163,13 @@ __global__ void __launch_bounds__(kSpecThreads) k_spec_fwd_cols(const double2* _
 
 // per row k1: the row FFT, the multiplier, the inverse row FFT and the inverse twiddle, in place
 __global__ void __launch_bounds__(kSpecThreads) k_spec_rows(const SpecDesc* __restrict__ cd, const int* __restrict__ pre, int ncurves,
-                                                            float2* __restrict__ u, long long ustride) {
+                                                            float2* __restrict__ u, long long ustride, int which) {
     extern __shared__ float2 sm[];
     const int c = spec_curve_of(pre, ncurves, blockIdx.x);
     const SpecDesc d = cd[c];
     const int N2 = 1 << d.lg2, k1 = blockIdx.x - pre[c];
     float2* row = u + blockIdx.y * ustride + d.uoff + (size_t)k1 * N2;
-    const float2* mrow = d.mult + (size_t)k1 * N2;
+    const float2* mrow = d.mult + ((size_t)which << d.lg) + (size_t)k1 * N2;
     const float2* trow = d.twN + (size_t)k1 * N2;
     for (int i = threadIdx.x; i < N2; i += blockDim.x) sm[brev(i, d.lg2)] = row[i];
     __syncthreads();
@@ -208,9 +212,9 @@ __global__ void __launch_bounds__(kSpecThreads) k_spec_inv_cols(const SpecDesc* 
     }
 }
 
-// z = 2 r + B u on every curve's nodes
+// z = base r + B u on every curve's nodes
 __global__ void k_spec_back(const double2* __restrict__ r, int ld, const SpecDesc* __restrict__ cd, const int* __restrict__ pre,
-                            int ncurves, const float2* __restrict__ u, long long ustride, double2* __restrict__ z) {
+                            int ncurves, const float2* __restrict__ u, long long ustride, double base, double2* __restrict__ z) {
     const int c = spec_curve_of(pre, ncurves, blockIdx.x);
     const SpecDesc d = cd[c];
     const int j = (blockIdx.x - pre[c]) * blockDim.x + threadIdx.x;
@@ -228,7 +232,15 @@ __global__ void k_spec_back(const double2* __restrict__ r, int ld, const SpecDes
     }
     const long long o = (d.off + j) * ld + blockIdx.y;
     const double2 x = r[o];
-    z[o] = make_double2(2.0 * x.x + (double)re, 2.0 * x.y + (double)im);
+    z[o] = make_double2(base * x.x + (double)re, base * x.y + (double)im);
+}
+
+// z = a x + b y
+__global__ void k_axpby(double2* z, double a, const double2* x, double b, const double2* y, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 p = x[i], q = y[i];
+    z[i] = make_double2(a * p.x + b * q.x, a * p.y + b * q.y);
 }
 
 // z += zn - 2 r: the network's correction on top of the spectral preconditioner
@@ -369,7 +381,7 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
         }
     }, 256);
     // the multiplier in transposed order, and the twiddles
-    std::vector<float2> mult((size_t)nu), twN((size_t)nu), tw1(std::max(1, N1 / 2)), tw2(std::max(1, N2 / 2));
+    std::vector<float2> mult((size_t)nu * 3), twN((size_t)nu), tw1(std::max(1, N1 / 2)), tw2(std::max(1, N2 / 2));
     const std::complex<double> ke(k, eps);
     for (int k1 = 0; k1 < N1; ++k1)
         for (int k2 = 0; k2 < N2; ++k2) {
@@ -378,7 +390,10 @@ int build_curve(const Discretisation& D, int c, double k, double eta, double eps
             const double xi = 2.0 * kPiH * f / L;
             const std::complex<double> sig = 0.5 + eta / (2.0 * std::sqrt(ke * ke - xi * xi));
             const std::complex<double> m = 1.0 / sig - 2.0;
+            const double g = std::abs(sig);
             mult[(size_t)k1 * N2 + k2] = make_float2((float)m.real(), (float)m.imag());
+            mult[(size_t)nu + (size_t)k1 * N2 + k2] = make_float2((float)(g - 0.5), 0.f);
+            mult[2 * (size_t)nu + (size_t)k1 * N2 + k2] = make_float2((float)(1.0 / g - 2.0), 0.f);
             const long long a = ((long long)k1 * k2) % nu;
             const double th = -2.0 * kPiH * (double)a / (double)nu;
             twN[(size_t)k1 * N2 + k2] = make_float2((float)std::cos(th), (float)std::sin(th));
@@ -405,20 +420,24 @@ void free_spectral(ifgf2d_ctx* ctx) {
 // z = M r on the context's stream (capturable; the tables stay fixed until the next set-up):
 // B interleaved vectors (point i of vector b at i * B + b; B = 1 for one vector) through the
 // grid buffer `u` of B * spectral_grid_size(sw) values; four launches for all curves
-void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s) {
+void spectral_launch_batch(SpectralWork* sw, const double2* r, double2* z, int B, float2* u, int Np, cudaStream_t s, int which) {
+    const double base = which == 1 ? 0.5 : 2.0;
     const long long us = sw->grid_total;
     const int nc = sw->ncurves;
     const int* pre = sw->pre.p;
     k_spec_fwd_cols<<<dim3(sw->blocks_cols, B), kSpecThreads, sw->smem_cols, s>>>(r, B, sw->desc.p, pre, nc, Np, u, us);
-    k_spec_rows<<<dim3(sw->blocks_rows, B), kSpecThreads, sw->smem_rows, s>>>(sw->desc.p, pre + (nc + 1), nc, u, us);
+    k_spec_rows<<<dim3(sw->blocks_rows, B), kSpecThreads, sw->smem_rows, s>>>(sw->desc.p, pre + (nc + 1), nc, u, us, which);
     k_spec_inv_cols<<<dim3(sw->blocks_cols, B), kSpecThreads, sw->smem_cols, s>>>(sw->desc.p, pre, nc, u, us);
-    k_spec_back<<<dim3(sw->blocks_back, B), 256, 0, s>>>(r, B, sw->desc.p, pre + 2 * (nc + 1), nc, u, us, z);
+    k_spec_back<<<dim3(sw->blocks_back, B), 256, 0, s>>>(r, B, sw->desc.p, pre + 2 * (nc + 1), nc, u, us, base, z);
 }
-void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s) {
-    spectral_launch_batch(sw, r, z, 1, sw->u.p, Np, s);
+void spectral_launch(SpectralWork* sw, const double2* r, double2* z, int Np, cudaStream_t s, int which) {
+    spectral_launch_batch(sw, r, z, 1, sw->u.p, Np, s, which);
 }
 long long spectral_grid_size(const SpectralWork* sw) { return sw ? sw->grid_total : 0; }
 
+void launch_axpby(double2* z, double a, const double2* x, double b, const double2* y, long long n, cudaStream_t s) {
+    k_axpby<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(z, a, x, b, y, n);
+}
 void launch_precond_sum(double2* z, const double2* zn, const double2* r, long long n, cudaStream_t s) {
     k_precond_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(z, zn, r, n);
 }
@@ -480,7 +499,11 @@ extern "C" int ifgf2d_spectral_setup(ifgf2d_ctx* ctx, double scale) {
 }
 
 extern "C" int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z) {
-    if (!ctx || !r || !z) return IFGF2D_ERR_ARG;
+    return ifgf2d_spectral_symbol(ctx, IFGF2D_SYMBOL_PRECONDITIONER, r, z);
+}
+
+extern "C" int ifgf2d_spectral_symbol(ifgf2d_ctx* ctx, int which, const double* r, double* z) {
+    if (!ctx || !r || !z || which < 0 || which > 2) return IFGF2D_ERR_ARG;
     if (!ctx->sw) return fail(ctx, IFGF2D_ERR_STATE, "ifgf2d_spectral_setup first");
     const long long N = ctx->D.N;
     if (!all_finite(r, 2 * N)) return fail(ctx, IFGF2D_ERR_NONFINITE, "non-finite value in the residual");
@@ -488,7 +511,7 @@ extern "C" int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z
     DBuf<double2> dr, dz;
     CK(dr.alloc(N)); CK(dz.alloc(N));
     CK(cudaMemcpyAsync(dr.p, r, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
-    ifgf::spectral_launch(ctx->sw, dr.p, dz.p, ctx->D.Np, ctx->stream);
+    ifgf::spectral_launch(ctx->sw, dr.p, dz.p, ctx->D.Np, ctx->stream, which);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(z, dz.p, sizeof(double2) * N, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -10,8 +10,10 @@ o ~ (e - 2 r) e^{-i phi} / sigma.  Training runs on the GPU with the library's o
 AdamW.  Solves use it through ForwardMap.solve_precond (flexible GMRES inside FP64 iterative
 refinement, plain GMRES when it stalls).
 
-Weights are stored as a flat binary: the 8-byte magic b"IFGFNET\\x01", the parameter count
-(int64), then the FP32 parameters in the order of include/ifgf2d.h.
+Weights are stored as a flat binary: the 8-byte magic b"IFGFNET\\x02", the parameter count
+(int64), the output weighting flag (int64; ifgf2d_net_set_output_weighting), then the FP32
+parameters in the order of include/ifgf2d.h.  Files with the magic b"IFGFNET\\x01" have no flag
+(unweighted).
 """
 from __future__ import annotations
 
@@ -24,7 +26,8 @@ import numpy as np
 
 from . import _lib
 
-MAGIC = b"IFGFNET\x01"
+MAGIC = b"IFGFNET\x02"
+MAGIC_V1 = b"IFGFNET\x01"
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "cfie_conv6x64.bin")
 # the network trained as a correction of the spectral preconditioner (ForwardMap.solve_flexible
 # with precond="spectral+net"): targets e - M_s r instead of e - 2 r
@@ -99,24 +102,37 @@ class PreconditionerNet:
             raise ValueError(f"expected {self.nparam} parameters, got {p.size}")
         self._check(_lib.load().ifgf2d_net_set_params(self._h, _fp(p)))
 
+    @property
+    def weighted(self):
+        """True when the output is the |sigma|-weighted correction of the spectral preconditioner"""
+        return _lib.load().ifgf2d_net_output_weighting(self._h) == 1
+
+    @weighted.setter
+    def weighted(self, flag):
+        self._check(_lib.load().ifgf2d_net_set_output_weighting(self._h, 1 if flag else 0))
+
     def save(self, path):
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
         with open(path, "wb") as f:
             f.write(MAGIC)
             f.write(struct.pack("<q", self.nparam))
+            f.write(struct.pack("<q", 1 if self.weighted else 0))
             f.write(self.params.astype("<f4").tobytes())
 
     @classmethod
     def load(cls, path=DEFAULT_WEIGHTS):
         with open(path, "rb") as f:
-            if f.read(8) != MAGIC:
+            magic = f.read(8)
+            if magic not in (MAGIC, MAGIC_V1):
                 raise NetError(f"{path}: not a preconditioner weight file")
             (n,) = struct.unpack("<q", f.read(8))
+            flags = struct.unpack("<q", f.read(8))[0] if magic == MAGIC else 0
             p = np.frombuffer(f.read(4 * n), dtype="<f4")
         net = cls()
         if n != net.nparam:
             raise NetError(f"{path}: {n} parameters, the network has {net.nparam}")
         net.params = p
+        net.weighted = bool(flags & 1)
         return net
 
     def gradient(self, samples):
@@ -154,10 +170,12 @@ def harvest(fm, k, rhs, stops=(1, 2, 4, 8, 16, 32), tol=1e-9, base=None):
     """(r, e, geom, k) pairs from the plain FP64 IFGF GMRES of one problem: the converged
     solution x*, then GMRES stopped after j iterations for every j in `stops`.  base="spectral":
     the network is to correct the spectral preconditioner M_s, so the stored error is
-    e - (M_s r - 2 r), whose target (e' - 2 r) is what M_s leaves of e."""
+    e - (M_s r - 2 r), whose target (e' - 2 r) is what M_s leaves of e.  base="spectral_weighted":
+    the stored error is 2 r + Op(|sigma|)(e - M_s r), so that the loss measures what M_s leaves in
+    the residual (A ~ Op(sigma) along the curve), and the network is applied through Op(1/|sigma|)."""
     xs = fm.gmres(rhs, accelerated=True, tol=tol, restart=300, max_iters=1000)
     geom = fm.geometry_features()
-    if base == "spectral":
+    if base in ("spectral", "spectral_weighted"):
         fm.spectral_setup()
     out = []
     for j in stops:
@@ -168,6 +186,8 @@ def harvest(fm, k, rhs, stops=(1, 2, 4, 8, 16, 32), tol=1e-9, base=None):
         e = xs - xj
         if base == "spectral":
             e = e - (fm.spectral_apply(r) - 2.0 * r)
+        elif base == "spectral_weighted":   # target Op(|sigma|) (e - M_s r): the residual-space error
+            e = 2.0 * r + fm.spectral_symbol(e - fm.spectral_apply(r), "magnitude")
         out.append((r, e, geom, k))
     return out
 
@@ -236,15 +256,16 @@ def main(argv=None):
     import time
     ap = argparse.ArgumentParser(description="harvest (residual, error) pairs from plain GMRES and train the network")
     ap.add_argument("--out", default=None)
-    ap.add_argument("--base", choices=("none", "spectral"), default="none",
-                    help="spectral: train the correction of the spectral preconditioner")
+    ap.add_argument("--base", choices=("none", "spectral", "spectral_weighted"), default="none",
+                    help="spectral: train the correction of the spectral preconditioner; spectral_weighted: the same with "
+                         "the |sigma|-weighted (residual-space) loss")
     ap.add_argument("--problems", type=int, default=160)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args(argv)
     t0 = time.perf_counter()
     base = None if args.base == "none" else args.base
-    out = args.out or (SPECTRAL_WEIGHTS if base == "spectral" else DEFAULT_WEIGHTS)
+    out = args.out or (SPECTRAL_WEIGHTS if base in ("spectral", "spectral_weighted") else DEFAULT_WEIGHTS)
     pairs = harvest_set(training_problems(args.problems, seed=args.seed), base=base)
     rng = np.random.default_rng(args.seed)
     idx = rng.permutation(len(pairs))
@@ -255,6 +276,7 @@ def main(argv=None):
     t0 = time.perf_counter()
     train(net, tr, steps=args.steps, seed=args.seed, val=val, log=lambda m: print(m, flush=True))
     print(f"trained in {time.perf_counter() - t0:.1f} s", flush=True)
+    net.weighted = base == "spectral_weighted"
     net.save(out)
     print("saved", out)
 

@@ -205,6 +205,11 @@ int ifgf2d_net_train_step(ifgf2d_net* net, int nseg, const int* len, const doubl
 /* z = M(r) per sample (complex interleaved), and / or the raw outputs o (2 floats per point) */
 int ifgf2d_net_apply(ifgf2d_net* net, int nseg, const int* len, const double* r, const double* geom, const double* k, double* z,
                      float* out2);
+/* 1: the network's output is a correction weighted by the flat symbol's magnitude (trained on
+ * targets Op(|sigma|) e, see ifgf2d_spectral_symbol); together with the spectral preconditioner
+ * the correction applied is then Op(1/|sigma|) of it.  0 (default): unweighted. */
+int ifgf2d_net_set_output_weighting(ifgf2d_net* net, int weighted);
+int ifgf2d_net_output_weighting(const ifgf2d_net* net);
 /* ifgf2d_solve with the network as right preconditioner: flexible GMRES (z_j = M(v_j)) on the
  * operator of `mode` inside FP64 iterative refinement (the stop test is the FP64 relative
  * residual, formed with the FP64 IFGF operator, or the direct one in IFGF2D_APPLY_DIRECT).  A
@@ -226,6 +231,14 @@ int ifgf2d_solve_precond(ifgf2d_ctx* ctx, ifgf2d_net* net, const double* rhs, do
 int ifgf2d_spectral_setup(ifgf2d_ctx* ctx, double scale);
 /* z = M r on host vectors (complex interleaved, N entries), for tests */
 int ifgf2d_spectral_apply(ifgf2d_ctx* ctx, const double* r, double* z);
+/* z = Op(m) r for one of the tables' symbols (host vectors): IFGF2D_SYMBOL_PRECONDITIONER is
+ * ifgf2d_spectral_apply; IFGF2D_SYMBOL_MAGNITUDE applies |sigma|, the operator's flat-boundary
+ * magnitude, and IFGF2D_SYMBOL_INVERSE_MAGNITUDE 1/|sigma|.  The last two weight the learned
+ * network's training targets and output (residual-space error). */
+#define IFGF2D_SYMBOL_PRECONDITIONER 0
+#define IFGF2D_SYMBOL_MAGNITUDE 1
+#define IFGF2D_SYMBOL_INVERSE_MAGNITUDE 2
+int ifgf2d_spectral_symbol(ifgf2d_ctx* ctx, int which, const double* r, double* z);
 /* ifgf2d_solve_precond with the preconditioner chosen by `precond`: IFGF2D_PRECOND_NET (net
  * required), IFGF2D_PRECOND_SPECTRAL (set up with the default scale on first use when
  * ifgf2d_spectral_setup was not called), or both: the spectral preconditioner plus the

@@ -123,10 +123,16 @@ class CurveTables:
         idx = (self.bk_base[:, None] + np.arange(self.T)[None, :]) % self.nu
         return np.sum(u[idx] * self.bk_w, axis=1)
 
-    def multiplier(self, k, eta, eps):
+    def multiplier(self, k, eta, eps, which=0):
+        """the multiplier m of z = b v + B F^-1 [m F W v]: 0 the preconditioner (1/sigma - 2, b = 2),
+        1 the flat symbol's magnitude (|sigma| - 1/2, b = 1/2), 2 its inverse (1/|sigma| - 2, b = 2)"""
         xi = 2.0 * np.pi * np.fft.fftfreq(self.nu, self.L / self.nu)
         ke = k + 1j * eps
         sig = 0.5 + eta / (2.0 * np.sqrt(ke * ke - xi * xi + 0j))
+        if which == 1:
+            return np.abs(sig) - 0.5
+        if which == 2:
+            return 1.0 / np.abs(sig) - 2.0
         return 1.0 / sig - 2.0
 
 
@@ -151,11 +157,13 @@ class SpectralPreconditioner:
             self.off.append(self.off[-1] + tb.n)
         self.mult = [tb.multiplier(k, self.eta, self.eps) for tb in self.tables]
 
-    def __call__(self, r):
+    def __call__(self, r, which=0):
+        """z = M r (which 0), or Op(|sigma|) r (1), Op(1/|sigma|) r (2)"""
         r = np.asarray(r, dtype=np.complex128)
-        z = 2.0 * r
+        z = (0.5 if which == 1 else 2.0) * r
         for c, tb in enumerate(self.tables):
             a, b = self.off[c], self.off[c + 1]
-            u = np.fft.ifft(self.mult[c] * np.fft.fft(tb.forward(r[a:b])))
+            m = self.mult[c] if which == 0 else tb.multiplier(self.k, self.eta, self.eps, which)
+            u = np.fft.ifft(m * np.fft.fft(tb.forward(r[a:b])))
             z[a:b] += tb.back(u)
         return z

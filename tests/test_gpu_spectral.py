@@ -136,3 +136,20 @@ def test_gpu_spectral_two_curves(lib, oracle):
     x = fm.solve_flexible(rhs, "spectral", tol=1e-6)
     assert fm.last_solve["converged"] and fm.last_solve["iters"] < it0
     assert np.linalg.norm(fm.compute_Ax_acc(x) - rhs) / np.linalg.norm(rhs) < 1e-6
+
+
+def test_gpu_spectral_magnitude_symbols(lib, oracle):
+    """The |sigma| and 1/|sigma| tables (the learned network's loss weighting) equal the numpy
+    restatement, and on a smooth density one undoes the other."""
+    k = 100.0
+    fm, cdesc = _pair(lib, oracle, "kite", k, 128)
+    fm.compute_precomputations(k)
+    fm.spectral_setup(0.25)
+    M = SpectralPreconditioner([cdesc], 16, k, eta=k, eps=0.25 * k ** (1 / 3))
+    r = oracle.seeded_density(fm.total_num_unknowns_, seed=6) - (0.5 + 0.5j)
+    for name, which in (("magnitude", 1), ("inverse_magnitude", 2)):
+        assert rel(fm.spectral_symbol(r, name), M(r, which)) < TOL_APPLY
+    t = cdesc[4]
+    v = np.exp(3j * t) + 0.5 * np.cos(7 * t) + 0.2j * np.sin(20 * t)
+    w = fm.spectral_symbol(fm.spectral_symbol(v, "magnitude"), "inverse_magnitude")
+    assert rel(w, v) < 1e-4
