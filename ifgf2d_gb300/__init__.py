@@ -528,6 +528,14 @@ class ForwardMap:
             _check(rc, self._h)
         return x
 
+    def solve_preconditioned(self, rhs, wavenumber, nlevels=0, tol=None, restart=None, max_iters=None, raise_on_noconv=False):
+        """ForwardMap.solve in the chosen form (not in the reference): set-up, then complex64 inner
+        solves inside FP64 iterative refinement with the spectral right preconditioner (flexible
+        GMRES).  Combined formulation, closed curves; the same answer within the tolerance."""
+        self.precomps_and_setup(wavenumber, nlevels)
+        return self.solve_flexible(rhs, "spectral", tol=tol, restart=restart, max_iters=max_iters, mixed=True,
+                                   raise_on_noconv=raise_on_noconv)
+
     def spectral_setup(self, scale=None):
         """Tables of the spectral right preconditioner (combined field, closed curves): the
         flat-boundary symbol's inverse along each curve, glancing damping eps = scale k^(1/3)

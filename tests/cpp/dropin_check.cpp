@@ -89,11 +89,15 @@ int main(int argc, char** argv) {
     Eigen::VectorXcd x_dev = gmres.solve(b);
     if (gmres.info() != Eigen::Success) { std::cerr << "device opGMRES did not converge\n"; return 1; }
     Eigen::VectorXcd x_solve = FC.solve(b, k, 0, true);
+    const int it_solve = FC.last_iterations();
+    const double err_solve = FC.last_error();
+    Eigen::VectorXcd x_pre = FC.solve_preconditioned(b, k, 0);   // the chosen form, same tolerance
     put(f, x_user);
     put(f, x_dev);
     put(f, x_solve);
-    const double meta[6] = {(double)it_user, err_user, (double)gmres.iterations(), gmres.error(), (double)FC.last_iterations(),
-                            FC.last_error()};
+    put(f, x_pre);
+    const double meta[8] = {(double)it_user, err_user, (double)gmres.iterations(), gmres.error(), (double)it_solve,
+                            err_solve, (double)FC.last_iterations(), FC.last_error()};
     f.write(reinterpret_cast<const char*>(meta), sizeof(meta));
 
     // the reference throws std::invalid_argument for nlevels < 3 (BoxTree.h:1024-1025)
@@ -104,7 +108,7 @@ int main(int argc, char** argv) {
     threw = false;
     try { FM.compute_Ax_unacc(x, y_unacc, 2.0 * k); } catch (const std::invalid_argument&) { threw = true; }
     if (!threw) { std::cerr << "a second wavenumber did not throw\n"; return 1; }
-    std::printf("dropin ok: N=%lld nlevels=%d iterations user %d device %d solve %d\n", n, boxes.nlevels(), it_user,
-                (int)gmres.iterations(), FC.last_iterations());
+    std::printf("dropin ok: N=%lld nlevels=%d iterations user %d device %d solve %d preconditioned %d\n", n, boxes.nlevels(),
+                it_user, (int)gmres.iterations(), it_solve, FC.last_iterations());
     return 0;
 }
