@@ -203,8 +203,10 @@ extern "C" int ifgf2d_get_near_singular(const ifgf2d_ctx* ctx, long long* idx, d
 }
 
 // ------------------------------------------------------------------ rectangular-polar precomputation
-extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
-    if (!ctx) return IFGF2D_ERR_ARG;
+// ForwardMap::compute_precomputations in two halves: the launch of the rectangular-polar
+// weights on the context's stream, and the wait for them with the bookkeeping.  ifgf2d_setup
+// builds the host tree between the two, while the GPU computes the weights.
+static int precompute_launch(ifgf2d_ctx* ctx, double k) {
     if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
     if (int rc = ensure_device(ctx)) return rc;
     AllocStream guard(ctx->stream);
@@ -218,6 +220,12 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     CK(cudaGetLastError());
     launch_rp_fold(ctx->M.p, ctx->cols.p, ncols, ctx->edge.p, ctx->patches.p, D.Np, ctx->W.p, ctx->stream);
     CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+static int precompute_finish(ifgf2d_ctx* ctx, double k) {
+    AllocStream guard(ctx->stream);
+    const Discretisation& D = ctx->D;
+    const int ncols = (int)ctx->hcols.size();
     CK(cudaStreamSynchronize(ctx->stream));
     if (ifgf::noalloc_prepare(ctx->device) != IFGF2D_OK)
         return fail(ctx, IFGF2D_ERR_CUDA, "loading the scratch array of ifgf2d_apply_direct_noalloc failed");
@@ -230,6 +238,12 @@ extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
     free_spectral(ctx);
     ctx->counts[6] = (long long)ncols * D.Np;
     return IFGF2D_OK;
+}
+
+extern "C" int ifgf2d_precompute(ifgf2d_ctx* ctx, double k) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (int rc = precompute_launch(ctx, k)) return rc;
+    return precompute_finish(ctx, k);
 }
 
 extern "C" int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, double* out) {
@@ -297,15 +311,22 @@ extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
 
 extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     if (!ctx) return IFGF2D_ERR_ARG;
-    if (!ctx->precomputed || ctx->k != k) {
-        int rc = ifgf2d_precompute(ctx, k);
+    // the rectangular-polar weights run on the GPU while the host builds the tree
+    const bool pre = !ctx->precomputed || ctx->k != k;
+    if (pre) {
+        int rc = precompute_launch(ctx, k);
         if (rc != IFGF2D_OK) return rc;
     }
     AllocStream guard(ctx->stream);
-    if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) {
-        int rc = ifgf2d_prepare(ctx, k, nlevels);
+    int rc_prep = IFGF2D_OK;
+    if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) rc_prep = ifgf2d_prepare(ctx, k, nlevels);
+    if (pre) {
+        const std::string prep_err = ctx->err;
+        int rc = precompute_finish(ctx, k);
         if (rc != IFGF2D_OK) return rc;
+        if (rc_prep != IFGF2D_OK) { ctx->err = prep_err; return rc_prep; }
     }
+    if (rc_prep != IFGF2D_OK) return rc_prep;
     ctx->prep_ready = false;
     return ifgf::setup_tables(ctx, k, ctx->prep_nlevels, nullptr);
 }
