@@ -72,7 +72,7 @@ __device__ __forceinline__ double radius_to_cheb(const LevelDesc& L, long long p
 __global__ void k_prop_plan(LevelDesc Lp, LevelDesc Lc, double min_x, double min_y, double k, int Ps, ChebNodes cn, int P,
                             const int* __restrict__ slot_parent, const int* __restrict__ slot_child_box,
                             const int* __restrict__ slot_pos, const int* __restrict__ slot_route,
-                            const long long* __restrict__ route_nonrel, long long nslots, PropE<double>* __restrict__ out64,
+                            const int* __restrict__ route_nonrel, long long nslots, PropE<double>* __restrict__ out64,
                             PropE<float>* __restrict__ out32, int* __restrict__ err) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nslots * P) return;
@@ -217,7 +217,7 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
     std::vector<char> up(T.nlevels, 0);
     const size_t ns = T.prop_slots.size();
     std::vector<DBuf<int>> sp(ns), scb(ns), spos(ns), sr(ns);
-    std::vector<DBuf<long long>> rn(ns);
+    std::vector<DBuf<int>> rn(ns);
     cudaError_t e = cudaSuccess;
     for (size_t q = 0; q < ns && e == cudaSuccess; ++q) {
         const PropSlots& S = T.prop_slots[q];
@@ -232,7 +232,7 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
         if (e == cudaSuccess) e = scb[q].upload(S.slot_child_box);
         if (e == cudaSuccess) e = spos[q].upload(S.slot_pos);
         if (e == cudaSuccess) e = sr[q].upload(S.slot_route);
-        if (e == cudaSuccess) e = rn[q].upload(S.route_nonrel);
+        if (e == cudaSuccess) e = rn[q].upload(S.route_nonrel.data(), S.route_nonrel.size());
         if (e != cudaSuccess) break;
         const long long n = nslots * T.P;
         const long long eb = level_entry_base ? level_entry_base[S.level] : S.entry_base;

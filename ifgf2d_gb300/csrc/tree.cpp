@@ -114,9 +114,22 @@ struct LevelGeo {
     long long rpos(double r) const {
         return (long long)(std::upper_bound(L->radial.begin(), L->radial.end(), r) - L->radial.begin()) - 1;
     }
+    // rpos(r) from a guess h: the interval [radial[h], radial[h + 1]) that holds r is the one
+    // upper_bound finds, so a right guess gives the same index without the search
+    long long rpos(double r, long long h) const {
+        const double* R = L->radial.data();
+        if (h >= 0 && h + 1 < (long long)L->radial.size() && R[h] <= r && r < R[h + 1]) return h;
+        return rpos(r);
+    }
     long long nonrel_of(long long m, double x, double y) const {   // Level.h:310-323
         double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
         return (long long)(y * L->ntheta / kPiT) * L->nrad + rpos(x);
+    }
+    // nonrel_of with a guess of the radial interval, updated to the one found
+    long long nonrel_of(long long m, double x, double y, long long& h) const {
+        double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
+        h = rpos(x, h);
+        return (long long)(y * L->ntheta / kPiT) * L->nrad + h;
     }
     double cheb_to_radius(long long pr, double s) const {          // Level.h:347-356
         const double rmin = L->scaling_r2s / L->radial[pr + 1];
@@ -143,9 +156,14 @@ struct LevelGeo {
         x = radius_to_cheb(pr, x);
         y = (y - da * pt) / da * 2.0 - 1.0;
     }
-    long long cart_to_cheb_cone(long long m, double& x, double& y) const {            // Level.h:439-453
+    long long cart_to_cheb_cone(long long m, double& x, double& y) const {
+        long long h = -1;
+        return cart_to_cheb_cone(m, x, y, h);
+    }
+    // with a guess of the radial interval, updated to the one found
+    long long cart_to_cheb_cone(long long m, double& x, double& y, long long& h) const {   // Level.h:439-453
         double cx, cy; center(m, cx, cy); x -= cx; y -= cy; to_polar(x, y);
-        const long long pr = rpos(x), pt = (long long)(y * L->ntheta / kPiT);
+        const long long pr = h = rpos(x, h), pt = (long long)(y * L->ntheta / kPiT);
         const double da = kPiT / L->ntheta;
         x = radius_to_cheb(pr, x);
         y = (y - da * pt) / da * 2.0 - 1.0;
@@ -202,7 +220,7 @@ void cousins_of(const TreeLevel& L, long long m, std::vector<int>& out) {
 // T.pp_ptr / pp_nchild.  `seen` is the caller's scratch table, all -1 on entry and on return: it
 // grows to the largest level's need once instead of being allocated and filled per level.
 std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long long>>& part, const std::vector<double>& ns,
-                         const std::vector<double>& na, std::vector<int>& seen) {
+                         const std::vector<double>& na, std::vector<int, NoInitAlloc<int>>& seen) {
     TreeLevel& L = T.L[l];
     LevelGeo G{&L, T.min_x, T.min_y};
     const int P = T.P, Ps = T.Ps;
@@ -214,7 +232,7 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
     // nu[r] distinct segments, ascending, at uq[r * P ...]
     struct Route { long long pnc; int pos; int first_pc; };
     std::vector<Route> routes;
-    std::vector<long long> rn, uq;
+    std::vector<int, NoInitAlloc<int>> rn, uq;   // cone segments fit an int (ntheta * nrad per box)
     std::vector<int> nu;
     std::vector<int> route_of;          // per (parent cone * 4 + pos): route index or -1
     std::vector<int> child_box;         // per (parent box * 4 + pos): child box index or -1
@@ -236,20 +254,72 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
         // pnc * 4 + pos -> route, over the parent level's cone segment numbers
         long long maxnc = 0;
         for (long long nc : Lp.cone_nonrel) maxnc = std::max(maxnc, nc);
-        if (seen.size() < (size_t)(maxnc + 1) * 4) seen.resize((size_t)(maxnc + 1) * 4, -1);
-        for (size_t pc = 0; pc < npar; ++pc) {
-            const long long pnc = Lp.cone_nonrel[pc];
-            for (int pos = 0; pos < 4; ++pos) {
-                if (child_box[(size_t)Lp.cone_box[pc] * 4 + pos] < 0) continue;
-                int& r = seen[(size_t)(pnc * 4 + pos)];
-                if (r < 0) {
-                    r = (int)routes.size();
-                    routes.push_back(Route{pnc, pos, (int)pc});
-                }
-                route_of[pc * 4 + pos] = r;
-            }
+        const size_t need = (size_t)(maxnc + 1) * 4;
+        if (seen.size() < need) {   // grown uninitialised, then filled with -1 in parallel
+            const size_t old = seen.size();
+            seen.resize(need);
+            parallel_for((long long)(need - old), [&](long long a, long long b) {
+                std::fill(seen.data() + old + a, seen.data() + old + b, -1);
+            }, 1 << 16);
         }
-        for (const Route& R : routes) seen[(size_t)(R.pnc * 4 + R.pos)] = -1;
+        // routes numbered in (first parent cone, position) order, in four parallel passes:
+        // (1) per (segment, position) the first parent cone that has it, an atomic minimum in
+        // `seen`; (2) per chunk of parent cones, how many routes start there; (3) the routes of
+        // each chunk from its offset, each marked in `seen` as -2 - route; (4) per parent cone and
+        // position, its route.  Loads and stores of `seen` are atomic (relaxed): pass 3 reads
+        // entries that other threads overwrite, and only compares them with its own cone.
+        auto has = [&](size_t pc, int pos) { return child_box[(size_t)Lp.cone_box[pc] * 4 + pos] >= 0; };
+        auto slot_of = [&](size_t pc, int pos) { return seen.data() + (size_t)(Lp.cone_nonrel[pc] * 4 + pos); };
+        parallel_for((long long)npar, [&](long long p0, long long p1) {
+            for (long long pc = p0; pc < p1; ++pc)
+                for (int pos = 0; pos < 4; ++pos) {
+                    if (!has(pc, pos)) continue;
+                    int* sp = slot_of(pc, pos);
+                    int cur = __atomic_load_n(sp, __ATOMIC_RELAXED);
+                    while ((cur < 0 || cur > pc) &&
+                           !__atomic_compare_exchange_n(sp, &cur, (int)pc, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+                    }
+                }
+        });
+        const long long nrc = std::max<long long>(1, std::min<long long>(8 * kMaxThreads, (long long)npar / 4096));
+        std::vector<long long> rbase(nrc + 1, 0);
+        auto chunk_range = [&](long long c, size_t& p0, size_t& p1) { p0 = npar * c / nrc; p1 = npar * (c + 1) / nrc; };
+        parallel_for(nrc, [&](long long c0, long long c1) {
+            for (long long c = c0; c < c1; ++c) {
+                size_t p0, p1;
+                chunk_range(c, p0, p1);
+                long long n = 0;
+                for (size_t pc = p0; pc < p1; ++pc)
+                    for (int pos = 0; pos < 4; ++pos) n += has(pc, pos) && __atomic_load_n(slot_of(pc, pos), __ATOMIC_RELAXED) == (int)pc;
+                rbase[c + 1] = n;
+            }
+        }, 1);
+        for (long long c = 0; c < nrc; ++c) rbase[c + 1] += rbase[c];
+        routes.resize((size_t)rbase[nrc]);
+        parallel_for(nrc, [&](long long c0, long long c1) {
+            for (long long c = c0; c < c1; ++c) {
+                size_t p0, p1;
+                chunk_range(c, p0, p1);
+                long long id = rbase[c];
+                for (size_t pc = p0; pc < p1; ++pc)
+                    for (int pos = 0; pos < 4; ++pos) {
+                        if (!has(pc, pos)) continue;
+                        int* sp = slot_of(pc, pos);
+                        if (__atomic_load_n(sp, __ATOMIC_RELAXED) != (int)pc) continue;
+                        routes[id] = Route{Lp.cone_nonrel[pc], pos, (int)pc};
+                        __atomic_store_n(sp, (int)(-2 - id), __ATOMIC_RELAXED);
+                        ++id;
+                    }
+            }
+        }, 1);
+        parallel_for((long long)npar, [&](long long p0, long long p1) {
+            for (long long pc = p0; pc < p1; ++pc)
+                for (int pos = 0; pos < 4; ++pos)
+                    if (has(pc, pos)) route_of[pc * 4 + pos] = -2 - *slot_of(pc, pos);
+        });
+        parallel_for((long long)routes.size(), [&](long long r0, long long r1) {
+            for (long long r = r0; r < r1; ++r) seen[(size_t)(routes[r].pnc * 4 + routes[r].pos)] = -1;
+        });
         rn.resize(routes.size() * P);
         uq.resize(routes.size() * P);
         nu.resize(routes.size());
@@ -259,8 +329,8 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
             for (long long r = r0; r < r1; ++r) {
                 const Route& R = routes[r];
                 const long long pm = Lp.boxes[Lp.cone_box[R.first_pc]];
-                long long* nr = rn.data() + r * P;
-                long long* u = uq.data() + r * P;
+                int* nr = rn.data() + r * P;
+                int* u = uq.data() + r * P;
                 const long long pr = R.pnc % Lp.nrad, pt = R.pnc / Lp.nrad;
                 const double da = kPiT / Lp.ntheta;
                 double cx, cy;
@@ -271,9 +341,10 @@ std::string finish_level(Tree& T, int l, std::vector<std::vector<unsigned long l
                     cs[j] = std::cos(th);
                     sn[j] = std::sin(th);
                 }
+                long long h = -1;
                 for (int it = 0; it < P; ++it) {
                     const double px = rr[it % Ps] * cs[it / Ps] + cx, py = rr[it % Ps] * sn[it / Ps] + cy;
-                    nr[it] = G.nonrel_of(pm * 4 + R.pos, px, py);
+                    nr[it] = (int)G.nonrel_of(pm * 4 + R.pos, px, py, h);
                 }
                 std::copy(nr, nr + P, u);
                 std::sort(u, u + P);
@@ -458,7 +529,7 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     for (int i = 0; i < Pang; ++i) na[Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Pang));
     const int P = T.P;
 
-    std::vector<int> seen;   // finish_level's route table
+    std::vector<int, NoInitAlloc<int>> seen;   // finish_level's route table
     // relevant cones, level by level (BoxTree.h:553-583).  A wanted cone is the key
     // (box index << 32 | nonrel cone); each level's keys are collected per thread, then sorted
     // and deduplicated, which gives the cones in (box, nonrel) order.
@@ -474,14 +545,16 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
             part.resize(nchunk);
             parallel_for(nchunk, [&](long long c0, long long c1) {
                 std::vector<int> cs;
+                std::vector<long long> hr;   // per cousin: the last target's radial interval
                 for (long long c = c0; c < c1; ++c) {
                     const long long i0 = N * c / nchunk, i1 = N * (c + 1) / nchunk;
                     long long old = -1;
                     auto& w = part[c];
                     for (long long i = i0; i < i1; ++i) {
                         const long long m = scode[i] >> shift;
-                        if (m != old) { cousins_of(L, m, cs); old = m; }
-                        for (int cb : cs) w.push_back(key(cb, G.nonrel_of(L.boxes[cb], T.xs[i], T.ys[i])));
+                        if (m != old) { cousins_of(L, m, cs); old = m; hr.assign(cs.size(), -1); }
+                        for (size_t j = 0; j < cs.size(); ++j)
+                            w.push_back(key(cs[j], G.nonrel_of(L.boxes[cs[j]], T.xs[i], T.ys[i], hr[j])));
                     }
                     sort_unique(w);
                 }
@@ -521,7 +594,8 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
         T.ip.resize(T.ip_ptr[N]);
         std::vector<char> bad(N, 0);
         parallel_for(N, [&](long long i0, long long i1) {
-            std::vector<int> cs;
+            std::vector<int> cs, hc;          // per cousin: the last target's cone
+            std::vector<long long> hr;        // and radial interval
             std::vector<int> o(i1 - i0);
             for (long long i = i0; i < i1; ++i) o[i - i0] = T.ip_ptr[i];
             for (int l = D; l >= 2; --l) {   // the reference interpolates level D first (BoxTree.h:1049-1061)
@@ -531,11 +605,13 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
                 long long old = -1;
                 for (long long i = i0; i < i1; ++i) {
                     const long long m = scode[i] >> shift;
-                    if (m != old) { cousins_of(L, m, cs); old = m; }
-                    for (int c : cs) {
+                    if (m != old) { cousins_of(L, m, cs); old = m; hr.assign(cs.size(), -1); hc.assign(cs.size(), -1); }
+                    for (size_t j = 0; j < cs.size(); ++j) {
+                        const int c = cs[j];
                         double lx = T.xs[i], ly = T.ys[i];
-                        const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly);
-                        const int cc = L.find_cone(c, nonrel);
+                        const long long nonrel = G.cart_to_cheb_cone(L.boxes[c], lx, ly, hr[j]);
+                        const int cc = hc[j] >= 0 && L.cone_nonrel[hc[j]] == nonrel ? hc[j] : L.find_cone(c, nonrel);
+                        hc[j] = cc;
                         if (cc < 0) { bad[i] = 1; T.ip[o[i - i0]++] = InterpEntry{0, l, 0.0, 0.0, 0.0, 0.0}; continue; }
                         const double r = G.cheb_to_radius(nonrel % L.nrad, lx);
                         const double sr = std::sqrt(r);
@@ -589,7 +665,7 @@ std::string build_target_tree(const Tree& S, const std::vector<double>& tx, cons
     for (int i = 0; i < E.Ps; ++i) ns[E.Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Ps));
     for (int i = 0; i < E.Pang; ++i) na[E.Pang - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * E.Pang));
     const int P = E.P;
-    std::vector<int> seen;   // finish_level's route table
+    std::vector<int, NoInitAlloc<int>> seen;   // finish_level's route table
     for (int l = 2; l < nlevels; ++l) {
         TreeLevel& L = E.L[l];
         LevelGeo G{&L, E.min_x, E.min_y};

@@ -16,6 +16,8 @@
 #include <string>
 #include <cstdint>
 #include <complex>
+#include <memory>
+#include <utility>
 
 namespace ifgf {
 
@@ -56,6 +58,17 @@ struct PropEntry {     // one (parent cone, child, node) term of the propagation
 // pair; slots are in parent-cone order, then child position, so slot q's entries are
 // pp[entry_base + q * P + node].  route_nonrel holds, per route (a parent cone segment and a
 // child position, BoxTree.h:299-428), the child's cone segment of each of the P parent nodes.
+// an allocator whose value-less construct leaves the element uninitialised, so that resizing a
+// large table that a parallel loop fills anyway costs no serial zero fill
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = NoInitAlloc<U>; };
+    NoInitAlloc() = default;
+    template <class U> NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U> void construct(U* p) noexcept { ::new ((void*)p) U; }
+    template <class U, class... A> void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+
 struct PropSlots {
     int level = 0;                        // child level l
     long long entry_base = 0;             // global index of the first entry
@@ -63,7 +76,7 @@ struct PropSlots {
     std::vector<int> slot_child_box;      // child box index at level l
     std::vector<int> slot_pos;            // child position 0..3 (child Morton = parent * 4 + pos)
     std::vector<int> slot_route;          // route index
-    std::vector<long long> route_nonrel;  // per route, P child cone segments in node order
+    std::vector<int, NoInitAlloc<int>> route_nonrel;   // per route, P child cone segments in node order
 };
 
 struct Tree {
