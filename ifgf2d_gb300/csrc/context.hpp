@@ -294,6 +294,24 @@ int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, do
 // level_entry_base[l] the first entry of the slots with children at level l.
 cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
                             const int* level_cone_base = nullptr, const long long* level_entry_base = nullptr);
+// The propagation plan computed level by level while the host builds the tree's cones: after
+// each level's cones and slots exist, add() uploads them and launches that level's entries into
+// buffers of their own on a stream of its own; gather() copies every level into pp64 / pp32 at
+// its entry offset once the plan is allocated, ordered after the work queued so far on `s` and
+// before the work queued on `s` next, and copies the error flag (as build_prop_plan's) to *err.
+// Errors of add() are kept and returned by gather().
+class PropPlanByLevel {
+public:
+    PropPlanByLevel();
+    ~PropPlanByLevel();
+    PropPlanByLevel(const PropPlanByLevel&) = delete;
+    PropPlanByLevel& operator=(const PropPlanByLevel&) = delete;
+    void add(const Tree& T, int level);
+    cudaError_t gather(PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s);
+private:
+    struct Impl;
+    Impl* d;
+};
 // the leaf-cone interpolation nodes of T (position, 1 / factorization; BoxTree.h:714-745) on the
 // device, P per leaf cone in cone order (plan_device.cu); stream handling as build_prop_plan
 cudaError_t build_leaf_nodes(const Tree& T, LeafNode* out, cudaStream_t s);

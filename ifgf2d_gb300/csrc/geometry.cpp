@@ -135,9 +135,14 @@ static std::vector<double> patch_limits(const HostCurve& c, double wl_per_patch,
     const int nwl = (int)std::ceil(L / lambda);
     const int nint = (int)std::ceil(nwl / wl_per_patch);
     const double span = c.tlim2 - c.tlim1;
-    for (int i = 0; i < nint; ++i)
-        bisect_to_length(c, c.tlim1 + span * i / (double)nint, c.tlim1 + span * (i + 1) / (double)nint,
-                         lambda * wl_per_patch, lims, n, w);
+    // the intervals bisect independently: in parallel, then concatenated in order
+    std::vector<std::vector<double>> part(std::max(nint, 0));
+    parallel_for(nint, [&](long long i0, long long i1) {
+        for (long long i = i0; i < i1; ++i)
+            bisect_to_length(c, c.tlim1 + span * i / (double)nint, c.tlim1 + span * (i + 1) / (double)nint,
+                             lambda * wl_per_patch, part[i], n, w);
+    }, 1);
+    for (const auto& q : part) lims.insert(lims.end(), q.begin(), q.end());
     return lims;
 }
 
@@ -163,8 +168,28 @@ static void interp_roots(const std::function<double(double)>& f, double a, doubl
         return z * b1 - b2 + c[0];
     };
     const int S = 4000;
+    // Grid steps over which the interpolant cannot change sign are skipped: |f'| <= M =
+    // sum k^2 |c_k| on [-1, 1] (Markov), so from a point where |f| > 2 g + M h j the next j
+    // steps keep |f| > g, and g = 1e-12 sum |c_k| is far above the evaluation's rounding error.
+    // The points evaluated, and the roots, are those of the full scan.
+    double M = 0.0, A = 0.0;
+    for (int k = 0; k < N; ++k) { M += (double)k * k * std::fabs(c[k]); A += std::fabs(c[k]); }
+    M = M * (1.0 + 1e-12) + 1e-300;
+    const double g = 1e-12 * A, h = 2.0 / S;
     double zl = -1.0, fl = ev(zl);
     for (int s = 1; s <= S; ++s) {
+        const double room = std::fabs(fl) - 2.0 * g;
+        if (room > 0.0) {
+            const double j = std::floor(room / (M * h));
+            if (j >= 2.0) {
+                const int skip = (int)std::min<double>(j - 1.0, (double)(S - s));
+                if (skip > 0) {
+                    s += skip;
+                    zl = -1.0 + 2.0 * (s - 1) / S;
+                    fl = ev(zl);
+                }
+            }
+        }
         const double zr = -1.0 + 2.0 * s / S, fr = ev(zr);
         if (fl == 0.0 && zl > -1.0) roots.push_back(lin_map(zl, -1, 1, a, b));
         else if ((fl < 0.0 && fr > 0.0) || (fl > 0.0 && fr < 0.0)) {
@@ -282,34 +307,46 @@ std::string discretise(const ifgf2d_curve* curves, int ncurves, const ifgf2d_jun
         if (np < 1) return "curve produced no patches";
         per[c] = np; first[c] = (int)D.num_patches; D.num_patches += np; past[c] = (int)D.num_patches;
         for (int pi = 0; pi < np; ++pi) {
-            const int pid = first[c] + pi;
             const double a = lims[pi], b = lims[pi + 1];
             D.t1.push_back(a); D.t2.push_back(b); D.curve_of.push_back(c);
             const bool open = !cv.closed;
             const int s1 = open && (np == 1 || pi == 0), s2 = open && (np == 1 || pi == np - 1);
             D.ist1sing.push_back(s1); D.ist2sing.push_back(s2);
-            for (int j = 0; j < Np && !on_device; ++j) {
-                const double z = D.fej_n[j];
-                double tm = z, ej = 0.0;
-                if (s1 && s2) { tm = edge_both(z, p); ej = dedge_both(z, p); }
-                else if (s1) { tm = edge_m1(z, p); ej = dedge_both(z, p); }
-                else if (s2) { tm = edge_p1(z, p); ej = dedge_p1(z, p); }
-                const double t = lin_map(tm, -1.0, 1.0, a, b);
-                const double nx = cv.yp(t), ny = -cv.xp(t);
-                const double nn = std::sqrt(nx * nx + ny * ny);
-                double cj = nn;
-                if (s1 || s2) cj *= ej;
-                D.x.push_back(cv.x(t)); D.y.push_back(cv.y(t));
-                D.kappa.push_back(cv.curvature(t));
-                D.nx.push_back(nx / nn); D.ny.push_back(ny / nn);
-                D.t.push_back(t);
-                D.wq.push_back(((b - a) / 2.0) * D.fej_w[j] * cj);
-                D.edge_jac.push_back(ej);
-                D.patch_of.push_back(pid);
-            }
         }
     }
     D.N = D.num_patches * Np;
+    // the points of each patch (Patch.tpp), patches in parallel
+    if (!on_device) {
+        for (auto* v : {&D.x, &D.y, &D.kappa, &D.nx, &D.ny, &D.t, &D.wq, &D.edge_jac}) v->resize(D.N);
+        D.patch_of.resize(D.N);
+        parallel_for(D.num_patches, [&](long long p0, long long p1) {
+            for (long long pid = p0; pid < p1; ++pid) {
+                const HostCurve& cv = D.curves[D.curve_of[pid]];
+                const double a = D.t1[pid], b = D.t2[pid];
+                const int s1 = D.ist1sing[pid], s2 = D.ist2sing[pid];
+                for (int j = 0; j < Np; ++j) {
+                    const long long i = pid * Np + j;
+                    const double z = D.fej_n[j];
+                    double tm = z, ej = 0.0;
+                    if (s1 && s2) { tm = edge_both(z, p); ej = dedge_both(z, p); }
+                    else if (s1) { tm = edge_m1(z, p); ej = dedge_both(z, p); }
+                    else if (s2) { tm = edge_p1(z, p); ej = dedge_p1(z, p); }
+                    const double t = lin_map(tm, -1.0, 1.0, a, b);
+                    const double nx = cv.yp(t), ny = -cv.xp(t);
+                    const double nn = std::sqrt(nx * nx + ny * ny);
+                    double cj = nn;
+                    if (s1 || s2) cj *= ej;
+                    D.x[i] = cv.x(t); D.y[i] = cv.y(t);
+                    D.kappa[i] = cv.curvature(t);
+                    D.nx[i] = nx / nn; D.ny[i] = ny / nn;
+                    D.t[i] = t;
+                    D.wq[i] = ((b - a) / 2.0) * D.fej_w[j] * cj;
+                    D.edge_jac[i] = ej;
+                    D.patch_of[i] = (int)pid;
+                }
+            }
+        }, 64);
+    }
     // candidate patches (ForwardMap.tpp:164-219); junction entries keep the reference's
     // `curve_patches_end` index, which names the patch after the touching curve
     std::vector<std::vector<long long>> cand(D.num_patches);

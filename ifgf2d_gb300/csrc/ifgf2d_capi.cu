@@ -278,11 +278,9 @@ static bool neighbourhood_ok(const Discretisation& D, int nlevels) {
     return true;
 }
 
-// the host part of the set-up: tree depth, neighbourhood check, tree and plans (no CUDA call)
-extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
-    if (!ctx) return IFGF2D_ERR_ARG;
-    if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
-    const int request = nlevels;
+// the tree depth: the requested one, checked, or (request <= 0) the deepest whose leaf
+// neighbourhoods hold every singular and near-singular pair
+static int choose_levels(ifgf2d_ctx* ctx, int& nlevels) {
     const Discretisation& D = ctx->D;
     if (nlevels <= 0) {
         nlevels = 0;
@@ -293,6 +291,22 @@ extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
         if (nlevels > 20) return fail(ctx, IFGF2D_ERR_NLEVELS, "nlevels too large");
         if (!neighbourhood_ok(D, nlevels)) return fail(ctx, IFGF2D_ERR_NEIGHBORHOOD, "Singular point not in neighborhood");
     }
+    return IFGF2D_OK;
+}
+
+static void record_counts(ifgf2d_ctx* ctx, int nlevels) {
+    const Tree& T = ctx->T;
+    ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
+    ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
+}
+
+// the host part of the set-up: tree depth, neighbourhood check, tree and plans (no CUDA call)
+extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
+    if (!ctx) return IFGF2D_ERR_ARG;
+    if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
+    const int request = nlevels;
+    const Discretisation& D = ctx->D;
+    if (int rc = choose_levels(ctx, nlevels)) return rc;
     // the device tables no longer match the host tree from here until ifgf2d_setup completes
     ctx->ifgf_ready = false;
     ctx->prep_ready = false;
@@ -303,45 +317,92 @@ extern "C" int ifgf2d_prepare(ifgf2d_ctx* ctx, double k, int nlevels) {
     ctx->prep_request = request;
     ctx->prep_nlevels = nlevels;
     ctx->nlevels = nlevels;
-    const Tree& T = ctx->T;
-    ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
-    ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
+    record_counts(ctx, nlevels);
     return IFGF2D_OK;
 }
 
+static int setup_boxes(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex);
+static int setup_cones(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex, DBuf<int>& perr,
+                       PropPlanByLevel* by_level = nullptr);
+static int setup_interp(ifgf2d_ctx* ctx, int nlevels, DBuf<int>& perr);
+
+// ForwardMap::precomps_and_setup.  Host and GPU take turns so that each works while the other
+// does: the host builds the tree's boxes; the GPU computes the near-field table, the
+// rectangular-polar weights and, level by level on a second stream, the propagation plan while
+// the host builds the cones; the GPU computes the leaf-cone tables while the host builds the
+// interpolation plan.  A tree that ifgf2d_prepare built beforehand is used as it is.
 extern "C" int ifgf2d_setup(ifgf2d_ctx* ctx, double k, int nlevels) {
     if (!ctx) return IFGF2D_ERR_ARG;
-    // the rectangular-polar weights run on the GPU while the host builds the tree
+    if (!(k > 0)) return fail(ctx, IFGF2D_ERR_ARG, "wavenumber must be real and > 0");
     const bool pre = !ctx->precomputed || ctx->k != k;
+    if (ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels) {
+        if (pre) {
+            if (int rc = precompute_launch(ctx, k)) return rc;
+            if (int rc = precompute_finish(ctx, k)) return rc;
+        }
+        AllocStream guard(ctx->stream);
+        ctx->prep_ready = false;
+        return ifgf::setup_tables(ctx, k, ctx->prep_nlevels, nullptr);
+    }
+    // a failed tree still leaves the weights computed, as the reference's order has them
+    const Discretisation& D = ctx->D;
+    int nl = nlevels;
+    std::string msg;
+    int rc = choose_levels(ctx, nl);
+    if (rc == IFGF2D_OK) {
+        ctx->ifgf_ready = false;
+        ctx->prep_ready = false;
+        msg = build_tree_boxes(D.x, D.y, nl, k, ctx->opt.Ps, ctx->opt.Pang, ctx->T);
+        if (!msg.empty()) rc = fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
+    }
+    if (int r = ensure_device(ctx)) return r;
+    DBuf<int> perr;
+    {   // the near-field table's uploads go first, while the stream is idle
+        AllocStream guard(ctx->stream);
+        if (pre) ctx->eta = ctx->opt.coupling > 0 ? ctx->opt.coupling : k;
+        if (rc == IFGF2D_OK) rc = setup_boxes(ctx, k, nl, nullptr);
+    }
     if (pre) {
-        int rc = precompute_launch(ctx, k);
-        if (rc != IFGF2D_OK) return rc;
+        if (int r = precompute_launch(ctx, k)) return r;
     }
     AllocStream guard(ctx->stream);
-    int rc_prep = IFGF2D_OK;
-    if (!(ctx->prep_ready && ctx->prep_k == k && ctx->prep_request == nlevels)) rc_prep = ifgf2d_prepare(ctx, k, nlevels);
-    if (pre) {
-        const std::string prep_err = ctx->err;
-        int rc = precompute_finish(ctx, k);
-        if (rc != IFGF2D_OK) return rc;
-        if (rc_prep != IFGF2D_OK) { ctx->err = prep_err; return rc_prep; }
+    PropPlanByLevel by_level;
+    if (rc == IFGF2D_OK) {
+        msg = build_tree_cones(ctx->T, [&](int l) { if (l > 2) by_level.add(ctx->T, l); });
+        if (!msg.empty()) rc = fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
     }
-    if (rc_prep != IFGF2D_OK) return rc_prep;
-    ctx->prep_ready = false;
-    return ifgf::setup_tables(ctx, k, ctx->prep_nlevels, nullptr);
+    if (pre) {   // waits for the weights (and the near-field table)
+        const std::string err = ctx->err;
+        if (int r = precompute_finish(ctx, k)) return r;
+        ctx->err = err;
+    }
+    if (rc != IFGF2D_OK) return rc;
+    if (int rc2 = setup_cones(ctx, k, nl, nullptr, perr, &by_level)) return rc2;
+    msg = build_tree_interp(ctx->T);
+    if (!msg.empty()) {
+        cudaStreamSynchronize(ctx->stream);
+        return fail(ctx, IFGF2D_ERR_GEOMETRY, msg);
+    }
+    record_counts(ctx, nl);
+    return setup_interp(ctx, nl, perr);
 }
 
-// The device tables of an IFGF set-up from the context's host tree (ctx->T) and discretisation.
+// The device tables of an IFGF set-up from the context's host tree (ctx->T) and discretisation,
+// in three stages that follow the tree's (build_tree_boxes, _cones, _interp): setup_boxes needs
+// the boxes, setup_cones the cones and the propagation slots, setup_interp the interpolation
+// plan.  The first two only queue work on the context's stream, so the host can build the next
+// stage of the tree meanwhile; setup_interp waits for all of it and then checks the
+// propagation plan's error flag `perr`, which setup_cones clears.
 // With `ex` (a group of obstacles, group.cu) the wavenumbers come per leaf box and leaf cone,
 // the leaf-cone nodes from the members' trees, and the propagation plan from ex->build_plan.
-int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex) {
+static int setup_boxes(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex) {
     const Discretisation& D = ctx->D;
     free_batch(ctx);
     free_eval(ctx);
+    ctx->ifgf_ready = false;
     Tree& T = ctx->T;
     ctx->nlevels = nlevels;
     const long long N = D.N;
-    const int P = T.P, Dl = nlevels - 1;
     // sorted-order tables
     std::vector<int> patch_s(N), nptr(N + 1, 0), nl;
     for (long long i = 0; i < N; ++i) {
@@ -390,6 +451,13 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
                       ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, ctx->patch_s.p, ctx->nsp_ptr_s.p, ctx->nsp_s.p, k,
                       ctx->form, ctx->eta, ctx->near.p, ctx->stream, ex ? ex->keta_leafbox : nullptr);
     CK(cudaGetLastError());
+    return IFGF2D_OK;
+}
+
+static int setup_cones(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex, DBuf<int>& perr,
+                       PropPlanByLevel* by_level) {
+    Tree& T = ctx->T;
+    const int P = T.P, Dl = nlevels - 1;
     // values-to-coefficients matrix of the cone interpolant (Interpolator.h:81-120)
     {
         const int Ps = T.Ps, Pa = T.Pang;
@@ -416,35 +484,43 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
         std::vector<float> Gs32(Gs.begin(), Gs.end());
         CK(ctx->Gsep32.upload(Gs32));
     }
-    // leaf cones
+    // The uploads come before the kernels that follow them: a copy from pageable host memory
+    // queued behind a running kernel holds the host until the kernel ends.  The leaf-cone nodes'
+    // kernel is short; the propagation plan's uploads wait for it at most.
     const TreeLevel& LD = T.L[Dl];
     const int ncl = (int)LD.cone_nonrel.size();
     std::vector<long long> loff(ncl + 1, 0);
     for (int c = 0; c < ncl; ++c) loff[c + 1] = loff[c] + (long long)P * T.leaf_count[LD.cone_box[c]];
-    // leaf-cone interpolation nodes, computed on the device
-    CK(ctx->leaf_nodes_d.alloc((size_t)ncl * P));
-    if (ex) CK(ex->build_nodes(ctx->leaf_nodes_d.p, ctx->stream));
-    else CK(build_leaf_nodes(T, ctx->leaf_nodes_d.p, ctx->stream));
     CK(ctx->leaf_cone_box.upload(LD.cone_box)); CK(ctx->leaf_off.upload(loff));
     CK(ctx->leafL.alloc(loff[ncl]));
+    CK(ctx->leaf_nodes_d.alloc((size_t)ncl * P));
+    CK(ctx->pp.alloc((size_t)T.pp_total)); CK(ctx->pp32.alloc((size_t)T.pp_total));
+    CK(ctx->pp_ptr.upload(T.pp_ptr)); CK(ctx->pp_nchild.upload(T.pp_nchild));
+    CK(perr.alloc(1));
+    CK(cudaMemsetAsync(perr.p, 0, sizeof(int), ctx->stream));
+    // leaf-cone interpolation nodes, computed on the device
+    if (ex) CK(ex->build_nodes(ctx->leaf_nodes_d.p, ctx->stream));
+    else CK(build_leaf_nodes(T, ctx->leaf_nodes_d.p, ctx->stream));
+    // propagation plan: the entries are computed on the device from the tree's slot form (or
+    // were, level by level, while the host built the cones)
+    if (ex) CK(ex->build_plan(ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+    else if (by_level) CK(by_level->gather(ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+    else CK(build_prop_plan(T, ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
+    // leaf-cone tables
     launch_leaf_setup(ctx->leaf_cone_box.p, ncl, ctx->leaf_start.p, ctx->leaf_count.p, ctx->leaf_off.p, ctx->leaf_nodes_d.p,
                       ctx->xs_s.p, ctx->ys_s.p, ctx->nxs_s.p, ctx->nys_s.p, T.Ps, T.Pang, k, ctx->form, ctx->eta, ctx->Gsep.p,
                       ctx->leafL.p, ctx->stream, ex ? ex->keta_leafcone : nullptr);
     CK(cudaGetLastError());
-    // propagation and interpolation plans: the propagation entries are computed on the device
-    // from the tree's slot form, the interpolation entries come from the host tree
-    {
-        CK(ctx->pp.alloc((size_t)T.pp_total)); CK(ctx->pp32.alloc((size_t)T.pp_total));
-        CK(ctx->pp_ptr.upload(T.pp_ptr)); CK(ctx->pp_nchild.upload(T.pp_nchild));
-        DBuf<int> perr;
-        CK(perr.alloc(1));
-        CK(cudaMemsetAsync(perr.p, 0, sizeof(int), ctx->stream));
-        if (ex) CK(ex->build_plan(ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
-        else CK(build_prop_plan(T, ctx->pp.p, ctx->pp32.p, perr.p, ctx->stream));
-        int bad = 0;
-        CK(cudaMemcpyAsync(&bad, perr.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
-        if (bad) return fail(ctx, IFGF2D_ERR_GEOMETRY, "internal: a propagation node's child cone is missing");
+    return IFGF2D_OK;
+}
+
+static int setup_interp(ifgf2d_ctx* ctx, int nlevels, DBuf<int>& perr) {
+    const Discretisation& D = ctx->D;
+    Tree& T = ctx->T;
+    const long long N = D.N;
+    const int P = T.P;
+    const int nleaf = (int)T.leaf_start.size();
+    {   // interpolation plan: the entries come from the host tree
         static_assert(sizeof(InterpEntry) == sizeof(InterpEntryD), "host and device plan layouts differ");
         CK(ctx->ip.upload(reinterpret_cast<const InterpEntryD*>(T.ip.data()), T.ip.size()));
         CK(ctx->ip_ptr.upload(T.ip_ptr));
@@ -487,7 +563,10 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
     launch_d2f(ctx->near.p, (long long)ctx->near.n, ctx->near32.p, ctx->stream);
     launch_d2f(ctx->leafL.p, (long long)ctx->leafL.n, ctx->leafL32.p, ctx->stream);
     CK(cudaGetLastError());
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, perr.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (bad) return fail(ctx, IFGF2D_ERR_GEOMETRY, "internal: a propagation node's child cone is missing");
     ctx->counts[0] = T.near_pairs; ctx->counts[1] = T.leaf_evals; ctx->counts[2] = T.prop_evals;
     ctx->counts[3] = T.interp_evals; ctx->counts[4] = T.total_cones; ctx->counts[5] = nlevels;
     ctx->counts[7] = (long long)(ctx->near.n + ctx->leafL.n + ctx->coef.n + ctx->W.n) * 16 + (long long)ctx->pp.n * sizeof(PropEntryD) +
@@ -495,6 +574,13 @@ int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
     ctx->ifgf_ready = true;
     if (ctx->gw) ctx->gw->drop_graphs();
     return IFGF2D_OK;
+}
+
+int ifgf::setup_tables(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra* ex) {
+    DBuf<int> perr;
+    if (int rc = setup_boxes(ctx, k, nlevels, ex)) return rc;
+    if (int rc = setup_cones(ctx, k, nlevels, ex, perr)) return rc;
+    return setup_interp(ctx, nlevels, perr);
 }
 
 extern "C" int ifgf2d_get_sorting(const ifgf2d_ctx* ctx, long long* s) {

@@ -13,6 +13,7 @@
 // is compiled without FMA contraction so the arithmetic rounds as the host's does, and only
 // the device's cos / sin / atan may differ from the host's by an ulp.
 #include "context.hpp"
+#include <memory>
 
 namespace ifgf {
 namespace {
@@ -211,7 +212,9 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
     // Chebyshev nodes of the cone interpolant, ascending (Chebyshev.h:10-24), as the host tree has them
     for (int i = 0; i < T.Ps; ++i) cn.s[T.Ps - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Ps));
     for (int i = 0; i < T.Pang; ++i) cn.a[T.Pang - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Pang));
-    // every input buffer lives until the synchronisation at the end
+    // every input buffer lives until the kernels ran.  All levels are uploaded before the first
+    // launch: a copy from pageable host memory queued behind a running kernel holds the host
+    // until the kernel ends.
     std::vector<LevelBufs> lb(T.nlevels);
     std::vector<LevelDesc> ld(T.nlevels);
     std::vector<char> up(T.nlevels, 0);
@@ -221,8 +224,7 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
     cudaError_t e = cudaSuccess;
     for (size_t q = 0; q < ns && e == cudaSuccess; ++q) {
         const PropSlots& S = T.prop_slots[q];
-        const long long nslots = (long long)S.slot_parent.size();
-        if (nslots == 0) continue;
+        if (S.slot_parent.empty()) continue;
         for (int l : {S.level - 1, S.level})
             if (!up[l] && e == cudaSuccess) {
                 e = upload_level(T.L[l], level_cone_base ? level_cone_base[l] : T.L[l].cone_base, lb[l], ld[l]);
@@ -233,7 +235,11 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
         if (e == cudaSuccess) e = spos[q].upload(S.slot_pos);
         if (e == cudaSuccess) e = sr[q].upload(S.slot_route);
         if (e == cudaSuccess) e = rn[q].upload(S.route_nonrel.data(), S.route_nonrel.size());
-        if (e != cudaSuccess) break;
+    }
+    for (size_t q = 0; q < ns && e == cudaSuccess; ++q) {
+        const PropSlots& S = T.prop_slots[q];
+        const long long nslots = (long long)S.slot_parent.size();
+        if (nslots == 0) continue;
         const long long n = nslots * T.P;
         const long long eb = level_entry_base ? level_entry_base[S.level] : S.entry_base;
         k_prop_plan<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ld[S.level - 1], ld[S.level], T.min_x, T.min_y, T.k, T.Ps, cn, T.P,
@@ -246,6 +252,104 @@ cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp
     if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;
     const cudaError_t es = cudaStreamSynchronize(s);
     return e != cudaSuccess ? e : es;
+}
+
+struct PropPlanByLevel::Impl {
+    struct Level {
+        long long entry_base = 0, n = 0;
+        DBuf<int> sp, scb, spos, sr, rn;
+        DBuf<PropE<double>> o64;
+        DBuf<PropE<float>> o32;
+    };
+    cudaStream_t st = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    cudaError_t status = cudaSuccess;
+    std::vector<std::unique_ptr<LevelBufs>> lb;
+    std::vector<LevelDesc> ld;
+    std::vector<char> up;
+    std::vector<std::unique_ptr<Level>> lv;
+    DBuf<int> err;
+    ChebNodes cn{};
+    ~Impl() {
+        lv.clear();   // stream-ordered frees on st, after its copies
+        lb.clear();
+        err.release();
+        if (ready) cudaEventDestroy(ready);
+        if (done) cudaEventDestroy(done);
+        if (st) cudaStreamDestroy(st);   // released once its queued work is done
+    }
+};
+
+PropPlanByLevel::PropPlanByLevel() : d(new Impl) {
+    d->status = cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking);
+    if (d->status == cudaSuccess) d->status = cudaEventCreateWithFlags(&d->ready, cudaEventDisableTiming);
+    if (d->status == cudaSuccess) d->status = cudaEventCreateWithFlags(&d->done, cudaEventDisableTiming);
+}
+PropPlanByLevel::~PropPlanByLevel() { delete d; }
+
+void PropPlanByLevel::add(const Tree& T, int l) {
+    Impl& I = *d;
+    if (I.status != cudaSuccess) return;
+    if (T.Ps > 8 || T.Pang > 8 || T.prop_slots.empty() || T.prop_slots.back().level != l) { I.status = cudaErrorInvalidValue; return; }
+    AllocStream guard(I.st);
+    cudaError_t e = cudaSuccess;
+    if (I.lb.empty()) {
+        for (int q = 0; q < T.nlevels; ++q) I.lb.emplace_back(new LevelBufs);
+        I.ld.resize(T.nlevels); I.up.assign(T.nlevels, 0);
+        for (int i = 0; i < T.Ps; ++i) I.cn.s[T.Ps - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Ps));
+        for (int i = 0; i < T.Pang; ++i) I.cn.a[T.Pang - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Pang));
+        e = I.err.alloc(1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(I.err.p, 0, sizeof(int), I.st);
+    }
+    // the levels' arrays are final once their cones exist: level l - 1 was uploaded with the
+    // previous level (as its child level), level l now
+    for (int q : {l - 1, l})
+        if (!I.up[q] && e == cudaSuccess) {
+            e = upload_level(T.L[q], T.L[q].cone_base, *I.lb[q], I.ld[q]);
+            I.up[q] = 1;
+        }
+    const PropSlots& S = T.prop_slots.back();
+    std::unique_ptr<Impl::Level> vp(new Impl::Level);
+    Impl::Level& v = *vp;
+    v.entry_base = S.entry_base;
+    v.n = (long long)S.slot_parent.size() * T.P;
+    if (v.n > 0 && e == cudaSuccess) {
+        if (e == cudaSuccess) e = v.sp.upload(S.slot_parent);
+        if (e == cudaSuccess) e = v.scb.upload(S.slot_child_box);
+        if (e == cudaSuccess) e = v.spos.upload(S.slot_pos);
+        if (e == cudaSuccess) e = v.sr.upload(S.slot_route);
+        if (e == cudaSuccess) e = v.rn.upload(S.route_nonrel.data(), S.route_nonrel.size());
+        if (e == cudaSuccess) e = v.o64.alloc((size_t)v.n);
+        if (e == cudaSuccess) e = v.o32.alloc((size_t)v.n);
+        if (e == cudaSuccess) {
+            k_prop_plan<<<(unsigned)((v.n + 255) / 256), 256, 0, I.st>>>(I.ld[l - 1], I.ld[l], T.min_x, T.min_y, T.k, T.Ps, I.cn, T.P,
+                                                                         v.sp.p, v.scb.p, v.spos.p, v.sr.p, v.rn.p,
+                                                                         (long long)S.slot_parent.size(), v.o64.p, v.o32.p, I.err.p);
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) { I.status = e; return; }
+    I.lv.push_back(std::move(vp));
+}
+
+cudaError_t PropPlanByLevel::gather(PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s) {
+    Impl& I = *d;
+    if (I.status != cudaSuccess) return I.status;
+    AllocStream guard(I.st);
+    cudaError_t e = cudaEventRecord(I.ready, s);   // the plan's allocation on s
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(I.st, I.ready, 0);
+    for (const auto& vp : I.lv) {
+        const Impl::Level& v = *vp;
+        if (v.n == 0 || e != cudaSuccess) continue;
+        e = cudaMemcpyAsync(pp64 + v.entry_base, v.o64.p, sizeof(PropE<double>) * (size_t)v.n, cudaMemcpyDeviceToDevice, I.st);
+        if (e == cudaSuccess && pp32)
+            e = cudaMemcpyAsync(pp32 + v.entry_base, v.o32.p, sizeof(PropE<float>) * (size_t)v.n, cudaMemcpyDeviceToDevice, I.st);
+    }
+    if (e == cudaSuccess && I.err.p) e = cudaMemcpyAsync(err, I.err.p, sizeof(int), cudaMemcpyDeviceToDevice, I.st);
+    if (e == cudaSuccess) e = cudaEventRecord(I.done, I.st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, I.done, 0);
+    I.lv.clear();   // the level buffers are freed on st after the copies
+    return e;
 }
 
 cudaError_t build_leaf_nodes(const Tree& T, LeafNode* out, cudaStream_t s) {

@@ -452,8 +452,8 @@ void target_list(const TreeLevel& L, int l, long long bx, long long by, std::vec
     for (auto& t : tmp) out.push_back(t.second);
 }
 // ---------------------------------------------------------------- build
-std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
-                       int Ps, int Pang, Tree& T) {
+std::string build_tree_boxes(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
+                             int Ps, int Pang, Tree& T) {
     if (nlevels < 3) return "IFGF accelerator requires at least 3 levels.";
     if (nlevels > 24) return "nlevels too large";
     T = Tree();
@@ -473,7 +473,8 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
     std::stable_sort(T.sorting.begin(), T.sorting.end(), [&](long long a, long long b) { return code[a] < code[b]; });
     T.inverse.resize(N);
     T.xs.resize(N); T.ys.resize(N);
-    std::vector<long long> scode(N);
+    std::vector<long long>& scode = T.codes;
+    scode.resize(N);
     for (long long i = 0; i < N; ++i) {
         T.inverse[T.sorting[i]] = i;
         T.xs[i] = x[T.sorting[i]]; T.ys[i] = y[T.sorting[i]]; scode[i] = code[T.sorting[i]];
@@ -523,6 +524,13 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
             T.near_pairs += nsrc * T.leaf_count[b];
         }
     }
+    return "";
+}
+
+std::string build_tree_cones(Tree& T, const std::function<void(int level)>& level_done) {
+    const long long N = T.N;
+    const int nlevels = T.nlevels, D = nlevels - 1, Ps = T.Ps, Pang = T.Pang;
+    const std::vector<long long>& scode = T.codes;
     // Chebyshev nodes of the cone interpolant (ascending, Chebyshev.h:10-24); GetInterpolationPoint
     std::vector<double> ns(Ps), na(Pang);
     for (int i = 0; i < Ps; ++i) ns[Ps - 1 - i] = std::cos(kPiT * (2.0 * i + 1.0) / (2.0 * Ps));
@@ -562,12 +570,20 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
         }
         std::string msg = finish_level(T, l, part, ns, na, seen);
         if (!msg.empty()) return msg;
+        if (level_done) level_done(l);
     }
     // leaf-level cones have no children: close the propagation CSR for them
     if (T.pp_ptr.empty()) T.pp_ptr.assign(1, 0);
     while ((long long)T.pp_ptr.size() - 1 < T.total_cones) { T.pp_ptr.push_back(T.pp_total); T.pp_nchild.push_back(0); }
     for (size_t c = 0; c < T.L[D].cone_nonrel.size(); ++c) T.leaf_evals += (long long)P * T.leaf_count[T.L[D].cone_box[c]];
+    return "";
+}
 
+std::string build_tree_interp(Tree& T) {
+    const long long N = T.N;
+    const int nlevels = T.nlevels, D = nlevels - 1;
+    const double k = T.k;
+    const std::vector<long long>& scode = T.codes;
     // interpolation plan (BoxTree.h:876-937): per sorted target, all levels, all cousins.  A
     // first pass counts each target's terms (its boxes' cousin counts), a second fills them in
     // place.
@@ -624,6 +640,14 @@ std::string build_tree(const std::vector<double>& x, const std::vector<double>& 
         T.interp_evals = T.ip_ptr[N];
     }
     return "";
+}
+
+std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
+                       int Ps, int Pang, Tree& T) {
+    std::string msg = build_tree_boxes(x, y, nlevels, k, Ps, Pang, T);
+    if (msg.empty()) msg = build_tree_cones(T);
+    if (msg.empty()) msg = build_tree_interp(T);
+    return msg;
 }
 
 }  // namespace ifgf

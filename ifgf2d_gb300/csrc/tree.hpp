@@ -16,6 +16,7 @@
 #include <string>
 #include <cstdint>
 #include <complex>
+#include <functional>
 #include <memory>
 #include <utility>
 
@@ -86,6 +87,7 @@ struct Tree {
     double min_x = 0, min_y = 0, boxsize0 = 0;
     std::vector<long long> sorting, inverse;   // sorted position -> original index, and back
     std::vector<double> xs, ys;                // Morton-sorted coordinates
+    std::vector<long long> codes;              // their leaf-level Morton codes
     std::vector<TreeLevel> L;                  // index = level; 0 and 1 unused
     // leaf boxes (level D = nlevels-1)
     std::vector<int> leaf_start, leaf_count, point_leaf;
@@ -107,6 +109,15 @@ struct Tree {
 // Build the tree for the given points (original order).  Returns "" or an error message.
 std::string build_tree(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
                        int Ps, int Pang, Tree& T);
+// build_tree in its three stages, for a caller that starts device work between them: the boxes
+// (Morton sort, relevant boxes, leaf neighbours), then the cones of every level with the
+// propagation plan's slot form, then the interpolation plan.  Each returns "" or an error
+// message and needs the stages before it.  build_tree_cones calls level_done(l) once level l's
+// cones and, for l > 2, its propagation slots (T.prop_slots.back()) are final.
+std::string build_tree_boxes(const std::vector<double>& x, const std::vector<double>& y, int nlevels, double k,
+                             int Ps, int Pang, Tree& T);
+std::string build_tree_cones(Tree& T, const std::function<void(int level)>& level_done = nullptr);
+std::string build_tree_interp(Tree& T);
 
 // Evaluation plan for off-surface targets (the accelerated form of ForwardMap::propagate_unacc,
 // ForwardMap.tpp:701-727).  E keeps the source boxes of S (sources, leaf ranges, Morton order)
