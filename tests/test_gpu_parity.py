@@ -284,6 +284,44 @@ def test_gpu_error_paths(lib):
         fm.compute_Ax_acc(np.ones(3, complex))
 
 
+@pytest.mark.parametrize("k,ppc", [(200.0, 256), (2000.0, 2048)])
+def test_gpu_staged_setup_equals_prepared_tree(lib, oracle, k, ppc):
+    """precomps_and_setup builds the tree in stages while the GPU computes the tables (the
+    propagation plan level by level on a second stream); a tree prepared beforehand goes through
+    the device stages back to back.  The two contexts hold the same operator, bit for bit."""
+    staged = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=ppc, formulation="combined")
+    staged.precomps_and_setup(k, 0)
+    prepared = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=ppc, formulation="combined")
+    prepared.prepare(k, 0)
+    prepared.precomps_and_setup(k, 0)
+    assert staged.nlevels == prepared.nlevels
+    assert staged.work_counts() == prepared.work_counts()
+    assert np.array_equal(staged.getSorting(), prepared.getSorting())
+    d = oracle.seeded_density(staged.total_num_unknowns_)
+    assert np.array_equal(staged.compute_Ax_acc(d), prepared.compute_Ax_acc(d))
+    assert np.array_equal(staged.compute_Ax_acc(d, mixed=True), prepared.compute_Ax_acc(d, mixed=True))
+    # a second set-up of the same context at another wavenumber
+    staged.precomps_and_setup(0.5 * k, 0)
+    prepared.prepare(0.5 * k, 0)
+    prepared.precomps_and_setup(0.5 * k, 0)
+    assert np.array_equal(staged.compute_Ax_acc(d), prepared.compute_Ax_acc(d))
+
+
+def test_gpu_failed_tree_keeps_the_weights(lib, oracle):
+    """A tree depth that fails the neighbourhood check raises, and the rectangular-polar weights
+    of the new wavenumber are still computed (the reference computes them before the tree)."""
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 100.0, Np=16, patches_per_curve=128)
+    ref = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 100.0, Np=16, patches_per_curve=128)
+    with pytest.raises(lib.NeighbourhoodError):
+        fm.precomps_and_setup(120.0, 12)
+    ref.compute_precomputations(120.0)
+    d = oracle.seeded_density(fm.total_num_unknowns_)
+    assert np.array_equal(fm.compute_Ax_unacc(d), ref.compute_Ax_unacc(d))
+    fm.precomps_and_setup(120.0, 0)
+    ref.precomps_and_setup(120.0, 0)
+    assert np.array_equal(fm.compute_Ax_acc(d), ref.compute_Ax_acc(d))
+
+
 # ---------------------------------------------------------------- combined field formulation
 # The double-layer part of the rectangular-polar integrals is ill-conditioned with respect to
 # the node positions: near the singular point (x - y).n_y / r^2 cancels, so a one-ulp change of
