@@ -1,3 +1,4 @@
+#include <atomic>
 #include <mutex>
 // ifgf2d_capi.cu -- the C ABI (include/ifgf2d.h): context, set-up, apply, GMRES, propagation.
 //
@@ -257,25 +258,35 @@ extern "C" int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, doub
 
 // ------------------------------------------------------------------ IFGF set-up
 // BoxTree::CheckIfSingandNearSingInNeighborhood (BoxTree.h:1079-1161) on leaf box coordinates
+// Every pair of a patch's points is adjacent exactly when the patch's leaf-box range spans at
+// most two boxes in x and in y, and a near-singular point is adjacent to all of a patch's points
+// exactly when it lies within one box of that whole range; so each patch needs its range only.
 static bool neighbourhood_ok(const Discretisation& D, int nlevels) {
     double mx, my, size;
     tree_root_box(D.x, D.y, mx, my, size);
     const int lev = nlevels - 1;
     const double bs = size / (double)(1LL << lev);
-    std::vector<long long> bx(D.N), by(D.N);
-    for (long long i = 0; i < D.N; ++i) {
-        bx[i] = (long long)((D.x[i] - mx) / bs); by[i] = (long long)((D.y[i] - my) / bs);
-        if (bx[i] < 0 || by[i] < 0 || bx[i] >= (1LL << lev) || by[i] >= (1LL << lev)) return false;
-    }
-    auto adj = [&](long long i, long long j) { return std::llabs(bx[i] - bx[j]) <= 1 && std::llabs(by[i] - by[j]) <= 1; };
-    for (long long i = 0; i < D.N; ++i) {
-        const long long p0 = (i / D.Np) * D.Np;
-        for (long long j = p0; j < p0 + D.Np; ++j) if (j != i && !adj(i, j)) return false;
-    }
-    for (long long p = 0; p < D.num_patches; ++p)
-        for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q)
-            for (long long j = p * D.Np; j < p * D.Np + D.Np; ++j) if (!adj(D.ns_idx[q], j)) return false;
-    return true;
+    const long long side = 1LL << lev;
+    auto box = [&](long long i, long long& bx, long long& by) {
+        bx = (long long)((D.x[i] - mx) / bs); by = (long long)((D.y[i] - my) / bs);
+        return bx >= 0 && by >= 0 && bx < side && by < side;
+    };
+    std::atomic<bool> ok{true};
+    parallel_for(D.num_patches, [&](long long p0, long long p1) {
+        for (long long p = p0; p < p1 && ok.load(std::memory_order_relaxed); ++p) {
+            long long x0 = side, x1 = -1, y0 = side, y1 = -1, bx, by;
+            for (long long i = p * D.Np; i < (p + 1) * D.Np; ++i) {
+                if (!box(i, bx, by)) { ok = false; break; }
+                x0 = std::min(x0, bx); x1 = std::max(x1, bx); y0 = std::min(y0, by); y1 = std::max(y1, by);
+            }
+            if (!ok.load(std::memory_order_relaxed)) break;
+            if (x1 - x0 > 1 || y1 - y0 > 1) { ok = false; break; }
+            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) {
+                if (!box(D.ns_idx[q], bx, by) || bx > x0 + 1 || bx < x1 - 1 || by > y0 + 1 || by < y1 - 1) { ok = false; break; }
+            }
+        }
+    }, 64);
+    return ok.load();
 }
 
 // the tree depth: the requested one, checked, or (request <= 0) the deepest whose leaf
@@ -409,11 +420,13 @@ static int setup_boxes(ifgf2d_ctx* ctx, double k, int nlevels, const SetupExtra*
         const long long o = T.sorting[i];
         patch_s[i] = D.patch_of[o];
     }
-    {
-        std::vector<std::vector<int>> per(N);
+    {   // per sorted point, the patches it is near-singular to, ascending: counted, then placed
+        for (long long q = 0; q < (long long)D.ns_idx.size(); ++q) nptr[T.inverse[D.ns_idx[q]] + 1]++;
+        for (long long i = 0; i < N; ++i) nptr[i + 1] += nptr[i];
+        nl.resize(nptr[N]);
+        std::vector<int> fill(nptr.begin(), nptr.end() - 1);
         for (long long p = 0; p < D.num_patches; ++p)
-            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) per[T.inverse[D.ns_idx[q]]].push_back((int)p);
-        for (long long i = 0; i < N; ++i) { for (int p : per[i]) nl.push_back(p); nptr[i + 1] = (int)nl.size(); }
+            for (int q = D.ns_ptr[p]; q < D.ns_ptr[p + 1]; ++q) nl[fill[T.inverse[D.ns_idx[q]]]++] = (int)p;
     }
     CK(ctx->sorting.upload(T.sorting)); CK(ctx->inverse.upload(T.inverse));
     CK(ctx->xs_s.upload(T.xs)); CK(ctx->ys_s.upload(T.ys));
