@@ -110,7 +110,10 @@ int ifgf2d_get_precomputations(ifgf2d_ctx* ctx, long long patch, double* out);
 /* ForwardMap::precomps_and_setup (ForwardMap/ForwardMap.tpp:542-565): precomputations,
  * BoxTree::Reinitialize (IFGF_Source/BoxTree.h:995-1008), the neighbourhood check
  * (BoxTree.h:1079-1161) and the exclusion sets (ForwardMap.tpp:567-607), all flattened into
- * device tables.  nlevels <= 0 picks the deepest tree that passes the neighbourhood check. */
+ * device tables.  nlevels <= 0 picks the deepest tree that passes the neighbourhood check.
+ * The host builds the tree in stages while the GPU computes the tables whose inputs exist; the
+ * call returns when all of it is done.  When the tree fails (IFGF2D_ERR_NEIGHBORHOOD, ...) the
+ * precomputations of the new wavenumber are still made, as the reference makes them first. */
 int ifgf2d_setup(ifgf2d_ctx* ctx, double wavenumber, int nlevels);
 /* The host part of ifgf2d_setup alone: tree depth, neighbourhood check, tree and plans.  It
  * makes no CUDA call, so it may run on any host thread while the GPU works on other contexts;
