@@ -294,23 +294,6 @@ int net_prepare_single(ifgf2d_net* net, long long N, const double* geom_host, do
 // level_entry_base[l] the first entry of the slots with children at level l.
 cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
                             const int* level_cone_base = nullptr, const long long* level_entry_base = nullptr);
-// build_prop_plan in two halves: upload() copies one tree's inputs to the device, launch()
-// queues the plan kernels on `s`.  A caller with several trees uploads all of them before it
-// launches any (a copy from pageable memory queued behind a running kernel holds the host).
-// The buffers are stream-ordered on the AllocStream stream of upload(); they are freed when the
-// object is destroyed, so it must outlive the launch on that stream.
-class PropPlanInputs {
-public:
-    PropPlanInputs();
-    ~PropPlanInputs();
-    PropPlanInputs(const PropPlanInputs&) = delete;
-    PropPlanInputs& operator=(const PropPlanInputs&) = delete;
-    cudaError_t upload(const Tree& T, const int* level_cone_base = nullptr, const long long* level_entry_base = nullptr);
-    cudaError_t launch(PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s);
-private:
-    struct Impl;
-    Impl* d;
-};
 // The propagation plan computed level by level while the host builds the tree's cones: after
 // each level's cones and slots exist, add() uploads them and launches that level's entries into
 // buffers of their own on a stream of its own; gather() copies every level into pp64 / pp32 at

@@ -13,7 +13,6 @@
 // GMRES then runs for all members at once with per-member (segmented) Gram-Schmidt sums,
 // rotations, estimates and stop tests (ifgf2d_group_solve).
 #include "context.hpp"
-#include <memory>
 #include "host_threads.hpp"
 
 #include <algorithm>
@@ -257,32 +256,11 @@ extern "C" int ifgf2d_group_create(ifgf2d_ctx* const* members, int n, ifgf2d_gro
     const int ncols = (int)g->hcols.size();
     CK(g->M.alloc((size_t)ncols * D.Np));
     CK(g->W.alloc((size_t)ncols * D.Np));
-    // The weights run on a second stream, after the work queued so far on the group's stream
-    // and before the work queued there after the tables: the tables' uploads then never wait
-    // behind them (a copy from pageable memory queued behind a running kernel holds the host).
-    cudaStream_t rp_stream = nullptr;
-    cudaEvent_t rp_ready = nullptr, rp_done = nullptr;
-    struct RpStream {
-        cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
-        // on every return: the weights are done before the buffers they read can be freed
-        ~RpStream() {
-            if (s) cudaStreamSynchronize(s);
-            if (a) cudaEventDestroy(a);
-            if (b) cudaEventDestroy(b);
-            if (s) cudaStreamDestroy(s);
-        }
-    } rp_guard{rp_stream, rp_ready, rp_done};
-    CK(cudaStreamCreateWithFlags(&rp_stream, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&rp_ready, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&rp_done, cudaEventDisableTiming));
-    CK(cudaEventRecord(rp_ready, g->stream));
-    CK(cudaStreamWaitEvent(rp_stream, rp_ready, 0));
     launch_rp_precompute(g->cols.p, ncols, g->patches.p, g->curves.p, g->nsn.p, g->nsw.p, D.Np, D.p, 0.0, g->form, 0.0, g->M.p,
-                         rp_stream, keta_col.p);
+                         g->stream, keta_col.p);
     CK(cudaGetLastError());
-    launch_rp_fold(g->M.p, g->cols.p, ncols, g->edge.p, g->patches.p, D.Np, g->W.p, rp_stream);
+    launch_rp_fold(g->M.p, g->cols.p, ncols, g->edge.p, g->patches.p, D.Np, g->W.p, g->stream);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(rp_done, rp_stream));
     g->precomputed = true;
     g->counts[6] = (long long)ncols * D.Np;
     // IFGF tables: (k, eta) per leaf box and leaf cone; the members' leaf nodes and plans on the device
@@ -307,25 +285,15 @@ extern "C" int ifgf2d_group_create(ifgf2d_ctx* const* members, int n, ifgf2d_gro
         }
         return cudaSuccess;
     };
-    // every member's plan inputs are uploaded before any member's plan kernels run
-    std::vector<std::unique_ptr<PropPlanInputs>> plan_in;
     ex.build_plan = [&](PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s) -> cudaError_t {
         for (int o = 0; o < n; ++o) {
-            plan_in.emplace_back(new PropPlanInputs);
-            const cudaError_t e = plan_in.back()->upload(members[o]->T, cbase[o].data(), ebase[o].data());
-            if (e != cudaSuccess) return e;
-        }
-        for (int o = 0; o < n; ++o) {
-            const cudaError_t e = plan_in[o]->launch(pp64, pp32, err, s);
+            const cudaError_t e = build_prop_plan(members[o]->T, pp64, pp32, err, s, cbase[o].data(), ebase[o].data());
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
     };
-    const int rc_tables = setup_tables(g, 0.0, T.nlevels, &ex);
-    // the group's stream takes up the weights (keta_col, read by them, lives until here)
-    CK(cudaStreamWaitEvent(g->stream, rp_done, 0));
+    if (int rc = setup_tables(g, 0.0, T.nlevels, &ex)) { G->err = g->err; return rc; }
     CK(cudaStreamSynchronize(g->stream));
-    if (rc_tables) { G->err = g->err; return rc_tables; }
     return IFGF2D_OK;
 }
 

@@ -205,84 +205,53 @@ cudaError_t upload_level(const TreeLevel& L, int cone_base, LevelBufs& B, LevelD
 
 }  // namespace
 
-struct PropPlanInputs::Impl {
-    const Tree* T = nullptr;
-    const long long* level_entry_base = nullptr;
-    std::vector<std::unique_ptr<LevelBufs>> lb;
-    std::vector<LevelDesc> ld;
-    std::vector<std::unique_ptr<DBuf<int>>> sp, scb, spos, sr, rn;
-    ChebNodes cn{};
-};
-PropPlanInputs::PropPlanInputs() : d(new Impl) {}
-PropPlanInputs::~PropPlanInputs() { delete d; }
-
-// All levels are uploaded before the first launch: a copy from pageable host memory queued
-// behind a running kernel holds the host until the kernel ends.
-cudaError_t PropPlanInputs::upload(const Tree& T, const int* level_cone_base, const long long* level_entry_base) {
+cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
+                            const int* level_cone_base, const long long* level_entry_base) {
     if (T.Ps > 8 || T.Pang > 8) return cudaErrorInvalidValue;
-    Impl& I = *d;
-    I.T = &T;
-    I.level_entry_base = level_entry_base;
+    ChebNodes cn{};
     // Chebyshev nodes of the cone interpolant, ascending (Chebyshev.h:10-24), as the host tree has them
-    for (int i = 0; i < T.Ps; ++i) I.cn.s[T.Ps - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Ps));
-    for (int i = 0; i < T.Pang; ++i) I.cn.a[T.Pang - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Pang));
-    for (int l = 0; l < T.nlevels; ++l) I.lb.emplace_back(nullptr);
-    I.ld.resize(T.nlevels);
+    for (int i = 0; i < T.Ps; ++i) cn.s[T.Ps - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Ps));
+    for (int i = 0; i < T.Pang; ++i) cn.a[T.Pang - 1 - i] = std::cos(kPiD * (2.0 * i + 1.0) / (2.0 * T.Pang));
+    // every input buffer lives until the kernels ran.  All levels are uploaded before the first
+    // launch: a copy from pageable host memory queued behind a running kernel holds the host
+    // until the kernel ends.
+    std::vector<LevelBufs> lb(T.nlevels);
+    std::vector<LevelDesc> ld(T.nlevels);
+    std::vector<char> up(T.nlevels, 0);
     const size_t ns = T.prop_slots.size();
-    for (size_t q = 0; q < ns; ++q) {
-        I.sp.emplace_back(new DBuf<int>); I.scb.emplace_back(new DBuf<int>); I.spos.emplace_back(new DBuf<int>);
-        I.sr.emplace_back(new DBuf<int>); I.rn.emplace_back(new DBuf<int>);
-    }
+    std::vector<DBuf<int>> sp(ns), scb(ns), spos(ns), sr(ns);
+    std::vector<DBuf<int>> rn(ns);
     cudaError_t e = cudaSuccess;
     for (size_t q = 0; q < ns && e == cudaSuccess; ++q) {
         const PropSlots& S = T.prop_slots[q];
         if (S.slot_parent.empty()) continue;
         for (int l : {S.level - 1, S.level})
-            if (!I.lb[l] && e == cudaSuccess) {
-                I.lb[l].reset(new LevelBufs);
-                e = upload_level(T.L[l], level_cone_base ? level_cone_base[l] : T.L[l].cone_base, *I.lb[l], I.ld[l]);
+            if (!up[l] && e == cudaSuccess) {
+                e = upload_level(T.L[l], level_cone_base ? level_cone_base[l] : T.L[l].cone_base, lb[l], ld[l]);
+                up[l] = 1;
             }
-        if (e == cudaSuccess) e = I.sp[q]->upload(S.slot_parent);
-        if (e == cudaSuccess) e = I.scb[q]->upload(S.slot_child_box);
-        if (e == cudaSuccess) e = I.spos[q]->upload(S.slot_pos);
-        if (e == cudaSuccess) e = I.sr[q]->upload(S.slot_route);
-        if (e == cudaSuccess) e = I.rn[q]->upload(S.route_nonrel.data(), S.route_nonrel.size());
+        if (e == cudaSuccess) e = sp[q].upload(S.slot_parent);
+        if (e == cudaSuccess) e = scb[q].upload(S.slot_child_box);
+        if (e == cudaSuccess) e = spos[q].upload(S.slot_pos);
+        if (e == cudaSuccess) e = sr[q].upload(S.slot_route);
+        if (e == cudaSuccess) e = rn[q].upload(S.route_nonrel.data(), S.route_nonrel.size());
     }
-    return e;
-}
-
-cudaError_t PropPlanInputs::launch(PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s) {
-    Impl& I = *d;
-    if (!I.T) return cudaErrorInvalidValue;
-    const Tree& T = *I.T;
-    cudaError_t e = cudaSuccess;
-    for (size_t q = 0; q < T.prop_slots.size() && e == cudaSuccess; ++q) {
+    for (size_t q = 0; q < ns && e == cudaSuccess; ++q) {
         const PropSlots& S = T.prop_slots[q];
         const long long nslots = (long long)S.slot_parent.size();
         if (nslots == 0) continue;
         const long long n = nslots * T.P;
-        const long long eb = I.level_entry_base ? I.level_entry_base[S.level] : S.entry_base;
-        k_prop_plan<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(I.ld[S.level - 1], I.ld[S.level], T.min_x, T.min_y, T.k, T.Ps, I.cn,
-                                                                 T.P, I.sp[q]->p, I.scb[q]->p, I.spos[q]->p, I.sr[q]->p,
-                                                                 I.rn[q]->p, nslots, pp64 + eb, pp32 ? pp32 + eb : nullptr, err);
+        const long long eb = level_entry_base ? level_entry_base[S.level] : S.entry_base;
+        k_prop_plan<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ld[S.level - 1], ld[S.level], T.min_x, T.min_y, T.k, T.Ps, cn, T.P,
+                                                                 sp[q].p, scb[q].p, spos[q].p, sr[q].p, rn[q].p, nslots,
+                                                                 pp64 + eb, pp32 ? pp32 + eb : nullptr, err);
         e = cudaGetLastError();
     }
-    return e;
-}
-
-cudaError_t build_prop_plan(const Tree& T, PropE<double>* pp64, PropE<float>* pp32, int* err, cudaStream_t s,
-                            const int* level_cone_base, const long long* level_entry_base) {
-    cudaError_t e;
-    {
-        PropPlanInputs in;   // its buffers live until the kernels ran (stream-ordered frees)
-        e = in.upload(T, level_cone_base, level_entry_base);
-        if (e == cudaSuccess) e = in.launch(pp64, pp32, err, s);
-        if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;
-        // plain (not stream-ordered) buffers need the kernels finished before they are freed
-        const cudaError_t es = cudaStreamSynchronize(s);
-        if (e == cudaSuccess) e = es;
-    }
-    return e;
+    // stream-ordered buffers are freed in stream order after the kernels; plain ones need the
+    // kernels finished first
+    if (alloc_stream() == s && e == cudaSuccess) return cudaSuccess;
+    const cudaError_t es = cudaStreamSynchronize(s);
+    return e != cudaSuccess ? e : es;
 }
 
 struct PropPlanByLevel::Impl {
