@@ -7,6 +7,7 @@
 #include <condition_variable>
 #include <functional>
 #include <mutex>
+#include <pthread.h>
 #include <thread>
 #include <vector>
 
@@ -33,6 +34,9 @@ public:
         static HostPool* p = new HostPool;   // never destroyed: the workers wait until process exit
         return *p;
     }
+    // false in a child process after fork(): the child has none of the workers, and a lock
+    // that another thread held at the fork stays held, so the child starts threads per loop
+    static bool usable() { return !forked().load(std::memory_order_relaxed); }
     // true on a thread that is running a chunk of a pool loop (a nested loop must not use the pool)
     static bool& inside() {
         static thread_local bool v = false;
@@ -65,7 +69,14 @@ private:
         long long n, chunk;
         int nchunks;
     };
-    HostPool() = default;
+    HostPool() {
+        static std::once_flag once;
+        std::call_once(once, [] { pthread_atfork(nullptr, nullptr, [] { forked().store(true); }); });
+    }
+    static std::atomic<bool>& forked() {
+        static std::atomic<bool> f{false};
+        return f;
+    }
     void grow(int want) {
         while ((int)workers_.size() < want) {
             workers_.emplace_back([this] { loop(); });
@@ -124,7 +135,7 @@ void parallel_for(long long n, F&& f, long long grain = 1024) {
     if (nt <= 1) { f(0LL, n); return; }
     const long long chunk = (n + nt - 1) / nt;
     const std::function<void(long long, long long)> job = [&f](long long b, long long e) { f(b, e); };
-    if (!HostPool::inside() && HostPool::get().run(n, chunk, (int)nt, job)) return;
+    if (!HostPool::inside() && HostPool::usable() && HostPool::get().run(n, chunk, (int)nt, job)) return;
     std::vector<std::thread> th;
     for (long long t = 0; t < nt; ++t) {
         const long long b = t * chunk, e = std::min(n, b + chunk);

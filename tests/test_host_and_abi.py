@@ -175,3 +175,35 @@ def test_group_create_checks_its_members_before_any_gpu_work(lib):
     d.prepare(150.0, 0)
     with pytest.raises(ValueError, match="formulation"):
         lib.Group([a, d])                       # different formulation
+
+
+@pytest.mark.filterwarnings("ignore:This process .* is multi-threaded:DeprecationWarning")
+def test_host_threads_after_fork(lib):
+    """The host loops run on a pool of worker threads kept for the process.  A child forked
+    after the pool started has none of its workers; its set-up must still run, on threads of its
+    own, and give the same tree."""
+    import os
+    import signal
+    import time
+    fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, 300.0, Np=16, patches_per_curve=320)
+    fm.prepare(300.0, 0)
+    before = fm.getSorting()
+    pid = os.fork()
+    if pid == 0:   # child: a second set-up on the inherited pool state
+        code = 1
+        try:
+            fm.prepare(300.0, 0)
+            code = 0 if (fm.getSorting() == before).all() else 2
+        finally:
+            os._exit(code)
+    deadline = time.time() + 120
+    while True:
+        done, status = os.waitpid(pid, os.WNOHANG)
+        if done:
+            break
+        if time.time() > deadline:
+            os.kill(pid, signal.SIGKILL)
+            os.waitpid(pid, 0)
+            raise AssertionError("the forked child's set-up did not finish")
+        time.sleep(0.05)
+    assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
