@@ -1,8 +1,8 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle -- needs a GPU.
 
 Tolerances: FP64 device Hankel within 5e-15 of scipy (relative to |H|); rectangular-polar
-weights and the direct forward map within 1e-12 of the oracle (relative, as the north-star
-bar for the plain form); the IFGF apply within 1e-11 of the oracle's own IFGF (same algorithm,
+weights and the direct forward map within 1e-12 of the oracle (relative, the parity bar of
+the plain form); the IFGF apply within 1e-11 of the oracle's own IFGF (same algorithm,
 same tree); the IFGF far field within the IFGF tolerance (5e-4 for 5x5 cones) of the
 exclusion-matched O(N^2) sum.
 """
