@@ -207,3 +207,20 @@ def test_host_threads_after_fork(lib):
             raise AssertionError("the forked child's set-up did not finish")
         time.sleep(0.05)
     assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
+
+
+def test_host_threads_concurrent_setups(lib):
+    """Host set-ups from several threads at once: one runs its loops on the worker pool, the
+    others find it busy and start threads of their own.  Every tree equals the one built alone."""
+    from concurrent.futures import ThreadPoolExecutor
+    ks = [150.0, 220.0, 300.0, 380.0, 260.0, 190.0]
+
+    def build(k):
+        fm = lib.ForwardMap(0.01, [lib.Kite()], (), 1.0, k, Np=16, patches_per_curve=int(1.024 * k) + 16)
+        fm.prepare(k, 0)
+        return fm.getSorting().tobytes(), tuple(sorted(fm.work_counts().items()))
+
+    alone = [build(k) for k in ks]
+    with ThreadPoolExecutor(len(ks)) as ex:
+        together = list(ex.map(build, ks * 2))
+    assert together == alone * 2
