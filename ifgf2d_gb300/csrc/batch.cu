@@ -20,6 +20,7 @@ struct BatchWork {
     DBuf<double2> rho64, coef64;
     DBuf<float2> rho32, coef32;
     DBuf<PropB<double>> pb64;
+    DBuf<double> rows64;                       // the FP64 plan terms' Chebyshev rows (FP64-pipe work the lanes share)
     DBuf<PropB<float>> pb32;
     DBuf<float2> W32;                          // complex64 copy of the singular-correction weights
     DBuf<float2> xt32;                         // complex64 copy of the interleaved input (mixed form)
@@ -142,6 +143,9 @@ int ensure_apply(ifgf2d_ctx* ctx, int B, bool mixed) {
             CK(W.pb64.alloc(ctx->pp.n));
             launch_sort_plan<double>(ctx->pp_ptr.p, ctx->T.total_cones, ctx->pp.p, ctx->T.P, W.pb64.p, ctx->stream);
             CK(cudaGetLastError());
+            CK(W.rows64.alloc(ctx->pp.n * (size_t)(ctx->T.Ps + ctx->T.Pang)));
+            launch_plan_rows<double>(W.pb64.p, (long long)ctx->pp.n, ctx->T.Ps, ctx->T.Pang, W.rows64.p, ctx->stream);
+            CK(cudaGetLastError());
         }
     }
     return IFGF2D_OK;
@@ -177,7 +181,9 @@ void far_b(ifgf2d_ctx* ctx, const V2<R>* rho, const V2<R>* near, const V2<R>* le
                 launch_prop_bk(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, W.t5err.p, s))
                 continue;
         }
-        launch_prop_b<R>(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, s);
+        const R* rows = nullptr;
+        if constexpr (sizeof(R) == 8) rows = ctx->bw->rows64.p;
+        launch_prop_b<R>(p0, p1, ctx->pp_ptr.p, ctx->pp_nchild.p, pb, T.Ps, T.Pang, Gsep, B, coef, s, rows);
     }
     bool grouped = false;
     if constexpr (sizeof(R) == 4) grouped = (ctx->tune_batch_tc & kBatchGroupedInterp) && B <= 64 && T.Ps == 5 && T.Pang == 5;

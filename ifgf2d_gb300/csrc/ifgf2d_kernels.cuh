@@ -164,9 +164,13 @@ template <typename R>
 void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* leaf_start, const int* leaf_count,
                    const long long* leaf_off, const V2<R>* L, const V2<R>* rho, int Ps, int Pang, int B, V2<R>* coef,
                    cudaStream_t s);
+// rows (optional): the terms' Chebyshev rows from launch_plan_rows, read instead of computed
 template <typename R>
 void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
-                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s);
+                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s, const R* rows = nullptr);
+// the Chebyshev rows T_0..T_{Ps-1}(s), T_0..T_{Pang-1}(th) of n batched plan terms, [term][Ps + Pang]
+template <typename R>
+void launch_plan_rows(const PropB<R>* pb, long long n, int Ps, int Pang, R* rows, cudaStream_t s);
 // the complex64 propagation on the tcgen05 tensor cores in 3xTF32 (batch_tcgen05.cu); false when
 // the shape is not supported (Ps x Pang other than 5 x 5, more than 64 right-hand sides) and
 // nothing was launched.  *err is set when a completion wait runs out.  The kernel's shared-memory

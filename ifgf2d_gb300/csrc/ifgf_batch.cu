@@ -213,10 +213,11 @@ struct PropBlock {
     static constexpr int bytes_per_warp = P * 32 * RPL * (int)sizeof(V2<R>);
     static constexpr int W = 32768 / bytes_per_warp >= 4 ? 4 : (32768 / bytes_per_warp >= 2 ? 2 : 1);
 };
-template <typename R, int PS, int PA, int WPB, int RPL>
+template <typename R, int PS, int PA, int WPB, int RPL, bool ROWS = false>
 __global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const long long* __restrict__ pp_ptr,
                                                      const int* __restrict__ pp_nchild, const PropB<R>* __restrict__ pb,
-                                                     const R* __restrict__ Gsep, int B, V2<R>* __restrict__ coef) {
+                                                     const R* __restrict__ Gsep, int B, V2<R>* __restrict__ coef,
+                                                     const R* __restrict__ rows = nullptr) {
     constexpr int P = PS * PA;
     __shared__ V2<R> sv[WPB][P][32 * RPL];
     __shared__ R sG[PS * PS + PA * PA];
@@ -255,8 +256,16 @@ __global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const
                 for (int q = 0; q < P; ++q) cc[k][q] = src[(long long)q * B + rr[k]];
         }
         R Ts[PS], Tt[PA];
-        cheb_row<R, PS>(E.s, Ts);
-        cheb_row<R, PA>(E.th, Tt);
+        if constexpr (ROWS) {   // the same rows, computed once per term by k_plan_rows
+            const R* rw = rows + (e0 + e) * (PS + PA);
+#pragma unroll
+            for (int q = 0; q < PS; ++q) Ts[q] = rw[q];
+#pragma unroll
+            for (int q = 0; q < PA; ++q) Tt[q] = rw[PS + q];
+        } else {
+            cheb_row<R, PS>(E.s, Ts);
+            cheb_row<R, PA>(E.th, Tt);
+        }
         V2<R> wv; wv.x = E.wr; wv.y = E.wi;
 #pragma unroll
         for (int k = 0; k < RPL; ++k) {
@@ -298,6 +307,24 @@ __global__ void __launch_bounds__(WPB * 32) k_prop_b(int pbegin, int pend, const
                 out[(long long)(n * PS + m) * B] = a;
             }
     }
+}
+
+// the Chebyshev rows T_q(s), T_a(th) of every batched plan term, [term][PS + PA]: the propagation
+// reads them once per warp instead of computing them in every lane (they are the same for all
+// the warp's right-hand sides), with the same cheb_row arithmetic
+template <typename R, int PS, int PA>
+__global__ void k_plan_rows(const PropB<R>* __restrict__ pb, long long n, R* __restrict__ rows) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const PropB<R> E = pb[e];
+    R Ts[PS], Tt[PA];
+    cheb_row<R, PS>(E.s, Ts);
+    cheb_row<R, PA>(E.th, Tt);
+    R* rw = rows + e * (PS + PA);
+#pragma unroll
+    for (int q = 0; q < PS; ++q) rw[q] = Ts[q];
+#pragma unroll
+    for (int q = 0; q < PA; ++q) rw[PS + q] = Tt[q];
 }
 
 // ------------------------------------------------------------------ propagation, TMA-staged
@@ -665,14 +692,22 @@ void launch_leaf_b(const int* cone_box, int ncones, int cone_base, const int* le
 }
 template <typename R>
 void launch_prop_b(int pbegin, int pend, const long long* pp_ptr, const int* pp_nchild, const PropB<R>* pb, int Ps, int Pang,
-                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s) {
+                   const R* Gsep, int B, V2<R>* coef, cudaStream_t s, const R* rows) {
     if (pend <= pbegin) return;
     constexpr int RPL = Rpl<R>::v;
     IFGF_DISPATCH_P(Ps, Pang, {
         constexpr int WPB = PropBlock<R, PS * PA, RPL>::W;
-        k_prop_b<R, PS, PA, WPB, RPL><<<dim3(nblk_b(pend - pbegin, WPB), nblk_b(B, 32 * RPL)), WPB * 32, 0, s>>>(
-            pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
+        const dim3 grid(nblk_b(pend - pbegin, WPB), nblk_b(B, 32 * RPL));
+        if (rows)
+            k_prop_b<R, PS, PA, WPB, RPL, true><<<grid, WPB * 32, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef, rows);
+        else
+            k_prop_b<R, PS, PA, WPB, RPL><<<grid, WPB * 32, 0, s>>>(pbegin, pend, pp_ptr, pp_nchild, pb, Gsep, B, coef);
     });
+}
+template <typename R>
+void launch_plan_rows(const PropB<R>* pb, long long n, int Ps, int Pang, R* rows, cudaStream_t s) {
+    if (n <= 0) return;
+    IFGF_DISPATCH_P(Ps, Pang, (k_plan_rows<R, PS, PA><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pb, n, rows)));
 }
 bool launch_interp_grp(const int4* items, int nitems, const InterpG* terms, const float2* coef, int Ps, int Pang,
                        const long long* sorting, int B, double2* yt, cudaStream_t s) {
@@ -719,7 +754,8 @@ void launch_bscale(const double2* w, const double2* hn, long long N, int B, doub
     template void launch_leaf_b<R>(const int*, int, int, const int*, const int*, const long long*, const V2<R>*,        \
                                    const V2<R>*, int, int, int, V2<R>*, cudaStream_t);                                  \
     template void launch_prop_b<R>(int, int, const long long*, const int*, const PropB<R>*, int, int, const R*, int,    \
-                                   V2<R>*, cudaStream_t);                                                               \
+                                   V2<R>*, cudaStream_t, const R*);                                                     \
+    template void launch_plan_rows<R>(const PropB<R>*, long long, int, int, R*, cudaStream_t);                         \
     template void launch_final_b<R>(int, const int*, const int*, const int*, const int*, const int*, const int*,        \
                                     const long long*, const V2<R>*, const V2<R>*, const int*, const InterpE<R>*,        \
                                     const V2<R>*, int, int, const long long*, int, double2*, cudaStream_t);
